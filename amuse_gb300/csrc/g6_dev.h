@@ -1,0 +1,108 @@
+/*
+ * g6_dev.h -- internal interface between the C host library (g6_host.c)
+ * and the CUDA launchers (kern_*.cu).  Plain C; not installed.
+ *
+ * HBM layout of the j-system (capacity `cap` slots, a multiple of G6_TILE):
+ *   t, dt, m, pot           double[cap]
+ *   x, v, a, j              double[3*cap], component-major: x[k*cap + slot]
+ *   id, nn                  int[cap]
+ *   jp                      predicted records, one per slot, padded to the
+ *                           next multiple of G6_TILE with zero-mass records
+ *                           far away:
+ *                             split: 48 B {xh,yh,zh,m}{xl,yl,zl,0}{vx,vy,vz,0}
+ *                             fp64 : 64 B {x,y,z,m}{vx,vy,vz,0}
+ * Accelerations and jerks are stored unscaled (the GRAPE-6 a/2, j/6 inputs
+ * are rescaled on the host), so the device predictor evaluates exactly
+ * ph4's expression (jdata.cc:736-744).
+ */
+#ifndef G6_DEV_H
+#define G6_DEV_H
+
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define G6_TILE 128 /* j records per shared-memory tile */
+
+enum { G6_PREC_SPLIT = 0, G6_PREC_FP64 = 1 };
+
+typedef struct {
+  int cap;
+  double *t, *dt, *m, *pot;
+  double *x, *v, *a, *j;
+  int *id, *nn;
+  void *jp_split; /* 48 B records */
+  void *jp_f64;   /* 64 B records */
+} g6_jstate;
+
+/* One staged j-update (g6_set_j_particle), 128 B. */
+typedef struct {
+  int addr, id;
+  double t, dt, m;
+  double x[3], v[3], a[3], j[3];
+} g6_jupd;
+
+/* One force evaluation. i-particles are either given explicitly
+ * (ipos/ivel, FP64, [ni][3]) or, when ilist != NULL, are the j-slots in
+ * ilist predicted to the same time (ipos/ivel ignored).  iself[i] is the
+ * j slot to exclude (the particle itself) or -1.                         */
+typedef struct {
+  int ni, nj, prec;
+  double eps2;
+  const double *ipos, *ivel; /* device, [ni][3] */
+  const int *ilist;          /* device, [ni] or NULL */
+  const int *iself;          /* device, [ni] or NULL (then = ilist) */
+  const g6_jstate *js;       /* j-system (device pointers inside) */
+  double ti;                 /* prediction time (for ilist mode) */
+  /* outputs (device) */
+  double *acc, *jerk, *pot;  /* [ni][3], [ni][3], [ni] */
+  int *nn;                   /* [ni] nearest j slot (-1 none) */
+  float *nn_r2;              /* [ni] (r^2 + eps^2) of nn, or NULL */
+  /* scratch for split-j partial sums (device) */
+  void *scratch;
+  size_t scratch_bytes;
+  int *err; /* device error word (0 = ok) */
+  /* launch shape override (0 = automatic) */
+  int force_jl, force_nsplit;
+} g6_force_args;
+
+/* Launch shape actually used (reported by g6k_force). */
+typedef struct {
+  int jl, nsplit, grid_x, grid_y, threads;
+} g6_shape;
+
+size_t g6k_scratch_bytes(int ni, int nj, int prec, int force_jl, int force_nsplit);
+int g6k_sm_count(void);
+
+int g6k_scatter(const g6_jstate *js, const g6_jupd *d_upd, int n, cudaStream_t st);
+int g6k_predict(const g6_jstate *js, int nj, double ti, int prec, cudaStream_t st);
+int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t st);
+
+/* FP64 Hermite corrector + Aarseth step on the listed slots (in place):
+ * idata.cc:399-514.  acc/jerk are the new values at tnext, [ni][3]. */
+int g6k_correct(const g6_jstate *js, int ni, const int *ilist, double tnext,
+                double eta, const double *acc, const double *jerk,
+                const double *pot, const int *nn, cudaStream_t st);
+/* Block scheduler: tnext = min(t+dt); ilist = slots with t+dt == tnext.
+ * Writes tnext to *d_tnext and the count to *d_ni. scratch >= 2*grid. */
+int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni,
+                 double *d_tnext, double *d_scratch, int scratch_len,
+                 cudaStream_t st);
+/* Initial time steps (jdata.cc:503-564 without the median limit). */
+int g6k_initial_step(const g6_jstate *js, int nj, double eta, double fac,
+                     double limit, double system_time, cudaStream_t st);
+/* Kinetic energy and sum m*pot (predicted to t) -> d_out[0..1]. */
+int g6k_energy_sums(const g6_jstate *js, int nj, double t, const double *pot_i,
+                    double *d_out, cudaStream_t st);
+/* Plain copy of acc/jerk/pot/time into the j-state for ilist (t, dt untouched
+ * except time = t0), used after the initial force evaluation. */
+int g6k_store_forces(const g6_jstate *js, int ni, const int *ilist,
+                     const double *acc, const double *jerk, const double *pot,
+                     const int *nn, cudaStream_t st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

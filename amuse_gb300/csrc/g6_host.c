@@ -1,0 +1,1215 @@
+/*
+ * g6_host.c -- host side of libsapporo.so (C11 + CUDA runtime C API).
+ *
+ * Implements the GRAPE-6 ABI of include/g6.h on one GPU.  Mirrors the
+ * behaviour of the reference host library (lib/sapporo_light/sapporo.cpp,
+ * send_fetch_data.cpp) with these differences by design:
+ *   - the j-store grows on demand (no nj_max = 131072 cap, sapporo.cpp:30);
+ *   - j updates are staged in pinned memory, deduplicated per slot with an
+ *     O(1) slot index (the reference uses a std::map, sapporo.cpp:83-110) and
+ *     applied with one copy + one scatter kernel per force call;
+ *   - inputs and outputs move with one asynchronous copy each way;
+ *   - errors return negative codes instead of exit(-1).
+ * There is no CPU force path: every force is computed by the CUDA kernels.
+ */
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime_api.h>
+
+#include "g6.h"
+#include "g6_dev.h"
+
+int g6k_clamp_steps(const g6_jstate *js, int nj, double dtmax, cudaStream_t st);
+int g6k_neighbours(const g6_jstate *js, int nj, int ni, int prec, const double *ipos,
+                   const double *h2, const int *iself, int *out, int maxn, cudaStream_t st);
+
+#define G6_DEFAULT_CAP 131072
+#define G6_DEFAULT_NPIPES 16384
+
+/* ------------------------------------------------------------ id map --- */
+/* Open addressing id -> slot (ids are arbitrary ints). */
+typedef struct {
+  int *key, *val;
+  int cap, n;
+} idmap;
+
+static unsigned hash_int(int k) {
+  unsigned x = (unsigned)k;
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+static void idmap_free(idmap *m) {
+  free(m->key);
+  free(m->val);
+  memset(m, 0, sizeof(*m));
+}
+
+static int idmap_put(idmap *m, int k, int v);
+
+static int idmap_grow(idmap *m) {
+  idmap n;
+  n.cap = m->cap ? 2 * m->cap : 1024;
+  n.n = 0;
+  n.key = (int *)malloc(sizeof(int) * n.cap);
+  n.val = (int *)malloc(sizeof(int) * n.cap);
+  if (!n.key || !n.val) {
+    free(n.key);
+    free(n.val);
+    return -1;
+  }
+  for (int i = 0; i < n.cap; i++) n.val[i] = -1;
+  for (int i = 0; i < m->cap; i++)
+    if (m->val[i] >= 0) idmap_put(&n, m->key[i], m->val[i]); /* drops erased entries */
+  idmap_free(m);
+  *m = n;
+  return 0;
+}
+
+static int idmap_put(idmap *m, int k, int v) {
+  if (2 * (m->n + 1) > m->cap && idmap_grow(m) != 0) return -1;
+  unsigned h = hash_int(k) & (unsigned)(m->cap - 1);
+  /* val == -1: empty; val < -1: erased entry (kept so probe chains hold). */
+  while (m->val[h] != -1 && m->key[h] != k) h = (h + 1) & (unsigned)(m->cap - 1);
+  if (m->val[h] == -1) m->n++;
+  m->key[h] = k;
+  m->val[h] = v;
+  return 0;
+}
+
+static int idmap_get(const idmap *m, int k) {
+  if (m->cap == 0) return -1;
+  unsigned h = hash_int(k) & (unsigned)(m->cap - 1);
+  while (m->val[h] != -1) {
+    if (m->key[h] == k) return m->val[h] >= 0 ? m->val[h] : -1;
+    h = (h + 1) & (unsigned)(m->cap - 1);
+  }
+  return -1;
+}
+
+/* ----------------------------------------------------------- context --- */
+typedef struct {
+  int is_open, device, npipes, prec;
+  cudaStream_t st;
+  cudaEvent_t ev_done, ev_upd, ev_t0, ev_t1, ev_t2;
+  g6_jstate js;
+  /* host mirrors (size cap) */
+  int *slot_id, *stage_pos;
+  idmap ids;
+  /* staged j updates (pinned) */
+  g6_jupd *h_upd, *d_upd;
+  int n_upd, cap_upd, cap_dupd, upd_inflight;
+  /* time / prediction state */
+  double ti;
+  int pred_valid, pred_nj, pred_prec;
+  double pred_t;
+  /* i / out buffers: pinned host block + device block, capacity cap_i */
+  int cap_i;
+  void *h_in, *d_in;   /* [ipos 3n][ivel 3n][h2 n] doubles, [iself n] ints */
+  void *h_out, *d_out; /* [err 2 ints][acc 3n][jerk 3n][pot n] doubles, [nn n] ints, [nnr2 n] floats */
+  int *d_err;
+  void *d_scratch;
+  size_t scratch_bytes;
+  /* pending g6calc */
+  int pending, pending_ni, pending_nj;
+  int *pending_ids; /* copy of index[] for the neighbour-list API */
+  int pending_cap;
+  /* device run (extension API) */
+  int run_n;
+  double run_t, run_eps2, run_eta;
+  int *d_ilist, *d_ni;
+  double *d_tnext, *d_sched, *d_esum, *d_racc, *d_rjerk, *d_rpot;
+  int *d_rnn;
+  int run_cap;
+  /* statistics */
+  int timing;
+  double st_predict_ms, st_force_ms, st_pairs, st_pred_bytes, st_nj;
+  g6_shape shape;
+  int predicted_this_call;
+  char err[256];
+} g6ctx;
+
+static g6ctx G;
+static int ilist_identity_n; /* d_ilist holds 0..n-1 for this n (0: unknown) */
+
+static void seterr(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(G.err, sizeof(G.err), fmt, ap);
+  va_end(ap);
+  fprintf(stderr, "libsapporo(gb300): %s\n", G.err);
+}
+
+#define CK(call)                                                   \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) {                                       \
+      seterr("%s failed: %s", #call, cudaGetErrorString(e_));      \
+      return G6_ERR_CUDA;                                          \
+    }                                                              \
+  } while (0)
+
+static void *pin_alloc(size_t bytes) {
+  void *p = NULL;
+  if (cudaHostAlloc(&p, bytes ? bytes : 16, cudaHostAllocDefault) != cudaSuccess) return NULL;
+  return p;
+}
+
+static void free_jstate(g6_jstate *js) {
+  cudaFree(js->t); cudaFree(js->dt); cudaFree(js->m); cudaFree(js->pot);
+  cudaFree(js->x); cudaFree(js->v); cudaFree(js->a); cudaFree(js->j);
+  cudaFree(js->id); cudaFree(js->nn);
+  cudaFree(js->jp_split); cudaFree(js->jp_f64);
+  memset(js, 0, sizeof(*js));
+}
+
+/* Grow the j-store to hold at least `need` slots (contents preserved). */
+static int grow_j(int need) {
+  if (need <= G.js.cap) return 0;
+  int cap = G.js.cap ? G.js.cap : G6_DEFAULT_CAP;
+  while (cap < need) cap *= 2;
+  cap = (cap + G6_TILE - 1) / G6_TILE * G6_TILE;
+  g6_jstate n;
+  memset(&n, 0, sizeof(n));
+  n.cap = cap;
+  size_t d = sizeof(double) * (size_t)cap;
+  int ok = cudaMalloc((void **)&n.t, d) == cudaSuccess &&
+           cudaMalloc((void **)&n.dt, d) == cudaSuccess &&
+           cudaMalloc((void **)&n.m, d) == cudaSuccess &&
+           cudaMalloc((void **)&n.pot, d) == cudaSuccess &&
+           cudaMalloc((void **)&n.x, 3 * d) == cudaSuccess &&
+           cudaMalloc((void **)&n.v, 3 * d) == cudaSuccess &&
+           cudaMalloc((void **)&n.a, 3 * d) == cudaSuccess &&
+           cudaMalloc((void **)&n.j, 3 * d) == cudaSuccess &&
+           cudaMalloc((void **)&n.id, sizeof(int) * (size_t)cap) == cudaSuccess &&
+           cudaMalloc((void **)&n.nn, sizeof(int) * (size_t)cap) == cudaSuccess &&
+           cudaMalloc(&n.jp_split, 48 * (size_t)cap) == cudaSuccess &&
+           cudaMalloc(&n.jp_f64, 64 * (size_t)cap) == cudaSuccess;
+  if (!ok) {
+    free_jstate(&n);
+    seterr("cannot allocate j-store for %d slots", cap);
+    return G6_ERR_NOMEM;
+  }
+  cudaMemsetAsync(n.t, 0, d, G.st);
+  cudaMemsetAsync(n.dt, 0, d, G.st);
+  cudaMemsetAsync(n.m, 0, d, G.st);
+  cudaMemsetAsync(n.pot, 0, d, G.st);
+  cudaMemsetAsync(n.x, 0, 3 * d, G.st);
+  cudaMemsetAsync(n.v, 0, 3 * d, G.st);
+  cudaMemsetAsync(n.a, 0, 3 * d, G.st);
+  cudaMemsetAsync(n.j, 0, 3 * d, G.st);
+  cudaMemsetAsync(n.id, 0xff, sizeof(int) * (size_t)cap, G.st);
+  cudaMemsetAsync(n.nn, 0xff, sizeof(int) * (size_t)cap, G.st);
+  if (G.js.cap) {
+    size_t od = sizeof(double) * (size_t)G.js.cap;
+    cudaMemcpyAsync(n.t, G.js.t, od, cudaMemcpyDeviceToDevice, G.st);
+    cudaMemcpyAsync(n.dt, G.js.dt, od, cudaMemcpyDeviceToDevice, G.st);
+    cudaMemcpyAsync(n.m, G.js.m, od, cudaMemcpyDeviceToDevice, G.st);
+    cudaMemcpyAsync(n.pot, G.js.pot, od, cudaMemcpyDeviceToDevice, G.st);
+    for (int k = 0; k < 3; k++) {
+      cudaMemcpyAsync(n.x + (size_t)k * cap, G.js.x + (size_t)k * G.js.cap, od,
+                      cudaMemcpyDeviceToDevice, G.st);
+      cudaMemcpyAsync(n.v + (size_t)k * cap, G.js.v + (size_t)k * G.js.cap, od,
+                      cudaMemcpyDeviceToDevice, G.st);
+      cudaMemcpyAsync(n.a + (size_t)k * cap, G.js.a + (size_t)k * G.js.cap, od,
+                      cudaMemcpyDeviceToDevice, G.st);
+      cudaMemcpyAsync(n.j + (size_t)k * cap, G.js.j + (size_t)k * G.js.cap, od,
+                      cudaMemcpyDeviceToDevice, G.st);
+    }
+    cudaMemcpyAsync(n.id, G.js.id, sizeof(int) * (size_t)G.js.cap, cudaMemcpyDeviceToDevice, G.st);
+    cudaMemcpyAsync(n.nn, G.js.nn, sizeof(int) * (size_t)G.js.cap, cudaMemcpyDeviceToDevice, G.st);
+  }
+  CK(cudaStreamSynchronize(G.st));
+  int *sid = (int *)realloc(G.slot_id, sizeof(int) * (size_t)cap);
+  int *spos = (int *)realloc(G.stage_pos, sizeof(int) * (size_t)cap);
+  if (!sid || !spos) {
+    if (sid) G.slot_id = sid;
+    if (spos) G.stage_pos = spos;
+    free_jstate(&n);
+    seterr("host allocation failed");
+    return G6_ERR_NOMEM;
+  }
+  for (int s = G.js.cap; s < cap; s++) {
+    sid[s] = -1;
+    spos[s] = -1;
+  }
+  G.slot_id = sid;
+  G.stage_pos = spos;
+  free_jstate(&G.js);
+  G.js = n;
+  G.pred_valid = 0;
+  return 0;
+}
+
+static int ensure_io(int ni) {
+  if (ni <= G.cap_i) return 0;
+  int cap = G.cap_i ? G.cap_i : 1024;
+  while (cap < ni) cap *= 2;
+  size_t in_b = (size_t)cap * (7 * sizeof(double) + sizeof(int));
+  size_t out_b = 16 + (size_t)cap * (7 * sizeof(double) + sizeof(int) + sizeof(float));
+  if (G.h_in) cudaFreeHost(G.h_in);
+  if (G.h_out) cudaFreeHost(G.h_out);
+  cudaFree(G.d_in);
+  cudaFree(G.d_out);
+  G.h_in = G.h_out = G.d_in = G.d_out = NULL;
+  G.cap_i = 0;
+  G.h_in = pin_alloc(in_b);
+  G.h_out = pin_alloc(out_b);
+  if (!G.h_in || !G.h_out || cudaMalloc(&G.d_in, in_b) != cudaSuccess ||
+      cudaMalloc(&G.d_out, out_b) != cudaSuccess) {
+    seterr("cannot allocate i/o buffers for %d i-particles", cap);
+    return G6_ERR_NOMEM;
+  }
+  CK(cudaMemsetAsync(G.d_out, 0, out_b, G.st));
+  G.d_err = (int *)G.d_out;
+  G.cap_i = cap;
+  int *pid = (int *)realloc(G.pending_ids, sizeof(int) * (size_t)cap);
+  if (!pid) return G6_ERR_NOMEM;
+  G.pending_ids = pid;
+  G.pending_cap = cap;
+  return 0;
+}
+
+/* Views into the i/o blocks for capacity cap_i. */
+#define IN_POS(b) ((double *)(b))
+#define IN_VEL(b) ((double *)(b) + 3 * (size_t)G.cap_i)
+#define IN_H2(b) ((double *)(b) + 6 * (size_t)G.cap_i)
+#define IN_SELF(b) ((int *)((double *)(b) + 7 * (size_t)G.cap_i))
+#define OUT_ERR(b) ((int *)(b))
+#define OUT_ACC(b) ((double *)((char *)(b) + 16))
+#define OUT_JERK(b) (OUT_ACC(b) + 3 * (size_t)G.cap_i)
+#define OUT_POT(b) (OUT_ACC(b) + 6 * (size_t)G.cap_i)
+#define OUT_NN(b) ((int *)(OUT_ACC(b) + 7 * (size_t)G.cap_i))
+#define OUT_NNR2(b) ((float *)(OUT_NN(b) + (size_t)G.cap_i))
+
+static int ensure_scratch(size_t bytes) {
+  if (bytes <= G.scratch_bytes) return 0;
+  cudaFree(G.d_scratch);
+  G.d_scratch = NULL;
+  G.scratch_bytes = 0;
+  size_t b = bytes + bytes / 4;
+  if (cudaMalloc(&G.d_scratch, b) != cudaSuccess) {
+    seterr("cannot allocate %zu B of split-j scratch", b);
+    return G6_ERR_NOMEM;
+  }
+  G.scratch_bytes = b;
+  return 0;
+}
+
+static int check_open(void) {
+  if (!G.is_open) {
+    seterr("library not opened (g6_open)");
+    return G6_ERR_NOT_OPEN;
+  }
+  return 0;
+}
+
+/* Apply staged j updates: one H2D copy + one scatter kernel. */
+static int flush_updates(void) {
+  if (G.n_upd == 0) return 0;
+  if (G.n_upd > G.cap_dupd) {
+    cudaFree(G.d_upd);
+    G.d_upd = NULL;
+    G.cap_dupd = 0;
+    int c = G.cap_upd;
+    if (cudaMalloc((void **)&G.d_upd, sizeof(g6_jupd) * (size_t)c) != cudaSuccess) {
+      seterr("cannot allocate update buffer");
+      return G6_ERR_NOMEM;
+    }
+    G.cap_dupd = c;
+  }
+  CK(cudaMemcpyAsync(G.d_upd, G.h_upd, sizeof(g6_jupd) * (size_t)G.n_upd,
+                     cudaMemcpyHostToDevice, G.st));
+  CK(cudaEventRecord(G.ev_upd, G.st));
+  G.upd_inflight = 1;
+  int rc = g6k_scatter(&G.js, G.d_upd, G.n_upd, G.st);
+  if (rc) {
+    seterr("scatter launch failed");
+    return G6_ERR_CUDA;
+  }
+  for (int u = 0; u < G.n_upd; u++) G.stage_pos[G.h_upd[u].addr] = -1;
+  G.n_upd = 0;
+  G.pred_valid = 0;
+  return 0;
+}
+
+static int predict_if_needed(int nj) {
+  G.predicted_this_call = 0;
+  if (G.pred_valid && G.pred_t == G.ti && G.pred_nj == nj && G.pred_prec == G.prec) return 0;
+  int need = (nj + G6_TILE - 1) / G6_TILE * G6_TILE;
+  int rc = grow_j(need);
+  if (rc) return rc;
+  if (G.timing) cudaEventRecord(G.ev_t0, G.st);
+  if (g6k_predict(&G.js, nj, G.ti, G.prec, G.st)) {
+    seterr("predictor launch failed");
+    return G6_ERR_CUDA;
+  }
+  if (G.timing) cudaEventRecord(G.ev_t1, G.st);
+  G.predicted_this_call = 1;
+  G.pred_valid = 1;
+  G.pred_t = G.ti;
+  G.pred_nj = nj;
+  G.pred_prec = G.prec;
+  return 0;
+}
+
+/* Run one force evaluation whose inputs are already on the device. */
+static int run_force(g6_force_args *a) {
+  size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, 0, 0);
+  int rc = ensure_scratch(need);
+  if (rc) return rc;
+  a->scratch = G.d_scratch;
+  a->scratch_bytes = G.scratch_bytes;
+  a->js = &G.js;
+  a->err = G.d_err;
+  if (G.timing) {
+    if (!G.predicted_this_call) cudaEventRecord(G.ev_t1, G.st);
+  }
+  rc = g6k_force(a, &G.shape, G.st);
+  if (rc) {
+    seterr("force launch failed (%d)", rc);
+    return G6_ERR_CUDA;
+  }
+  if (G.timing) cudaEventRecord(G.ev_t2, G.st);
+  G.st_pairs = (double)a->ni * (double)(a->nj > 0 ? a->nj - 1 : 0);
+  G.st_nj = a->nj;
+  G.st_pred_bytes = G.predicted_this_call
+                        ? (double)a->nj * (15.0 * 8.0 + (G.prec == G6_PREC_FP64 ? 64.0 : 48.0))
+                        : 0.0;
+  return 0;
+}
+
+static void collect_timing(void) {
+  if (!G.timing) return;
+  float ms = 0;
+  G.st_predict_ms = 0;
+  if (G.predicted_this_call && cudaEventElapsedTime(&ms, G.ev_t0, G.ev_t1) == cudaSuccess)
+    G.st_predict_ms = ms;
+  if (cudaEventElapsedTime(&ms, G.ev_t1, G.ev_t2) == cudaSuccess) G.st_force_ms = ms;
+}
+
+/* ===================================================== Part 1: g6 ABI === */
+
+int g6_open_(int *id) {
+  int dev = id ? *id : 0;
+  if (G.is_open) return 0;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    seterr("no CUDA device found");
+    return G6_ERR_DEVICE;
+  }
+  if (dev < 0 || dev >= ndev) {
+    seterr("cluster id %d: no such CUDA device (have %d)", dev, ndev);
+    return G6_ERR_DEVICE;
+  }
+  memset(&G, 0, sizeof(G));
+  G.device = dev;
+  CK(cudaSetDevice(dev));
+  CK(cudaStreamCreateWithFlags(&G.st, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&G.ev_done, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&G.ev_upd, cudaEventDisableTiming));
+  CK(cudaEventCreate(&G.ev_t0));
+  CK(cudaEventCreate(&G.ev_t1));
+  CK(cudaEventCreate(&G.ev_t2));
+  G.npipes = G6_DEFAULT_NPIPES;
+  const char *e = getenv("G6_NPIPES");
+  if (e && atoi(e) > 0 && atoi(e) <= (1 << 20)) G.npipes = atoi(e);
+  G.prec = G6_PREC_SPLIT;
+  e = getenv("G6_PRECISION");
+  if (e && (!strcmp(e, "fp64") || !strcmp(e, "FP64"))) G.prec = G6_PREC_FP64;
+  G.is_open = 1;
+  int rc = grow_j(G6_DEFAULT_CAP);
+  if (rc == 0) rc = ensure_io(G.npipes < 4096 ? G.npipes : 4096);
+  if (rc) {
+    G.is_open = 0;
+    return rc;
+  }
+  return 0;
+}
+
+int g6_close_(int *id) {
+  (void)id;
+  if (!G.is_open) return 0;
+  cudaStreamSynchronize(G.st);
+  free_jstate(&G.js);
+  if (G.h_upd) cudaFreeHost(G.h_upd);
+  if (G.h_in) cudaFreeHost(G.h_in);
+  if (G.h_out) cudaFreeHost(G.h_out);
+  cudaFree(G.d_upd); cudaFree(G.d_in); cudaFree(G.d_out); cudaFree(G.d_scratch);
+  cudaFree(G.d_ilist); cudaFree(G.d_ni); cudaFree(G.d_tnext); cudaFree(G.d_sched);
+  cudaFree(G.d_esum); cudaFree(G.d_racc); cudaFree(G.d_rjerk); cudaFree(G.d_rpot);
+  cudaFree(G.d_rnn);
+  cudaEventDestroy(G.ev_done); cudaEventDestroy(G.ev_upd);
+  cudaEventDestroy(G.ev_t0); cudaEventDestroy(G.ev_t1); cudaEventDestroy(G.ev_t2);
+  cudaStreamDestroy(G.st);
+  free(G.slot_id);
+  free(G.stage_pos);
+  free(G.pending_ids);
+  idmap_free(&G.ids);
+  memset(&G, 0, sizeof(G));
+  ilist_identity_n = 0;
+  return 0;
+}
+
+int g6_npipes_(void) { return G.is_open ? G.npipes : G6_DEFAULT_NPIPES; }
+int g6_set_tunit_(double *t) { (void)t; return 0; }
+int g6_set_xunit_(double *x) { (void)x; return 0; }
+
+int g6_set_ti_(int *id, double *ti) {
+  (void)id;
+  int rc = check_open();
+  if (rc) return rc;
+  G.ti = *ti;
+  return 0;
+}
+
+int g6_set_j_particle_(int *cluster_id, int *address, int *index, double *tj, double *dtj,
+                       double *mass, double k18[3], double j6[3], double a2[3], double v[3],
+                       double x[3]) {
+  (void)cluster_id;
+  (void)k18;
+  int rc = check_open();
+  if (rc) return rc;
+  const int addr = *address;
+  if (addr < 0) {
+    seterr("g6_set_j_particle: negative address %d", addr);
+    return G6_ERR_ARG;
+  }
+  if (addr >= G.js.cap) {
+    rc = grow_j(addr + 1);
+    if (rc) return rc;
+  }
+  if (G.upd_inflight) {
+    /* The previous staging buffer may still be in flight. */
+    cudaEventSynchronize(G.ev_upd);
+    G.upd_inflight = 0;
+  }
+  int pos = G.stage_pos[addr];
+  if (pos < 0) {
+    if (G.n_upd == G.cap_upd) {
+      int c = G.cap_upd ? 2 * G.cap_upd : 4096;
+      g6_jupd *nb = (g6_jupd *)pin_alloc(sizeof(g6_jupd) * (size_t)c);
+      if (!nb) {
+        seterr("cannot allocate pinned staging (%d records)", c);
+        return G6_ERR_NOMEM;
+      }
+      if (G.h_upd) {
+        memcpy(nb, G.h_upd, sizeof(g6_jupd) * (size_t)G.n_upd);
+        cudaFreeHost(G.h_upd);
+      }
+      G.h_upd = nb;
+      G.cap_upd = c;
+    }
+    pos = G.n_upd++;
+    G.stage_pos[addr] = pos;
+  }
+  g6_jupd *r = &G.h_upd[pos];
+  r->addr = addr;
+  r->id = *index;
+  r->t = *tj;
+  r->dt = *dtj;
+  r->m = *mass;
+  for (int k = 0; k < 3; k++) {
+    r->x[k] = x[k];
+    r->v[k] = v[k];
+    r->a[k] = a2[k] * 2.0;
+    r->j[k] = j6[k] * 6.0;
+  }
+  if (G.slot_id[addr] != *index) {
+    if (G.slot_id[addr] >= 0 && idmap_get(&G.ids, G.slot_id[addr]) == addr)
+      idmap_put(&G.ids, G.slot_id[addr], -2 - addr); /* tombstone: not found */
+    G.slot_id[addr] = *index;
+    if (idmap_put(&G.ids, *index, addr)) {
+      seterr("id map allocation failed");
+      return G6_ERR_NOMEM;
+    }
+  }
+  return 0;
+}
+
+/* Common body of the explicit-i force call with host arrays. */
+static int start_force_host(int nj, int ni, const int *index, const double *xi,
+                            const double *vi, const int *self_slot, double eps2,
+                            const double *h2) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (G.pending) {
+    cudaEventSynchronize(G.ev_done);
+    G.pending = 0;
+  }
+  if (nj < 0 || ni < 0) {
+    seterr("negative nj/ni");
+    return G6_ERR_ARG;
+  }
+  if (ni == 0) {
+    G.pending = 1;
+    G.pending_ni = 0;
+    return 0;
+  }
+  if (nj == 0) {
+    seterr("nj = 0");
+    return G6_ERR_ARG;
+  }
+  rc = ensure_io(ni);
+  if (rc) return rc;
+  rc = flush_updates();
+  if (rc) return rc;
+  rc = predict_if_needed(nj);
+  if (rc) return rc;
+  memcpy(IN_POS(G.h_in), xi, sizeof(double) * 3 * (size_t)ni);
+  memcpy(IN_VEL(G.h_in), vi, sizeof(double) * 3 * (size_t)ni);
+  if (h2)
+    memcpy(IN_H2(G.h_in), h2, sizeof(double) * (size_t)ni);
+  else
+    for (int i = 0; i < ni; i++) IN_H2(G.h_in)[i] = 0.0;
+  G.pending_nj = nj;
+  int *hs = IN_SELF(G.h_in);
+  if (self_slot) {
+    memcpy(hs, self_slot, sizeof(int) * (size_t)ni);
+  } else {
+    for (int i = 0; i < ni; i++) {
+      int s = idmap_get(&G.ids, index[i]);
+      hs[i] = (s >= 0 && s < nj) ? s : -1;
+    }
+  }
+  /* Three copies of the live prefix of each section. */
+  CK(cudaMemcpyAsync(IN_POS(G.d_in), IN_POS(G.h_in), sizeof(double) * 3 * (size_t)ni,
+                     cudaMemcpyHostToDevice, G.st));
+  CK(cudaMemcpyAsync(IN_VEL(G.d_in), IN_VEL(G.h_in), sizeof(double) * 3 * (size_t)ni,
+                     cudaMemcpyHostToDevice, G.st));
+  CK(cudaMemcpyAsync(IN_SELF(G.d_in), hs, sizeof(int) * (size_t)ni, cudaMemcpyHostToDevice,
+                     G.st));
+  g6_force_args a;
+  memset(&a, 0, sizeof(a));
+  a.ni = ni;
+  a.nj = nj;
+  a.prec = G.prec;
+  a.eps2 = eps2;
+  a.ipos = IN_POS(G.d_in);
+  a.ivel = IN_VEL(G.d_in);
+  a.iself = IN_SELF(G.d_in);
+  a.ti = G.ti;
+  a.acc = OUT_ACC(G.d_out);
+  a.jerk = OUT_JERK(G.d_out);
+  a.pot = OUT_POT(G.d_out);
+  a.nn = OUT_NN(G.d_out);
+  a.nn_r2 = OUT_NNR2(G.d_out);
+  rc = run_force(&a);
+  if (rc) return rc;
+  /* Error word + live prefix of each output section. */
+  CK(cudaMemcpyAsync(G.h_out, G.d_out, 16, cudaMemcpyDeviceToHost, G.st));
+  CK(cudaMemcpyAsync(OUT_ACC(G.h_out), OUT_ACC(G.d_out), sizeof(double) * 3 * (size_t)ni,
+                     cudaMemcpyDeviceToHost, G.st));
+  CK(cudaMemcpyAsync(OUT_JERK(G.h_out), OUT_JERK(G.d_out), sizeof(double) * 3 * (size_t)ni,
+                     cudaMemcpyDeviceToHost, G.st));
+  CK(cudaMemcpyAsync(OUT_POT(G.h_out), OUT_POT(G.d_out), sizeof(double) * (size_t)ni,
+                     cudaMemcpyDeviceToHost, G.st));
+  CK(cudaMemcpyAsync(OUT_NN(G.h_out), OUT_NN(G.d_out), sizeof(int) * (size_t)ni,
+                     cudaMemcpyDeviceToHost, G.st));
+  CK(cudaMemcpyAsync(OUT_NNR2(G.h_out), OUT_NNR2(G.d_out), sizeof(float) * (size_t)ni,
+                     cudaMemcpyDeviceToHost, G.st));
+  CK(cudaEventRecord(G.ev_done, G.st));
+  G.pending = 1;
+  G.pending_ni = ni;
+  if (index && ni <= G.pending_cap) memcpy(G.pending_ids, index, sizeof(int) * (size_t)ni);
+  return 0;
+}
+
+static int finish_force(int ni) {
+  if (!G.pending) {
+    seterr("lasthalf without firsthalf");
+    return G6_ERR_STATE;
+  }
+  if (ni != G.pending_ni) {
+    seterr("lasthalf ni=%d differs from firsthalf ni=%d", ni, G.pending_ni);
+    return G6_ERR_ARG;
+  }
+  cudaError_t e = cudaEventSynchronize(G.ev_done);
+  G.pending = 0;
+  if (e != cudaSuccess) {
+    seterr("force call failed: %s", cudaGetErrorString(e));
+    return G6_ERR_CUDA;
+  }
+  collect_timing();
+  if (ni > 0 && OUT_ERR(G.h_out)[0] != 0) {
+    seterr("force kernel reported error word 0x%x", OUT_ERR(G.h_out)[0]);
+    cudaMemsetAsync(G.d_err, 0, sizeof(int), G.st);
+    return G6_ERR_KERNEL;
+  }
+  return 0;
+}
+
+static int firsthalf_rc;
+
+void g6calc_firsthalf_(int *cluster_id, int *nj, int *ni, int index[], double xi[][3],
+                       double vi[][3], double aold[][3], double j6old[][3], double phiold[],
+                       double *eps2, double h2[]) {
+  (void)cluster_id;
+  (void)aold;
+  (void)j6old;
+  (void)phiold;
+  if (G.is_open && *ni > G.npipes) {
+    seterr("g6calc_firsthalf: ni=%d > npipes=%d", *ni, G.npipes);
+    firsthalf_rc = G6_ERR_ARG;
+    return;
+  }
+  firsthalf_rc = start_force_host(*nj, *ni, index, &xi[0][0], &vi[0][0], NULL, *eps2, h2);
+}
+
+int g6calc_lasthalf_(int *cluster_id, int *nj, int *ni, int index[], double xi[][3],
+                     double vi[][3], double *eps2, double h2[], double acc[][3],
+                     double jerk[][3], double pot[]) {
+  (void)cluster_id; (void)nj; (void)index; (void)xi; (void)vi; (void)eps2; (void)h2;
+  if (firsthalf_rc) {
+    int rc = firsthalf_rc;
+    firsthalf_rc = 0;
+    return rc;
+  }
+  int rc = finish_force(*ni);
+  if (rc) return rc;
+  const int n = *ni;
+  memcpy(&acc[0][0], OUT_ACC(G.h_out), sizeof(double) * 3 * (size_t)n);
+  memcpy(&jerk[0][0], OUT_JERK(G.h_out), sizeof(double) * 3 * (size_t)n);
+  memcpy(pot, OUT_POT(G.h_out), sizeof(double) * (size_t)n);
+  return 0;
+}
+
+int g6calc_lasthalf2_(int *cluster_id, int *nj, int *ni, int index[], double xi[][3],
+                      double vi[][3], double *eps2, double h2[], double acc[][3],
+                      double jerk[][3], double pot[], int *inn) {
+  int rc = g6calc_lasthalf_(cluster_id, nj, ni, index, xi, vi, eps2, h2, acc, jerk, pot);
+  if (rc) return rc;
+  const int *nn = OUT_NN(G.h_out);
+  for (int i = 0; i < *ni; i++) inn[i] = nn[i] >= 0 ? G.slot_id[nn[i]] : -1;
+  return 0;
+}
+
+int g6_initialize_jp_buffer_(int *cluster_id, int *buf_size) {
+  (void)cluster_id;
+  (void)buf_size;
+  return 0;
+}
+int g6_flush_jp_buffer_(int *cluster_id) { (void)cluster_id; return 0; }
+int g6_reset_(int *cluster_id) { (void)cluster_id; return 0; }
+int g6_reset_fofpga_(int *cluster_id) { (void)cluster_id; return 0; }
+
+/* ---- neighbour lists (sapporo.cpp:234-272) ---- */
+/* Computed on demand from the i-particles of the last g6calc call: a
+   separate pass over the predicted j records (r^2 <= h2[i], self
+   excluded), so the force kernel carries no list logic. */
+static int *h_ngb, *d_ngb;
+static int ngb_cap, ngb_ni, ngb_valid;
+
+int g6_read_neighbour_list_(int *cluster_id) {
+  (void)cluster_id;
+  int rc = check_open();
+  if (rc) return rc;
+  if (G.pending) {
+    seterr("g6_read_neighbour_list before g6calc_lasthalf");
+    return G6_ERR_STATE;
+  }
+  const int ni = G.pending_ni;
+  if (ni <= 0) return 0;
+  const size_t per = (size_t)(G6_NGB_MAX + 1);
+  if (ni > ngb_cap) {
+    if (h_ngb) cudaFreeHost(h_ngb);
+    cudaFree(d_ngb);
+    h_ngb = (int *)pin_alloc(sizeof(int) * per * (size_t)ni);
+    if (!h_ngb || cudaMalloc((void **)&d_ngb, sizeof(int) * per * (size_t)ni) != cudaSuccess) {
+      ngb_cap = 0;
+      seterr("cannot allocate neighbour lists");
+      return G6_ERR_NOMEM;
+    }
+    ngb_cap = ni;
+  }
+  CK(cudaMemcpyAsync(IN_H2(G.d_in), IN_H2(G.h_in), sizeof(double) * (size_t)ni,
+                     cudaMemcpyHostToDevice, G.st));
+  if (g6k_neighbours(&G.js, G.pending_nj, ni, G.prec, IN_POS(G.d_in), IN_H2(G.d_in),
+                     IN_SELF(G.d_in), d_ngb, G6_NGB_MAX, G.st)) {
+    seterr("neighbour kernel launch failed");
+    return G6_ERR_CUDA;
+  }
+  CK(cudaMemcpyAsync(h_ngb, d_ngb, sizeof(int) * per * (size_t)ni, cudaMemcpyDeviceToHost, G.st));
+  CK(cudaStreamSynchronize(G.st));
+  ngb_ni = ni;
+  ngb_valid = 1;
+  int overflow = 0;
+  for (int i = 0; i < ni; i++)
+    if (h_ngb[per * i] > G6_NGB_MAX) overflow = 1;
+  return overflow;
+}
+
+static int cmp_int(const void *a, const void *b) {
+  int x = *(const int *)a, y = *(const int *)b;
+  return (x > y) - (x < y);
+}
+
+int g6_get_neighbour_list_(int *cluster_id, int *ipipe, int *maxlength, int *n_neighbours,
+                           int neighbour_list[]) {
+  (void)cluster_id;
+  if (!ngb_valid) {
+    seterr("g6_get_neighbour_list before g6_read_neighbour_list");
+    return G6_ERR_STATE;
+  }
+  if (*ipipe < 0 || *ipipe >= ngb_ni) {
+    seterr("g6_get_neighbour_list: ipipe=%d out of range [0,%d)", *ipipe, ngb_ni);
+    return G6_ERR_ARG;
+  }
+  const int *row = h_ngb + (size_t)(G6_NGB_MAX + 1) * (size_t)(*ipipe);
+  int len = row[0];
+  int overflow = len > G6_NGB_MAX;
+  if (len > G6_NGB_MAX) len = G6_NGB_MAX;
+  int n = len < *maxlength ? len : *maxlength;
+  if (len > *maxlength) overflow = 1;
+  memcpy(neighbour_list, row + 1, sizeof(int) * (size_t)(n > 0 ? n : 0));
+  qsort(neighbour_list, (size_t)(n > 0 ? n : 0), sizeof(int), cmp_int);
+  *n_neighbours = n;
+  return overflow;
+}
+
+/* ================================================ Part 2: by-value ===== */
+#define WEAK __attribute__((weak))
+WEAK int g6_open(int id) { return g6_open_(&id); }
+WEAK int g6_close(int id) { return g6_close_(&id); }
+WEAK int g6_npipes(void) { return g6_npipes_(); }
+WEAK int g6_set_tunit(double t) { return g6_set_tunit_(&t); }
+WEAK int g6_set_xunit(double x) { return g6_set_xunit_(&x); }
+WEAK int g6_set_ti(int id, double ti) { return g6_set_ti_(&id, &ti); }
+WEAK int g6_set_j_particle(int cluster_id, int address, int index, double tj, double dtj,
+                           double mass, double k18[3], double j6[3], double a2[3], double v[3],
+                           double x[3]) {
+  return g6_set_j_particle_(&cluster_id, &address, &index, &tj, &dtj, &mass, k18, j6, a2, v, x);
+}
+WEAK void g6calc_firsthalf(int cluster_id, int nj, int ni, int index[], double xi[][3],
+                           double vi[][3], double aold[][3], double j6old[][3], double phiold[],
+                           double eps2, double h2[]) {
+  g6calc_firsthalf_(&cluster_id, &nj, &ni, index, xi, vi, aold, j6old, phiold, &eps2, h2);
+}
+WEAK int g6calc_lasthalf(int cluster_id, int nj, int ni, int index[], double xi[][3],
+                         double vi[][3], double eps2, double h2[], double acc[][3],
+                         double jerk[][3], double pot[]) {
+  return g6calc_lasthalf_(&cluster_id, &nj, &ni, index, xi, vi, &eps2, h2, acc, jerk, pot);
+}
+WEAK int g6calc_lasthalf2(int cluster_id, int nj, int ni, int index[], double xi[][3],
+                          double vi[][3], double eps2, double h2[], double acc[][3],
+                          double jerk[][3], double pot[], int inn[]) {
+  return g6calc_lasthalf2_(&cluster_id, &nj, &ni, index, xi, vi, &eps2, h2, acc, jerk, pot, inn);
+}
+WEAK int g6_initialize_jp_buffer(int cluster_id, int buf_size) {
+  return g6_initialize_jp_buffer_(&cluster_id, &buf_size);
+}
+WEAK int g6_flush_jp_buffer(int cluster_id) { return g6_flush_jp_buffer_(&cluster_id); }
+WEAK int g6_reset(int cluster_id) { return g6_reset_(&cluster_id); }
+WEAK int g6_reset_fofpga(int cluster_id) { return g6_reset_fofpga_(&cluster_id); }
+WEAK int g6_read_neighbour_list(int cluster_id) { return g6_read_neighbour_list_(&cluster_id); }
+WEAK int g6_get_neighbour_list(int cluster_id, int ipipe, int maxlength, int *n_neighbours,
+                               int neighbour_list[]) {
+  return g6_get_neighbour_list_(&cluster_id, &ipipe, &maxlength, n_neighbours, neighbour_list);
+}
+
+/* ============================================== Part 3: extension ====== */
+
+int g6x_set_precision(int prec) {
+  if (prec != G6X_SPLIT && prec != G6X_FP64) return G6_ERR_ARG;
+  G.prec = prec;
+  return 0;
+}
+int g6x_get_precision(void) { return G.prec; }
+int g6x_set_npipes(int npipes) {
+  if (npipes < 1 || npipes > (1 << 20)) return G6_ERR_ARG;
+  G.npipes = npipes;
+  return 0;
+}
+const char *g6x_last_error(void) { return G.err; }
+void *g6x_stream(void) { return (void *)G.st; }
+int g6x_timing(int on) {
+  G.timing = on ? 1 : 0;
+  return 0;
+}
+int g6x_stats(double out[8]) {
+  out[0] = G.st_predict_ms;
+  out[1] = G.st_force_ms;
+  out[2] = G.st_pairs;
+  out[3] = G.shape.jl;
+  out[4] = G.shape.nsplit;
+  out[5] = G.shape.grid_x;
+  out[6] = G.st_pred_bytes;
+  out[7] = G.st_nj;
+  return 0;
+}
+
+int g6x_load(int n, const int *ids, const double *mass, const double (*x)[3],
+             const double (*v)[3], const double (*acc)[3], const double (*jerk)[3],
+             const double *t, const double *dt) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (n <= 0) return G6_ERR_ARG;
+  rc = grow_j((n + G6_TILE - 1) / G6_TILE * G6_TILE);
+  if (rc) return rc;
+  /* Staged updates for these slots are superseded. */
+  if (G.upd_inflight) {
+    cudaEventSynchronize(G.ev_upd);
+    G.upd_inflight = 0;
+  }
+  for (int u = 0; u < G.n_upd; u++) G.stage_pos[G.h_upd[u].addr] = -1;
+  G.n_upd = 0;
+  const size_t nd = sizeof(double) * (size_t)n;
+  const int cap = G.js.cap;
+  double *tmp = (double *)malloc(nd);
+  if (!tmp) return G6_ERR_NOMEM;
+  CK(cudaMemcpy(G.js.m, mass, nd, cudaMemcpyHostToDevice));
+  if (t) {
+    CK(cudaMemcpy(G.js.t, t, nd, cudaMemcpyHostToDevice));
+  } else {
+    CK(cudaMemset(G.js.t, 0, nd));
+  }
+  if (dt) {
+    CK(cudaMemcpy(G.js.dt, dt, nd, cudaMemcpyHostToDevice));
+  } else {
+    CK(cudaMemset(G.js.dt, 0, nd));
+  }
+  const double(*src[4])[3] = {x, v, acc, jerk};
+  double *dst[4] = {G.js.x, G.js.v, G.js.a, G.js.j};
+  for (int q = 0; q < 4; q++) {
+    for (int k = 0; k < 3; k++) {
+      for (int s = 0; s < n; s++) tmp[s] = src[q] ? src[q][s][k] : 0.0;
+      CK(cudaMemcpy(dst[q] + (size_t)k * cap, tmp, nd, cudaMemcpyHostToDevice));
+    }
+  }
+  free(tmp);
+  idmap_free(&G.ids);
+  for (int s = 0; s < n; s++) {
+    G.slot_id[s] = ids ? ids[s] : s;
+    if (idmap_put(&G.ids, G.slot_id[s], s)) return G6_ERR_NOMEM;
+  }
+  CK(cudaMemcpy(G.js.id, G.slot_id, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
+  G.pred_valid = 0;
+  G.run_n = n;
+  G.run_t = 0;
+  return 0;
+}
+
+int g6x_read(int n, double (*x)[3], double (*v)[3], double (*acc)[3], double (*jerk)[3],
+             double *pot, double *t, double *dt, int *nn) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (n <= 0 || n > G.js.cap) return G6_ERR_ARG;
+  CK(cudaStreamSynchronize(G.st));
+  const size_t nd = sizeof(double) * (size_t)n;
+  const int cap = G.js.cap;
+  if (pot) CK(cudaMemcpy(pot, G.js.pot, nd, cudaMemcpyDeviceToHost));
+  if (t) CK(cudaMemcpy(t, G.js.t, nd, cudaMemcpyDeviceToHost));
+  if (dt) CK(cudaMemcpy(dt, G.js.dt, nd, cudaMemcpyDeviceToHost));
+  if (nn) CK(cudaMemcpy(nn, G.js.nn, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+  double(*dst[4])[3] = {x, v, acc, jerk};
+  const double *src[4] = {G.js.x, G.js.v, G.js.a, G.js.j};
+  double *tmp = (double *)malloc(nd);
+  if (!tmp) return G6_ERR_NOMEM;
+  for (int q = 0; q < 4; q++) {
+    if (!dst[q]) continue;
+    for (int k = 0; k < 3; k++) {
+      CK(cudaMemcpy(tmp, src[q] + (size_t)k * cap, nd, cudaMemcpyDeviceToHost));
+      for (int s = 0; s < n; s++) dst[q][s][k] = tmp[s];
+    }
+  }
+  free(tmp);
+  return 0;
+}
+
+int g6x_force(double ti, double eps2, int nj, int ni, const double (*xi)[3],
+              const double (*vi)[3], const int *self_slot, double (*acc)[3],
+              double (*jerk)[3], double *pot, int *nn, float *nn_r2) {
+  int rc = check_open();
+  if (rc) return rc;
+  G.ti = ti;
+  int *self = NULL;
+  if (!self_slot) {
+    /* explicit points: nothing excluded */
+    self = (int *)malloc(sizeof(int) * (size_t)(ni > 0 ? ni : 1));
+    if (!self) return G6_ERR_NOMEM;
+    for (int i = 0; i < ni; i++) self[i] = -1;
+  }
+  rc = start_force_host(nj, ni, NULL, &xi[0][0], &vi[0][0], self_slot ? self_slot : self, eps2,
+                        NULL);
+  free(self);
+  if (rc) return rc;
+  rc = finish_force(ni);
+  if (rc) return rc;
+  if (acc) memcpy(&acc[0][0], OUT_ACC(G.h_out), sizeof(double) * 3 * (size_t)ni);
+  if (jerk) memcpy(&jerk[0][0], OUT_JERK(G.h_out), sizeof(double) * 3 * (size_t)ni);
+  if (pot) memcpy(pot, OUT_POT(G.h_out), sizeof(double) * (size_t)ni);
+  if (nn) memcpy(nn, OUT_NN(G.h_out), sizeof(int) * (size_t)ni);
+  if (nn_r2) memcpy(nn_r2, OUT_NNR2(G.h_out), sizeof(float) * (size_t)ni);
+  return 0;
+}
+
+static int read_err_word(void) {
+  int herr = 0;
+  if (G.d_err && cudaMemcpy(&herr, G.d_err, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess &&
+      herr) {
+    seterr("force kernel reported error word 0x%x", herr);
+    cudaMemset(G.d_err, 0, sizeof(int));
+    return G6_ERR_KERNEL;
+  }
+  return 0;
+}
+
+int g6x_force_dev(double ti, double eps2, int nj, int ni, const double *d_xi,
+                  const double *d_vi, const int *d_self_slot, double *d_acc, double *d_jerk,
+                  double *d_pot, int *d_nn, float *d_nn_r2, int sync) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (ni <= 0 || nj <= 0) return ni == 0 ? 0 : G6_ERR_ARG;
+  G.ti = ti;
+  rc = ensure_io(1);
+  if (rc) return rc;
+  rc = flush_updates();
+  if (rc) return rc;
+  rc = predict_if_needed(nj);
+  if (rc) return rc;
+  g6_force_args a;
+  memset(&a, 0, sizeof(a));
+  a.ni = ni;
+  a.nj = nj;
+  a.prec = G.prec;
+  a.eps2 = eps2;
+  a.ipos = d_xi;
+  a.ivel = d_vi;
+  a.iself = d_self_slot;
+  a.ti = ti;
+  a.acc = d_acc;
+  a.jerk = d_jerk;
+  a.pot = d_pot;
+  a.nn = d_nn;
+  a.nn_r2 = d_nn_r2;
+  rc = run_force(&a);
+  if (rc) return rc;
+  if (sync) {
+    CK(cudaStreamSynchronize(G.st));
+    collect_timing();
+    return read_err_word();
+  }
+  return 0;
+}
+
+int g6x_force_slots(double ti, double eps2, int nj, int ni, const int *d_ilist, double *d_acc,
+                    double *d_jerk, double *d_pot, int *d_nn, int sync) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (ni <= 0 || nj <= 0) return ni == 0 ? 0 : G6_ERR_ARG;
+  G.ti = ti;
+  rc = ensure_io(1);
+  if (rc) return rc;
+  rc = flush_updates();
+  if (rc) return rc;
+  rc = predict_if_needed(nj);
+  if (rc) return rc;
+  g6_force_args a;
+  memset(&a, 0, sizeof(a));
+  a.ni = ni;
+  a.nj = nj;
+  a.prec = G.prec;
+  a.eps2 = eps2;
+  a.ilist = d_ilist;
+  a.ti = ti;
+  a.acc = d_acc;
+  a.jerk = d_jerk;
+  a.pot = d_pot;
+  a.nn = d_nn;
+  rc = run_force(&a);
+  if (rc) return rc;
+  if (sync) {
+    CK(cudaStreamSynchronize(G.st));
+    collect_timing();
+    return read_err_word();
+  }
+  return 0;
+}
+
+/* ---- device-resident block-step driver ---- */
+
+static int ensure_run_buffers(int n) {
+  if (n <= G.run_cap) return 0;
+  cudaFree(G.d_ilist); cudaFree(G.d_ni); cudaFree(G.d_tnext); cudaFree(G.d_sched);
+  cudaFree(G.d_esum); cudaFree(G.d_racc); cudaFree(G.d_rjerk); cudaFree(G.d_rpot);
+  cudaFree(G.d_rnn);
+  G.run_cap = 0;
+  ilist_identity_n = 0;
+  size_t nd = sizeof(double) * (size_t)n;
+  int ok = cudaMalloc((void **)&G.d_ilist, sizeof(int) * (size_t)n) == cudaSuccess &&
+           cudaMalloc((void **)&G.d_ni, sizeof(int) * 2) == cudaSuccess &&
+           cudaMalloc((void **)&G.d_tnext, sizeof(double) * 2) == cudaSuccess &&
+           cudaMalloc((void **)&G.d_sched, sizeof(double) * 4) == cudaSuccess &&
+           cudaMalloc((void **)&G.d_esum, sizeof(double) * (size_t)(4 + 2 * (n / 256 + 2))) ==
+               cudaSuccess &&
+           cudaMalloc((void **)&G.d_racc, 3 * nd) == cudaSuccess &&
+           cudaMalloc((void **)&G.d_rjerk, 3 * nd) == cudaSuccess &&
+           cudaMalloc((void **)&G.d_rpot, nd) == cudaSuccess &&
+           cudaMalloc((void **)&G.d_rnn, sizeof(int) * (size_t)n) == cudaSuccess;
+  if (!ok) {
+    seterr("cannot allocate run buffers");
+    return G6_ERR_NOMEM;
+  }
+  G.run_cap = n;
+  return 0;
+}
+
+static int identity_list(int n) {
+  if (ilist_identity_n == n) return 0;
+  int *h = (int *)malloc(sizeof(int) * (size_t)n);
+  if (!h) return G6_ERR_NOMEM;
+  for (int s = 0; s < n; s++) h[s] = s;
+  cudaError_t e = cudaMemcpy(G.d_ilist, h, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
+  free(h);
+  ilist_identity_n = e == cudaSuccess ? n : 0;
+  return e == cudaSuccess ? 0 : G6_ERR_CUDA;
+}
+
+static int cmp_dbl(const void *a, const void *b) {
+  double x = *(const double *)a, y = *(const double *)b;
+  return (x > y) - (x < y);
+}
+
+int g6x_run_init(double eps2, double eta) {
+  int rc = check_open();
+  if (rc) return rc;
+  const int n = G.run_n;
+  if (n <= 0) return G6_ERR_STATE;
+  rc = ensure_run_buffers(n);
+  if (rc) return rc;
+  rc = identity_list(n);
+  if (rc) return rc;
+  G.run_eps2 = eps2;
+  G.run_eta = eta;
+  G.run_t = 0;
+  /* idata::setup: forces on all at t = 0 (commit_particles). */
+  rc = g6x_force_slots(0.0, eps2, n, n, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot, G.d_rnn, 0);
+  if (rc) return rc;
+  if (g6k_store_forces(&G.js, n, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot, G.d_rnn, G.st))
+    return G6_ERR_CUDA;
+  /* force_initial_timestep(0.0625, 0.03125, 8.0) (interface.cc:29-31). */
+  if (g6k_initial_step(&G.js, n, eta, 0.0625, 0.03125, 0.0, G.st)) return G6_ERR_CUDA;
+  double *h = (double *)malloc(sizeof(double) * (size_t)n);
+  if (!h) return G6_ERR_NOMEM;
+  CK(cudaMemcpyAsync(h, G.js.dt, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, G.st));
+  CK(cudaStreamSynchronize(G.st));
+  qsort(h, (size_t)n, sizeof(double), cmp_dbl);
+  const double dtmax = 8.0 * h[n / 2];
+  free(h);
+  if (g6k_clamp_steps(&G.js, n, dtmax, G.st)) return G6_ERR_CUDA;
+  G.pred_valid = 0;
+  CK(cudaStreamSynchronize(G.st));
+  return read_err_word();
+}
+
+int g6x_run(double t_end, long long *blocks, double *particle_steps) {
+  int rc = check_open();
+  if (rc) return rc;
+  const int n = G.run_n;
+  if (n <= 0 || G.run_cap < n) return G6_ERR_STATE;
+  long long nb = 0;
+  double ns = 0;
+  int hbuf[2];
+  double tn;
+  while (G.run_t < t_end) {
+    ilist_identity_n = 0;
+    if (g6k_schedule(&G.js, n, G.d_ilist, G.d_ni, G.d_tnext, G.d_sched, 4, G.st))
+      return G6_ERR_CUDA;
+    CK(cudaMemcpyAsync(hbuf, G.d_ni, sizeof(int), cudaMemcpyDeviceToHost, G.st));
+    CK(cudaMemcpyAsync(&tn, G.d_tnext, sizeof(double), cudaMemcpyDeviceToHost, G.st));
+    CK(cudaStreamSynchronize(G.st));
+    const int ni = hbuf[0];
+    if (ni <= 0 || ni > n || !(tn > G.run_t)) {
+      seterr("scheduler produced ni=%d tnext=%.17g at t=%.17g", ni, tn, G.run_t);
+      return G6_ERR_STATE;
+    }
+    rc = g6x_force_slots(tn, G.run_eps2, n, ni, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot,
+                         G.d_rnn, 0);
+    if (rc) return rc;
+    if (g6k_correct(&G.js, ni, G.d_ilist, tn, G.run_eta, G.d_racc, G.d_rjerk, G.d_rpot,
+                    G.d_rnn, G.st))
+      return G6_ERR_CUDA;
+    G.pred_valid = 0; /* j-state changed */
+    G.run_t = tn;
+    nb++;
+    ns += ni;
+  }
+  CK(cudaStreamSynchronize(G.st));
+  if (blocks) *blocks = nb;
+  if (particle_steps) *particle_steps = ns;
+  return read_err_word();
+}
+
+int g6x_correct(int ni, const int *slots, double tnext, double eta, const double (*acc)[3],
+                const double (*jerk)[3]) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (ni <= 0) return 0;
+  if (ni > G.js.cap) return G6_ERR_ARG;
+  for (int i = 0; i < ni; i++)
+    if (slots[i] < 0 || slots[i] >= G.js.cap) {
+      seterr("g6x_correct: slot %d out of range", slots[i]);
+      return G6_ERR_ARG;
+    }
+  rc = ensure_run_buffers(ni > G.run_n ? ni : (G.run_n > 0 ? G.run_n : ni));
+  if (rc) return rc;
+  ilist_identity_n = 0;
+  CK(cudaMemcpyAsync(G.d_ilist, slots, sizeof(int) * (size_t)ni, cudaMemcpyHostToDevice, G.st));
+  CK(cudaMemcpyAsync(G.d_racc, acc, sizeof(double) * 3 * (size_t)ni, cudaMemcpyHostToDevice,
+                     G.st));
+  CK(cudaMemcpyAsync(G.d_rjerk, jerk, sizeof(double) * 3 * (size_t)ni, cudaMemcpyHostToDevice,
+                     G.st));
+  if (g6k_correct(&G.js, ni, G.d_ilist, tnext, eta, G.d_racc, G.d_rjerk, NULL, NULL, G.st))
+    return G6_ERR_CUDA;
+  G.pred_valid = 0;
+  CK(cudaStreamSynchronize(G.st));
+  return 0;
+}
+
+int g6x_step_all(double tnext) {
+  int rc = check_open();
+  if (rc) return rc;
+  const int n = G.run_n;
+  if (n <= 0 || G.run_cap < n) return G6_ERR_STATE;
+  rc = identity_list(n);
+  if (rc) return rc;
+  rc = g6x_force_slots(tnext, G.run_eps2, n, n, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot,
+                       G.d_rnn, 0);
+  if (rc) return rc;
+  if (g6k_correct(&G.js, n, G.d_ilist, tnext, G.run_eta, G.d_racc, G.d_rjerk, G.d_rpot,
+                  G.d_rnn, G.st))
+    return G6_ERR_CUDA;
+  G.pred_valid = 0;
+  G.run_t = tnext;
+  return 0;
+}
+
+double g6x_system_time(void) { return G.run_t; }
+
+int g6x_energy(double *kinetic, double *potential) {
+  int rc = check_open();
+  if (rc) return rc;
+  const int n = G.run_n;
+  if (n <= 0 || G.run_cap < n) return G6_ERR_STATE;
+  /* jdata::get_energy: pot of all particles predicted to system time. */
+  rc = identity_list(n);
+  if (rc) return rc;
+  rc = g6x_force_slots(G.run_t, G.run_eps2, n, n, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot,
+                       G.d_rnn, 0);
+  if (rc) return rc;
+  if (g6k_energy_sums(&G.js, n, G.run_t, G.d_rpot, G.d_esum, G.st)) return G6_ERR_CUDA;
+  double h[2];
+  CK(cudaMemcpyAsync(h, G.d_esum, sizeof(h), cudaMemcpyDeviceToHost, G.st));
+  CK(cudaStreamSynchronize(G.st));
+  if (kinetic) *kinetic = h[0] / 2;
+  if (potential) *potential = h[1] / 2;
+  return read_err_word();
+}

@@ -1,0 +1,787 @@
+// kern_force.cu -- the i-block Hermite force kernel (acc, jerk, pot, nearest
+// neighbour) for sm_103a, in two arithmetic policies:
+//
+//   split: positions as double-single (hi+lo float pairs), relative
+//          position formed by (xj_hi - xi_hi) + (xj_lo - xi_lo), all pair
+//          arithmetic in FP32 (one MUFU rsqrt per pair), per-tile FP32
+//          partial sums folded into compensated (TwoSum) hi/lo totals.
+//   fp64:  the same pair formula in plain FP64 (the "plain FP64 GPU"
+//          kernel; also the GPU-side oracle at N=2^20).
+//
+// The pair formula is ph4's (src/amuse_ph4/src/idata.cc:188-226):
+//   dx = xj - xi, dv = vj - vi, r2 = |dx|^2 + eps2 (+2^-52 as ph4),
+//   rinv = r2^-1/2, mr3i = m rinv^3,
+//   acc += mr3i dx, jerk += mr3i (dv - 3 (dx.dv)/r2 dx), pot -= m rinv,
+//   nn = argmin r2 over j != self (first j on ties).
+// The GRAPE-6 semantics of the g6 API excludes the i-particle itself by
+// identity (lib/sapporo_light/dev_evaluate_gravity.cu:80-84 compares ids);
+// here the host resolves id -> j slot once per call and the kernel skips
+// that slot.
+//
+// Structure (one CTA = 256 threads = 8 warps, 2 i-particles per thread):
+//   * j-tiles of 128 records are streamed HBM/L2 -> shared memory with
+//     cp.async.bulk (TMA, non-tensor) completing on an mbarrier, 4 stages.
+//   * JL j-lanes share each i-particle (JL = 1 for large i-blocks, up to
+//     128 for tiny ones); j is also split across CTAs (grid.y) so that small
+//     active blocks still fill all 152 SMs.
+//   * Lanes of one i merge with warp shuffles (plus shared memory across
+//     warps for JL > 32); CTAs of one i merge in a second pass kernel, in
+//     fixed order, with float-float (split) or FP64 adds: deterministic.
+//   * Nearest neighbour: the hot loop keeps only a running min of r2 (one
+//     FMNMX per pair); a tile in which some lane's min improved is
+//     re-scanned with bit-identical arithmetic to find the index.
+//   * A tile that holds the self slot of one of the warp's i-particles takes
+//     a checked copy of the loop (rinv = 0, r2 -> +inf for self).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "g6_dev.h"
+
+// 32-byte aligned FP64 quadruple (CUDA 13 deprecates the unaligned double4).
+struct __align__(32) G6D4 {
+  double x, y, z, w;
+};
+__host__ __device__ __forceinline__ G6D4 g6d4(double x, double y, double z, double w) {
+  G6D4 r;
+  r.x = x; r.y = y; r.z = z; r.w = w;
+  return r;
+}
+
+namespace {
+
+constexpr int NT = 256;      // threads per CTA
+constexpr int TJ = G6_TILE;  // j records per tile
+constexpr int NSTAGE = 4;    // TMA ring depth
+constexpr int IPT = 2;       // i-particles per thread
+constexpr float FAR = 1.0e18f;
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound per wait
+
+enum { ERR_TMA_TIMEOUT = 1, ERR_SHAPE = 2 };
+
+struct __align__(16) RecS {
+  float4 ph, pl, v;
+};
+struct __align__(16) RecD {
+  G6D4 p, v;
+};
+static_assert(sizeof(RecS) == 48, "split record");
+static_assert(sizeof(RecD) == 64, "fp64 record");
+
+// ---------------------------------------------------------------- PTX ---
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, uint32_t bytes,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+      "[%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false after WAIT_NS of global time.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (gtimer() - t0 > WAIT_NS) return false;
+  }
+}
+
+// ------------------------------------------------------- float-float ---
+// Knuth TwoSum folded into a (hi, lo) accumulator.
+__device__ __forceinline__ void ff_acc(float &hi, float &lo, float p) {
+  const float s = __fadd_rn(hi, p);
+  const float bb = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  hi = s;
+  lo = __fadd_rn(lo, e);
+}
+// (ah, al) += (bh, bl), renormalised.
+__device__ __forceinline__ void ff_add(float &ah, float &al, float bh, float bl) {
+  const float s = __fadd_rn(ah, bh);
+  const float bb = __fsub_rn(s, ah);
+  float e = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+  e = __fadd_rn(e, __fadd_rn(al, bl));
+  ah = __fadd_rn(s, e);
+  al = __fsub_rn(e, __fsub_rn(ah, s));
+}
+
+// ------------------------------------------------------------ policies ---
+struct SplitP {
+  using Rec = RecS;
+  using R = float;
+  struct I {
+    float xh, yh, zh, xl, yl, zl, vx, vy, vz;
+  };
+  struct Part {  // per-fold-period partial sums
+    float a[3], j[3], p;
+  };
+  struct Tot {  // compensated totals
+    float ah[3], al[3], jh[3], jl[3], ph, pl;
+  };
+  struct Out {  // partial record exchanged between CTAs, 64 B
+    float2 a[3], j[3], p;
+    float nnr2;
+    int nn;
+  };
+  __device__ static void split(double d, float &h, float &l) {
+    h = __double2float_rn(d);
+    l = __double2float_rn(d - (double)h);
+  }
+  __device__ static I load_i_explicit(const double *p, const double *v) {
+    I s;
+    split(p[0], s.xh, s.xl);
+    split(p[1], s.yh, s.yl);
+    split(p[2], s.zh, s.zl);
+    s.vx = __double2float_rn(v[0]);
+    s.vy = __double2float_rn(v[1]);
+    s.vz = __double2float_rn(v[2]);
+    return s;
+  }
+  __device__ static I load_i_rec(const Rec &r) {
+    I s;
+    s.xh = r.ph.x; s.yh = r.ph.y; s.zh = r.ph.z;
+    s.xl = r.pl.x; s.yl = r.pl.y; s.zl = r.pl.z;
+    s.vx = r.v.x; s.vy = r.v.y; s.vz = r.v.z;
+    return s;
+  }
+  __device__ static void zero(Part &q) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) q.a[k] = q.j[k] = 0.f;
+    q.p = 0.f;
+  }
+  __device__ static void zero(Tot &t) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) t.ah[k] = t.al[k] = t.jh[k] = t.jl[k] = 0.f;
+    t.ph = t.pl = 0.f;
+  }
+  __device__ static void fold(Tot &t, const Part &q) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      ff_acc(t.ah[k], t.al[k], q.a[k]);
+      ff_acc(t.jh[k], t.jl[k], q.j[k]);
+    }
+    ff_acc(t.ph, t.pl, q.p);
+  }
+  // r^2 + eps^2 for the nearest-neighbour key: must be bit-identical in the
+  // main loop and in the re-scan.
+  __device__ static __forceinline__ float r2e(const I &s, const Rec &r, float eps2,
+                                              float &dx, float &dy, float &dz) {
+    dx = __fadd_rn(__fsub_rn(r.ph.x, s.xh), __fsub_rn(r.pl.x, s.xl));
+    dy = __fadd_rn(__fsub_rn(r.ph.y, s.yh), __fsub_rn(r.pl.y, s.yl));
+    dz = __fadd_rn(__fsub_rn(r.ph.z, s.zh), __fsub_rn(r.pl.z, s.zl));
+    float r2 = __fmaf_rn(dx, dx, eps2);
+    r2 = __fmaf_rn(dy, dy, r2);
+    return __fmaf_rn(dz, dz, r2);
+  }
+  template <bool CHECK>
+  __device__ static __forceinline__ void pair(const I &s, const Rec &r, float eps2, Part &q,
+                                              float &nnmin, bool is_self) {
+    float dx, dy, dz;
+    const float r2 = r2e(s, r, eps2, dx, dy, dz);
+    float rinv = rsqrtf(r2);
+    if (CHECK) {
+      rinv = is_self ? 0.f : rinv;
+      nnmin = fminf(nnmin, is_self ? __int_as_float(0x7f800000) : r2);
+    } else {
+      nnmin = fminf(nnmin, r2);
+    }
+    const float dvx = r.v.x - s.vx, dvy = r.v.y - s.vy, dvz = r.v.z - s.vz;
+    const float rv = dx * dvx + dy * dvy + dz * dvz;
+    const float rinv2 = rinv * rinv;
+    const float mri = r.ph.w * rinv;
+    const float mr3i = mri * rinv2;
+    const float a3 = -3.0f * (rv * rinv2);
+    q.a[0] = fmaf(mr3i, dx, q.a[0]);
+    q.a[1] = fmaf(mr3i, dy, q.a[1]);
+    q.a[2] = fmaf(mr3i, dz, q.a[2]);
+    q.j[0] = fmaf(mr3i, fmaf(a3, dx, dvx), q.j[0]);
+    q.j[1] = fmaf(mr3i, fmaf(a3, dy, dvy), q.j[1]);
+    q.j[2] = fmaf(mr3i, fmaf(a3, dz, dvz), q.j[2]);
+    q.p += mri;
+  }
+  __device__ static void to_out(const Tot &t, float nnr2, int nn, Out &o) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      o.a[k] = make_float2(t.ah[k], t.al[k]);
+      o.j[k] = make_float2(t.jh[k], t.jl[k]);
+    }
+    o.p = make_float2(t.ph, t.pl);
+    o.nnr2 = nnr2;
+    o.nn = nn;
+  }
+  __device__ static void merge(Out &a, const Out &b) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      ff_add(a.a[k].x, a.a[k].y, b.a[k].x, b.a[k].y);
+      ff_add(a.j[k].x, a.j[k].y, b.j[k].x, b.j[k].y);
+    }
+    ff_add(a.p.x, a.p.y, b.p.x, b.p.y);
+    if (b.nnr2 < a.nnr2 || (b.nnr2 == a.nnr2 && b.nn < a.nn)) {
+      a.nnr2 = b.nnr2;
+      a.nn = b.nn;
+    }
+  }
+  __device__ static void write_final(const Out &o, int i, double *acc, double *jerk,
+                                     double *pot) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      acc[3 * i + k] = (double)o.a[k].x + (double)o.a[k].y;
+      jerk[3 * i + k] = (double)o.j[k].x + (double)o.j[k].y;
+    }
+    pot[i] = -((double)o.p.x + (double)o.p.y);
+  }
+};
+
+struct F64P {
+  using Rec = RecD;
+  using R = double;
+  struct I {
+    double x, y, z, vx, vy, vz;
+  };
+  struct Part {
+    double a[3], j[3], p;
+  };
+  struct Tot {
+    double a[3], j[3], p;
+  };
+  struct Out {  // 80 B
+    double a[3], j[3], p;
+    double nnr2;
+    int nn, pad;
+  };
+  __device__ static I load_i_explicit(const double *p, const double *v) {
+    I s;
+    s.x = p[0]; s.y = p[1]; s.z = p[2];
+    s.vx = v[0]; s.vy = v[1]; s.vz = v[2];
+    return s;
+  }
+  __device__ static I load_i_rec(const Rec &r) {
+    I s;
+    s.x = r.p.x; s.y = r.p.y; s.z = r.p.z;
+    s.vx = r.v.x; s.vy = r.v.y; s.vz = r.v.z;
+    return s;
+  }
+  __device__ static void zero(Part &q) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) q.a[k] = q.j[k] = 0.0;
+    q.p = 0.0;
+  }
+  __device__ static void zero(Tot &t) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) t.a[k] = t.j[k] = 0.0;
+    t.p = 0.0;
+  }
+  __device__ static void fold(Tot &t, const Part &q) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      t.a[k] += q.a[k];
+      t.j[k] += q.j[k];
+    }
+    t.p += q.p;
+  }
+  __device__ static __forceinline__ double r2e(const I &s, const Rec &r, double eps2,
+                                               double &dx, double &dy, double &dz) {
+    dx = r.p.x - s.x;
+    dy = r.p.y - s.y;
+    dz = r.p.z - s.z;
+    double r2 = __fma_rn(dx, dx, eps2);
+    r2 = __fma_rn(dy, dy, r2);
+    return __fma_rn(dz, dz, r2);
+  }
+  // 1/sqrt(x) in FP64: FP32 MUFU seed, then two Newton-Raphson steps
+  // y <- y (3 - x y^2) / 2 (quadratic convergence: 2^-22 -> 2^-44 -> 2^-88).
+  __device__ static __forceinline__ double rsqrt64(double x) {
+    double y = (double)rsqrtf((float)x);
+    const double hx = 0.5 * x;
+    y = y * __fma_rn(-hx * y, y, 1.5);
+    y = y * __fma_rn(-hx * y, y, 1.5);
+    return y;
+  }
+  template <bool CHECK>
+  __device__ static __forceinline__ void pair(const I &s, const Rec &r, double eps2, Part &q,
+                                              double &nnmin, bool is_self) {
+    double dx, dy, dz;
+    const double r2 = r2e(s, r, eps2, dx, dy, dz);
+    double rinv = rsqrt64(r2);
+    if (CHECK) {
+      rinv = is_self ? 0.0 : rinv;
+      nnmin = fmin(nnmin, is_self ? __longlong_as_double(0x7ff0000000000000ll) : r2);
+    } else {
+      nnmin = fmin(nnmin, r2);
+    }
+    const double dvx = r.v.x - s.vx, dvy = r.v.y - s.vy, dvz = r.v.z - s.vz;
+    const double rv = dx * dvx + dy * dvy + dz * dvz;
+    const double rinv2 = rinv * rinv;
+    const double mri = r.p.w * rinv;
+    const double mr3i = mri * rinv2;
+    const double a3 = -3.0 * (rv * rinv2);
+    q.a[0] = fma(mr3i, dx, q.a[0]);
+    q.a[1] = fma(mr3i, dy, q.a[1]);
+    q.a[2] = fma(mr3i, dz, q.a[2]);
+    q.j[0] = fma(mr3i, fma(a3, dx, dvx), q.j[0]);
+    q.j[1] = fma(mr3i, fma(a3, dy, dvy), q.j[1]);
+    q.j[2] = fma(mr3i, fma(a3, dz, dvz), q.j[2]);
+    q.p += mri;
+  }
+  __device__ static void to_out(const Tot &t, double nnr2, int nn, Out &o) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      o.a[k] = t.a[k];
+      o.j[k] = t.j[k];
+    }
+    o.p = t.p;
+    o.nnr2 = nnr2;
+    o.nn = nn;
+    o.pad = 0;
+  }
+  __device__ static void merge(Out &a, const Out &b) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      a.a[k] += b.a[k];
+      a.j[k] += b.j[k];
+    }
+    a.p += b.p;
+    if (b.nnr2 < a.nnr2 || (b.nnr2 == a.nnr2 && b.nn < a.nn)) {
+      a.nnr2 = b.nnr2;
+      a.nn = b.nn;
+    }
+  }
+  __device__ static void write_final(const Out &o, int i, double *acc, double *jerk,
+                                     double *pot) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      acc[3 * i + k] = o.a[k];
+      jerk[3 * i + k] = o.j[k];
+    }
+    pot[i] = -o.p;
+  }
+};
+
+// Shuffle helpers for Out (field by field).
+template <class O>
+__device__ __forceinline__ O shfl_xor_out(const O &o, int m) {
+  O r;
+  const int *src = reinterpret_cast<const int *>(&o);
+  int *dst = reinterpret_cast<int *>(&r);
+#pragma unroll
+  for (int w = 0; w < (int)(sizeof(O) / 4); w++) dst[w] = __shfl_xor_sync(0xffffffffu, src[w], m);
+  return r;
+}
+
+struct KParams {
+  int ni, nj, nsplit, jsplit;  // jsplit: j per CTA-split (multiple of TJ)
+  double eps2;
+  const double *ipos, *ivel;
+  const int *ilist, *iself;
+  const void *jrec;
+  double *acc, *jerk, *pot;
+  int *nn;
+  float *nn_r2;
+  void *part;  // [nsplit][ni_pad] Out records when nsplit > 1
+  int ni_pad;
+  int *err;
+};
+
+// Number of j per thread between compensated folds.
+constexpr int FOLD_J = 64;
+
+template <class P, int JL>
+__global__ void __launch_bounds__(NT, 2) force_kernel(KParams kp) {
+  using Rec = typename P::Rec;
+  using R = typename P::R;
+  constexpr int NIL = NT / JL;           // i-lanes per CTA
+  constexpr int ISLOTS = NIL * IPT;      // i-particles per CTA
+  constexpr int JPT = TJ / JL;           // j per thread per tile
+  constexpr int FOLD_TILES = (FOLD_J / JPT) > 0 ? (FOLD_J / JPT) : 1;
+  static_assert(JL >= 1 && JL <= TJ && (TJ % JL) == 0, "JL");
+
+  __shared__ __align__(128) Rec tiles[NSTAGE][TJ];
+  __shared__ __align__(8) uint64_t full[NSTAGE];
+
+  const int tid = threadIdx.x;
+  const int jl = tid % JL;
+  const int il = tid / JL;
+  const int lane = tid & 31;
+
+  // ---- i-particles of this thread ----
+  typename P::I I[IPT];
+  int self[IPT];
+  bool valid[IPT];
+#pragma unroll
+  for (int k = 0; k < IPT; k++) {
+    const int i = blockIdx.x * ISLOTS + k * NIL + il;
+    valid[k] = i < kp.ni;
+    const int ii = valid[k] ? i : 0;
+    if (kp.ilist) {
+      const int slot = kp.ilist[ii];
+      I[k] = P::load_i_rec(reinterpret_cast<const Rec *>(kp.jrec)[slot]);
+      self[k] = valid[k] ? (kp.iself ? kp.iself[ii] : slot) : -1;
+    } else {
+      I[k] = P::load_i_explicit(kp.ipos + 3 * ii, kp.ivel + 3 * ii);
+      self[k] = valid[k] && kp.iself ? kp.iself[ii] : -1;
+    }
+  }
+
+  // ---- j-range of this CTA ----
+  const int js = blockIdx.y * kp.jsplit;
+  int je = js + kp.jsplit;
+  const int nj_pad = (kp.nj + TJ - 1) / TJ * TJ;
+  if (je > nj_pad) je = nj_pad;
+  const int ntiles = je > js ? (je - js) / TJ : 0;
+  const Rec *gj = reinterpret_cast<const Rec *>(kp.jrec) + js;
+
+  if (tid == 0) {
+#pragma unroll
+    for (int s = 0; s < NSTAGE; s++) mbar_init(&full[s], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  int issued = 0;  // tiles issued so far (meaningful in thread 0 only)
+  if (tid == 0) {
+    for (int s = 0; s < NSTAGE && s < ntiles; s++) {
+      mbar_expect_tx(&full[s], TJ * sizeof(Rec));
+      tma_load_1d(&tiles[s][0], gj + s * TJ, TJ * sizeof(Rec), &full[s]);
+      issued = s + 1;
+    }
+  }
+
+  const R eps2 = (R)kp.eps2 + (R)(1.0 / 4503599627370496.0);  // + 2^-52 (ph4)
+  typename P::Part q[IPT];
+  typename P::Tot T[IPT];
+  R nnmin[IPT], nnbest[IPT];
+  int nnidx[IPT];
+#pragma unroll
+  for (int k = 0; k < IPT; k++) {
+    P::zero(q[k]);
+    P::zero(T[k]);
+    nnmin[k] = nnbest[k] = (R)__int_as_float(0x7f800000);
+    nnidx[k] = -1;
+  }
+
+  bool failed = false;
+  int t_fail = 0;
+  for (int t = 0; t < ntiles; t++) {
+    const int s = t % NSTAGE;
+    const bool to = !mbar_wait_bounded(&full[s], (t / NSTAGE) & 1);
+    if (__syncthreads_or(to)) {
+      failed = true;
+      t_fail = t;
+      break;
+    }
+    // Everyone has finished tile t-1: refill its stage.
+    if (tid == 0 && t >= 1 && t - 1 + NSTAGE < ntiles) {
+      const int s1 = (t - 1) % NSTAGE;
+      mbar_expect_tx(&full[s1], TJ * sizeof(Rec));
+      tma_load_1d(&tiles[s1][0], gj + (t - 1 + NSTAGE) * TJ, TJ * sizeof(Rec), &full[s1]);
+      issued = t - 1 + NSTAGE + 1;
+    }
+    const Rec *tile = &tiles[s][0];
+    const int tj0 = js + t * TJ;
+
+    // Does this tile hold the self slot of any i of this warp?
+    bool mine = false;
+#pragma unroll
+    for (int k = 0; k < IPT; k++) mine |= (unsigned)(self[k] - tj0) < (unsigned)TJ;
+    const bool slow = __any_sync(0xffffffffu, mine);
+
+    if (!slow) {
+#pragma unroll 4
+      for (int u = 0; u < JPT; u++) {
+        const Rec r = tile[jl + JL * u];
+#pragma unroll
+        for (int k = 0; k < IPT; k++)
+          P::template pair<false>(I[k], r, eps2, q[k], nnmin[k], false);
+      }
+    } else {
+      for (int u = 0; u < JPT; u++) {
+        const int jj = jl + JL * u;
+        const Rec r = tile[jj];
+#pragma unroll
+        for (int k = 0; k < IPT; k++)
+          P::template pair<true>(I[k], r, eps2, q[k], nnmin[k], tj0 + jj == self[k]);
+      }
+    }
+
+    // Nearest neighbour: re-scan this tile where the running min improved.
+    bool imp = false;
+#pragma unroll
+    for (int k = 0; k < IPT; k++) imp |= nnmin[k] < nnbest[k];
+    if (__any_sync(0xffffffffu, imp)) {
+      for (int u = 0; u < JPT; u++) {
+        const int jj = jl + JL * u;
+        const Rec r = tile[jj];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+          if (nnmin[k] < nnbest[k]) {
+            R dx, dy, dz;
+            const R r2 = P::r2e(I[k], r, eps2, dx, dy, dz);
+            if (r2 == nnmin[k] && tj0 + jj != self[k]) {
+              nnbest[k] = r2;
+              nnidx[k] = tj0 + jj;
+            }
+          }
+        }
+      }
+    }
+
+    if ((t + 1) % FOLD_TILES == 0) {
+#pragma unroll
+      for (int k = 0; k < IPT; k++) {
+        P::fold(T[k], q[k]);
+        P::zero(q[k]);
+      }
+    }
+  }
+
+  if (failed) {
+    // Drain this CTA's outstanding copies (bounded) before leaving.
+    if (tid == 0) {
+      atomicOr(kp.err, ERR_TMA_TIMEOUT);
+      for (int u = t_fail; u < issued; u++)
+        (void)mbar_wait_bounded(&full[u % NSTAGE], (u / NSTAGE) & 1);
+    }
+    return;
+  }
+
+  // ---- merge: fold remainders, then j-lanes, then (maybe) CTAs ----
+  typename P::Out o[IPT];
+#pragma unroll
+  for (int k = 0; k < IPT; k++) {
+    P::fold(T[k], q[k]);
+    P::to_out(T[k], nnbest[k], nnidx[k], o[k]);
+  }
+  if (JL > 1) {
+#pragma unroll
+    for (int m = 1; m < (JL < 32 ? JL : 32); m <<= 1) {
+#pragma unroll
+      for (int k = 0; k < IPT; k++) {
+        typename P::Out other = shfl_xor_out(o[k], m);
+        // Lower lane first keeps the order fixed.
+        if (lane & m) {
+          P::merge(other, o[k]);
+          o[k] = other;
+        } else {
+          P::merge(o[k], other);
+        }
+      }
+    }
+  }
+  (void)lane;
+  if (JL > 32) {
+    // Cross-warp: warps w0..w0+JL/32-1 own one i-lane group.
+    __syncthreads();
+    typename P::Out *buf = reinterpret_cast<typename P::Out *>(&tiles[0][0]);
+    static_assert(sizeof(typename P::Out) * IPT * (NT / 32) <= sizeof(Rec) * TJ * NSTAGE, "smem");
+    const int warp = tid >> 5;
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < IPT; k++) buf[warp * IPT + k] = o[k];
+    }
+    __syncthreads();
+    if (jl == 0) {
+      constexpr int WPG = JL / 32;
+#pragma unroll
+      for (int k = 0; k < IPT; k++) {
+        typename P::Out acc = buf[warp * IPT + k];
+        for (int w = 1; w < WPG; w++) P::merge(acc, buf[(warp + w) * IPT + k]);
+        o[k] = acc;
+      }
+    }
+  }
+  if (jl != 0) return;
+#pragma unroll
+  for (int k = 0; k < IPT; k++) {
+    if (!valid[k]) continue;
+    const int i = blockIdx.x * ISLOTS + k * NIL + il;
+    if (kp.nsplit == 1) {
+      P::write_final(o[k], i, kp.acc, kp.jerk, kp.pot);
+      kp.nn[i] = (o[k].nn >= 0 && o[k].nn < kp.nj) ? o[k].nn : -1;
+      if (kp.nn_r2) kp.nn_r2[i] = (float)o[k].nnr2;
+    } else {
+      reinterpret_cast<typename P::Out *>(kp.part)[(size_t)blockIdx.y * kp.ni_pad + i] = o[k];
+    }
+  }
+}
+
+// Second pass: merge the nsplit partial records of each i in split order.
+template <class P>
+__global__ void reduce_kernel(KParams kp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kp.ni) return;
+  const typename P::Out *part = reinterpret_cast<const typename P::Out *>(kp.part);
+  typename P::Out o = part[i];
+  for (int s = 1; s < kp.nsplit; s++) P::merge(o, part[(size_t)s * kp.ni_pad + i]);
+  P::write_final(o, i, kp.acc, kp.jerk, kp.pot);
+  kp.nn[i] = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
+  if (kp.nn_r2) kp.nn_r2[i] = (float)o.nnr2;
+}
+
+int g_sms = 0;
+
+int sm_count() {
+  if (g_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms <= 0) g_sms = 152;
+  }
+  return g_sms;
+}
+
+// Launch shape: JL from the i-block size, nsplit so that the grid covers
+// about two resident CTAs per SM, with at least 4 tiles per split.
+void choose_shape(int ni, int nj, int force_jl, int force_nsplit, int *jl_out, int *nsplit_out,
+                  int *jsplit_out) {
+  int jl = 1;
+  if (force_jl > 0) {
+    jl = force_jl;
+  } else {
+    // smallest JL whose CTA i-capacity (512/JL) still holds >= ni, so the
+    // i-slots are not wasted; JL = 1 for ni >= 512.
+    while (jl < TJ && (NT / (jl * 2)) * IPT >= ni && ni > 0) jl *= 2;
+  }
+  const int islots = (NT / jl) * IPT;
+  const int gx = (ni + islots - 1) / islots;
+  const int ntiles = (nj + TJ - 1) / TJ;
+  int nsplit;
+  if (force_nsplit > 0) {
+    nsplit = force_nsplit;
+  } else {
+    // Pick the split count that best fills whole waves of resident CTAs
+    // (2 per SM), with at least 4 tiles per split and at most 64 splits.
+    const int slots = 2 * sm_count();
+    int max_split = ntiles / 4 > 1 ? ntiles / 4 : 1;
+    if (max_split > 64) max_split = 64;
+    nsplit = 1;
+    double best = -1.0;
+    for (int c = 1; c <= max_split; c++) {
+      const long long total = (long long)gx * c;
+      const long long waves = (total + slots - 1) / slots;
+      const double eff = (double)total / (double)(waves * slots);
+      if (eff > best + 0.02) {
+        best = eff;
+        nsplit = c;
+      }
+      if (total >= 8LL * slots) break;
+    }
+  }
+  if (nsplit > ntiles && ntiles > 0) nsplit = ntiles;
+  if (nsplit < 1) nsplit = 1;
+  const int tiles_per = ntiles > 0 ? (ntiles + nsplit - 1) / nsplit : 1;
+  nsplit = ntiles > 0 ? (ntiles + tiles_per - 1) / tiles_per : 1;
+  *jl_out = jl;
+  *nsplit_out = nsplit;
+  *jsplit_out = tiles_per * TJ;
+}
+
+template <class P>
+int launch(const KParams &kp, int jl, int gx, cudaStream_t st) {
+  dim3 grid(gx, kp.nsplit), block(NT);
+  switch (jl) {
+#define G6_CASE(J) \
+  case J:          \
+    force_kernel<P, J><<<grid, block, 0, st>>>(kp); \
+    break;
+    G6_CASE(1)
+    G6_CASE(2)
+    G6_CASE(4)
+    G6_CASE(8)
+    G6_CASE(16)
+    G6_CASE(32)
+    G6_CASE(64)
+    G6_CASE(128)
+#undef G6_CASE
+    default:
+      return -2;
+  }
+  if (kp.nsplit > 1) reduce_kernel<P><<<(kp.ni + 127) / 128, 128, 0, st>>>(kp);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+}  // namespace
+
+extern "C" int g6k_sm_count(void) { return sm_count(); }
+
+extern "C" size_t g6k_scratch_bytes(int ni, int nj, int prec, int force_jl, int force_nsplit) {
+  int jl, nsplit, jsplit;
+  choose_shape(ni, nj, force_jl, force_nsplit, &jl, &nsplit, &jsplit);
+  if (nsplit <= 1) return 0;
+  const size_t rec = prec == G6_PREC_FP64 ? sizeof(F64P::Out) : sizeof(SplitP::Out);
+  return (size_t)nsplit * (size_t)ni * rec;
+}
+
+extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t st) {
+  if (a->ni <= 0) return 0;
+  if (a->nj <= 0) return -1;
+  int jl, nsplit, jsplit;
+  choose_shape(a->ni, a->nj, a->force_jl, a->force_nsplit, &jl, &nsplit, &jsplit);
+  if (jl < 1 || jl > TJ || (jl & (jl - 1))) return -2;
+  KParams kp;
+  kp.ni = a->ni;
+  kp.nj = a->nj;
+  kp.nsplit = nsplit;
+  kp.jsplit = jsplit;
+  kp.eps2 = a->eps2;
+  kp.ipos = a->ipos;
+  kp.ivel = a->ivel;
+  kp.ilist = a->ilist;
+  kp.iself = a->iself;
+  kp.acc = a->acc;
+  kp.jerk = a->jerk;
+  kp.pot = a->pot;
+  kp.nn = a->nn;
+  kp.nn_r2 = a->nn_r2;
+  kp.part = a->scratch;
+  kp.ni_pad = a->ni;
+  kp.err = a->err;
+  const size_t need = nsplit > 1 ? g6k_scratch_bytes(a->ni, a->nj, a->prec, jl, nsplit) : 0;
+  if (need > a->scratch_bytes) return -4;
+  const int islots = (NT / jl) * IPT;
+  const int gx = (a->ni + islots - 1) / islots;
+  if (shape) {
+    shape->jl = jl;
+    shape->nsplit = nsplit;
+    shape->grid_x = gx;
+    shape->grid_y = nsplit;
+    shape->threads = NT;
+  }
+  if (a->prec == G6_PREC_FP64) {
+    kp.jrec = a->js->jp_f64;
+    return launch<F64P>(kp, jl, gx, st);
+  }
+  kp.jrec = a->js->jp_split;
+  return launch<SplitP>(kp, jl, gx, st);
+}

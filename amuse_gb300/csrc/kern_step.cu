@@ -1,0 +1,288 @@
+// kern_step.cu -- FP64 kernels around the force evaluation for the
+// device-resident block-step driver (extension API):
+//
+//   correct_kernel   Hermite corrector + Aarseth step with power-of-2
+//                    quantisation, src/amuse_ph4/src/idata.cc:399-514.
+//                    The i-particle prediction it corrects is ph4's host
+//                    i-prediction (idata.cc:346-365).  Written with explicit
+//                    round-to-nearest intrinsics (no contraction into FMA)
+//                    so that it rounds exactly like the x86 CPU code.
+//   schedule kernels tnext = min_j (t_j + dt_j) and the list of slots with
+//                    t_j + dt_j == tnext (the block of scheduler::get_list,
+//                    src/amuse_ph4/src/scheduler.cc:66-79).
+//   initial_step     jdata::set_initial_timestep (jdata.cc:503-564).
+//   energy sums      sum m |v_p|^2 and sum m pot (jdata.cc:582-680).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "g6_dev.h"
+
+namespace {
+
+constexpr int PT = 256;
+
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+__global__ void correct_kernel(g6_jstate js, int ni, const int *__restrict__ ilist, double tnext,
+                               double eta, const double *__restrict__ acc,
+                               const double *__restrict__ jerk, const double *__restrict__ pot,
+                               const int *__restrict__ nn) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ni) return;
+  const int s = ilist[i];
+  const int cap = js.cap;
+  const double t0 = js.t[s];
+  const double dt = dsub(tnext, t0);
+  const double dt2 = dmul(dt, dt);
+  double xp[3], vp[3];
+  double a2 = 0, j2 = 0, k2 = 0, l2 = 0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double x = js.x[k * cap + s], v = js.v[k * cap + s];
+    const double oa = js.a[k * cap + s], oj = js.j[k * cap + s];
+    if (dt == 0) {
+      xp[k] = x;
+      vp[k] = v;
+    } else {
+      // x + dt*(v + 0.5*dt*(a + dt*j/3)),  v + dt*(a + 0.5*dt*j)
+      const double hdt = dmul(0.5, dt);
+      xp[k] = dadd(x, dmul(dt, dadd(v, dmul(hdt, dadd(oa, ddiv(dmul(dt, oj), 3.0))))));
+      vp[k] = dadd(v, dmul(dt, dadd(oa, dmul(hdt, oj))));
+    }
+    const double ia = acc[3 * i + k], ij = jerk[3 * i + k];
+    const double da = dsub(oa, ia);
+    const double alpha = dsub(dmul(-3.0, da), dmul(dt, dadd(dmul(2.0, oj), ij)));
+    const double beta = dadd(dmul(2.0, da), dmul(dt, dadd(oj, ij)));
+    xp[k] = dadd(xp[k], dmul(dadd(ddiv(alpha, 12.0), ddiv(beta, 20.0)), dt2));
+    vp[k] = dadd(vp[k], dmul(dadd(ddiv(alpha, 3.0), ddiv(beta, 4.0)), dt));
+    a2 = dadd(a2, dmul(ia, ia));
+    const double dj = dmul(dt, ij);
+    j2 = dadd(j2, dmul(dj, dj));
+    const double ak = dmul(2.0, alpha);
+    k2 = dadd(k2, dmul(ak, ak));
+    const double bl = dmul(6.0, beta);
+    l2 = dadd(l2, dmul(bl, bl));
+  }
+  double newstep = dmul(dmul(eta, dt),
+                        __dsqrt_rn(ddiv(dadd(__dsqrt_rn(dmul(a2, k2)), j2),
+                                        dadd(__dsqrt_rn(dmul(j2, l2)), k2))));
+  const double olds = js.dt[s];
+  int expo;
+  double oldstep2 = ddiv(olds, dmul(2.0, frexp(olds, &expo)));
+  for (int guard = 0; guard < 1100 && fmod(tnext, oldstep2) != 0; guard++) oldstep2 = ddiv(oldstep2, 2.0);
+  if (newstep < oldstep2) {
+    newstep = ddiv(oldstep2, 2.0);
+  } else {
+    const double t2 = dmul(2.0, oldstep2);
+    if (newstep >= t2 && fmod(tnext, t2) == 0)
+      newstep = t2;
+    else
+      newstep = oldstep2;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    js.x[k * cap + s] = xp[k];
+    js.v[k * cap + s] = vp[k];
+    js.a[k * cap + s] = acc[3 * i + k];
+    js.j[k * cap + s] = jerk[3 * i + k];
+  }
+  js.t[s] = tnext;
+  js.dt[s] = newstep;
+  if (pot) js.pot[s] = pot[i];
+  if (nn) js.nn[s] = nn[i];
+}
+
+__global__ void store_kernel(g6_jstate js, int ni, const int *__restrict__ ilist,
+                             const double *__restrict__ acc, const double *__restrict__ jerk,
+                             const double *__restrict__ pot, const int *__restrict__ nn) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ni) return;
+  const int s = ilist[i];
+  const int cap = js.cap;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    js.a[k * cap + s] = acc[3 * i + k];
+    js.j[k * cap + s] = jerk[3 * i + k];
+  }
+  if (pot) js.pot[s] = pot[i];
+  if (nn) js.nn[s] = nn[i];
+}
+
+// t + dt >= 0 always, so the IEEE bit pattern orders like an unsigned int.
+__global__ void sched_init(unsigned long long *dmin, int *dni) {
+  *dmin = 0x7ff0000000000000ull;  // +inf
+  *dni = 0;
+}
+
+__global__ void sched_min(g6_jstate js, int nj, unsigned long long *dmin) {
+  __shared__ unsigned long long w[PT / 32];
+  unsigned long long m = 0x7ff0000000000000ull;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nj; s += gridDim.x * blockDim.x) {
+    const unsigned long long b = __double_as_longlong(js.t[s] + js.dt[s]);
+    m = b < m ? b : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+    m = x < m ? x : m;
+  }
+  if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < PT / 32; k++) m = w[k] < m ? w[k] : m;
+    atomicMin(dmin, m);
+  }
+}
+
+__global__ void sched_list(g6_jstate js, int nj, const unsigned long long *dmin, int *ilist,
+                           int *dni, double *dtnext) {
+  const double tn = __longlong_as_double((long long)*dmin);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *dtnext = tn;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nj; s += gridDim.x * blockDim.x) {
+    if (js.t[s] + js.dt[s] == tn) {
+      const int k = atomicAdd(dni, 1);
+      ilist[k] = s;
+    }
+  }
+}
+
+__global__ void initial_step_kernel(g6_jstate js, int nj, double eta, double fac, double limit,
+                                    double system_time) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nj) return;
+  const int cap = js.cap;
+  double a2 = 0, j2 = 0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double a = js.a[k * cap + s], j = js.j[k * cap + s];
+    a2 = dadd(a2, dmul(a, a));
+    j2 = dadd(j2, dmul(j, j));
+  }
+  double fs;
+  if (eta == 0.0)
+    fs = limit;
+  else if (a2 == 0.0 || j2 == 0.0)
+    fs = dmul(fac, eta);
+  else
+    fs = dmul(dmul(fac, eta), __dsqrt_rn(ddiv(a2, j2)));
+  if (isnan(fs)) fs = dmul(fac, eta);
+  int expo;
+  fs = ddiv(fs, dmul(2.0, frexp(fs, &expo)));
+  for (int g = 0; g < 1100 && fmod(system_time, fs) != 0; g++) fs = ddiv(fs, 2.0);
+  for (int g = 0; g < 1100 && fs > limit; g++) fs = ddiv(fs, 2.0);
+  js.dt[s] = fs;
+  js.t[s] = system_time;
+}
+
+__global__ void clamp_step_kernel(g6_jstate js, int nj, double dtmax) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nj) return;
+  double d = js.dt[s];
+  for (int g = 0; g < 1100 && d > dtmax; g++) d = ddiv(d, 2.0);
+  js.dt[s] = d;
+}
+
+// Per-block partial sums of m|v_p|^2 and m*pot, in fixed order.
+__global__ void energy_partial(g6_jstate js, int nj, double t, const double *__restrict__ pot,
+                               double *part) {
+  __shared__ double sk[PT], sp[PT];
+  const int cap = js.cap;
+  double kin = 0, pe = 0;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nj) {
+    const double m = js.m[s];
+    const double dt = t - js.t[s];
+    double v2 = 0;
+    for (int k = 0; k < 3; k++) {
+      double v = js.v[k * cap + s];
+      if (dt != 0) {
+        const double a = js.a[k * cap + s], j = js.j[k * cap + s];
+        v = dadd(v, dmul(dt, dadd(a, dmul(dmul(0.5, dt), j))));
+      }
+      v2 = dadd(v2, dmul(v, v));
+    }
+    kin = dmul(m, v2);
+    pe = pot ? dmul(m, pot[s]) : 0.0;
+  }
+  sk[threadIdx.x] = kin;
+  sp[threadIdx.x] = pe;
+  __syncthreads();
+  for (int o = PT / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sk[threadIdx.x] += sk[threadIdx.x + o];
+      sp[threadIdx.x] += sp[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sk[0];
+    part[2 * blockIdx.x + 1] = sp[0];
+  }
+}
+
+__global__ void energy_final(const double *part, int nb, double *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double k = 0, p = 0;
+  for (int b = 0; b < nb; b++) {
+    k += part[2 * b];
+    p += part[2 * b + 1];
+  }
+  out[0] = k;
+  out[1] = p;
+}
+
+}  // namespace
+
+extern "C" int g6k_correct(const g6_jstate *js, int ni, const int *ilist, double tnext,
+                           double eta, const double *acc, const double *jerk, const double *pot,
+                           const int *nn, cudaStream_t st) {
+  if (ni <= 0) return 0;
+  correct_kernel<<<(ni + 127) / 128, 128, 0, st>>>(*js, ni, ilist, tnext, eta, acc, jerk, pot, nn);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+extern "C" int g6k_store_forces(const g6_jstate *js, int ni, const int *ilist, const double *acc,
+                                const double *jerk, const double *pot, const int *nn,
+                                cudaStream_t st) {
+  if (ni <= 0) return 0;
+  store_kernel<<<(ni + PT - 1) / PT, PT, 0, st>>>(*js, ni, ilist, acc, jerk, pot, nn);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+extern "C" int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni, double *d_tnext,
+                            double *d_scratch, int scratch_len, cudaStream_t st) {
+  if (nj <= 0 || scratch_len < 1) return -1;
+  unsigned long long *dmin = reinterpret_cast<unsigned long long *>(d_scratch);
+  int grid = (nj + PT - 1) / PT;
+  const int cap_grid = 4 * g6k_sm_count();
+  if (grid > cap_grid) grid = cap_grid;
+  sched_init<<<1, 1, 0, st>>>(dmin, d_ni);
+  sched_min<<<grid, PT, 0, st>>>(*js, nj, dmin);
+  sched_list<<<grid, PT, 0, st>>>(*js, nj, dmin, d_ilist, d_ni, d_tnext);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+extern "C" int g6k_initial_step(const g6_jstate *js, int nj, double eta, double fac, double limit,
+                                double system_time, cudaStream_t st) {
+  if (nj <= 0) return 0;
+  initial_step_kernel<<<(nj + PT - 1) / PT, PT, 0, st>>>(*js, nj, eta, fac, limit, system_time);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+extern "C" int g6k_clamp_steps(const g6_jstate *js, int nj, double dtmax, cudaStream_t st) {
+  if (nj <= 0) return 0;
+  clamp_step_kernel<<<(nj + PT - 1) / PT, PT, 0, st>>>(*js, nj, dtmax);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+// d_out must hold 2 + 2*ceil(nj/256) doubles; results in d_out[0..1].
+extern "C" int g6k_energy_sums(const g6_jstate *js, int nj, double t, const double *pot_i,
+                               double *d_out, cudaStream_t st) {
+  if (nj <= 0) return 0;
+  const int nb = (nj + PT - 1) / PT;
+  energy_partial<<<nb, PT, 0, st>>>(*js, nj, t, pot_i, d_out + 2);
+  energy_final<<<1, 32, 0, st>>>(d_out + 2, nb, d_out);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}

@@ -1,0 +1,348 @@
+"""Benchmark: Hermite pair-interactions/s of the split-precision force path.
+
+Workload (the precision configuration): Plummer sphere N = 2^20, equal mass,
+eps2 = 1e-6, FP64 state, seeded synthetic input (numpy seed 1, AMUSE's
+generator restated in amuse_gb300.ic).  One step = one shared Hermite step of
+all N particles on the device: FP64 j-prediction, split-precision force on
+all N i-particles (N*(N-1) pair interactions), FP64 corrector.  Inputs are
+resident in HBM; L2 is flushed (256 MB write) between timed steps.
+
+Reported next to it:
+  e2e          the same metric through the GRAPE-6 C ABI with host buffers
+               (g6_set_j_particle for all N, g6_set_ti, g6calc_firsthalf /
+               lasthalf2 chunked by npipes, as ph4's gpu.cc calls it);
+  fp64         the plain FP64 GPU kernel's pairs/s (on a 16384-particle
+               i-subset against all N j) and the speed-up over it;
+  roofline     the force kernel against the FP32 peak, 60 flop/pair (ph4's
+               convention, src/amuse_ph4/src/jdata.cc:1038);
+  cpu_baseline the oracle port of ph4's CPU force loop on the host cores
+               (bounded i-sample against all N j).
+
+--impl reference times the reference's CPU force path (ph4's
+idata::get_partial_acc_and_jerk restated in oracle/, all host threads).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOP_PER_PAIR = 60.0
+N_DEFAULT = 1 << 20
+EPS2 = 1e-6
+ETA = 0.01
+DT_STEP = 2.0 ** -12
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def workload(n):
+    from amuse_gb300 import ic
+    np.random.seed(1)
+    return ic.plummer(n, do_scale=False)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [q.strip() for q in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+                power.append(float(p[3]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "power_w_max": max(power) if power else None, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_baseline(mass, pos, vel, seconds, threads):
+    """ph4 CPU force loop (oracle port) on a bounded i-sample against all j."""
+    import oracle
+    oracle.build_port()
+    n = len(mass)
+    probe = max(threads, 8)
+    t0 = time.perf_counter()
+    oracle.force(mass, pos, vel, EPS2, pos[:probe], vel[:probe], threads=threads)
+    dt = time.perf_counter() - t0
+    rate = probe * (n - 1) / max(dt, 1e-9)
+    ni = int(max(threads, min(n, rate * seconds / (n - 1))))
+    t0 = time.perf_counter()
+    oracle.force(mass, pos, vel, EPS2, pos[:ni], vel[:ni], threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": ni * (n - 1) / dt, "unit": "pair-interactions/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{ni} i-particles x {n} j (ph4 idata::get_partial_acc_and_jerk "
+                      f"restated in oracle/g6_oracle.c, {threads} threads, {dt:.1f} s)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    mass, pos, vel = workload(args.n)
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(mass, pos, vel, max(1.0, args.cpu_seconds / 4), threads)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(mass, pos, vel, args.cpu_seconds / 2, threads))
+    v = statistics.median([c["value"] for c in vals])
+    line = {
+        "impl": "reference", "metric": "Hermite pair-interactions/s (force, acc+jerk+pot+nn)",
+        "value": v, "unit": "pair-interactions/s", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Plummer)",
+        "config": {"workload": f"plummer N={args.n} equal mass eps2={EPS2}, all-i force",
+                   "n": args.n},
+        "cpu_baseline": {"value": v, "unit": "pair-interactions/s", "cores": threads,
+                         "kind": "port", "sample": vals[-1]["sample"]},
+        "e2e": {"value": v, "unit": "pair-interactions/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    import amuse_gb300 as ag
+    from amuse_gb300 import build as b
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    b.build()
+    n = args.n
+    mass, pos, vel = workload(n)
+    g6 = ag.G6X(local)
+    g6.set_precision(ag.SPLIT)
+    g6.load_particles(mass, pos, vel)
+    g6.run_init(EPS2, ETA)
+    k0, u0 = g6.energy()
+    e0 = k0 + u0
+    stream = torch.cuda.ExternalStream(g6.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    t = 0.0
+
+    def one_step():
+        nonlocal t
+        t += DT_STEP
+        g6.step_all(t)
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    g6.timing(True)
+    times, fms, pms, launches = [], [], [], 0
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e_a = torch.cuda.Event(enable_timing=True)
+        e_b = torch.cuda.Event(enable_timing=True)
+        e_a.record(stream)
+        one_step()
+        e_b.record(stream)
+        e_b.synchronize()
+        times.append(e_a.elapsed_time(e_b) / 1e3)
+        st = g6.stats()
+        fms.append(st["force_ms"])
+        pms.append(st["predict_ms"])
+        launches += 3 + (1 if st["nsplit"] > 1 else 0)  # predict, force, (reduce), correct
+    torch.cuda.synchronize()
+    g6.timing(False)
+    clocks = sampler.stop()
+    if world > 1:
+        tt = torch.tensor([sum(times)], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total = float(tt.item())
+    else:
+        total = sum(times)
+    k1, u1 = g6.energy()
+    e1 = k1 + u1
+    pairs_step = n * (n - 1)
+    value = world * args.steps * pairs_step / total
+    force_s = statistics.mean(fms) / 1e3
+    achieved = FLOP_PER_PAIR * pairs_step / force_s / 1e12
+    pk = peaks()
+    sm_max = pk.get("sm_max_mhz", 2070.0)
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = nsm * 128 * 2 * sm_max * 1e6 / 1e12
+    pred_gbs = (n * (15 * 8 + 4 + 48)) / (statistics.mean(pms) / 1e3) / 1e9 if pms[0] > 0 else None
+
+    # plain FP64 GPU kernel on an i-subset (same j-set, same per-pair work)
+    g6.set_precision(ag.FP64)
+    nsub = 16384
+    d_il = torch.arange(nsub, dtype=torch.int32, device=f"cuda:{local}")
+    d_acc = torch.empty(nsub * 3, dtype=torch.float64, device=f"cuda:{local}")
+    d_jerk = torch.empty_like(d_acc)
+    d_pot = torch.empty(nsub, dtype=torch.float64, device=f"cuda:{local}")
+    d_nn = torch.empty(nsub, dtype=torch.int32, device=f"cuda:{local}")
+    g6.timing(True)
+    fp64_ms = []
+    for r in range(3):
+        g6.force_slots(t, EPS2, n, d_il.data_ptr(), nsub, d_acc.data_ptr(), d_jerk.data_ptr(),
+                       d_pot.data_ptr(), d_nn.data_ptr(), sync=True)
+        if r:
+            fp64_ms.append(g6.stats()["force_ms"])
+    g6.timing(False)
+    g6.set_precision(ag.SPLIT)
+    fp64_rate = nsub * (n - 1) / (statistics.mean(fp64_ms) / 1e3)
+    split_rate = pairs_step / force_s
+
+    # end to end through the GRAPE-6 ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        x, v = pos.copy(), vel.copy()
+        ids = np.arange(1, n + 1, dtype=np.int32)
+        out = dict(acc=np.zeros((n, 3)), jerk=np.zeros((n, 3)), pot=np.zeros(n),
+                   nn=np.zeros(n, np.int32))
+        # warm (pinned buffers, capacities)
+        ag.drive_load(mass, x, v, ids=ids)
+        ag.drive_force(n, 0.0, EPS2, ids, x, v, want_nn=True, out=out)
+        e2e_t = []
+        for _ in range(max(1, min(args.steps, 2))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ag.drive_load(mass, x, v, ids=ids)          # j updates for all N (ph4 update_gpu)
+            ag.drive_force(n, 0.0, EPS2, ids, x, v, want_nn=True, out=out)
+            e2e_t.append(time.perf_counter() - t0)
+        e2e = {"value": pairs_step / statistics.median(e2e_t), "unit": "pair-interactions/s",
+               "h2d_bytes_per_step": n * (128 + 6 * 8 + 8 + 4),
+               "d2h_bytes_per_step": n * (7 * 8 + 4 + 4) + 16 * ((n + 16383) // 16384),
+               "path": "g6_set_j_particle x N + g6_set_ti + g6calc_firsthalf/lasthalf2 "
+                       "chunks of g6_npipes()=16384 (libg6drive.so, ph4 gpu.cc order)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(mass, pos, vel, args.cpu_seconds, os.cpu_count() or 1)
+
+    if rank == 0:
+        line = {
+            "metric": "Hermite pair-interactions/s (force, acc+jerk+pot+nn), split-precision",
+            "value": value, "unit": "pair-interactions/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Plummer, AMUSE generator restated)",
+            "config": {"workload": f"plummer N={n} equal mass eps2={EPS2}; shared Hermite step "
+                                   f"dt=2^-12 of all N (predict+force+correct)",
+                       "n": n, "eps2": EPS2, "l2": "flushed (256 MB write) between steps",
+                       "parallelism": f"replicas x{world}"},
+            "energy": {"dE_over_E": (e1 - e0) / abs(e0), "steps": args.warmup + args.steps,
+                       "E0": e0, "E1": e1},
+            "fp64": {"value": fp64_rate, "unit": "pair-interactions/s",
+                     "sample": f"{nsub} i x {n} j", "split_over_fp64": split_rate / fp64_rate},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+                         "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                         "kernel": "force_kernel<SplitP,1>",
+                         "peak_source": f"{nsm} SMs x 128 FP32 lanes x 2 flop x {sm_max:.0f} MHz "
+                                        "(sm_max_mhz, MEASURED_PEAKS.json; it holds no FP32 figure)",
+                         "flop_per_pair": FLOP_PER_PAIR, "force_ms": 1e3 * force_s},
+            "predictor": {"ms": statistics.mean(pms), "GB_s": pred_gbs,
+                          "bytes_per_j": 15 * 8 + 4 + 48,
+                          "hbm_peak_gbs": pk.get("hbm_gbs")},
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

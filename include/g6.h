@@ -1,0 +1,188 @@
+/*
+ * g6.h -- public C ABI of libsapporo.so (GB300 / sm_103a build).
+ *
+ * Part 1 is the GRAPE-6 API exactly as AMUSE's callers bind it: the 16
+ * trailing-underscore, all-pointer symbols of lib/sapporo_light/g6lib.h:5-51
+ * (sapporoG6lib.cpp:5-78), used by phiGRAPE through gfortran name mangling
+ * and by ph4 through its by-value wrappers (src/amuse_ph4/src/grape.h).
+ * Part 2 is the by-value set of ph4's grape.h / lib/g6lib/g6lib.h:58-128,
+ * exported as WEAK symbols (ph4 defines its own strong copies in grape.cc).
+ * Part 3 is the extension API (g6x_*), which has no GRAPE-6 counterpart:
+ * device-resident state, the FP64 corrector / block-step driver, precision
+ * selection and statistics.
+ *
+ * Conventions (shared by all parts): arrays `double x[][3]` are row-major
+ * [n][3] (= Fortran x(3,n)); 0 means success and a negative value an error
+ * (the reference exits the process instead, sapporo.cpp:26-27,76-79,255-257);
+ * one context per process; not re-entrant.
+ */
+#ifndef G6_GB300_H
+#define G6_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes. */
+#define G6_OK 0
+#define G6_ERR_NOT_OPEN (-1)   /* g6_open not called / failed */
+#define G6_ERR_ARG (-2)        /* bad argument (address, ni > npipes, ...) */
+#define G6_ERR_CUDA (-3)       /* CUDA runtime error */
+#define G6_ERR_NOMEM (-4)      /* device or pinned allocation failed */
+#define G6_ERR_DEVICE (-5)     /* no such CUDA device */
+#define G6_ERR_KERNEL (-6)     /* a kernel reported a timeout (error word) */
+#define G6_ERR_STATE (-7)      /* call out of order (e.g. lasthalf w/o firsthalf) */
+
+/* ---------------- Part 1: GRAPE-6 ABI (pointer arguments) ---------------- */
+
+/* sapporo.cpp:19-41: select CUDA device *id, allocate the j-store. */
+int g6_open_(int *id);
+/* sapporo.cpp:43-56: release device memory. */
+int g6_close_(int *id);
+/* sapporo.cpp:64-66: max i-particles per g6calc call (<= 16384 by
+   default, phiGRAPE's NGP bound; env G6_NPIPES overrides). */
+int g6_npipes_(void);
+/* sapporoG6lib.cpp:10-11: accepted and ignored. */
+int g6_set_tunit_(double *);
+int g6_set_xunit_(double *);
+/* sapporo.cpp:58-62: time to which j-particles are predicted. */
+int g6_set_ti_(int *id, double *ti);
+/* sapporo.cpp:68-112: stage one j record for slot *address; index = id used
+   for self-exclusion and returned as neighbour; a2 = acc/2, j6 = jerk/6,
+   k18 (snap/18) is ignored as in the reference. */
+int g6_set_j_particle_(int *cluster_id, int *address, int *index, double *tj, double *dtj,
+                       double *mass, double k18[3], double j6[3], double a2[3], double v[3],
+                       double x[3]);
+/* sapporo.cpp:114-152: start the force on ni i-particles from j slots
+   [0, nj) predicted to the last set_ti (pending j updates applied first).
+   aold/j6old/phiold are ignored as in the reference; h2 is the neighbour
+   radius^2 (used by the neighbour-list API).  Asynchronous. */
+void g6calc_firsthalf_(int *cluster_id, int *nj, int *ni, int index[], double xi[][3],
+                       double vi[][3], double aold[][3], double j6old[][3], double phiold[],
+                       double *eps2, double h2[]);
+/* sapporo.cpp:154-182: wait and OVERWRITE acc, jerk, pot of the ni
+   i-particles of the preceding firsthalf. */
+int g6calc_lasthalf_(int *cluster_id, int *nj, int *ni, int index[], double xi[][3],
+                     double vi[][3], double *eps2, double h2[], double acc[][3],
+                     double jerk[][3], double pot[]);
+/* sapporo.cpp:185-232: as lasthalf, plus nnbindex[i] = index (id) of the
+   nearest j (self excluded), -1 if none. */
+int g6calc_lasthalf2_(int *cluster_id, int *nj, int *ni, int index[], double xi[][3],
+                      double vi[][3], double *eps2, double h2[], double acc[][3],
+                      double jerk[][3], double pot[], int *inn);
+/* sapporoG6lib.cpp:58-61: no-ops returning 0. */
+int g6_initialize_jp_buffer_(int *cluster_id, int *buf_size);
+int g6_flush_jp_buffer_(int *cluster_id);
+int g6_reset_(int *cluster_id);
+int g6_reset_fofpga_(int *cluster_id);
+/* sapporo.cpp:234-246: fetch the neighbour lists (r^2 <= h2[i], self
+   excluded) of the last force call; returns 1 if any list overflowed its
+   G6_NGB_MAX entries, 0 otherwise. */
+int g6_read_neighbour_list_(int *cluster_id);
+/* sapporo.cpp:248-272: copy the sorted neighbour ids of i-particle *ipipe
+   into neighbour_list (at most *maxlength), set *n_neighbours; returns 1
+   on overflow. */
+int g6_get_neighbour_list_(int *cluster_id, int *ipipe, int *maxlength, int *n_neighbours,
+                           int neighbour_list[]);
+
+#define G6_NGB_MAX 256 /* per-i neighbour capacity (sapporo_defs.h NGB_PP) */
+
+/* ---------------- Part 2: by-value forms (weak) ---------------------------- */
+
+int g6_open(int id);
+int g6_close(int id);
+int g6_npipes(void);
+int g6_set_tunit(double t);
+int g6_set_xunit(double x);
+int g6_set_ti(int id, double ti);
+int g6_set_j_particle(int cluster_id, int address, int index, double tj, double dtj, double mass,
+                      double k18[3], double j6[3], double a2[3], double v[3], double x[3]);
+void g6calc_firsthalf(int cluster_id, int nj, int ni, int index[], double xi[][3],
+                      double vi[][3], double aold[][3], double j6old[][3], double phiold[],
+                      double eps2, double h2[]);
+int g6calc_lasthalf(int cluster_id, int nj, int ni, int index[], double xi[][3], double vi[][3],
+                    double eps2, double h2[], double acc[][3], double jerk[][3], double pot[]);
+int g6calc_lasthalf2(int cluster_id, int nj, int ni, int index[], double xi[][3],
+                     double vi[][3], double eps2, double h2[], double acc[][3],
+                     double jerk[][3], double pot[], int inn[]);
+int g6_initialize_jp_buffer(int cluster_id, int buf_size);
+int g6_flush_jp_buffer(int cluster_id);
+int g6_reset(int cluster_id);
+int g6_reset_fofpga(int cluster_id);
+int g6_read_neighbour_list(int cluster_id);
+int g6_get_neighbour_list(int cluster_id, int ipipe, int maxlength, int *n_neighbours,
+                          int neighbour_list[]);
+
+/* ---------------- Part 3: extension API (no GRAPE-6 counterpart) ---------- */
+
+#define G6X_SPLIT 0 /* double-single positions, FP32 pair arithmetic (default) */
+#define G6X_FP64 1  /* plain FP64 pair arithmetic */
+
+/* Precision of subsequent force evaluations. */
+int g6x_set_precision(int prec);
+int g6x_get_precision(void);
+/* Change the i-chunk bound reported by g6_npipes (1 .. 1<<20). */
+int g6x_set_npipes(int npipes);
+/* Last error message ("" if none). */
+const char *g6x_last_error(void);
+
+/* Bulk-load n particles into slots [0, n) from host arrays (replaces n
+   g6_set_j_particle calls); acc/jerk unscaled.  Resets the device run. */
+int g6x_load(int n, const int *ids, const double *mass, const double (*x)[3],
+             const double (*v)[3], const double (*acc)[3], const double (*jerk)[3],
+             const double *t, const double *dt);
+/* Read the device j-state of slots [0, n) back to host arrays (any may be
+   NULL). */
+int g6x_read(int n, double (*x)[3], double (*v)[3], double (*acc)[3], double (*jerk)[3],
+             double *pot, double *t, double *dt, int *nn);
+
+/* Blocking force on ni explicit i-particles (host arrays) against slots
+   [0, nj) predicted to ti.  self_slot[i] (or NULL) is the slot to exclude;
+   nn[i] is a j SLOT (-1 none); nn_r2[i] = r^2 + eps2 of it (FP32); either
+   may be NULL.  Any ni (no npipes bound). */
+int g6x_force(double ti, double eps2, int nj, int ni, const double (*xi)[3],
+              const double (*vi)[3], const int *self_slot, double (*acc)[3],
+              double (*jerk)[3], double *pot, int *nn, float *nn_r2);
+/* Same with all arrays in device memory (no host copies, asynchronous on the
+   library stream unless sync != 0). */
+int g6x_force_dev(double ti, double eps2, int nj, int ni, const double *d_xi,
+                  const double *d_vi, const int *d_self_slot, double *d_acc, double *d_jerk,
+                  double *d_pot, int *d_nn, float *d_nn_r2, int sync);
+/* Force on the device-resident slots d_ilist[0..ni) predicted to ti (i data
+   taken from the predicted j records; self excluded by slot). */
+int g6x_force_slots(double ti, double eps2, int nj, int ni, const int *d_ilist, double *d_acc,
+                    double *d_jerk, double *d_pot, int *d_nn, int sync);
+
+/* Device-resident ph4-style integration of the loaded particles:
+   g6x_run_init  -- forces at t = 0 and initial steps (jdata.cc:503-580),
+   g6x_run       -- block steps (predict all j, force on the block, FP64
+                    corrector + Aarseth step) until system time >= t_end,
+   g6x_energy    -- kinetic and potential energy at the system time,
+   g6x_step_all  -- one shared step of all particles to tnext (the
+                    benchmark step: predict + force on all + correct). */
+int g6x_run_init(double eps2, double eta);
+int g6x_run(double t_end, long long *blocks, double *particle_steps);
+int g6x_energy(double *kinetic, double *potential);
+int g6x_step_all(double tnext);
+/* FP64 corrector + Aarseth step (idata.cc:399-514) applied on the device to
+   the listed slots with the given new acc/jerk (host arrays, [ni][3]);
+   positions/velocities are predicted from the stored state to tnext first
+   (idata.cc:346-365).  Blocking. */
+int g6x_correct(int ni, const int *slots, double tnext, double eta, const double (*acc)[3],
+                const double (*jerk)[3]);
+double g6x_system_time(void);
+
+/* Statistics of the last force call: out[0] predictor ms, out[1] force ms
+   (incl. second pass), out[2] pair interactions, out[3] JL, out[4] nsplit,
+   out[5] grid.x, out[6] predictor bytes, out[7] nj.  Timing is measured
+   with CUDA events only while g6x_timing(1) is set. */
+int g6x_timing(int on);
+int g6x_stats(double out[8]);
+
+/* Device pointers of the predicted j records (for tools) and the stream. */
+void *g6x_stream(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

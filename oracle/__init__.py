@@ -1,0 +1,150 @@
+"""Oracle package -- TEST INFRASTRUCTURE ONLY.
+
+ctypes bindings for
+  * ``liborc.so``   -- the C restatement of ph4's FP64 CPU path (g6_oracle.c),
+  * ``_ref/libph4ref.so`` -- the unmodified ph4 objects built from the
+    reference sources (present only where the reference checkout exists).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may
+import this package, and only as the checker / the timed CPU baseline.
+The shipped library never loads either .so.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_PORT = os.path.join(HERE, "liborc.so")
+_REF = os.path.join(HERE, "_ref", "libph4ref.so")
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_c_int, _c_dbl, _c_long = ctypes.c_int, ctypes.c_double, ctypes.c_long
+
+_port_lib = None
+_ref_lib = None
+
+
+def build_port():
+    subprocess.check_call(["make", "-s", "-C", HERE, "port"])
+
+
+def build_ref(ref_root="/root/reference"):
+    """Compile the unmodified ph4 CPU objects (needs the reference sources)."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}", "-j8"])
+
+
+def port():
+    global _port_lib
+    if _port_lib is None:
+        if not os.path.exists(_PORT):
+            build_port()
+        lib = ctypes.CDLL(_PORT)
+        lib.orc_force.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_int, _dp, _dp,
+                                  _dp, _dp, _dp, _ip, _dp]
+        lib.orc_force.restype = None
+        lib.orc_force_mt.argtypes = [_c_int, _c_int, _dp, _dp, _dp, _c_dbl, _c_int,
+                                     _dp, _dp, _dp, _dp, _dp, _ip, _dp]
+        lib.orc_force_mt.restype = _c_int
+        lib.orc_predict.argtypes = [_c_int, _c_dbl, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        lib.orc_predict.restype = None
+        lib.orc_correct.argtypes = [_c_int, _c_dbl, _c_dbl, _dp, _dp, _dp, _dp, _dp,
+                                    _dp, _dp, _dp]
+        lib.orc_correct.restype = None
+        lib.orc_initial_step.argtypes = [_c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl,
+                                         _dp, _dp, _dp]
+        lib.orc_initial_step.restype = None
+        lib.orc_run.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_dbl, _c_int,
+                                _dp, _dp, _dp, _dp, _dp, _dp, _c_long]
+        lib.orc_run.restype = _c_long
+        _port_lib = lib
+    return _port_lib
+
+
+def ref_available():
+    return os.path.exists(_REF)
+
+
+def ref():
+    global _ref_lib
+    if _ref_lib is None:
+        lib = ctypes.CDLL(_REF)
+        lib.ph4ref_force.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_int, _dp, _dp,
+                                     _dp, _dp, _dp, _ip, _dp]
+        lib.ph4ref_correct.argtypes = [_c_int, _c_dbl, _c_dbl, _dp, _dp, _dp, _dp, _dp,
+                                       _dp, _dp, _dp]
+        lib.ph4ref_run.argtypes = [_c_int, _dp, _ip, _dp, _dp, _c_dbl, _c_dbl, _c_dbl,
+                                   _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        _ref_lib = lib
+    return _ref_lib
+
+
+def _c(a, dt=np.float64):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def force(mass, jpos, jvel, eps2, ipos, ivel, threads=1, lib=None):
+    """FP64 ph4 force (idata.cc:147-237) -> dict(acc, jerk, pot, nn, dnn).
+
+    nn is a j index (-1 when no neighbour)."""
+    mass, jpos, jvel, ipos, ivel = map(_c, (mass, jpos, jvel, ipos, ivel))
+    nj, ni = len(mass), len(ipos)
+    acc = np.zeros((ni, 3)); jerk = np.zeros((ni, 3)); pot = np.zeros(ni)
+    nn = np.zeros(ni, np.int32); dnn = np.zeros(ni)
+    if lib == "ref":
+        ref().ph4ref_force(nj, mass, jpos, jvel, eps2, ni, ipos, ivel, acc, jerk, pot, nn, dnn)
+    elif threads == 1:
+        port().orc_force(nj, mass, jpos, jvel, eps2, ni, ipos, ivel, acc, jerk, pot, nn, dnn)
+    else:
+        port().orc_force_mt(threads, nj, mass, jpos, jvel, eps2, ni, ipos, ivel, acc, jerk,
+                            pot, nn, dnn)
+    return dict(acc=acc, jerk=jerk, pot=pot, nn=nn, dnn=dnn)
+
+
+def predict(t, time, pos, vel, acc, jerk):
+    time, pos, vel, acc, jerk = map(_c, (time, pos, vel, acc, jerk))
+    pp = np.zeros_like(pos); pv = np.zeros_like(vel)
+    port().orc_predict(len(time), t, time, pos, vel, acc, jerk, pp, pv)
+    return pp, pv
+
+
+def correct(tnext, eta, itime, istep, ipos, ivel, old_acc, old_jerk, iacc, ijerk, lib=None):
+    """ph4 corrector + Aarseth step (idata.cc:399-514); returns new arrays."""
+    itime, istep, ipos, ivel = (_c(a).copy() for a in (itime, istep, ipos, ivel))
+    old_acc, old_jerk, iacc, ijerk = map(_c, (old_acc, old_jerk, iacc, ijerk))
+    f = ref().ph4ref_correct if lib == "ref" else port().orc_correct
+    f(len(itime), tnext, eta, itime, istep, ipos, ivel, old_acc, old_jerk, iacc, ijerk)
+    return dict(time=itime, timestep=istep, pos=ipos, vel=ivel)
+
+
+def initial_step(acc, jerk, eta, system_time=0.0, fac=0.0625, limit=0.03125, limitm=8.0):
+    acc, jerk = _c(acc), _c(jerk)
+    ts = np.zeros(len(acc))
+    port().orc_initial_step(len(acc), system_time, eta, fac, limit, limitm, acc, jerk, ts)
+    return ts
+
+
+def run(mass, pos, vel, eps2, eta, t_end, threads=1, lib=None, ids=None, max_blocks=0):
+    """Block-step ph4 run, CPU mode.  Returns final state + E0/E1."""
+    mass, pos, vel = _c(mass), _c(pos).copy(), _c(vel).copy()
+    n = len(mass)
+    acc = np.zeros((n, 3)); jerk = np.zeros((n, 3)); pot = np.zeros(n)
+    time = np.zeros(n); step = np.zeros(n)
+    if lib == "ref":
+        ids = _c(np.arange(1, n + 1) if ids is None else ids, np.int32)
+        stats = np.zeros(5)
+        pos_o = np.zeros_like(pos); vel_o = np.zeros_like(vel)
+        ref().ph4ref_run(n, mass, ids, pos, vel, eps2, eta, t_end, pos_o, vel_o, acc, jerk,
+                         pot, time, step, stats)
+        return dict(pos=pos_o, vel=vel_o, acc=acc, jerk=jerk, pot=pot, time=time,
+                    timestep=step, E0=stats[0], E1=stats[1], total_steps=stats[2],
+                    t=stats[3], blocks=stats[4])
+    stats = np.zeros(4)
+    blocks = port().orc_run(n, mass, pos, vel, eps2, eta, t_end, threads, acc, jerk, pot,
+                            time, step, stats, max_blocks)
+    return dict(pos=pos, vel=vel, acc=acc, jerk=jerk, pot=pot, time=time, timestep=step,
+                E0=stats[0], E1=stats[1], total_steps=stats[2], t=stats[3], blocks=blocks)

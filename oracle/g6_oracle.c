@@ -1,0 +1,374 @@
+/*
+ * g6_oracle.c -- TEST INFRASTRUCTURE ONLY (the oracle).
+ *
+ * A plain-C restatement of AMUSE ph4's FP64 CPU Hermite path, used by the
+ * test-suite, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg
+ * as the checker.  Nothing in the shipped library links, loads or calls this
+ * file; the product (libsapporo.so) has no CPU force path at all.
+ *
+ * Every function follows the reference loop-for-loop so that, compiled with
+ * -O2 -ffp-contract=off, it is bit-identical to the unmodified ph4 objects
+ * (pinned by tests/test_oracle.py against fixtures generated from
+ * the reference build, see oracle/Makefile target `ref`).
+ *
+ *   orc_force          src/amuse_ph4/src/idata.cc:147-237   (get_partial_acc_and_jerk)
+ *   orc_predict        src/amuse_ph4/src/jdata.cc:710-750   (predict_all)
+ *   orc_correct        src/amuse_ph4/src/idata.cc:399-514   (correct + Aarseth step)
+ *   orc_initial_step   src/amuse_ph4/src/jdata.cc:503-564   (set_initial_timestep)
+ *   orc_run            src/amuse_ph4/src/jdata.cc:752-795 + idata.cc:832-881
+ *                      (block-step loop of interface.cc:614-711, CPU mode,
+ *                      manage_encounters = 0)
+ *   orc_hermite_fixed  src/amuse_hermite/interface.cc:266-281,387-552
+ *                      (shared fixed-step Hermite, test_mode)
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_TINY (1.0 / 4503599627370496.0) /* 2^-52, stdinc.h:33 */
+#define ORC_INF 1.0e300                     /* stdinc.h:32 */
+
+/* ------------------------------------------------------------------ */
+/* Force: idata::get_partial_acc_and_jerk (idata.cc:147-237).          */
+/* j-arrays are the predicted j-system; i-arrays the predicted i's.     */
+/* nn[i] is a j index (-1 if none); dnn[i] = sqrt(min r2).             */
+/* ------------------------------------------------------------------ */
+static void force_range(int i0, int i1, int nj, const double *mass,
+                        const double *jpos, const double *jvel, double eps2,
+                        const double *ipos, const double *ivel, double *acc,
+                        double *jerk, double *pot, int *nn, double *dnn) {
+  double dx[3], dv[3], r2, xv, r2i, ri, mri, mr3i, a3;
+  for (int i = i0; i < i1; i++) {
+    double lpot = 0, ldnn = ORC_INF;
+    int lnn = -1;
+    double la[3] = {0, 0, 0}, lj[3] = {0, 0, 0};
+    for (int j = 0; j < nj; j++) {
+      if (mass[j] > ORC_TINY) {
+        r2 = xv = 0;
+        for (int k = 0; k < 3; k++) {
+          dx[k] = jpos[3 * j + k] - ipos[3 * i + k];
+          dv[k] = jvel[3 * j + k] - ivel[3 * i + k];
+          r2 += dx[k] * dx[k];
+          xv += dx[k] * dv[k];
+        }
+        r2i = 1 / (r2 + eps2 + ORC_TINY);
+        ri = sqrt(r2i);
+        mri = mass[j] * ri;
+        mr3i = mri * r2i;
+        a3 = -3 * xv * r2i;
+        if (r2 > ORC_TINY) {
+          lpot -= mri;
+          if (r2 < ldnn) {
+            ldnn = r2;
+            lnn = j;
+          }
+        }
+        for (int k = 0; k < 3; k++) {
+          la[k] += mr3i * dx[k];
+          lj[k] += mr3i * (dv[k] + a3 * dx[k]);
+        }
+      }
+    }
+    pot[i] = lpot;
+    for (int k = 0; k < 3; k++) {
+      acc[3 * i + k] = la[k];
+      jerk[3 * i + k] = lj[k];
+    }
+    if (nn) nn[i] = lnn;
+    if (dnn) dnn[i] = sqrt(ldnn);
+  }
+}
+
+void orc_force(int nj, const double *mass, const double *jpos,
+               const double *jvel, double eps2, int ni, const double *ipos,
+               const double *ivel, double *acc, double *jerk, double *pot,
+               int *nn, double *dnn) {
+  force_range(0, ni, nj, mass, jpos, jvel, eps2, ipos, ivel, acc, jerk, pot,
+              nn, dnn);
+}
+
+/* Multi-threaded wrapper: k threads over disjoint i-ranges, each running
+   the same scalar loop (the reference has no threading; this is the
+   all-cores CPU baseline). */
+struct force_job {
+  int i0, i1, nj;
+  const double *mass, *jpos, *jvel, *ipos, *ivel;
+  double eps2;
+  double *acc, *jerk, *pot, *dnn;
+  int *nn;
+};
+
+static void *force_thread(void *arg) {
+  struct force_job *f = (struct force_job *)arg;
+  force_range(f->i0, f->i1, f->nj, f->mass, f->jpos, f->jvel, f->eps2,
+              f->ipos, f->ivel, f->acc, f->jerk, f->pot, f->nn, f->dnn);
+  return NULL;
+}
+
+int orc_force_mt(int nthreads, int nj, const double *mass, const double *jpos,
+                 const double *jvel, double eps2, int ni, const double *ipos,
+                 const double *ivel, double *acc, double *jerk, double *pot,
+                 int *nn, double *dnn) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > ni) nthreads = ni > 0 ? ni : 1;
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+  struct force_job *jobs =
+      (struct force_job *)malloc(sizeof(struct force_job) * nthreads);
+  if (!th || !jobs) {
+    free(th);
+    free(jobs);
+    return -1;
+  }
+  int started = 0;
+  for (int t = 0; t < nthreads; t++) {
+    struct force_job f = {(int)((long long)ni * t / nthreads),
+                          (int)((long long)ni * (t + 1) / nthreads),
+                          nj, mass, jpos, jvel, ipos, ivel, eps2,
+                          acc, jerk, pot, dnn, nn};
+    jobs[t] = f;
+    if (pthread_create(&th[t], NULL, force_thread, &jobs[t]) == 0)
+      started = t + 1;
+    else
+      break;
+  }
+  for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+  /* Any range that could not get a thread runs on this one. */
+  for (int t = started; t < nthreads; t++) force_thread(&jobs[t]);
+  free(th);
+  free(jobs);
+  return nthreads;
+}
+
+/* ------------------------------------------------------------------ */
+/* Predictor: jdata::predict_all (jdata.cc:710-750); identical to the   */
+/* GPU-mode i-predictor idata::predict (idata.cc:346-365).              */
+/* ------------------------------------------------------------------ */
+void orc_predict(int n, double t, const double *time, const double *pos,
+                 const double *vel, const double *acc, const double *jerk,
+                 double *pred_pos, double *pred_vel) {
+  for (int j = 0; j < n; j++) {
+    double dt = t - time[j];
+    if (dt == 0) {
+      for (int k = 0; k < 3; k++) {
+        pred_pos[3 * j + k] = pos[3 * j + k];
+        pred_vel[3 * j + k] = vel[3 * j + k];
+      }
+    } else {
+      for (int k = 0; k < 3; k++) {
+        pred_pos[3 * j + k] =
+            pos[3 * j + k] +
+            dt * (vel[3 * j + k] +
+                  0.5 * dt * (acc[3 * j + k] + dt * jerk[3 * j + k] / 3));
+        pred_vel[3 * j + k] =
+            vel[3 * j + k] + dt * (acc[3 * j + k] + 0.5 * dt * jerk[3 * j + k]);
+      }
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Corrector + Aarseth step: idata::correct (idata.cc:399-514).         */
+/* ipos/ivel hold the predicted values on entry, corrected on exit.     */
+/* itime/itimestep are updated in place.                                */
+/* ------------------------------------------------------------------ */
+void orc_correct(int ni, double tnext, double eta, double *itime,
+                 double *itimestep, double *ipos, double *ivel,
+                 const double *old_acc, const double *old_jerk,
+                 const double *iacc, const double *ijerk) {
+  for (int i = 0; i < ni; i++) {
+    double dt = tnext - itime[i];
+    double dt2 = dt * dt;
+    double a2 = 0, j2 = 0, k2 = 0, l2 = 0;
+    for (int k = 0; k < 3; k++) {
+      double alpha = -3 * (old_acc[3 * i + k] - iacc[3 * i + k]) -
+                     dt * (2 * old_jerk[3 * i + k] + ijerk[3 * i + k]);
+      double beta = 2 * (old_acc[3 * i + k] - iacc[3 * i + k]) +
+                    dt * (old_jerk[3 * i + k] + ijerk[3 * i + k]);
+      ipos[3 * i + k] += (alpha / 12 + beta / 20) * dt2;
+      ivel[3 * i + k] += (alpha / 3 + beta / 4) * dt;
+      a2 += pow(iacc[3 * i + k], 2);
+      j2 += pow(dt * ijerk[3 * i + k], 2);
+      k2 += pow(2 * alpha, 2);
+      l2 += pow(6 * beta, 2);
+    }
+    double newstep = eta * dt * sqrt((sqrt(a2 * k2) + j2) / (sqrt(j2 * l2) + k2));
+    int exponent;
+    double oldstep2 = itimestep[i] / (2 * frexp(itimestep[i], &exponent));
+    while (fmod(tnext, oldstep2) != 0) oldstep2 /= 2;
+    if (newstep < oldstep2) {
+      newstep = oldstep2 / 2;
+    } else {
+      double t2 = 2 * oldstep2;
+      if (newstep >= t2 && fmod(tnext, t2) == 0)
+        newstep = t2;
+      else
+        newstep = oldstep2;
+    }
+    itime[i] = tnext;
+    itimestep[i] = newstep;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Initial step: jdata::set_initial_timestep (jdata.cc:503-564), with   */
+/* all steps forced to zero first (force_initial_timestep, :566-580).   */
+/* ------------------------------------------------------------------ */
+static int cmp_double(const void *a, const void *b) {
+  double x = *(const double *)a, y = *(const double *)b;
+  return (x > y) - (x < y);
+}
+
+void orc_initial_step(int n, double system_time, double eta, double fac,
+                      double limit, double limitm, const double *acc,
+                      const double *jerk, double *timestep) {
+  for (int j = 0; j < n; j++) {
+    double a2 = 0, j2 = 0;
+    for (int k = 0; k < 3; k++) {
+      a2 += pow(acc[3 * j + k], 2);
+      j2 += pow(jerk[3 * j + k], 2);
+    }
+    double firststep;
+    if (eta == 0.0)
+      firststep = limit;
+    else if (a2 == 0.0 || j2 == 0.0)
+      firststep = fac * eta;
+    else
+      firststep = fac * eta * sqrt(a2 / j2);
+    if (isnan(firststep)) firststep = fac * eta;
+    int exponent;
+    firststep /= 2 * frexp(firststep, &exponent);
+    while (fmod(system_time, firststep) != 0) firststep /= 2;
+    while (firststep > limit) firststep /= 2;
+    timestep[j] = firststep;
+  }
+  if (limitm > 0 && n > 0) {
+    double *tmp = (double *)malloc(sizeof(double) * n);
+    memcpy(tmp, timestep, sizeof(double) * n);
+    qsort(tmp, n, sizeof(double), cmp_double);
+    double dtmax = limitm * tmp[n / 2];
+    free(tmp);
+    for (int j = 0; j < n; j++)
+      while (timestep[j] > dtmax) timestep[j] /= 2;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Energy: jdata::get_energy(false) (jdata.cc:582-680): pot via the     */
+/* force path at system_time, kin from predicted velocities.            */
+/* ------------------------------------------------------------------ */
+static double energy_at(int n, double t, const double *mass, const double *time,
+                        const double *pos, const double *vel, const double *acc,
+                        const double *jerk, double eps2, double *scratch,
+                        int nthreads) {
+  double *pp = scratch, *pv = scratch + 3 * n, *a = scratch + 6 * n,
+         *jk = scratch + 9 * n, *pot = scratch + 12 * n;
+  orc_predict(n, t, time, pos, vel, acc, jerk, pp, pv);
+  orc_force_mt(nthreads, n, mass, pp, pv, eps2, n, pp, pv, a, jk, pot, NULL,
+               NULL);
+  double pot2 = 0, kin2 = 0;
+  for (int i = 0; i < n; i++) pot2 += mass[i] * pot[i];
+  for (int j = 0; j < n; j++) {
+    double v2 = 0;
+    for (int k = 0; k < 3; k++) v2 += pow(pv[3 * j + k], 2);
+    kin2 += mass[j] * v2;
+  }
+  return pot2 / 2 + kin2 / 2;
+}
+
+/* ------------------------------------------------------------------ */
+/* Full block-step run, CPU mode, one process, manage_encounters = 0:  */
+/* commit_particles (interface.cc:317-347) then evolve_model            */
+/* (interface.cc:614-711) -> jdata::advance (jdata.cc:752-795) ->        */
+/* idata::advance (idata.cc:832-881).  The block is found with the O(N) */
+/* search of idata::set_list (idata.cc:796-806, the "#if 0" branch);     */
+/* it selects the same set as the list scheduler, and each particle's   */
+/* update is independent of the order within the block.                 */
+/* State arrays are updated in place; returns block steps taken.        */
+/* stats (optional, length 4): E0, E1, total particle steps, t_final.   */
+/* ------------------------------------------------------------------ */
+long orc_run(int n, const double *mass, double *pos, double *vel, double eps2,
+             double eta, double t_end, int nthreads, double *acc, double *jerk,
+             double *pot, double *time, double *timestep, double *stats,
+             long max_blocks) {
+  double *pp = (double *)malloc(sizeof(double) * 3 * n);
+  double *pv = (double *)malloc(sizeof(double) * 3 * n);
+  double *scratch = (double *)malloc(sizeof(double) * 13 * n);
+  int *ilist = (int *)malloc(sizeof(int) * n);
+  double *ip = (double *)malloc(sizeof(double) * 3 * n);
+  double *iv = (double *)malloc(sizeof(double) * 3 * n);
+  double *oa = (double *)malloc(sizeof(double) * 3 * n);
+  double *oj = (double *)malloc(sizeof(double) * 3 * n);
+  double *ia = (double *)malloc(sizeof(double) * 3 * n);
+  double *ij = (double *)malloc(sizeof(double) * 3 * n);
+  double *ipot = (double *)malloc(sizeof(double) * n);
+  double *it = (double *)malloc(sizeof(double) * n);
+  double *its = (double *)malloc(sizeof(double) * n);
+  double system_time = 0;
+  /* commit_particles: initialize_arrays (time = 0, acc = jerk = 0),
+     predict_all(0, true), idata::setup -> forces on all, scatter. */
+  for (int j = 0; j < n; j++) {
+    time[j] = 0;
+    timestep[j] = 0;
+  }
+  memset(acc, 0, sizeof(double) * 3 * n);
+  memset(jerk, 0, sizeof(double) * 3 * n);
+  orc_predict(n, 0.0, time, pos, vel, acc, jerk, pp, pv);
+  orc_force_mt(nthreads, n, mass, pp, pv, eps2, n, pp, pv, acc, jerk, pot,
+               NULL, NULL);
+  /* force_initial_timestep(0.0625, 0.03125, 8.0) (interface.cc:29-31). */
+  orc_initial_step(n, 0.0, eta, 0.0625, 0.03125, 8.0, acc, jerk, timestep);
+  double e0 = energy_at(n, system_time, mass, time, pos, vel, acc, jerk, eps2,
+                        scratch, nthreads);
+  long blocks = 0;
+  double steps = 0;
+  while (system_time < t_end && (max_blocks <= 0 || blocks < max_blocks)) {
+    double tnext = ORC_INF;
+    for (int j = 0; j < n; j++)
+      if (time[j] + timestep[j] < tnext) tnext = time[j] + timestep[j];
+    int ni = 0;
+    for (int j = 0; j < n; j++)
+      if (time[j] + timestep[j] == tnext) ilist[ni++] = j;
+    orc_predict(n, tnext, time, pos, vel, acc, jerk, pp, pv);
+    for (int i = 0; i < ni; i++) {
+      int j = ilist[i];
+      it[i] = time[j];
+      its[i] = timestep[j];
+      for (int k = 0; k < 3; k++) {
+        ip[3 * i + k] = pp[3 * j + k];
+        iv[3 * i + k] = pv[3 * j + k];
+        oa[3 * i + k] = acc[3 * j + k];
+        oj[3 * i + k] = jerk[3 * j + k];
+      }
+    }
+    orc_force_mt(nthreads, n, mass, pp, pv, eps2, ni, ip, iv, ia, ij, ipot,
+                 NULL, NULL);
+    orc_correct(ni, tnext, eta, it, its, ip, iv, oa, oj, ia, ij);
+    for (int i = 0; i < ni; i++) {
+      int j = ilist[i];
+      pot[j] = ipot[i];
+      time[j] = it[i];
+      timestep[j] = its[i];
+      for (int k = 0; k < 3; k++) {
+        pos[3 * j + k] = ip[3 * i + k];
+        vel[3 * j + k] = iv[3 * i + k];
+        acc[3 * j + k] = ia[3 * i + k];
+        jerk[3 * j + k] = ij[3 * i + k];
+      }
+    }
+    blocks++;
+    steps += ni;
+    system_time = tnext;
+  }
+  double e1 = energy_at(n, system_time, mass, time, pos, vel, acc, jerk, eps2,
+                        scratch, nthreads);
+  if (stats) {
+    stats[0] = e0;
+    stats[1] = e1;
+    stats[2] = steps;
+    stats[3] = system_time;
+  }
+  free(pp); free(pv); free(scratch); free(ilist); free(ip); free(iv);
+  free(oa); free(oj); free(ia); free(ij); free(ipot); free(it); free(its);
+  return blocks;
+}

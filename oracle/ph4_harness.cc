@@ -1,0 +1,176 @@
+// ph4_harness.cc -- TEST INFRASTRUCTURE ONLY.
+//
+// A small C-ABI driver around the UNMODIFIED ph4 objects (compiled from the
+// reference sources by oracle/Makefile into oracle/_ref/libph4ref.so).  It
+// drives jdata/idata/scheduler the way the ph4 worker does
+// (src/amuse_ph4/interface.cc:82-119 initialize_code, :317-347
+// commit_particles, :614-711 evolve_model), in CPU mode (no -DGPU), one
+// process (-DNOMPI), with manage_encounters = 0 so that eps2 = 0 runs never
+// enter resolve_encounter (jdata.cc:859-863).  It is used only to generate
+// golden fixtures and to pin the C restatement in g6_oracle.c.
+#include <cstdio>
+#include <cstring>
+#include <iostream>
+
+#include "idata.h"
+#include "jdata.h"
+#include "scheduler.h"
+#include "stopcond.h"
+
+extern "C" {
+
+// Force only: the j-system is given already predicted; ph4's
+// idata::get_partial_acc_and_jerk (idata.cc:147-237) runs on it unchanged.
+// nn[i] is a j index, dnn[i] the nearest-neighbour distance.
+int ph4ref_force(int nj, const double *mass, const double *jpos,
+                 const double *jvel, double eps2, int ni, const double *ipos,
+                 const double *ivel, double *acc, double *jerk, double *pot,
+                 int *nn, double *dnn) {
+  static jdata *jd = NULL;
+  static idata *id = NULL;
+  static int cap_j = 0;
+  if (!jd) {
+    jd = new jdata;
+    std::streambuf *old = std::cout.rdbuf(NULL);
+    id = new idata(NULL);  // prints a notice about the NULL jdata pointer
+    std::cout.rdbuf(old);
+  }
+  if (nj > cap_j) {
+    // Leaked on purpose: jdata::cleanup() expects arrays made by
+    // add_particle(); this harness owns only what it touches.
+    jd->mass = new real[nj];
+    jd->pred_pos = new real[nj][3];
+    jd->pred_vel = new real[nj][3];
+    cap_j = nj;
+  }
+  jd->nj = nj;
+  jd->eps2 = eps2;
+  for (int j = 0; j < nj; j++) {
+    jd->mass[j] = mass[j];
+    for (int k = 0; k < 3; k++) {
+      jd->pred_pos[j][k] = jpos[3 * j + k];
+      jd->pred_vel[j][k] = jvel[3 * j + k];
+    }
+  }
+  id->jdat = jd;
+  id->set_ni(ni);
+  id->ni = ni;
+  for (int i = 0; i < ni; i++) {
+    id->ilist[i] = i;
+    for (int k = 0; k < 3; k++) {
+      id->ipos[i][k] = ipos[3 * i + k];
+      id->ivel[i][k] = ivel[3 * i + k];
+    }
+  }
+  id->get_partial_acc_and_jerk();
+  for (int i = 0; i < ni; i++) {
+    pot[i] = id->ipot[i];
+    nn[i] = id->inn[i];
+    dnn[i] = id->idnn[i];
+    for (int k = 0; k < 3; k++) {
+      acc[3 * i + k] = id->iacc[i][k];
+      jerk[3 * i + k] = id->ijerk[i][k];
+    }
+  }
+  return 0;
+}
+
+// Corrector + Aarseth step on a list, through ph4's idata::correct
+// (idata.cc:399-514).  ipos/ivel: predicted in, corrected out.
+int ph4ref_correct(int ni, double tnext, double eta, double *itime,
+                   double *itimestep, double *ipos, double *ivel,
+                   const double *old_acc, const double *old_jerk,
+                   const double *iacc, const double *ijerk) {
+  static jdata *jd = NULL;
+  static idata *id = NULL;
+  if (!jd) {
+    jd = new jdata;
+    std::streambuf *old = std::cout.rdbuf(NULL);
+    id = new idata(NULL);
+    std::cout.rdbuf(old);
+  }
+  jd->eta = eta;
+  id->jdat = jd;
+  id->set_ni(ni);
+  id->ni = ni;
+  for (int i = 0; i < ni; i++) {
+    id->itime[i] = itime[i];
+    id->itimestep[i] = itimestep[i];
+    for (int k = 0; k < 3; k++) {
+      id->ipos[i][k] = ipos[3 * i + k];
+      id->ivel[i][k] = ivel[3 * i + k];
+      id->old_acc[i][k] = old_acc[3 * i + k];
+      id->old_jerk[i][k] = old_jerk[3 * i + k];
+      id->iacc[i][k] = iacc[3 * i + k];
+      id->ijerk[i][k] = ijerk[3 * i + k];
+    }
+  }
+  id->correct(tnext);
+  for (int i = 0; i < ni; i++) {
+    itime[i] = id->itime[i];
+    itimestep[i] = id->itimestep[i];
+    for (int k = 0; k < 3; k++) {
+      ipos[3 * i + k] = id->ipos[i][k];
+      ivel[3 * i + k] = id->ivel[i][k];
+    }
+  }
+  return 0;
+}
+
+// Full run: initialize_code + add_particle + commit_particles +
+// evolve_model(t_end), CPU mode.  State is returned in j order (the order
+// particles were added).  stats: E0, E1, total_steps, system_time,
+// block_steps.
+int ph4ref_run(int n, const double *mass, const int *ids, const double *pos,
+               const double *vel, double eps2, double eta, double t_end,
+               double *pos_out, double *vel_out, double *acc_out,
+               double *jerk_out, double *pot_out, double *time_out,
+               double *step_out, double *stats) {
+  std::streambuf *old = std::cout.rdbuf(NULL);  // ph4 is chatty on cout
+  jdata *jd = new jdata;
+  jd->setup_gpu();
+  jd->system_time = 0;
+  jd->sync_time = 0;
+  jd->set_manage_encounters(0);
+  jd->eps2 = eps2;
+  jd->eta = eta;
+  for (int j = 0; j < n; j++) {
+    vec p(pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]);
+    vec v(vel[3 * j], vel[3 * j + 1], vel[3 * j + 2]);
+    jd->add_particle(mass[j], 0.0, p, v, ids[j]);
+  }
+  // commit_particles (interface.cc:317-347); sync_times() is a no-op here.
+  jd->initialize_arrays();
+  idata *id = new idata(jd);
+  jd->force_initial_timestep(0.0625, 0.03125, 8.0);
+  scheduler *s = new scheduler(jd);
+  double e0 = jd->get_energy();
+  // evolve_model (interface.cc:614-711), no force_sync.
+  while (jd->system_time < t_end)
+    if (jd->advance_and_check_encounter()) break;
+  double e1 = jd->get_energy();
+  std::cout.rdbuf(old);
+  for (int j = 0; j < n; j++) {
+    pot_out[j] = jd->pot[j];
+    time_out[j] = jd->time[j];
+    step_out[j] = jd->timestep[j];
+    for (int k = 0; k < 3; k++) {
+      pos_out[3 * j + k] = jd->pos[j][k];
+      vel_out[3 * j + k] = jd->vel[j][k];
+      acc_out[3 * j + k] = jd->acc[j][k];
+      jerk_out[3 * j + k] = jd->jerk[j][k];
+    }
+  }
+  stats[0] = e0;
+  stats[1] = e1;
+  stats[2] = jd->total_steps;
+  stats[3] = jd->system_time;
+  stats[4] = jd->block_steps;
+  (void)s;
+  (void)id;
+  // jdata/idata/scheduler are leaked: ph4's cleanup paths assume the
+  // worker process exits afterwards.
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,131 @@
+"""Generate the golden fixtures in this directory.
+
+Runs in the development container only (it needs the reference checkout):
+  * AMUSE's own IC generators (src/amuse/ic/plummer.py, salpeter.py),
+    imported from the reference tree, give the inputs;
+  * the unmodified ph4 CPU objects, compiled by ``make -C oracle ref`` into
+    oracle/_ref/libph4ref.so, give the outputs (force: idata.cc:147-237,
+    corrector: idata.cc:399-514, full block-step run: interface.cc:317-711).
+
+Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+"""
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+
+def amuse_plummer(n, do_scale):
+    from amuse.ic.plummer import new_plummer_model
+    from amuse.units import nbody_system as nb
+    p = new_plummer_model(n, do_scale=do_scale)
+    pos = np.stack([p.x.value_in(nb.length), p.y.value_in(nb.length), p.z.value_in(nb.length)], 1)
+    vel = np.stack([p.vx.value_in(nb.speed), p.vy.value_in(nb.speed), p.vz.value_in(nb.speed)], 1)
+    return p.mass.value_in(nb.mass), pos, vel
+
+
+def amuse_salpeter(n, mmin, mmax):
+    from amuse.ic.salpeter import new_powerlaw_mass_distribution_nbody
+    from amuse.units import nbody_system as nb
+    m = new_powerlaw_mass_distribution_nbody(n, alpha=-2.35, mass_min=mmin | nb.mass,
+                                             mass_max=mmax | nb.mass)
+    return m.value_in(nb.mass)
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **arrays)
+    print("wrote", name, os.path.getsize(path), "bytes")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    sys.path.insert(0, os.path.join(args.ref, "src"))
+    import oracle
+    oracle.build_ref(args.ref)
+
+    # 1. IC generators (pins amuse_gb300/ic.py).
+    np.random.seed(1)
+    m0, x0, v0 = amuse_plummer(256, False)
+    np.random.seed(1)
+    m1, x1, v1 = amuse_plummer(256, True)
+    np.random.seed(3)
+    ms = amuse_salpeter(512, 0.1, 100.0)
+    save("ic_amuse.npz", plummer_mass=m0, plummer_pos=x0, plummer_vel=v0,
+         scaled_mass=m1, scaled_pos=x1, scaled_vel=v1, salpeter_mass=ms)
+
+    # 2. Force on all i, C1 shape: N=1024 scaled Plummer, eps2=1e-4.
+    np.random.seed(1)
+    m, x, v = amuse_plummer(1024, True)
+    f = oracle.force(m, x, v, 1e-4, x, v, lib="ref")
+    save("force_plummer1024_eps1e-4.npz", mass=m, pos=x, vel=v, eps2=1e-4, **f)
+
+    # 3. Force, C2 shape at reduced N: Salpeter masses 0.1..100, re-scaled,
+    #    eps2=1e-6; a random i-subset whose positions are offset from the
+    #    j-set (as after an i-prediction), plus zero-offset members.
+    np.random.seed(2)
+    m, x, v = amuse_plummer(4096, False)
+    m = amuse_salpeter(4096, 0.1, 100.0)
+    from amuse_gb300 import ic as myic
+    myic.move_to_center(m, x, v)
+    myic.scale_to_standard(m, x, v)
+    rng = np.random.RandomState(7)
+    isel = rng.choice(4096, 700, replace=False)
+    ipos = x[isel].copy()
+    ivel = v[isel].copy()
+    ipos[:350] += rng.normal(scale=1e-7, size=(350, 3))
+    f = oracle.force(m, x, v, 1e-6, ipos, ivel, lib="ref")
+    save("force_salpeter4096_eps1e-6.npz", mass=m, pos=x, vel=v, eps2=1e-6, isel=isel,
+         ipos=ipos, ivel=ivel, **f)
+
+    # 4. Unsoftened force (eps2 = 0), N=128, plus a zero-mass j and a
+    #    duplicated position (excluded from pot/nn by the r2 > 2^-52 rule).
+    np.random.seed(4)
+    m, x, v = amuse_plummer(128, True)
+    m = m.copy()
+    m[5] = 0.0
+    f = oracle.force(m, x, v, 0.0, x, v, lib="ref")
+    save("force_plummer128_eps0.npz", mass=m, pos=x, vel=v, eps2=0.0, **f)
+
+    # 5. Corrector + Aarseth step on states from a short run.
+    np.random.seed(5)
+    m, x, v = amuse_plummer(512, True)
+    r = oracle.run(m, x, v, 1e-4, 0.01, 0.0625, lib="ref")
+    rng = np.random.RandomState(11)
+    old_acc = r["acc"]
+    old_jerk = r["jerk"]
+    ts = r["timestep"]
+    tnext = r["t"] + np.min(ts)
+    new_acc = old_acc + rng.normal(scale=1e-3, size=old_acc.shape) * np.abs(old_acc)
+    new_jerk = old_jerk + rng.normal(scale=1e-2, size=old_jerk.shape) * np.abs(old_jerk)
+    itime = np.full(512, tnext) - ts
+    c = oracle.correct(tnext, 0.01, itime, ts, r["pos"], r["vel"], old_acc, old_jerk,
+                       new_acc, new_jerk, lib="ref")
+    save("correct512.npz", tnext=tnext, eta=0.01, itime=itime, istep=ts, ipos=r["pos"],
+         ivel=r["vel"], old_acc=old_acc, old_jerk=old_jerk, iacc=new_acc, ijerk=new_jerk,
+         out_time=c["time"], out_step=c["timestep"], out_pos=c["pos"], out_vel=c["vel"])
+
+    # 6. Full block-step runs through the unmodified ph4 loop.
+    #    a) C1: N=1024 scaled Plummer, eps2=1e-4, eta=0.01, to t=1 (seed 1).
+    np.random.seed(1)
+    m, x, v = amuse_plummer(1024, True)
+    r = oracle.run(m, x, v, 1e-4, 0.01, 1.0, lib="ref")
+    save("run_plummer1024_t1.npz", mass=m, pos0=x, vel0=v, eps2=1e-4, eta=0.01, t_end=1.0,
+         **{k: np.asarray(r[k]) for k in r})
+    #    b) a short unsoftened-ish run (eps2=1e-6), N=256, to t=0.125.
+    np.random.seed(6)
+    m, x, v = amuse_plummer(256, True)
+    r = oracle.run(m, x, v, 1e-6, 0.01, 0.125, lib="ref")
+    save("run_plummer256_eps1e-6.npz", mass=m, pos0=x, vel0=v, eps2=1e-6, eta=0.01,
+         t_end=0.125, **{k: np.asarray(r[k]) for k in r})
+
+
+if __name__ == "__main__":
+    main()

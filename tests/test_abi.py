@@ -1,0 +1,95 @@
+"""The C ABI boundary, checked without a GPU: the library builds, loads and
+exports every function include/g6.h declares; host-side argument checks
+return error codes.  No kernel is launched here."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+import amuse_gb300 as ag
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "g6.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?(?:int|void|double|char)\s*\*?\s*(\w+)\s*\(",
+                                 src, flags=re.M)))
+
+
+def exported(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True,
+                         check=True).stdout
+    return {line.split()[-1]: line.split()[-2] for line in out.splitlines() if line.strip()}
+
+
+def test_header_lists_the_16_grape6_symbols():
+    fns = declared_functions()
+    for s in ag.ABI_SYMBOLS:
+        assert s in fns
+    assert len(ag.ABI_SYMBOLS) == 16
+
+
+def test_every_declared_symbol_is_exported(lib_built):
+    syms = exported(ag.LIB_PATH)
+    missing = [f for f in declared_functions() if f not in syms]
+    assert not missing, missing
+    # by-value forms are weak so that ph4's grape.cc copies take precedence
+    for s in ag.BYVALUE_SYMBOLS:
+        assert syms[s] in ("W", "V"), (s, syms[s])
+    for s in ag.ABI_SYMBOLS + ag.EXT_SYMBOLS:
+        assert syms[s] == "T", s
+
+
+def test_library_loads_and_binds(lib_built):
+    lib = ag.load()
+    for s in ag.ABI_SYMBOLS + ag.BYVALUE_SYMBOLS + ag.EXT_SYMBOLS:
+        assert hasattr(lib, s)
+    drv = ag.driver()
+    for s in ("drv_load", "drv_update", "drv_force"):
+        assert hasattr(drv, s)
+
+
+def test_no_cpu_force_path_in_library(lib_built):
+    # The product library must not carry the oracle's symbols.
+    syms = exported(ag.LIB_PATH)
+    assert not any(s.startswith(("orc_", "ph4ref_")) for s in syms)
+
+
+def test_calls_before_open_fail_cleanly(lib_built):
+    lib = ag.load()
+    if lib.g6x_get_precision() is None:
+        pytest.skip()
+    ti = ctypes.c_double(0.0)
+    cid = ctypes.c_int(0)
+    # not opened in this process (no GPU here): negative code, no crash
+    if os.environ.get("CUDA_VISIBLE_DEVICES", None) == "" or not _has_gpu():
+        assert lib.g6_set_ti_(ctypes.byref(cid), ctypes.byref(ti)) == -1
+        assert lib.g6_open_(ctypes.byref(cid)) in (-5, -3)
+        assert lib.g6_npipes_() == 16384
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def test_driver_ffi_stub_compiles(tmp_path, lib_built):
+    """The binding a ph4 maintainer adds: grape.cc's by-value calls resolve
+    against libsapporo.so with nothing but the header and -lsapporo."""
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include "g6.h"\n'
+        "int main(void){ int id=0; double t=0; if (g6_open(0)) return 0;\n"
+        " g6_set_ti_(&id,&t); return g6_npipes() > 0 ? 0 : 1; }\n")
+    exe = tmp_path / "caller"
+    subprocess.run(["gcc", str(src), "-I", os.path.dirname(HEADER), "-L", ag.LIB_DIR,
+                    "-lsapporo", "-Wl,-rpath," + ag.LIB_DIR, "-o", str(exe)], check=True)
+    assert exe.exists()

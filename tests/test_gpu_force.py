@@ -1,0 +1,251 @@
+"""GPU parity of the force path through the C ABI, against the oracle.
+
+Tolerances (stated per quantity, split precision):
+  acc  : per-particle relative error |da|/|a| <= 1e-6 at p99, <= 1e-5 max
+  pot  : relative error <= 1e-6 max
+  jerk : relative error <= 1e-5 at p99 (FP32 velocities), reported
+  nn   : identical ids except at distance ties (FP64 r^2 within 1e-5 rel.)
+FP64 precision: acc/jerk/pot relative error <= 1e-12.
+"""
+import numpy as np
+import pytest
+
+import amuse_gb300 as ag
+import oracle
+from amuse_gb300 import ic
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+TOL = {ag.SPLIT: dict(acc99=1e-6, accmax=1e-5, pot=1e-6, jerk99=1e-5),
+       ag.FP64: dict(acc99=1e-12, accmax=1e-12, pot=1e-12, jerk99=1e-12)}
+
+
+def vrel(a, b):
+    return np.linalg.norm(a - b, axis=-1) / np.maximum(np.linalg.norm(b, axis=-1), 1e-300)
+
+
+def check_force(out, ref, prec, jpos=None, ipos=None, nn_is_id=False, label=""):
+    t = TOL[prec]
+    ea = vrel(out["acc"], ref["acc"])
+    ej = vrel(out["jerk"], ref["jerk"])
+    ep = np.abs(out["pot"] - ref["pot"]) / np.abs(ref["pot"])
+    print(f"{label} prec={prec} acc p50={np.median(ea):.2e} p99={np.percentile(ea, 99):.2e} "
+          f"max={ea.max():.2e} | jerk p99={np.percentile(ej, 99):.2e} max={ej.max():.2e} | "
+          f"pot max={ep.max():.2e}")
+    assert np.percentile(ea, 99) <= t["acc99"]
+    assert ea.max() <= t["accmax"]
+    assert ep.max() <= t["pot"]
+    assert np.percentile(ej, 99) <= t["jerk99"]
+    if "nn" in out and jpos is not None:
+        got = out["nn"] - (1 if nn_is_id else 0)
+        want = ref["nn"]
+        bad = np.nonzero(got != want)[0]
+        for i in bad:
+            assert got[i] >= 0
+            d_got = np.sum((jpos[got[i]] - ipos[i]) ** 2)
+            d_want = np.sum((jpos[want[i]] - ipos[i]) ** 2)
+            assert abs(d_got - d_want) <= 1e-5 * d_want, (i, got[i], want[i], d_got, d_want)
+        return len(bad)
+    return 0
+
+
+@pytest.fixture(params=[ag.SPLIT, ag.FP64], ids=["split", "fp64"])
+def prec(request, g6):
+    g6.set_precision(request.param)
+    yield request.param
+    g6.set_precision(ag.SPLIT)
+
+
+def test_force_c1_golden_via_g6_api(g6, prec):
+    """Config-1 inputs through g6_set_j_particle + chunked g6calc calls."""
+    g = golden("force_plummer1024_eps1e-4.npz")
+    n = len(g["mass"])
+    ids = np.arange(1, n + 1)
+    ag.drive_load(g["mass"], g["pos"], g["vel"], ids=ids)
+    out = ag.drive_force(n, 0.0, 1e-4, ids, g["pos"], g["vel"], want_nn=True)
+    check_force(out, g, prec, g["pos"], g["pos"], nn_is_id=True, label="C1")
+
+
+def test_force_salpeter_offsets(g6, prec):
+    """Config-2 shape (Salpeter masses, eps2=1e-6); half the i-particles are
+    displaced by ~1e-7 (not their j copy: ids outside the j-set)."""
+    g = golden("force_salpeter4096_eps1e-6.npz")
+    n = len(g["mass"])
+    ids = np.arange(1, n + 1)
+    ag.drive_load(g["mass"], g["pos"], g["vel"], ids=ids)
+    iids = g["isel"] + 1
+    iids[:350] = -1 - np.arange(350)
+    out = ag.drive_force(n, 0.0, 1e-6, iids, g["ipos"], g["ivel"], want_nn=True)
+    check_force(out, g, prec, g["pos"], g["ipos"], nn_is_id=True, label="salpeter")
+
+
+def test_force_eps0_zero_mass(g6, prec):
+    g = golden("force_plummer128_eps0.npz")
+    n = len(g["mass"])
+    ids = np.arange(1, n + 1)
+    ag.drive_load(g["mass"], g["pos"], g["vel"], ids=ids)
+    out = ag.drive_force(n, 0.0, 0.0, ids, g["pos"], g["vel"], want_nn=True)
+    # GRAPE semantics: a massless j may be a neighbour (the CPU skips it).
+    keep = (out["nn"] - 1) != 5
+    ref = {k: (g[k][keep] if k != "nn" else g[k][keep]) for k in ("acc", "jerk", "pot", "nn")}
+    got = {k: out[k][keep] for k in ("acc", "jerk", "pot", "nn")}
+    check_force(got, ref, prec, g["pos"], g["pos"][keep], nn_is_id=True, label="eps0")
+
+
+@pytest.mark.parametrize("ni", [1, 2, 3, 7, 32, 100, 255, 256, 511, 512, 1000, 4096])
+def test_force_block_sizes(g6, prec, ni):
+    """Every launch shape (j-lanes 1..128, split-j across CTAs) vs the oracle."""
+    np.random.seed(11)
+    m, x, v = ic.plummer(4096)
+    rng = np.random.RandomState(ni)
+    sel = np.sort(rng.choice(4096, ni, replace=False))
+    g6.load_particles(m, x, v)
+    out = g6.force(0.0, 1e-4, 4096, x[sel], v[sel], self_slot=sel)
+    ref = oracle.force(m, x, v, 1e-4, x[sel], v[sel])
+    check_force(out, ref, prec, x, x[sel], label=f"ni={ni}")
+
+
+def test_chunking_by_npipes(g6):
+    np.random.seed(12)
+    m, x, v = ic.plummer(2048)
+    ids = np.arange(1, 2049)
+    ag.drive_load(m, x, v, ids=ids)
+    full = ag.drive_force(2048, 0.0, 1e-4, ids, x, v)
+    g6.set_npipes(300)
+    try:
+        part = ag.drive_force(2048, 0.0, 1e-4, ids, x, v)
+    finally:
+        g6.set_npipes(16384)
+    # different i-chunks may pick different launch shapes: equal to rounding
+    assert np.allclose(part["acc"], full["acc"], rtol=1e-6, atol=0)
+    assert np.array_equal(part["nn"], full["nn"])
+
+
+def test_predictor_and_time_offsets(g6, prec):
+    """j-particles at different times with acc/jerk, predicted on the GPU."""
+    np.random.seed(13)
+    n = 3000
+    m, x, v = ic.plummer(n)
+    base = oracle.force(m, x, v, 1e-4, x, v)
+    rng = np.random.RandomState(5)
+    t = rng.choice([0.0, 1 / 64, 1 / 32, 3 / 64], n)
+    ti = 1 / 16
+    ids = np.arange(1, n + 1)
+    ag.drive_load(m, x, v, acc=base["acc"], jerk=base["jerk"], t=t, dt=np.full(n, 1 / 64),
+                  ids=ids)
+    pp, pv = oracle.predict(ti, t, x, v, base["acc"], base["jerk"])
+    out = ag.drive_force(n, ti, 1e-4, ids, pp, pv)
+    ref = oracle.force(m, pp, pv, 1e-4, pp, pv)
+    check_force(out, ref, prec, pp, pp, nn_is_id=True, label="predict")
+
+
+def test_corrector_bitexact(g6):
+    """Device FP64 corrector + Aarseth step == oracle (predict + correct)."""
+    np.random.seed(14)
+    n = 1024
+    m, x, v = ic.plummer(n)
+    f0 = oracle.force(m, x, v, 1e-4, x, v)
+    rng = np.random.RandomState(3)
+    dt = 2.0 ** -rng.randint(6, 12, n)
+    tnext = 1.0 / 64
+    t = tnext - dt
+    g6.load_particles(m, x, v, acc=f0["acc"], jerk=f0["jerk"], t=t, dt=dt)
+    pp, pv = oracle.predict(tnext, t, x, v, f0["acc"], f0["jerk"])
+    f1 = oracle.force(m, pp, pv, 1e-4, pp, pv)
+    slots = np.arange(n)
+    g6.correct(slots, tnext, 0.01, f1["acc"], f1["jerk"])
+    got = g6.read_particles(n)
+    ref = oracle.correct(tnext, 0.01, t, dt, pp, pv, f0["acc"], f0["jerk"], f1["acc"], f1["jerk"])
+    assert np.array_equal(got["timestep"], ref["timestep"])
+    assert np.array_equal(got["time"], ref["time"])
+    assert np.array_equal(got["pos"], ref["pos"])
+    assert np.array_equal(got["vel"], ref["vel"])
+
+
+def test_deterministic(g6):
+    np.random.seed(15)
+    m, x, v = ic.plummer(5000)
+    g6.load_particles(m, x, v)
+    sel = np.arange(0, 5000, 7)
+    a = g6.force(0.0, 1e-6, 5000, x[sel], v[sel], self_slot=sel)
+    b = g6.force(0.0, 1e-6, 5000, x[sel], v[sel], self_slot=sel)
+    for k in a:
+        assert np.array_equal(a[k], b[k])
+
+
+# --- known answers (src/amuse_ph4/tests/test_ph4.py) through the GPU ------
+
+def _pair(g6, m1, m2, x2, eps2, pts=None):
+    mass = np.array([m1, m2])
+    pos = np.array([[0.0, 0, 0], [x2, 0, 0]])
+    g6.load_particles(mass, pos, np.zeros((2, 3)))
+    if pts is None:
+        return g6.force(0.0, eps2, 2, pos, np.zeros((2, 3)), self_slot=[0, 1])
+    return g6.force(0.0, eps2, 2, pts, np.zeros_like(pts))
+
+
+def test_kat_pairs(g6, prec):
+    tol = 1e-7 if prec == ag.SPLIT else 1e-14
+    f = _pair(g6, 10.0, 10.0, 2.0, 0.01)
+    assert f["pot"][0] == pytest.approx(-10.0 / np.sqrt(4.01), rel=tol)
+    f = _pair(g6, 10.0, 1.0, 2.0, 0.0)
+    assert f["pot"][0] == pytest.approx(-0.5, rel=tol)
+    assert f["pot"][1] == pytest.approx(-5.0, rel=tol)
+    assert f["nn"][0] == 1 and f["nn"][1] == 0
+
+
+def test_kat_field_points(g6, prec):
+    pots = [-4.57110767688, -2.66662518639, -2.13331892165]
+    for x, pref in zip((0.25, 0.5, 0.75), pots):
+        pts = np.array([[x, 0, 0], [2.0 - x, 0, 0]])
+        f = _pair(g6, 1.0, 1.0, 2.0, 1e-5, pts)
+        assert f["pot"][0] == pytest.approx(pref, rel=1e-5)
+        assert f["pot"][1] == pytest.approx(f["pot"][0], rel=1e-5)
+        fx = -1.0 / x ** 2 + 1.0 / (2.0 - x) ** 2
+        assert f["acc"][0, 0] == pytest.approx(fx, rel=1e-2)
+        assert f["acc"][0, 0] == pytest.approx(-f["acc"][1, 0], rel=1e-5)
+
+
+def test_neighbour_lists(g6, prec):
+    np.random.seed(16)
+    n = 2000
+    m, x, v = ic.plummer(n)
+    ids = np.arange(1, n + 1)
+    ag.drive_load(m, x, v, ids=ids)
+    sel = np.arange(0, n, 13)
+    h2 = np.full(len(sel), 0.01)
+    h2[::2] = 0.05
+    g6.set_ti(0.0)
+    g6.calc(n, ids[sel], x[sel], v[sel], 1e-4, h2=h2)
+    over = g6.read_neighbour_list()
+    d2 = np.sum((x[None, :, :] - x[sel, None, :]) ** 2, axis=-1)
+    any_over = False
+    for q, i in enumerate(sel):
+        want = np.sort(ids[(d2[q] <= h2[q]) & (np.arange(n) != i)])
+        got, rc = g6.get_neighbour_list(q)
+        if len(want) > ag.NGB_MAX:
+            any_over = True
+            assert rc == 1
+            continue
+        assert np.array_equal(got, want), q
+    assert over == (1 if any_over else 0)
+
+
+def test_error_codes(g6):
+    np.random.seed(17)
+    m, x, v = ic.plummer(64)
+    ids = np.arange(1, 65)
+    ag.drive_load(m, x, v, ids=ids)
+    g6.set_npipes(16)
+    try:
+        with pytest.raises(ag.G6Error):
+            g6.calc(64, ids, x, v, 1e-4)  # ni > npipes
+    finally:
+        g6.set_npipes(16384)
+    with pytest.raises(ag.G6Error):
+        g6.set_j_particle(-1, 1, 0.0, 0.0, 1.0, np.zeros(3), np.zeros(3), np.zeros(3),
+                          np.zeros(3), np.zeros(3))
+    # a normal call still works afterwards
+    acc, jerk, pot, nn = g6.calc(64, ids, x, v, 1e-4)
+    assert np.all(np.isfinite(acc))

@@ -835,6 +835,10 @@ int g6x_timing(int on) {
   return 0;
 }
 int g6x_stats(double out[8]) {
+  if (G.timing && G.is_open) {
+    cudaEventSynchronize(G.ev_t2);
+    collect_timing();
+  }
   out[0] = G.st_predict_ms;
   out[1] = G.st_force_ms;
   out[2] = G.st_pairs;
@@ -890,6 +894,7 @@ int g6x_load(int n, const int *ids, const double *mass, const double (*x)[3],
     G.slot_id[s] = ids ? ids[s] : s;
     if (idmap_put(&G.ids, G.slot_id[s], s)) return G6_ERR_NOMEM;
   }
+  for (int s = n; s < G.js.cap; s++) G.slot_id[s] = -1; /* slots beyond n are unused */
   CK(cudaMemcpy(G.js.id, G.slot_id, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
   G.pred_valid = 0;
   G.run_n = n;

@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define G6_TILE 128 /* j records per shared-memory tile */
+#define G6_TILE 256 /* j records per shared-memory tile */
 
 enum { G6_PREC_SPLIT = 0, G6_PREC_FP64 = 1 };
 
@@ -66,6 +66,7 @@ typedef struct {
   int *err; /* device error word (0 = ok) */
   /* launch shape override (0 = automatic) */
   int force_jl, force_nsplit;
+  int want_nn; /* 0: nn[] = -1 (no nearest-neighbour search) */
 } g6_force_args;
 
 /* Launch shape actually used (reported by g6k_force). */

@@ -535,8 +535,19 @@ int g6_set_j_particle_(int *cluster_id, int *address, int *index, double *tj, do
   return 0;
 }
 
-/* Common body of the explicit-i force call with host arrays. */
-static int start_force_host(int nj, int ni, const int *index, const double *xi,
+/* The explicit-i force call with host arrays runs in two phases, so that
+ * the kernel knows whether the caller wants nearest neighbours:
+ *   stage_force_host  (g6calc_firsthalf): apply staged j updates, predict
+ *                      the j-system, copy the i-particles to the device;
+ *   launch_force_host (g6calc_lasthalf / lasthalf2): launch the force kernel
+ *                      with or without the nearest-neighbour search, then
+ *                      copy the results back.
+ * Both AMUSE callers issue lasthalf right after firsthalf (ph4 gpu.cc:394-407,
+ * phiGRAPE gravity.F:104-111), so nothing overlaps in between either way. */
+static int staged, staged_ni, staged_nj;
+static double staged_eps2;
+
+static int stage_force_host(int nj, int ni, const int *index, const double *xi,
                             const double *vi, const int *self_slot, double eps2,
                             const double *h2) {
   int rc = check_open();
@@ -545,54 +556,70 @@ static int start_force_host(int nj, int ni, const int *index, const double *xi,
     cudaEventSynchronize(G.ev_done);
     G.pending = 0;
   }
+  staged = 0;
   if (nj < 0 || ni < 0) {
     seterr("negative nj/ni");
     return G6_ERR_ARG;
   }
-  if (ni == 0) {
-    G.pending = 1;
-    G.pending_ni = 0;
-    return 0;
-  }
-  if (nj == 0) {
+  if (ni > 0 && nj == 0) {
     seterr("nj = 0");
     return G6_ERR_ARG;
   }
-  rc = ensure_io(ni);
-  if (rc) return rc;
-  rc = flush_updates();
-  if (rc) return rc;
-  rc = predict_if_needed(nj);
-  if (rc) return rc;
-  memcpy(IN_POS(G.h_in), xi, sizeof(double) * 3 * (size_t)ni);
-  memcpy(IN_VEL(G.h_in), vi, sizeof(double) * 3 * (size_t)ni);
-  if (h2)
-    memcpy(IN_H2(G.h_in), h2, sizeof(double) * (size_t)ni);
-  else
-    for (int i = 0; i < ni; i++) IN_H2(G.h_in)[i] = 0.0;
-  G.pending_nj = nj;
-  int *hs = IN_SELF(G.h_in);
-  if (self_slot) {
-    memcpy(hs, self_slot, sizeof(int) * (size_t)ni);
-  } else {
-    for (int i = 0; i < ni; i++) {
-      int s = idmap_get(&G.ids, index[i]);
-      hs[i] = (s >= 0 && s < nj) ? s : -1;
+  if (ni > 0) {
+    rc = ensure_io(ni);
+    if (rc) return rc;
+    rc = flush_updates();
+    if (rc) return rc;
+    rc = predict_if_needed(nj);
+    if (rc) return rc;
+    memcpy(IN_POS(G.h_in), xi, sizeof(double) * 3 * (size_t)ni);
+    memcpy(IN_VEL(G.h_in), vi, sizeof(double) * 3 * (size_t)ni);
+    if (h2)
+      memcpy(IN_H2(G.h_in), h2, sizeof(double) * (size_t)ni);
+    else
+      for (int i = 0; i < ni; i++) IN_H2(G.h_in)[i] = 0.0;
+    int *hs = IN_SELF(G.h_in);
+    if (self_slot) {
+      memcpy(hs, self_slot, sizeof(int) * (size_t)ni);
+    } else {
+      for (int i = 0; i < ni; i++) {
+        int s = idmap_get(&G.ids, index[i]);
+        hs[i] = (s >= 0 && s < nj) ? s : -1;
+      }
     }
+    /* One copy of the live prefix of each input section. */
+    CK(cudaMemcpyAsync(IN_POS(G.d_in), IN_POS(G.h_in), sizeof(double) * 3 * (size_t)ni,
+                       cudaMemcpyHostToDevice, G.st));
+    CK(cudaMemcpyAsync(IN_VEL(G.d_in), IN_VEL(G.h_in), sizeof(double) * 3 * (size_t)ni,
+                       cudaMemcpyHostToDevice, G.st));
+    CK(cudaMemcpyAsync(IN_SELF(G.d_in), hs, sizeof(int) * (size_t)ni, cudaMemcpyHostToDevice,
+                       G.st));
+    if (index && ni <= G.pending_cap) memcpy(G.pending_ids, index, sizeof(int) * (size_t)ni);
   }
-  /* Three copies of the live prefix of each section. */
-  CK(cudaMemcpyAsync(IN_POS(G.d_in), IN_POS(G.h_in), sizeof(double) * 3 * (size_t)ni,
-                     cudaMemcpyHostToDevice, G.st));
-  CK(cudaMemcpyAsync(IN_VEL(G.d_in), IN_VEL(G.h_in), sizeof(double) * 3 * (size_t)ni,
-                     cudaMemcpyHostToDevice, G.st));
-  CK(cudaMemcpyAsync(IN_SELF(G.d_in), hs, sizeof(int) * (size_t)ni, cudaMemcpyHostToDevice,
-                     G.st));
+  G.pending_nj = nj;
+  staged = 1;
+  staged_ni = ni;
+  staged_nj = nj;
+  staged_eps2 = eps2;
+  return 0;
+}
+
+static int launch_force_host(int want_nn) {
+  if (!staged) {
+    seterr("lasthalf without firsthalf");
+    return G6_ERR_STATE;
+  }
+  staged = 0;
+  const int ni = staged_ni;
+  G.pending = 1;
+  G.pending_ni = ni;
+  if (ni == 0) return 0;
   g6_force_args a;
   memset(&a, 0, sizeof(a));
   a.ni = ni;
-  a.nj = nj;
+  a.nj = staged_nj;
   a.prec = G.prec;
-  a.eps2 = eps2;
+  a.eps2 = staged_eps2;
   a.ipos = IN_POS(G.d_in);
   a.ivel = IN_VEL(G.d_in);
   a.iself = IN_SELF(G.d_in);
@@ -602,8 +629,12 @@ static int start_force_host(int nj, int ni, const int *index, const double *xi,
   a.pot = OUT_POT(G.d_out);
   a.nn = OUT_NN(G.d_out);
   a.nn_r2 = OUT_NNR2(G.d_out);
-  rc = run_force(&a);
-  if (rc) return rc;
+  a.want_nn = want_nn;
+  int rc = run_force(&a);
+  if (rc) {
+    G.pending = 0;
+    return rc;
+  }
   /* Error word + live prefix of each output section. */
   CK(cudaMemcpyAsync(G.h_out, G.d_out, 16, cudaMemcpyDeviceToHost, G.st));
   CK(cudaMemcpyAsync(OUT_ACC(G.h_out), OUT_ACC(G.d_out), sizeof(double) * 3 * (size_t)ni,
@@ -612,14 +643,13 @@ static int start_force_host(int nj, int ni, const int *index, const double *xi,
                      cudaMemcpyDeviceToHost, G.st));
   CK(cudaMemcpyAsync(OUT_POT(G.h_out), OUT_POT(G.d_out), sizeof(double) * (size_t)ni,
                      cudaMemcpyDeviceToHost, G.st));
-  CK(cudaMemcpyAsync(OUT_NN(G.h_out), OUT_NN(G.d_out), sizeof(int) * (size_t)ni,
-                     cudaMemcpyDeviceToHost, G.st));
-  CK(cudaMemcpyAsync(OUT_NNR2(G.h_out), OUT_NNR2(G.d_out), sizeof(float) * (size_t)ni,
-                     cudaMemcpyDeviceToHost, G.st));
+  if (want_nn) {
+    CK(cudaMemcpyAsync(OUT_NN(G.h_out), OUT_NN(G.d_out), sizeof(int) * (size_t)ni,
+                       cudaMemcpyDeviceToHost, G.st));
+    CK(cudaMemcpyAsync(OUT_NNR2(G.h_out), OUT_NNR2(G.d_out), sizeof(float) * (size_t)ni,
+                       cudaMemcpyDeviceToHost, G.st));
+  }
   CK(cudaEventRecord(G.ev_done, G.st));
-  G.pending = 1;
-  G.pending_ni = ni;
-  if (index && ni <= G.pending_cap) memcpy(G.pending_ids, index, sizeof(int) * (size_t)ni);
   return 0;
 }
 
@@ -629,10 +659,12 @@ static int finish_force(int ni) {
     return G6_ERR_STATE;
   }
   if (ni != G.pending_ni) {
+    cudaEventSynchronize(G.ev_done);
+    G.pending = 0;
     seterr("lasthalf ni=%d differs from firsthalf ni=%d", ni, G.pending_ni);
     return G6_ERR_ARG;
   }
-  cudaError_t e = cudaEventSynchronize(G.ev_done);
+  cudaError_t e = ni > 0 ? cudaEventSynchronize(G.ev_done) : cudaSuccess;
   G.pending = 0;
   if (e != cudaSuccess) {
     seterr("force call failed: %s", cudaGetErrorString(e));
@@ -658,34 +690,42 @@ void g6calc_firsthalf_(int *cluster_id, int *nj, int *ni, int index[], double xi
   (void)phiold;
   if (G.is_open && *ni > G.npipes) {
     seterr("g6calc_firsthalf: ni=%d > npipes=%d", *ni, G.npipes);
+    staged = 0;
     firsthalf_rc = G6_ERR_ARG;
     return;
   }
-  firsthalf_rc = start_force_host(*nj, *ni, index, &xi[0][0], &vi[0][0], NULL, *eps2, h2);
+  firsthalf_rc = stage_force_host(*nj, *ni, index, &xi[0][0], &vi[0][0], NULL, *eps2, h2);
+}
+
+static int lasthalf_common(int ni, int want_nn, double acc[][3], double jerk[][3],
+                           double pot[]) {
+  if (firsthalf_rc) {
+    int rc = firsthalf_rc;
+    firsthalf_rc = 0;
+    return rc;
+  }
+  int rc = launch_force_host(want_nn);
+  if (rc) return rc;
+  rc = finish_force(ni);
+  if (rc) return rc;
+  memcpy(&acc[0][0], OUT_ACC(G.h_out), sizeof(double) * 3 * (size_t)ni);
+  memcpy(&jerk[0][0], OUT_JERK(G.h_out), sizeof(double) * 3 * (size_t)ni);
+  memcpy(pot, OUT_POT(G.h_out), sizeof(double) * (size_t)ni);
+  return 0;
 }
 
 int g6calc_lasthalf_(int *cluster_id, int *nj, int *ni, int index[], double xi[][3],
                      double vi[][3], double *eps2, double h2[], double acc[][3],
                      double jerk[][3], double pot[]) {
   (void)cluster_id; (void)nj; (void)index; (void)xi; (void)vi; (void)eps2; (void)h2;
-  if (firsthalf_rc) {
-    int rc = firsthalf_rc;
-    firsthalf_rc = 0;
-    return rc;
-  }
-  int rc = finish_force(*ni);
-  if (rc) return rc;
-  const int n = *ni;
-  memcpy(&acc[0][0], OUT_ACC(G.h_out), sizeof(double) * 3 * (size_t)n);
-  memcpy(&jerk[0][0], OUT_JERK(G.h_out), sizeof(double) * 3 * (size_t)n);
-  memcpy(pot, OUT_POT(G.h_out), sizeof(double) * (size_t)n);
-  return 0;
+  return lasthalf_common(*ni, 0, acc, jerk, pot);
 }
 
 int g6calc_lasthalf2_(int *cluster_id, int *nj, int *ni, int index[], double xi[][3],
                       double vi[][3], double *eps2, double h2[], double acc[][3],
                       double jerk[][3], double pot[], int *inn) {
-  int rc = g6calc_lasthalf_(cluster_id, nj, ni, index, xi, vi, eps2, h2, acc, jerk, pot);
+  (void)cluster_id; (void)nj; (void)index; (void)xi; (void)vi; (void)eps2; (void)h2;
+  int rc = lasthalf_common(*ni, 1, acc, jerk, pot);
   if (rc) return rc;
   const int *nn = OUT_NN(G.h_out);
   for (int i = 0; i < *ni; i++) inn[i] = nn[i] >= 0 ? G.slot_id[nn[i]] : -1;
@@ -942,9 +982,11 @@ int g6x_force(double ti, double eps2, int nj, int ni, const double (*xi)[3],
     if (!self) return G6_ERR_NOMEM;
     for (int i = 0; i < ni; i++) self[i] = -1;
   }
-  rc = start_force_host(nj, ni, NULL, &xi[0][0], &vi[0][0], self_slot ? self_slot : self, eps2,
+  rc = stage_force_host(nj, ni, NULL, &xi[0][0], &vi[0][0], self_slot ? self_slot : self, eps2,
                         NULL);
   free(self);
+  if (rc) return rc;
+  rc = launch_force_host(nn != NULL || nn_r2 != NULL);
   if (rc) return rc;
   rc = finish_force(ni);
   if (rc) return rc;
@@ -995,6 +1037,7 @@ int g6x_force_dev(double ti, double eps2, int nj, int ni, const double *d_xi,
   a.pot = d_pot;
   a.nn = d_nn;
   a.nn_r2 = d_nn_r2;
+  a.want_nn = d_nn != NULL || d_nn_r2 != NULL;
   rc = run_force(&a);
   if (rc) return rc;
   if (sync) {
@@ -1029,6 +1072,7 @@ int g6x_force_slots(double ti, double eps2, int nj, int ni, const int *d_ilist, 
   a.jerk = d_jerk;
   a.pot = d_pot;
   a.nn = d_nn;
+  a.want_nn = d_nn != NULL;
   rc = run_force(&a);
   if (rc) return rc;
   if (sync) {
@@ -1137,10 +1181,10 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
       return G6_ERR_STATE;
     }
     rc = g6x_force_slots(tn, G.run_eps2, n, ni, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot,
-                         G.d_rnn, 0);
+                         NULL, 0);
     if (rc) return rc;
     if (g6k_correct(&G.js, ni, G.d_ilist, tn, G.run_eta, G.d_racc, G.d_rjerk, G.d_rpot,
-                    G.d_rnn, G.st))
+                    NULL, G.st))
       return G6_ERR_CUDA;
     G.pred_valid = 0; /* j-state changed */
     G.run_t = tn;
@@ -1187,10 +1231,10 @@ int g6x_step_all(double tnext) {
   rc = identity_list(n);
   if (rc) return rc;
   rc = g6x_force_slots(tnext, G.run_eps2, n, n, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot,
-                       G.d_rnn, 0);
+                       NULL, 0);
   if (rc) return rc;
   if (g6k_correct(&G.js, n, G.d_ilist, tnext, G.run_eta, G.d_racc, G.d_rjerk, G.d_rpot,
-                  G.d_rnn, G.st))
+                  NULL, G.st))
     return G6_ERR_CUDA;
   G.pred_valid = 0;
   G.run_t = tnext;
@@ -1208,7 +1252,7 @@ int g6x_energy(double *kinetic, double *potential) {
   rc = identity_list(n);
   if (rc) return rc;
   rc = g6x_force_slots(G.run_t, G.run_eps2, n, n, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot,
-                       G.d_rnn, 0);
+                       NULL, 0);
   if (rc) return rc;
   if (g6k_energy_sums(&G.js, n, G.run_t, G.d_rpot, G.d_esum, G.st)) return G6_ERR_CUDA;
   double h[2];

@@ -19,17 +19,19 @@
 // that slot.
 //
 // Structure (one CTA = 256 threads = 8 warps, 2 i-particles per thread):
-//   * j-tiles of 128 records are streamed HBM/L2 -> shared memory with
-//     cp.async.bulk (TMA, non-tensor) completing on an mbarrier, 4 stages.
+//   * j-tiles of 256 records are streamed HBM/L2 -> shared memory with
+//     cp.async.bulk (TMA, non-tensor) completing on an mbarrier; warps
+//     consume the ring independently (no CTA barrier in the loop).
 //   * JL j-lanes share each i-particle (JL = 1 for large i-blocks, up to
-//     128 for tiny ones); j is also split across CTAs (grid.y) so that small
+//     256 for tiny ones); j is also split across CTAs (grid.y) so that small
 //     active blocks still fill all 152 SMs.
 //   * Lanes of one i merge with warp shuffles (plus shared memory across
 //     warps for JL > 32); CTAs of one i merge in a second pass kernel, in
 //     fixed order, with float-float (split) or FP64 adds: deterministic.
-//   * Nearest neighbour: the hot loop keeps only a running min of r2 (one
-//     FMNMX per pair); a tile in which some lane's min improved is
-//     re-scanned with bit-identical arithmetic to find the index.
+//   * Nearest neighbour (optional, a template flag): the hot loop keeps only
+//     a running min of r2 (one FMNMX per pair) and the tile where it last
+//     improved; after the loop that tile is re-read from L2 and re-scanned
+//     with bit-identical arithmetic to find the index.
 //   * A tile that holds the self slot of one of the warp's i-particles takes
 //     a checked copy of the loop (rinv = 0, r2 -> +inf for self).
 #include <cuda_runtime.h>
@@ -49,11 +51,23 @@ __host__ __device__ __forceinline__ G6D4 g6d4(double x, double y, double z, doub
 
 namespace {
 
-constexpr int NT = 256;      // threads per CTA
+// Tuning constants (compile-time; the defaults are the measured best).
+#ifndef G6_NT
+#define G6_NT 256
+#endif
+#ifndef G6_IPT
+#define G6_IPT 2
+#endif
+#ifndef G6_UNROLL
+#define G6_UNROLL 4
+#endif
+#ifndef G6_MINB
+#define G6_MINB 2
+#endif
+constexpr int NT = G6_NT;    // threads per CTA
 constexpr int TJ = G6_TILE;  // j records per tile
-constexpr int NSTAGE = 4;    // TMA ring depth
-constexpr int IPT = 2;       // i-particles per thread
-constexpr float FAR = 1.0e18f;
+constexpr int IPT = G6_IPT;  // i-particles per thread
+constexpr int UNROLL = G6_UNROLL;  // j-loop unroll factor
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound per wait
 
 enum { ERR_TMA_TIMEOUT = 1, ERR_SHAPE = 2 };
@@ -109,6 +123,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// Bounded wait that also gives up when another warp of the CTA raised
+// *abort (false in both cases).
+__device__ __forceinline__ bool mbar_wait_abortable(uint64_t *bar, uint32_t parity,
+                                                    volatile int *abort) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+    if (gtimer() - t0 > WAIT_NS) return false;
+  }
+}
 // Bounded wait: false after WAIT_NS of global time.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
   if (mbar_try_wait(bar, parity)) return true;
@@ -117,6 +143,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     if (mbar_try_wait(bar, parity)) return true;
     if (gtimer() - t0 > WAIT_NS) return false;
   }
+}
+
+// One MUFU.RSQ, flush-to-zero (r2 >= eps2 + 2^-52 is never subnormal).
+#ifndef G6_RSQRT_NR
+#define G6_RSQRT_NR 0
+#endif
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  if (G6_RSQRT_NR) {
+    // one Newton-Raphson step y <- y + y (1 - x y^2) / 2
+    const float e = fmaf(-x * y, y, 1.0f);
+    y = fmaf(0.5f * y, e, y);
+  }
+  return y;
 }
 
 // ------------------------------------------------------- float-float ---
@@ -142,6 +183,8 @@ __device__ __forceinline__ void ff_add(float &ah, float &al, float bh, float bl)
 struct SplitP {
   using Rec = RecS;
   using R = float;
+  static constexpr int NSTAGE = 3;  // TMA ring depth (3 x 12 KB)
+  static constexpr int MINB = G6_MINB;  // resident CTAs per SM
   struct I {
     float xh, yh, zh, xl, yl, zl, vx, vy, vz;
   };
@@ -206,16 +249,16 @@ struct SplitP {
     r2 = __fmaf_rn(dy, dy, r2);
     return __fmaf_rn(dz, dz, r2);
   }
-  template <bool CHECK>
+  template <bool CHECK, bool NN>
   __device__ static __forceinline__ void pair(const I &s, const Rec &r, float eps2, Part &q,
                                               float &nnmin, bool is_self) {
     float dx, dy, dz;
     const float r2 = r2e(s, r, eps2, dx, dy, dz);
-    float rinv = rsqrtf(r2);
+    float rinv = rsqrt_approx(r2);
     if (CHECK) {
       rinv = is_self ? 0.f : rinv;
-      nnmin = fminf(nnmin, is_self ? __int_as_float(0x7f800000) : r2);
-    } else {
+      if (NN) nnmin = fminf(nnmin, is_self ? __int_as_float(0x7f800000) : r2);
+    } else if (NN) {
       nnmin = fminf(nnmin, r2);
     }
     const float dvx = r.v.x - s.vx, dvy = r.v.y - s.vy, dvz = r.v.z - s.vz;
@@ -268,6 +311,8 @@ struct SplitP {
 struct F64P {
   using Rec = RecD;
   using R = double;
+  static constexpr int NSTAGE = 2;  // TMA ring depth (2 x 16 KB)
+  static constexpr int MINB = 1;
   struct I {
     double x, y, z, vx, vy, vz;
   };
@@ -330,7 +375,7 @@ struct F64P {
     y = y * __fma_rn(-hx * y, y, 1.5);
     return y;
   }
-  template <bool CHECK>
+  template <bool CHECK, bool NN>
   __device__ static __forceinline__ void pair(const I &s, const Rec &r, double eps2, Part &q,
                                               double &nnmin, bool is_self) {
     double dx, dy, dz;
@@ -338,8 +383,8 @@ struct F64P {
     double rinv = rsqrt64(r2);
     if (CHECK) {
       rinv = is_self ? 0.0 : rinv;
-      nnmin = fmin(nnmin, is_self ? __longlong_as_double(0x7ff0000000000000ll) : r2);
-    } else {
+      if (NN) nnmin = fmin(nnmin, is_self ? __longlong_as_double(0x7ff0000000000000ll) : r2);
+    } else if (NN) {
       nnmin = fmin(nnmin, r2);
     }
     const double dvx = r.v.x - s.vx, dvy = r.v.y - s.vy, dvz = r.v.z - s.vz;
@@ -413,13 +458,15 @@ struct KParams {
   void *part;  // [nsplit][ni_pad] Out records when nsplit > 1
   int ni_pad;
   int *err;
+  int want_nn;
 };
 
 // Number of j per thread between compensated folds.
 constexpr int FOLD_J = 64;
 
-template <class P, int JL>
-__global__ void __launch_bounds__(NT, 2) force_kernel(KParams kp) {
+template <class P, int JL, bool NN>
+__global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
+  constexpr int NSTAGE = P::NSTAGE;
   using Rec = typename P::Rec;
   using R = typename P::R;
   constexpr int NIL = NT / JL;           // i-lanes per CTA
@@ -430,6 +477,9 @@ __global__ void __launch_bounds__(NT, 2) force_kernel(KParams kp) {
 
   __shared__ __align__(128) Rec tiles[NSTAGE][TJ];
   __shared__ __align__(8) uint64_t full[NSTAGE];
+  __shared__ int released[NSTAGE];
+  __shared__ int issued_s;
+  __shared__ volatile int abort_s;
 
   const int tid = threadIdx.x;
   const int jl = tid % JL;
@@ -463,18 +513,22 @@ __global__ void __launch_bounds__(NT, 2) force_kernel(KParams kp) {
   const int ntiles = je > js ? (je - js) / TJ : 0;
   const Rec *gj = reinterpret_cast<const Rec *>(kp.jrec) + js;
 
+  constexpr int NWARP = NT / 32;
   if (tid == 0) {
 #pragma unroll
-    for (int s = 0; s < NSTAGE; s++) mbar_init(&full[s], 1);
+    for (int s = 0; s < NSTAGE; s++) {
+      mbar_init(&full[s], 1);
+      released[s] = 0;
+    }
+    issued_s = ntiles < NSTAGE ? ntiles : NSTAGE;
+    abort_s = 0;
     fence_barrier_init();
   }
   __syncthreads();
-  int issued = 0;  // tiles issued so far (meaningful in thread 0 only)
   if (tid == 0) {
     for (int s = 0; s < NSTAGE && s < ntiles; s++) {
       mbar_expect_tx(&full[s], TJ * sizeof(Rec));
       tma_load_1d(&tiles[s][0], gj + s * TJ, TJ * sizeof(Rec), &full[s]);
-      issued = s + 1;
     }
   }
 
@@ -482,31 +536,29 @@ __global__ void __launch_bounds__(NT, 2) force_kernel(KParams kp) {
   typename P::Part q[IPT];
   typename P::Tot T[IPT];
   R nnmin[IPT], nnbest[IPT];
-  int nnidx[IPT];
+  int nnidx[IPT], besttile[IPT];
 #pragma unroll
   for (int k = 0; k < IPT; k++) {
     P::zero(q[k]);
     P::zero(T[k]);
     nnmin[k] = nnbest[k] = (R)__int_as_float(0x7f800000);
     nnidx[k] = -1;
+    besttile[k] = -1;
   }
 
+  // Warps consume tiles independently: no CTA barrier in the loop.  Each
+  // warp releases a stage after reading it; the warp whose release completes
+  // a use of the stage (all NWARP warps done) refills it with tile t+NSTAGE.
+  // The per-stage release counter only grows: use k of stage s ends when it
+  // reaches (k+1)*NWARP.
   bool failed = false;
-  int t_fail = 0;
   for (int t = 0; t < ntiles; t++) {
     const int s = t % NSTAGE;
-    const bool to = !mbar_wait_bounded(&full[s], (t / NSTAGE) & 1);
-    if (__syncthreads_or(to)) {
+    const bool ok = mbar_wait_abortable(&full[s], (t / NSTAGE) & 1, &abort_s);
+    if (!__all_sync(0xffffffffu, ok)) {
       failed = true;
-      t_fail = t;
+      if (lane == 0) abort_s = 1;
       break;
-    }
-    // Everyone has finished tile t-1: refill its stage.
-    if (tid == 0 && t >= 1 && t - 1 + NSTAGE < ntiles) {
-      const int s1 = (t - 1) % NSTAGE;
-      mbar_expect_tx(&full[s1], TJ * sizeof(Rec));
-      tma_load_1d(&tiles[s1][0], gj + (t - 1 + NSTAGE) * TJ, TJ * sizeof(Rec), &full[s1]);
-      issued = t - 1 + NSTAGE + 1;
     }
     const Rec *tile = &tiles[s][0];
     const int tj0 = js + t * TJ;
@@ -518,12 +570,12 @@ __global__ void __launch_bounds__(NT, 2) force_kernel(KParams kp) {
     const bool slow = __any_sync(0xffffffffu, mine);
 
     if (!slow) {
-#pragma unroll 4
+#pragma unroll UNROLL
       for (int u = 0; u < JPT; u++) {
         const Rec r = tile[jl + JL * u];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
-          P::template pair<false>(I[k], r, eps2, q[k], nnmin[k], false);
+          P::template pair<false, NN>(I[k], r, eps2, q[k], nnmin[k], false);
       }
     } else {
       for (int u = 0; u < JPT; u++) {
@@ -531,30 +583,19 @@ __global__ void __launch_bounds__(NT, 2) force_kernel(KParams kp) {
         const Rec r = tile[jj];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
-          P::template pair<true>(I[k], r, eps2, q[k], nnmin[k], tj0 + jj == self[k]);
+          P::template pair<true, NN>(I[k], r, eps2, q[k], nnmin[k], tj0 + jj == self[k]);
       }
     }
 
-    // Nearest neighbour: re-scan this tile where the running min improved.
-    bool imp = false;
+    // Nearest neighbour: remember the tile in which the running min last
+    // improved (strict <, so the earliest tile wins ties); its index within
+    // the tile is recovered once, after the loop.
 #pragma unroll
-    for (int k = 0; k < IPT; k++) imp |= nnmin[k] < nnbest[k];
-    if (__any_sync(0xffffffffu, imp)) {
-      for (int u = 0; u < JPT; u++) {
-        const int jj = jl + JL * u;
-        const Rec r = tile[jj];
-#pragma unroll
-        for (int k = 0; k < IPT; k++) {
-          if (nnmin[k] < nnbest[k]) {
-            R dx, dy, dz;
-            const R r2 = P::r2e(I[k], r, eps2, dx, dy, dz);
-            if (r2 == nnmin[k] && tj0 + jj != self[k]) {
-              nnbest[k] = r2;
-              nnidx[k] = tj0 + jj;
-            }
-          }
-        }
-      }
+    for (int k = 0; k < IPT; k++) {
+      if (!NN) break;
+      const bool imp = nnmin[k] < nnbest[k];
+      nnbest[k] = imp ? nnmin[k] : nnbest[k];
+      besttile[k] = imp ? t : besttile[k];
     }
 
     if ((t + 1) % FOLD_TILES == 0) {
@@ -564,16 +605,51 @@ __global__ void __launch_bounds__(NT, 2) force_kernel(KParams kp) {
         P::zero(q[k]);
       }
     }
+
+    // Release stage s; the last releaser refills it.
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();
+      const int c = atomicAdd(&released[s], 1);
+      if (c == (t / NSTAGE + 1) * NWARP - 1 && t + NSTAGE < ntiles) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&full[s], TJ * sizeof(Rec));
+        tma_load_1d(&tiles[s][0], gj + (t + NSTAGE) * TJ, TJ * sizeof(Rec), &full[s]);
+        atomicMax(&issued_s, t + NSTAGE + 1);
+      }
+    }
   }
 
-  if (failed) {
-    // Drain this CTA's outstanding copies (bounded) before leaving.
+  if (__syncthreads_or(failed)) {
+    // Drain the copies still in flight (bounded) before the CTA leaves.
     if (tid == 0) {
       atomicOr(kp.err, ERR_TMA_TIMEOUT);
-      for (int u = t_fail; u < issued; u++)
+      const int hi = issued_s;
+      for (int u = hi - NSTAGE > 0 ? hi - NSTAGE : 0; u < hi; u++)
         (void)mbar_wait_bounded(&full[u % NSTAGE], (u / NSTAGE) & 1);
     }
     return;
+  }
+
+  // ---- nearest neighbour: find the first j of the best tile (this lane's
+  // j subset) whose r^2 equals the running min, with the same arithmetic,
+  // reading the records back from global memory (L2). ----
+#pragma unroll
+  for (int k = 0; k < IPT; k++) {
+    if (!NN || besttile[k] < 0) continue;
+    const Rec *g = gj + besttile[k] * TJ;
+    const int tj0 = js + besttile[k] * TJ;
+    bool found = false;
+    for (int u = 0; u < JPT && !found; u++) {
+      const int jj = jl + JL * u;
+      const Rec r = g[jj];
+      R dx, dy, dz;
+      const R r2 = P::r2e(I[k], r, eps2, dx, dy, dz);
+      if (r2 == nnbest[k] && tj0 + jj != self[k]) {
+        nnidx[k] = tj0 + jj;
+        found = true;
+      }
+    }
   }
 
   // ---- merge: fold remainders, then j-lanes, then (maybe) CTAs ----
@@ -628,7 +704,7 @@ __global__ void __launch_bounds__(NT, 2) force_kernel(KParams kp) {
     const int i = blockIdx.x * ISLOTS + k * NIL + il;
     if (kp.nsplit == 1) {
       P::write_final(o[k], i, kp.acc, kp.jerk, kp.pot);
-      kp.nn[i] = (o[k].nn >= 0 && o[k].nn < kp.nj) ? o[k].nn : -1;
+      if (kp.nn) kp.nn[i] = (o[k].nn >= 0 && o[k].nn < kp.nj) ? o[k].nn : -1;
       if (kp.nn_r2) kp.nn_r2[i] = (float)o[k].nnr2;
     } else {
       reinterpret_cast<typename P::Out *>(kp.part)[(size_t)blockIdx.y * kp.ni_pad + i] = o[k];
@@ -645,7 +721,7 @@ __global__ void reduce_kernel(KParams kp) {
   typename P::Out o = part[i];
   for (int s = 1; s < kp.nsplit; s++) P::merge(o, part[(size_t)s * kp.ni_pad + i]);
   P::write_final(o, i, kp.acc, kp.jerk, kp.pot);
-  kp.nn[i] = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
+  if (kp.nn) kp.nn[i] = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
   if (kp.nn_r2) kp.nn_r2[i] = (float)o.nnr2;
 }
 
@@ -663,57 +739,104 @@ int sm_count() {
 
 // Launch shape: JL from the i-block size, nsplit so that the grid covers
 // about two resident CTAs per SM, with at least 4 tiles per split.
-void choose_shape(int ni, int nj, int force_jl, int force_nsplit, int *jl_out, int *nsplit_out,
-                  int *jsplit_out) {
-  int jl = 1;
-  if (force_jl > 0) {
-    jl = force_jl;
-  } else {
-    // smallest JL whose CTA i-capacity (512/JL) still holds >= ni, so the
-    // i-slots are not wasted; JL = 1 for ni >= 512.
-    while (jl < TJ && (NT / (jl * 2)) * IPT >= ni && ni > 0) jl *= 2;
+// Launch shape from a small cost model.  A CTA streams tiles_per tiles of
+// its j-range; per tile each thread spends ~A issue slots of fixed work
+// (wait, release, bookkeeping) plus B per j-record for its 2 i-particles
+// (JPT = 256/JL records), plus F per CTA (i-loads, lane merges, output).
+// Resident CTAs run in waves of MINB per SM, so
+//   cost = waves * (tiles_per * (A + B * JPT) + F) * (1 + 0.002 * nsplit)
+// (the last factor charges the partial-sum traffic of the second pass).
+// Candidates: JL from the smallest that does not waste CTA i-slots up to
+// 256 (more j-lanes = more CTAs for small blocks), and every distinct split
+// count up to 4 resident waves' worth.  Large blocks (a full wave of CTAs at
+// JL = 1) stay at JL = 1.  The last few shapes are cached (block steps
+// repeat the same ni).
+struct ShapeKey {
+  int ni, nj, prec, fjl, fns;
+  int jl, nsplit, jsplit;
+};
+ShapeKey g_shape_cache[64];
+
+void choose_shape(int ni, int nj, int prec, int force_jl, int force_nsplit, int *jl_out,
+                  int *nsplit_out, int *jsplit_out) {
+  const unsigned h = ((unsigned)ni * 2654435761u ^ (unsigned)nj * 40503u ^ (unsigned)prec) & 63u;
+  ShapeKey &c = g_shape_cache[h];
+  if (c.ni == ni && c.nj == nj && c.prec == prec && c.fjl == force_jl && c.fns == force_nsplit &&
+      c.jl > 0) {
+    *jl_out = c.jl;
+    *nsplit_out = c.nsplit;
+    *jsplit_out = c.jsplit;
+    return;
   }
-  const int islots = (NT / jl) * IPT;
-  const int gx = (ni + islots - 1) / islots;
-  const int ntiles = (nj + TJ - 1) / TJ;
-  int nsplit;
-  if (force_nsplit > 0) {
-    nsplit = force_nsplit;
-  } else {
-    // Pick the split count that best fills whole waves of resident CTAs
-    // (2 per SM), with at least 4 tiles per split and at most 64 splits.
-    const int slots = 2 * sm_count();
-    int max_split = ntiles / 4 > 1 ? ntiles / 4 : 1;
-    if (max_split > 64) max_split = 64;
-    nsplit = 1;
-    double best = -1.0;
-    for (int c = 1; c <= max_split; c++) {
-      const long long total = (long long)gx * c;
-      const long long waves = (total + slots - 1) / slots;
-      const double eff = (double)total / (double)(waves * slots);
-      if (eff > best + 0.02) {
-        best = eff;
-        nsplit = c;
+  const int ntiles = nj > 0 ? (nj + TJ - 1) / TJ : 1;
+  const int minb = prec == G6_PREC_FP64 ? F64P::MINB : SplitP::MINB;
+  const int slots = minb * sm_count();
+  const double A = 150.0, F = 3000.0;
+  const double B = prec == G6_PREC_FP64 ? 76.0 * 32.0 : 76.0;
+  int jl0 = 1;
+  while (jl0 < TJ && (NT / (jl0 * 2)) * IPT >= ni && ni > 0) jl0 *= 2;
+  int jl_lo = jl0, jl_hi = TJ;
+  if (force_jl > 0) jl_lo = jl_hi = force_jl;
+  else if (jl0 == 1 && (ni + (NT * IPT) - 1) / (NT * IPT) >= slots) jl_hi = 1;
+  const int max_ns = ntiles < 4 * slots ? ntiles : 4 * slots;
+  double best = 1e300;
+  int bjl = jl_lo, bns = 1;
+  for (int jl = jl_lo; jl <= jl_hi; jl *= 2) {
+    const int islots = (NT / jl) * IPT;
+    const long long gx = (ni + islots - 1) / islots;
+    // distinct split counts: all small ones, then those from small tiles_per
+    int cand[512];
+    int nc = 0;
+    if (force_nsplit > 0) {
+      cand[nc++] = force_nsplit;
+    } else {
+      for (int q = 1; q <= 128 && q <= max_ns; q++) cand[nc++] = q;
+      for (int tp = 1; tp <= 256 && nc < 512; tp++) {
+        const int q = (ntiles + tp - 1) / tp;
+        if (q > 128 && q <= max_ns) cand[nc++] = q;
       }
-      if (total >= 8LL * slots) break;
+    }
+    for (int k = 0; k < nc; k++) {
+      int ns = cand[k] < 1 ? 1 : cand[k];
+      if (ns > ntiles) ns = ntiles;
+      const int tp = (ntiles + ns - 1) / ns;
+      ns = (ntiles + tp - 1) / tp;
+      const long long ctas = gx * ns;
+      const long long waves = (ctas + slots - 1) / slots;
+      const double cost =
+          (double)waves * (tp * (A + B * (double)(TJ / jl)) + F) * (1.0 + 0.002 * ns);
+      if (cost < best * 0.999) {
+        best = cost;
+        bjl = jl;
+        bns = ns;
+      }
     }
   }
-  if (nsplit > ntiles && ntiles > 0) nsplit = ntiles;
-  if (nsplit < 1) nsplit = 1;
-  const int tiles_per = ntiles > 0 ? (ntiles + nsplit - 1) / nsplit : 1;
-  nsplit = ntiles > 0 ? (ntiles + tiles_per - 1) / tiles_per : 1;
-  *jl_out = jl;
-  *nsplit_out = nsplit;
-  *jsplit_out = tiles_per * TJ;
+  const int tp = (ntiles + bns - 1) / bns;
+  *jl_out = bjl;
+  *nsplit_out = (ntiles + tp - 1) / tp;
+  *jsplit_out = tp * TJ;
+  c.ni = ni;
+  c.nj = nj;
+  c.prec = prec;
+  c.fjl = force_jl;
+  c.fns = force_nsplit;
+  c.jl = *jl_out;
+  c.nsplit = *nsplit_out;
+  c.jsplit = *jsplit_out;
 }
 
 template <class P>
 int launch(const KParams &kp, int jl, int gx, cudaStream_t st) {
   dim3 grid(gx, kp.nsplit), block(NT);
-  switch (jl) {
-#define G6_CASE(J) \
-  case J:          \
-    force_kernel<P, J><<<grid, block, 0, st>>>(kp); \
+  // Without nearest neighbours only the large-block shape has its own
+  // instantiation; small blocks are latency-bound and keep the nn code.
+  if (jl == 1 && !kp.want_nn) {
+    force_kernel<P, 1, false><<<grid, block, 0, st>>>(kp);
+  } else switch (jl) {
+#define G6_CASE(J)                                         \
+  case J:                                                  \
+    force_kernel<P, J, true><<<grid, block, 0, st>>>(kp); \
     break;
     G6_CASE(1)
     G6_CASE(2)
@@ -723,6 +846,7 @@ int launch(const KParams &kp, int jl, int gx, cudaStream_t st) {
     G6_CASE(32)
     G6_CASE(64)
     G6_CASE(128)
+    G6_CASE(256)
 #undef G6_CASE
     default:
       return -2;
@@ -737,7 +861,7 @@ extern "C" int g6k_sm_count(void) { return sm_count(); }
 
 extern "C" size_t g6k_scratch_bytes(int ni, int nj, int prec, int force_jl, int force_nsplit) {
   int jl, nsplit, jsplit;
-  choose_shape(ni, nj, force_jl, force_nsplit, &jl, &nsplit, &jsplit);
+  choose_shape(ni, nj, prec, force_jl, force_nsplit, &jl, &nsplit, &jsplit);
   if (nsplit <= 1) return 0;
   const size_t rec = prec == G6_PREC_FP64 ? sizeof(F64P::Out) : sizeof(SplitP::Out);
   return (size_t)nsplit * (size_t)ni * rec;
@@ -745,9 +869,10 @@ extern "C" size_t g6k_scratch_bytes(int ni, int nj, int prec, int force_jl, int 
 
 extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t st) {
   if (a->ni <= 0) return 0;
-  if (a->nj <= 0) return -1;
+  if (a->nj <= 0 || !a->acc || !a->jerk || !a->pot || !a->js || !a->err) return -1;
+  if (!a->ilist && (!a->ipos || !a->ivel)) return -1;
   int jl, nsplit, jsplit;
-  choose_shape(a->ni, a->nj, a->force_jl, a->force_nsplit, &jl, &nsplit, &jsplit);
+  choose_shape(a->ni, a->nj, a->prec, a->force_jl, a->force_nsplit, &jl, &nsplit, &jsplit);
   if (jl < 1 || jl > TJ || (jl & (jl - 1))) return -2;
   KParams kp;
   kp.ni = a->ni;
@@ -767,6 +892,7 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
   kp.part = a->scratch;
   kp.ni_pad = a->ni;
   kp.err = a->err;
+  kp.want_nn = a->want_nn;
   const size_t need = nsplit > 1 ? g6k_scratch_bytes(a->ni, a->nj, a->prec, jl, nsplit) : 0;
   if (need > a->scratch_bytes) return -4;
   const int islots = (NT / jl) * IPT;

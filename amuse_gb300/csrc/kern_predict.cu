@@ -10,7 +10,7 @@
 //   split: x_p as a double-single pair (hi = rn(x_p), lo = rn(x_p - hi)),
 //          v_p and m in FP32                      -> 48 B record
 //   fp64 : x_p, v_p, m in FP64                     -> 64 B record
-// Slots [nj, roundup(nj, 128)) get zero-mass records far away so the force
+// Slots [nj, roundup(nj, G6_TILE)) get zero-mass records far away so the force
 // kernel streams whole tiles.  Streams 15 doubles + 1 int per slot
 // (coalesced, component-major arrays) and writes one record.
 #include <cuda_runtime.h>

@@ -80,8 +80,19 @@ def build(verbose=False, force=False):
             if verbose and out.strip():
                 print(out)
     so = os.path.join(LIB, "libsapporo.so")
+    vscript = os.path.join(OBJ, "exports.map")
+    with open(vscript, "w") as f:  # export the public ABI only (g6*, g6x*)
+        f.write("{ global: g6_*; g6calc*; g6x_*; local: *; };\n")
     if force or _newer(objs, so):
-        _run([nvcc, *ARCH, "-shared", "-o", so, *objs, "-lpthread", "-ldl", "-lrt"])
+        _run([nvcc, *ARCH, "-shared", "-o", so, *objs, "-lpthread", "-ldl", "-lrt",
+              "-Xlinker", "--version-script=" + vscript])
+    # pkg-config file under the name AMUSE's configure scripts look for
+    # (lib/sapporo_light/Makefile:5-24 installs sapporo_light.pc)
+    with open(os.path.join(LIB, "sapporo_light.pc"), "w") as f:
+        f.write(f"prefix={ROOT}\nlibdir={LIB}\nincludedir={INCLUDE}\n\n"
+                "Name: sapporo_light\nDescription: GRAPE-6 ABI on GB300 (sm_103a)\n"
+                "Version: 2.0\nLibs: -L${libdir} -lsapporo -Wl,-rpath,${libdir}\n"
+                "Cflags: -I${includedir}\n")
     drv_src = os.path.join(CSRC, "g6_ph4drive.c")
     drv = os.path.join(LIB, "libg6drive.so")
     if force or _newer([drv_src, so] + headers, drv):

@@ -45,7 +45,7 @@ ABI_SYMBOLS = [
 BYVALUE_SYMBOLS = [s[:-1] for s in ABI_SYMBOLS]
 EXT_SYMBOLS = [
     "g6x_set_precision", "g6x_get_precision", "g6x_set_npipes", "g6x_last_error", "g6x_load",
-    "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_slots", "g6x_run_init", "g6x_run",
+    "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
     "g6x_energy", "g6x_step_all", "g6x_correct", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
 ]
 
@@ -96,6 +96,7 @@ def load():
     lib.g6x_force.argtypes = [D, D, I, I, _pd, _pd, _pi, _pd, _pd, _pd, _pi, _pf]
     lib.g6x_force_dev.argtypes = [D, D, I, I, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, I]
     lib.g6x_force_slots.argtypes = [D, D, I, I, _vp, _vp, _vp, _vp, _vp, I]
+    lib.g6x_force_dev_noalloc.argtypes = [D, D, I, I, _vp, _vp, _vp, _vp, _vp, _vp, _vp, I]
     lib.g6x_run_init.argtypes = [D, D]
     lib.g6x_run.argtypes = [D, ctypes.POINTER(ctypes.c_longlong), _pd]
     lib.g6x_energy.argtypes = [_pd, _pd]
@@ -264,6 +265,13 @@ class G6X(G6):
                   d_nnr2=None, sync=True):
         _check(self.lib.g6x_force_dev(ti, eps2, nj, ni, d_xi, d_vi, d_self, d_acc, d_jerk, d_pot,
                                       d_nn, d_nnr2, 1 if sync else 0), "g6x_force_dev")
+
+    def force_dev_noalloc(self, ti, eps2, nj, ni, d_xi, d_vi, d_self, d_acc, d_jerk, d_pot,
+                          d_nn=None, sync=True):
+        """g6x_force_dev without any device allocation (fixed 16 MiB scratch)."""
+        _check(self.lib.g6x_force_dev_noalloc(ti, eps2, nj, ni, d_xi, d_vi, d_self, d_acc,
+                                              d_jerk, d_pot, d_nn, 1 if sync else 0),
+               "g6x_force_dev_noalloc")
 
     def run_init(self, eps2, eta):
         _check(self.lib.g6x_run_init(eps2, eta), "g6x_run_init")

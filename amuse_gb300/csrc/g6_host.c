@@ -1262,3 +1262,83 @@ int g6x_energy(double *kinetic, double *potential) {
   if (potential) *potential = h[1] / 2;
   return read_err_word();
 }
+
+/* ---- force without any device allocation ----
+ * For callers that must not allocate device memory during the call: code
+ * whose device memory is owned and budgeted by a host framework (the
+ * framework hands out every buffer, so a library cudaMalloc would either fail
+ * or break its accounting), or code that cannot tolerate the implicit device
+ * synchronisation and latency of cudaMalloc/cudaFree in its step loop.  The
+ * j-system must already be resident (loaded and sized by earlier calls); the
+ * split-j partial sums go to a fixed 16 MiB device array inside the library
+ * instead of the growable scratch buffer.  Calls needing more than that, a
+ * larger j-store, or a larger update buffer are refused, never allocated. */
+size_t g6k_static_scratch_capacity(void);
+int g6k_force_static(const g6_force_args *a, g6_shape *shape, cudaStream_t st, size_t *need_out);
+
+int g6x_force_dev_noalloc(double ti, double eps2, int nj, int ni, const double *d_xi,
+                          const double *d_vi, const int *d_self_slot, double *d_acc,
+                          double *d_jerk, double *d_pot, int *d_nn, int sync) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (ni < 0 || nj < 0) return G6_ERR_ARG;
+  if (ni == 0) return 0;
+  if (nj == 0 || !d_xi || !d_vi || !d_acc || !d_jerk || !d_pot) {
+    seterr("g6x_force_dev_noalloc: nj = 0 or a NULL input/output pointer");
+    return G6_ERR_ARG;
+  }
+  const int nj_pad = (nj + G6_TILE - 1) / G6_TILE * G6_TILE;
+  if (nj_pad > G.js.cap) {
+    seterr("g6x_force_dev_noalloc: nj=%d exceeds the j-store (%d slots); it would need an "
+           "allocation", nj, G.js.cap);
+    return G6_ERR_ARG;
+  }
+  if (G.n_upd > G.cap_dupd) {
+    seterr("g6x_force_dev_noalloc: %d staged j updates exceed the update buffer (%d); it would "
+           "need an allocation", G.n_upd, G.cap_dupd);
+    return G6_ERR_ARG;
+  }
+  if (!G.d_err) {
+    seterr("g6x_force_dev_noalloc: library i/o buffers missing");
+    return G6_ERR_STATE;
+  }
+  G.ti = ti;
+  rc = flush_updates(); /* copies into the existing update buffer only */
+  if (rc) return rc;
+  rc = predict_if_needed(nj); /* the j-store already holds nj_pad slots */
+  if (rc) return rc;
+  g6_force_args a;
+  memset(&a, 0, sizeof(a));
+  a.ni = ni;
+  a.nj = nj;
+  a.prec = G.prec;
+  a.eps2 = eps2;
+  a.ipos = d_xi;
+  a.ivel = d_vi;
+  a.iself = d_self_slot;
+  a.ti = ti;
+  a.acc = d_acc;
+  a.jerk = d_jerk;
+  a.pot = d_pot;
+  a.nn = d_nn;
+  a.want_nn = d_nn != NULL;
+  a.js = &G.js;
+  a.err = G.d_err;
+  size_t need = 0;
+  rc = g6k_force_static(&a, &G.shape, G.st, &need);
+  if (rc == -4) {
+    seterr("g6x_force_dev_noalloc: ni=%d, nj=%d needs %zu B of split-j scratch, more than the "
+           "fixed %zu B; use g6x_force_dev or fewer i-particles per call", ni, nj, need,
+           g6k_static_scratch_capacity());
+    return G6_ERR_ARG;
+  }
+  if (rc) {
+    seterr("g6x_force_dev_noalloc: launch failed (%d)", rc);
+    return G6_ERR_CUDA;
+  }
+  if (sync) {
+    CK(cudaStreamSynchronize(G.st));
+    return read_err_word();
+  }
+  return 0;
+}

@@ -905,3 +905,43 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
   kp.jrec = a->js->jp_split;
   return launch<SplitP>(kp, jl, gx, st);
 }
+
+// ---------------------------------------------------------------------------
+// Fixed scratch for callers that cannot allocate device memory.
+//
+// The split-j partial sums normally live in a buffer that the host library
+// grows with cudaMalloc on demand.  g6k_force_static instead places them in
+// this file-scope array, which every GPU that loads the library holds (16 MiB)
+// until the process exits.  Its device address is looked up once per device,
+// on the first call made with that device current.  Every call shares the
+// array: nothing in it has to start at zero (each partial record is written
+// by exactly one CTA before the second pass reads it), and calls that overlap
+// on the GPU (different streams, or host threads) race on it.
+#define G6_STATIC_SCRATCH_BYTES (16u << 20)
+static __device__ __align__(256) unsigned char g6_static_scratch[G6_STATIC_SCRATCH_BYTES];
+
+extern "C" size_t g6k_static_scratch_capacity(void) { return G6_STATIC_SCRATCH_BYTES; }
+
+// Returns 0, -1/-2/-3 as g6k_force, -4 when the launch shape needs more than
+// G6_STATIC_SCRATCH_BYTES of scratch (*need_out tells how much), -5 when the
+// array's device address cannot be obtained.
+extern "C" int g6k_force_static(const g6_force_args *a, g6_shape *shape, cudaStream_t st,
+                                size_t *need_out) {
+  static void *addr[64];
+  static int have[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -5;
+  if (!have[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g6_static_scratch) != cudaSuccess || p == nullptr) return -5;
+    addr[dev] = p;
+    have[dev] = 1;
+  }
+  const size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->force_jl, a->force_nsplit);
+  if (need_out) *need_out = need;
+  if (need > G6_STATIC_SCRATCH_BYTES) return -4;
+  g6_force_args b = *a;
+  b.scratch = addr[dev];
+  b.scratch_bytes = G6_STATIC_SCRATCH_BYTES;
+  return g6k_force(&b, shape, st);
+}

@@ -148,6 +148,20 @@ int g6x_force(double ti, double eps2, int nj, int ni, const double (*xi)[3],
 int g6x_force_dev(double ti, double eps2, int nj, int ni, const double *d_xi,
                   const double *d_vi, const int *d_self_slot, double *d_acc, double *d_jerk,
                   double *d_pot, int *d_nn, float *d_nn_r2, int sync);
+/* As g6x_force_dev, but the call allocates no device memory: no reference
+   counterpart (the GRAPE-6 library has nothing like it).  For callers that
+   may not allocate during the call -- device memory owned and budgeted by a
+   host framework, or step loops that cannot absorb cudaMalloc's implicit
+   synchronisation.  The split-j partial sums use a fixed 16 MiB array that
+   every GPU loading the library holds until exit; the first call on a device
+   looks up that array's address (do it before any stream capture).  A call
+   whose launch shape needs more scratch, or whose nj exceeds the j-store
+   already allocated, or with more staged j updates than the update buffer
+   holds, returns G6_ERR_ARG instead of allocating.  All calls share the
+   array: calls that overlap on the GPU race and must not be issued. */
+int g6x_force_dev_noalloc(double ti, double eps2, int nj, int ni, const double *d_xi,
+                          const double *d_vi, const int *d_self_slot, double *d_acc,
+                          double *d_jerk, double *d_pot, int *d_nn, int sync);
 /* Force on the device-resident slots d_ilist[0..ni) predicted to ti (i data
    taken from the predicted j records; self excluded by slot). */
 int g6x_force_slots(double ti, double eps2, int nj, int ni, const int *d_ilist, double *d_acc,

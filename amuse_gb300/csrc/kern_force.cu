@@ -18,12 +18,12 @@
 // here the host resolves id -> j slot once per call and the kernel skips
 // that slot.
 //
-// Structure (one CTA = 256 threads = 8 warps, 2 i-particles per thread):
+// Structure (one CTA = 128 threads = 4 warps, 4 i-particles per thread):
 //   * j-tiles of 256 records are streamed HBM/L2 -> shared memory with
 //     cp.async.bulk (TMA, non-tensor) completing on an mbarrier; warps
 //     consume the ring independently (no CTA barrier in the loop).
 //   * JL j-lanes share each i-particle (JL = 1 for large i-blocks, up to
-//     256 for tiny ones); j is also split across CTAs (grid.y) so that small
+//     128 for tiny ones); j is also split across CTAs (grid.y) so that small
 //     active blocks still fill all 152 SMs.
 //   * Lanes of one i merge with warp shuffles (plus shared memory across
 //     warps for JL > 32); CTAs of one i merge in a second pass kernel, in
@@ -53,10 +53,10 @@ namespace {
 
 // Tuning constants (compile-time; the defaults are the measured best).
 #ifndef G6_NT
-#define G6_NT 256
+#define G6_NT 128
 #endif
 #ifndef G6_IPT
-#define G6_IPT 2
+#define G6_IPT 4
 #endif
 #ifndef G6_UNROLL
 #define G6_UNROLL 4
@@ -68,6 +68,7 @@ constexpr int NT = G6_NT;    // threads per CTA
 constexpr int TJ = G6_TILE;  // j records per tile
 constexpr int IPT = G6_IPT;  // i-particles per thread
 constexpr int UNROLL = G6_UNROLL;  // j-loop unroll factor
+constexpr int JLMAX = TJ < NT ? TJ : NT;  // j-lanes per i at most
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound per wait
 
 enum { ERR_TMA_TIMEOUT = 1, ERR_SHAPE = 2 };
@@ -467,7 +468,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   constexpr int ISLOTS = NIL * IPT;      // i-particles per CTA
   constexpr int JPT = TJ / JL;           // j per thread per tile
   constexpr int FOLD_TILES = (FOLD_J / JPT) > 0 ? (FOLD_J / JPT) : 1;
-  static_assert(JL >= 1 && JL <= TJ && (TJ % JL) == 0, "JL");
+  static_assert(JL >= 1 && JL <= JLMAX && (TJ % JL) == 0, "JL");
 
   __shared__ __align__(128) Rec tiles[NSTAGE][TJ];
   __shared__ __align__(8) uint64_t full[NSTAGE];
@@ -735,7 +736,7 @@ int sm_count() {
 // about two resident CTAs per SM, with at least 4 tiles per split.
 // Launch shape from a small cost model.  A CTA streams tiles_per tiles of
 // its j-range; per tile each thread spends ~A issue slots of fixed work
-// (wait, release, bookkeeping) plus B per j-record for its 2 i-particles
+// (wait, release, bookkeeping) plus B per j-record for its IPT i-particles
 // (JPT = 256/JL records), plus F per CTA (i-loads, lane merges, output).
 // Resident CTAs run in waves of MINB per SM, so
 //   cost = waves * (tiles_per * (A + B * JPT) + F) * (1 + 0.002 * nsplit)
@@ -766,10 +767,10 @@ void choose_shape(int ni, int nj, int prec, int force_jl, int force_nsplit, int 
   const int minb = prec == G6_PREC_FP64 ? F64P::MINB : SplitP::MINB;
   const int slots = minb * sm_count();
   const double A = 150.0, F = 3000.0;
-  const double B = prec == G6_PREC_FP64 ? 76.0 * 32.0 : 76.0;
+  const double B = (prec == G6_PREC_FP64 ? 32.0 : 1.0) * 37.0 * IPT;
   int jl0 = 1;
-  while (jl0 < TJ && (NT / (jl0 * 2)) * IPT >= ni && ni > 0) jl0 *= 2;
-  int jl_lo = jl0, jl_hi = TJ;
+  while (jl0 < JLMAX && (NT / (jl0 * 2)) * IPT >= ni && ni > 0) jl0 *= 2;
+  int jl_lo = jl0, jl_hi = JLMAX;
   if (force_jl > 0) jl_lo = jl_hi = force_jl;
   else if (jl0 == 1 && (ni + (NT * IPT) - 1) / (NT * IPT) >= slots) jl_hi = 1;
   const int max_ns = ntiles < 4 * slots ? ntiles : 4 * slots;
@@ -840,7 +841,9 @@ int launch(const KParams &kp, int jl, int gx, cudaStream_t st) {
     G6_CASE(32)
     G6_CASE(64)
     G6_CASE(128)
+#if G6_NT >= 256
     G6_CASE(256)
+#endif
 #undef G6_CASE
     default:
       return -2;
@@ -867,7 +870,7 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
   if (!a->ilist && (!a->ipos || !a->ivel)) return -1;
   int jl, nsplit, jsplit;
   choose_shape(a->ni, a->nj, a->prec, a->force_jl, a->force_nsplit, &jl, &nsplit, &jsplit);
-  if (jl < 1 || jl > TJ || (jl & (jl - 1))) return -2;
+  if (jl < 1 || jl > JLMAX || (jl & (jl - 1))) return -2;
   KParams kp;
   kp.ni = a->ni;
   kp.nj = a->nj;

@@ -46,7 +46,8 @@ BYVALUE_SYMBOLS = [s[:-1] for s in ABI_SYMBOLS]
 EXT_SYMBOLS = [
     "g6x_set_precision", "g6x_get_precision", "g6x_set_npipes", "g6x_last_error", "g6x_load",
     "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
-    "g6x_energy", "g6x_step_all", "g6x_correct", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
+    "g6x_energy", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
+    "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
 ]
 
 _lib = None
@@ -102,6 +103,11 @@ def load():
     lib.g6x_energy.argtypes = [_pd, _pd]
     lib.g6x_step_all.argtypes = [D]
     lib.g6x_correct.argtypes = [I, _pi, D, D, _pd, _pd]
+    _pll = ctypes.POINTER(ctypes.c_longlong)
+    lib.g6x_batch_run.argtypes = [I, _pi, _pd, _pd, _pd, _pd, D, I, ctypes.c_longlong, I, _pd,
+                                  _pll, _pd, _pi, _pd]
+    lib.g6x_batch_config.argtypes = [I, I]
+    lib.g6x_batch_tune.argtypes = [I, _pi, _pd, _pd, _pd, _pd, D, I, I, D, _pd]
     lib.g6x_system_time.restype = D
     lib.g6x_timing.argtypes = [I]
     lib.g6x_stats.argtypes = [_pd]
@@ -289,6 +295,44 @@ class G6X(G6):
         _check(self.lib.g6x_correct(n, _ptr(slots, ctypes.c_int), tnext, eta,
                                     _ptr(acc, ctypes.c_double), _ptr(jerk, ctypes.c_double)),
                "g6x_correct")
+
+    def batch_run(self, n_per_sys, t_end, mass, pos, vel, eta=0.14, n_iter=2, max_steps=0,
+                  exact=False):
+        """Integrate many few-body systems (smallN's scheme); returns a dict
+        with pos, vel (updated copies), t_final, steps, wall_ms, status, elapsed_ms."""
+        n_per_sys = _i32(n_per_sys)
+        nsys = len(n_per_sys)
+        t_end = _f64(np.broadcast_to(np.asarray(t_end, dtype=np.float64), (nsys,)))
+        nb = int(n_per_sys.sum())
+        mass = _f64(mass)
+        pos = _f64(pos, (nb, 3)).copy()
+        vel = _f64(vel, (nb, 3)).copy()
+        tf = np.zeros(nsys); st = np.zeros(nsys, np.int64); wall = np.zeros(nsys)
+        status = np.zeros(nsys, np.int32); el = ctypes.c_double(0)
+        P = lambda a: _ptr(a, ctypes.c_double)
+        _check(self.lib.g6x_batch_run(nsys, _ptr(n_per_sys, ctypes.c_int), P(t_end), P(mass),
+                                      P(pos), P(vel), eta, n_iter, int(max_steps),
+                                      1 if exact else 0, P(tf),
+                                      st.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                      P(wall), _ptr(status, ctypes.c_int), ctypes.byref(el)),
+               "g6x_batch_run")
+        return dict(pos=pos, vel=vel, t_final=tf, steps=st, wall_ms=wall, status=status,
+                    elapsed_ms=el.value)
+
+    def batch_config(self, warps_per_cta, ctas_per_sm):
+        _check(self.lib.g6x_batch_config(warps_per_cta, ctas_per_sm), "g6x_batch_config")
+
+    def batch_tune(self, n_per_sys, t_end, mass, pos, vel, eta=0.14, n_iter=2, exact=False,
+                   frac=0.1):
+        n_per_sys = _i32(n_per_sys)
+        nsys = len(n_per_sys)
+        t_end = _f64(np.broadcast_to(np.asarray(t_end, dtype=np.float64), (nsys,)))
+        out = np.zeros(3)
+        P = lambda a: _ptr(a, ctypes.c_double)
+        _check(self.lib.g6x_batch_tune(nsys, _ptr(n_per_sys, ctypes.c_int), P(t_end),
+                                       P(_f64(mass)), P(_f64(pos)), P(_f64(vel)), eta, n_iter,
+                                       1 if exact else 0, frac, P(out)), "g6x_batch_tune")
+        return dict(warps_per_cta=int(out[0]), ctas_per_sm=int(out[1]), ms=out[2])
 
     def step_all(self, tnext):
         _check(self.lib.g6x_step_all(tnext), "g6x_step_all")

@@ -1342,3 +1342,251 @@ int g6x_force_dev_noalloc(double ti, double eps2, int nj, int ni, const double *
   }
   return 0;
 }
+
+/* ===================================== batched few-body systems ======= */
+/* Many independent systems (n <= 64 each) integrated with smallN's scheme
+ * in one persistent kernel fed by a device work queue (kern_batch.cu).  The
+ * queue-reset + kernel pair is captured in a CUDA graph, re-captured only
+ * when buffers or parameters change.  Launch shape (warps per CTA, CTAs per
+ * SM) comes from g6x_batch_tune or defaults to 4 x 2. */
+int g6k_batch_max_n(void);
+int g6k_batch_launch(int nsys, const int *order, const int *off, const double *t_end,
+                     const double *mass, double *pos, double *vel, double eta, int n_iter,
+                     long long max_steps, int exact, int warps_per_cta, int ctas, int *queue,
+                     double *t_out, long long *steps_out, unsigned long long *wall_ns,
+                     int *status, cudaStream_t st);
+
+static struct {
+  int cap_sys, cap_body;
+  int *d_order, *d_off, *d_queue, *d_status;
+  double *d_tend, *d_mass, *d_pos, *d_vel, *d_tout;
+  long long *d_steps;
+  unsigned long long *d_wall;
+  int wpc, cps; /* warps per CTA, CTAs per SM */
+  cudaGraphExec_t gexec;
+  int g_nsys, g_exact, g_niter, g_wpc, g_cps;
+  double g_eta;
+  long long g_maxsteps;
+  void *g_key;
+} BT = {0, 0, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, 4, 2,
+        NULL, 0, 0, 0, 0, 0, 0.0, 0, NULL};
+
+static int batch_ensure(int nsys, int nbody) {
+  if (nsys > BT.cap_sys) {
+    cudaFree(BT.d_order); cudaFree(BT.d_off); cudaFree(BT.d_tend); cudaFree(BT.d_tout);
+    cudaFree(BT.d_steps); cudaFree(BT.d_wall); cudaFree(BT.d_status);
+    BT.cap_sys = 0;
+    size_t s = (size_t)nsys;
+    if (cudaMalloc((void **)&BT.d_order, sizeof(int) * s) != cudaSuccess ||
+        cudaMalloc((void **)&BT.d_off, sizeof(int) * (s + 1)) != cudaSuccess ||
+        cudaMalloc((void **)&BT.d_tend, sizeof(double) * s) != cudaSuccess ||
+        cudaMalloc((void **)&BT.d_tout, sizeof(double) * s) != cudaSuccess ||
+        cudaMalloc((void **)&BT.d_steps, sizeof(long long) * s) != cudaSuccess ||
+        cudaMalloc((void **)&BT.d_wall, sizeof(unsigned long long) * s) != cudaSuccess ||
+        cudaMalloc((void **)&BT.d_status, sizeof(int) * s) != cudaSuccess) {
+      seterr("cannot allocate batch buffers for %d systems", nsys);
+      return G6_ERR_NOMEM;
+    }
+    BT.cap_sys = nsys;
+  }
+  if (nbody > BT.cap_body) {
+    cudaFree(BT.d_mass); cudaFree(BT.d_pos); cudaFree(BT.d_vel);
+    BT.cap_body = 0;
+    size_t b = (size_t)nbody;
+    if (cudaMalloc((void **)&BT.d_mass, sizeof(double) * b) != cudaSuccess ||
+        cudaMalloc((void **)&BT.d_pos, sizeof(double) * 3 * b) != cudaSuccess ||
+        cudaMalloc((void **)&BT.d_vel, sizeof(double) * 3 * b) != cudaSuccess) {
+      seterr("cannot allocate batch buffers for %d bodies", nbody);
+      return G6_ERR_NOMEM;
+    }
+    BT.cap_body = nbody;
+  }
+  if (!BT.d_queue && cudaMalloc((void **)&BT.d_queue, sizeof(int)) != cudaSuccess)
+    return G6_ERR_NOMEM;
+  return 0;
+}
+
+static int cmp_desc_n(const void *a, const void *b) {
+  const int *x = (const int *)a, *y = (const int *)b; /* (n, index) pairs */
+  if (x[0] != y[0]) return y[0] - x[0];
+  return x[1] - y[1];
+}
+
+/* Launch through a (cached) CUDA graph: queue reset + persistent kernel. */
+static int batch_graph_launch(int nsys, double eta, int n_iter, long long max_steps, int exact) {
+  const int ctas = BT.cps * g6k_sm_count();
+  if (!BT.gexec || BT.g_nsys != nsys || BT.g_exact != exact || BT.g_niter != n_iter ||
+      BT.g_eta != eta || BT.g_maxsteps != max_steps || BT.g_wpc != BT.wpc ||
+      BT.g_cps != BT.cps || BT.g_key != (void *)BT.d_pos) {
+    if (BT.gexec) {
+      cudaGraphExecDestroy(BT.gexec);
+      BT.gexec = NULL;
+    }
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(G.st, cudaStreamCaptureModeThreadLocal));
+    int rc = g6k_batch_launch(nsys, BT.d_order, BT.d_off, BT.d_tend, BT.d_mass, BT.d_pos,
+                              BT.d_vel, eta, n_iter, max_steps, exact, BT.wpc, ctas, BT.d_queue,
+                              BT.d_tout, BT.d_steps, BT.d_wall, BT.d_status, G.st);
+    cudaError_t e = cudaStreamEndCapture(G.st, &g);
+    if (rc || e != cudaSuccess) {
+      seterr("batch graph capture failed (%d, %s)", rc, cudaGetErrorString(e));
+      return G6_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&BT.gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      seterr("batch graph instantiate failed: %s", cudaGetErrorString(e));
+      BT.gexec = NULL;
+      return G6_ERR_CUDA;
+    }
+    BT.g_nsys = nsys;
+    BT.g_exact = exact;
+    BT.g_niter = n_iter;
+    BT.g_eta = eta;
+    BT.g_maxsteps = max_steps;
+    BT.g_wpc = BT.wpc;
+    BT.g_cps = BT.cps;
+    BT.g_key = (void *)BT.d_pos;
+  }
+  CK(cudaGraphLaunch(BT.gexec, G.st));
+  return 0;
+}
+
+int g6x_batch_config(int warps_per_cta, int ctas_per_sm) {
+  if (warps_per_cta < 1 || warps_per_cta > 8 || ctas_per_sm < 1 || ctas_per_sm > 16)
+    return G6_ERR_ARG;
+  BT.wpc = warps_per_cta;
+  BT.cps = ctas_per_sm;
+  return 0;
+}
+
+int g6x_batch_run(int nsys, const int *n_per_sys, const double *t_end, const double *mass,
+                  double (*pos)[3], double (*vel)[3], double eta, int n_iter,
+                  long long max_steps, int exact, double *t_final, long long *steps,
+                  double *wall_ms, int *status, double *elapsed_ms) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (nsys <= 0 || !n_per_sys || !t_end || !mass || !pos || !vel || n_iter < 0 || eta <= 0)
+    return G6_ERR_ARG;
+  const int maxn = g6k_batch_max_n();
+  int *off = (int *)malloc(sizeof(int) * (size_t)(nsys + 1));
+  int *pairs = (int *)malloc(sizeof(int) * 2 * (size_t)nsys);
+  int *order = (int *)malloc(sizeof(int) * (size_t)nsys);
+  if (!off || !pairs || !order) {
+    free(off); free(pairs); free(order);
+    return G6_ERR_NOMEM;
+  }
+  off[0] = 0;
+  for (int s = 0; s < nsys; s++) {
+    if (n_per_sys[s] < 2 || n_per_sys[s] > maxn) {
+      seterr("g6x_batch_run: system %d has n=%d (supported 2..%d)", s, n_per_sys[s], maxn);
+      free(off); free(pairs); free(order);
+      return G6_ERR_ARG;
+    }
+    off[s + 1] = off[s] + n_per_sys[s];
+    pairs[2 * s] = n_per_sys[s];
+    pairs[2 * s + 1] = s;
+  }
+  /* largest systems first: the queue then balances like LPT scheduling */
+  qsort(pairs, (size_t)nsys, 2 * sizeof(int), cmp_desc_n);
+  for (int q = 0; q < nsys; q++) order[q] = pairs[2 * q + 1];
+  const int nb = off[nsys];
+  rc = batch_ensure(nsys, nb);
+  if (rc == 0) {
+    cudaMemcpyAsync(BT.d_order, order, sizeof(int) * (size_t)nsys, cudaMemcpyHostToDevice, G.st);
+    cudaMemcpyAsync(BT.d_off, off, sizeof(int) * (size_t)(nsys + 1), cudaMemcpyHostToDevice, G.st);
+    cudaMemcpyAsync(BT.d_tend, t_end, sizeof(double) * (size_t)nsys, cudaMemcpyHostToDevice, G.st);
+    cudaMemcpyAsync(BT.d_mass, mass, sizeof(double) * (size_t)nb, cudaMemcpyHostToDevice, G.st);
+    cudaMemcpyAsync(BT.d_pos, &pos[0][0], sizeof(double) * 3 * (size_t)nb, cudaMemcpyHostToDevice,
+                    G.st);
+    cudaMemcpyAsync(BT.d_vel, &vel[0][0], sizeof(double) * 3 * (size_t)nb, cudaMemcpyHostToDevice,
+                    G.st);
+    cudaEventRecord(G.ev_t0, G.st);
+    rc = batch_graph_launch(nsys, eta, n_iter, max_steps > 0 ? max_steps : (1LL << 40), exact);
+    cudaEventRecord(G.ev_t1, G.st);
+  }
+  free(off); free(pairs); free(order);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(&pos[0][0], BT.d_pos, sizeof(double) * 3 * (size_t)nb, cudaMemcpyDeviceToHost,
+                     G.st));
+  CK(cudaMemcpyAsync(&vel[0][0], BT.d_vel, sizeof(double) * 3 * (size_t)nb, cudaMemcpyDeviceToHost,
+                     G.st));
+  unsigned long long *wall = (unsigned long long *)malloc(sizeof(unsigned long long) * (size_t)nsys);
+  if (!wall) return G6_ERR_NOMEM;
+  CK(cudaMemcpyAsync(wall, BT.d_wall, sizeof(unsigned long long) * (size_t)nsys,
+                     cudaMemcpyDeviceToHost, G.st));
+  if (t_final)
+    CK(cudaMemcpyAsync(t_final, BT.d_tout, sizeof(double) * (size_t)nsys, cudaMemcpyDeviceToHost,
+                       G.st));
+  if (steps)
+    CK(cudaMemcpyAsync(steps, BT.d_steps, sizeof(long long) * (size_t)nsys,
+                       cudaMemcpyDeviceToHost, G.st));
+  if (status)
+    CK(cudaMemcpyAsync(status, BT.d_status, sizeof(int) * (size_t)nsys, cudaMemcpyDeviceToHost,
+                       G.st));
+  cudaError_t e = cudaStreamSynchronize(G.st);
+  if (e != cudaSuccess) {
+    free(wall);
+    seterr("batch run failed: %s", cudaGetErrorString(e));
+    return G6_ERR_CUDA;
+  }
+  if (wall_ms)
+    for (int s = 0; s < nsys; s++) wall_ms[s] = (double)wall[s] * 1e-6;
+  free(wall);
+  if (elapsed_ms) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, G.ev_t0, G.ev_t1);
+    *elapsed_ms = ms;
+  }
+  return 0;
+}
+
+/* Autotuner: time every (warps per CTA, CTAs per SM) shape whose warps fit
+ * the register file on a copy of the given systems (shortened to frac of
+ * their end time) and keep the fastest.  out[0..2] = best wpc, cps, ms. */
+int g6x_batch_tune(int nsys, const int *n_per_sys, const double *t_end, const double *mass,
+                   const double (*pos)[3], const double (*vel)[3], double eta, int n_iter,
+                   int exact, double frac, double out[3]) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (nsys <= 0 || frac <= 0) return G6_ERR_ARG;
+  int nb = 0;
+  for (int s = 0; s < nsys; s++) nb += n_per_sys[s];
+  double *te = (double *)malloc(sizeof(double) * (size_t)nsys);
+  double(*p)[3] = (double(*)[3])malloc(sizeof(double) * 3 * (size_t)nb);
+  double(*v)[3] = (double(*)[3])malloc(sizeof(double) * 3 * (size_t)nb);
+  if (!te || !p || !v) {
+    free(te); free(p); free(v);
+    return G6_ERR_NOMEM;
+  }
+  for (int s = 0; s < nsys; s++) te[s] = t_end[s] * frac;
+  static const int shapes[][2] = {{1, 8}, {2, 4}, {2, 6}, {4, 2}, {4, 3}, {8, 1}, {1, 4},
+                                  {2, 2}, {4, 1}, {1, 12}, {3, 4}, {6, 2}};
+  const int nshape = (int)(sizeof(shapes) / sizeof(shapes[0]));
+  double best = 1e300;
+  int bw = BT.wpc, bc = BT.cps;
+  for (int k = 0; k < nshape; k++) {
+    memcpy(p, pos, sizeof(double) * 3 * (size_t)nb);
+    memcpy(v, vel, sizeof(double) * 3 * (size_t)nb);
+    BT.wpc = shapes[k][0];
+    BT.cps = shapes[k][1];
+    double ms = 0;
+    rc = g6x_batch_run(nsys, n_per_sys, te, mass, p, v, eta, n_iter, 0, exact, NULL, NULL, NULL,
+                       NULL, &ms);
+    if (rc) break;
+    if (ms < best) {
+      best = ms;
+      bw = shapes[k][0];
+      bc = shapes[k][1];
+    }
+  }
+  free(te); free(p); free(v);
+  BT.wpc = bw;
+  BT.cps = bc;
+  if (out) {
+    out[0] = bw;
+    out[1] = bc;
+    out[2] = best;
+  }
+  return rc;
+}

@@ -1,0 +1,384 @@
+// kern_batch.cu -- many independent few-body systems in one persistent
+// launch (the encounters that AMUSE's multiples module hands to smallN).
+//
+// Each warp takes a system from a device work queue (an atomic counter over
+// a host-chosen order, largest systems first), integrates it to its end
+// time, writes it back and takes the next one, so uneven systems balance
+// themselves.  The integrator is smallN's (src/amuse_ph4/src/smallN.cc)
+// without the unperturbed-binary tree: a shared-step, time-symmetrised
+// 4th-order Hermite scheme --
+//   predict_loworder (hdyn.h:192-201) from the stored old acc/jerk,
+//   n_iter + 1 force evaluations per step, each followed by
+//   correct_acc_and_jerk / correct_pos_and_vel (smallN.cc:487-531) for the
+//   iterated step new_dt (smallN.cc:617-660),
+//   step from the Kepler criterion eta * sqrt(min over pairs of
+//   min(0.5 r^3 / (m_i + m_j), r^2 / v^2)) (smallN.cc:85-116, :318-363).
+// State is FP64.  Lane l owns bodies l and l + 32 (n <= 64).
+//
+// EXACT = true evaluates every expression with the same IEEE operations, in
+// the same order, as smallN on the CPU (each pair in its (i < j) orientation,
+// contributions accumulated in smallN's pair order, no fused multiply-adds,
+// IEEE divides and square roots), so results are bit-identical to smallN.
+// EXACT = false uses one reciprocal square root per pair and FMAs (about 7x
+// fewer FP64 instructions; results differ from smallN at the last-bit
+// level, which chaotic systems amplify).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace {
+
+constexpr int MAXN = 64;
+constexpr int WARPS_MAX = 8;
+
+
+__device__ __forceinline__ double ADD(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double SUB(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double MUL(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double DIV(double a, double b) { return __ddiv_rn(a, b); }
+
+struct Body {
+  double m, inv_m;
+  double pos[3], vel[3], pp[3], pv[3], acc[3], jerk[3], oacc[3], ojerk[3];
+};
+
+struct WarpSmem {
+  double pp[MAXN][3];
+  double pv[MAXN][3];
+  double m[MAXN];
+};
+
+// 1/sqrt(x): FP32 MUFU seed, two Newton-Raphson steps.
+__device__ __forceinline__ double rsqrt64(double x) {
+  double y = (double)rsqrtf((float)x);
+  const double hx = 0.5 * x;
+  y = y * fma(-hx * y, y, 1.5);
+  y = y * fma(-hx * y, y, 1.5);
+  return y;
+}
+
+// Contribution of the pair (a, b), a < b in smallN's orientation, to body
+// `me` (me == a or me == b), plus the pair's Kepler time-step^2.
+template <bool EXACT>
+__device__ __forceinline__ double pair_term(const WarpSmem &S, int a, int b, bool me_is_a,
+                                            double inv_me, double acc[3], double jerk[3]) {
+  const double ma = S.m[a], mb = S.m[b];
+  double dx[3], dv[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    dx[k] = SUB(S.pp[b][k], S.pp[a][k]);
+    dv[k] = SUB(S.pv[b][k], S.pv[a][k]);
+  }
+  if (EXACT) {
+    const double d2 = ADD(ADD(MUL(dx[0], dx[0]), MUL(dx[1], dx[1])), MUL(dx[2], dx[2]));
+    const double d = __dsqrt_rn(d2);
+    const double d3 = MUL(d2, d);
+    const double xv = ADD(ADD(MUL(dx[0], dv[0]), MUL(dx[1], dv[1])), MUL(dx[2], dv[2]));
+    const double d5 = MUL(d3, d2);
+    const double s = me_is_a ? inv_me : -inv_me;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double iforce = DIV(MUL(mb, dx[k]), d3);
+      const double ijerk = MUL(mb, SUB(DIV(dv[k], d3), DIV(MUL(MUL(3.0, dx[k]), xv), d5)));
+      const double force = MUL(ma, iforce);
+      const double jk = MUL(ma, ijerk);
+      acc[k] = ADD(acc[k], MUL(s, force));
+      jerk[k] = ADD(jerk[k], MUL(s, jk));
+    }
+    const double mass = ADD(mb, ma);
+    const double vel2 = ADD(ADD(MUL(dv[0], dv[0]), MUL(dv[1], dv[1])), MUL(dv[2], dv[2]));
+    const double dtff2 = DIV(MUL(0.5, d3), mass);
+    const double dtv2 = DIV(d2, fabs(vel2));
+    return fmin(dtff2, dtv2);
+  } else {
+    const double d2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+    const double rinv = rsqrt64(d2);
+    const double rinv2 = rinv * rinv;
+    const double rinv3 = rinv * rinv2;
+    const double xv = dx[0] * dv[0] + dx[1] * dv[1] + dx[2] * dv[2];
+    const double mo = me_is_a ? mb : -ma;  // force/m_me on me
+    const double f = mo * rinv3;
+    const double a3 = -3.0 * xv * rinv2;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      acc[k] = fma(f, dx[k], acc[k]);
+      jerk[k] = fma(f, fma(a3, dx[k], dv[k]), jerk[k]);
+    }
+    (void)inv_me;
+    const double vel2 = dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2];
+    const double d3 = d2 * d2 * rinv;
+    const double dtff2 = 0.5 * d3 / (ma + mb);
+    const double dtv2 = d2 / vel2;
+    return fmin(dtff2, dtv2);
+  }
+}
+
+// acc/jerk of the lane's bodies from the predicted state in S; returns the
+// system's min Kepler step^2 (warp-uniform).
+template <bool EXACT>
+__device__ double forces(const WarpSmem &S, int n, int lane, Body B[2]) {
+  double ts2 = __longlong_as_double(0x7ff0000000000000ll);
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int i = lane + 32 * q;
+#pragma unroll
+    for (int k = 0; k < 3; k++) B[q].acc[k] = B[q].jerk[k] = 0.0;
+    if (i >= n) continue;
+    if (EXACT) {
+      // smallN's pair order: (j, i) for j < i first, then (i, j) for j > i,
+      // each pair in its (i < j) orientation.
+      for (int j = 0; j < i; j++)
+        ts2 = fmin(ts2, pair_term<true>(S, j, i, false, B[q].inv_m, B[q].acc, B[q].jerk));
+      for (int j = i + 1; j < n; j++)
+        ts2 = fmin(ts2, pair_term<true>(S, i, j, true, B[q].inv_m, B[q].acc, B[q].jerk));
+    } else {
+      // orientation-free (same instruction stream in every lane)
+      for (int j = 0; j < n; j++) {
+        if (j == i) continue;
+        ts2 = fmin(ts2, pair_term<false>(S, i, j, true, B[q].inv_m, B[q].acc, B[q].jerk));
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ts2 = fmin(ts2, __shfl_xor_sync(0xffffffffu, ts2, o));
+  return ts2;
+}
+
+__device__ __forceinline__ void publish(WarpSmem &S, int n, int lane, const Body B[2]) {
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int i = lane + 32 * q;
+    if (i < n) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        S.pp[i][k] = B[q].pp[k];
+        S.pv[i][k] = B[q].pv[k];
+      }
+    }
+  }
+  __syncwarp();
+}
+
+template <bool EXACT>
+__global__ void batch_kernel(int nsys, const int *__restrict__ order, const int *__restrict__ off,
+                             const double *__restrict__ t_end_s, const double *__restrict__ mass,
+                             double *pos, double *vel, double eta, int n_iter,
+                             long long max_steps, int *queue, double *t_out, long long *steps_out,
+                             unsigned long long *wall_ns, int *status) {
+  __shared__ WarpSmem smem[WARPS_MAX];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  WarpSmem &S = smem[w];
+  while (true) {
+    int q = 0;
+    if (lane == 0) q = atomicAdd(queue, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= nsys) break;
+    const int s = order[q];
+    unsigned long long t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    const int base = off[s];
+    const int n = off[s + 1] - base;
+    const double t_end = t_end_s[s];
+    if (n < 2 || n > MAXN) {
+      if (lane == 0) {
+        status[s] = 2;  // unsupported size (host also checks)
+        steps_out[s] = 0;
+        t_out[s] = 0.0;
+      }
+      continue;
+    }
+    Body B[2];
+#pragma unroll
+    for (int qq = 0; qq < 2; qq++) {
+      const int i = lane + 32 * qq;
+      const int ii = i < n ? i : 0;
+      B[qq].m = mass[base + ii];
+      B[qq].inv_m = EXACT ? DIV(1.0, B[qq].m) : 1.0 / B[qq].m;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        B[qq].pos[k] = pos[3 * (base + ii) + k];
+        B[qq].vel[k] = vel[3 * (base + ii) + k];
+        B[qq].pp[k] = B[qq].pos[k];  // init_pred
+        B[qq].pv[k] = B[qq].vel[k];
+        B[qq].oacc[k] = B[qq].ojerk[k] = 0.0;  // hdyn() zeroes them
+      }
+      if (i < n) S.m[i] = B[qq].m;
+    }
+    publish(S, n, lane, B);
+    double t = 0.0, t_pred = -1.0;
+    double dt = EXACT ? MUL(eta, __dsqrt_rn(forces<EXACT>(S, n, lane, B)))
+                      : eta * sqrt(forces<EXACT>(S, n, lane, B));
+    long long nsteps = 0;
+    int st = 0;
+    while (t < t_end) {
+      if (nsteps >= max_steps) {
+        st = 1;  // step budget exhausted
+        break;
+      }
+      const double tn = EXACT ? ADD(t, dt) : t + dt;
+      if (tn != t_pred) {  // predict_loworder_all
+        const double h = EXACT ? SUB(tn, t) : tn - t;
+        const double h3 = EXACT ? DIV(h, 3.0) : h / 3.0;
+        const double h2 = EXACT ? DIV(h, 2.0) : h * 0.5;
+#pragma unroll
+        for (int qq = 0; qq < 2; qq++) {
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            const double oj = B[qq].ojerk[k], oa = B[qq].oacc[k];
+            if (EXACT) {
+              B[qq].pp[k] = ADD(MUL(ADD(MUL(ADD(MUL(oj, h3), oa), h2), B[qq].vel[k]), h), B[qq].pos[k]);
+              B[qq].pv[k] = ADD(MUL(ADD(MUL(oj, h2), oa), h), B[qq].vel[k]);
+            } else {
+              B[qq].pp[k] = fma(fma(fma(oj, h3, oa), h2, B[qq].vel[k]), h, B[qq].pos[k]);
+              B[qq].pv[k] = fma(fma(oj, h2, oa), h, B[qq].vel[k]);
+            }
+          }
+        }
+        t_pred = tn;
+      }
+#pragma unroll
+      for (int qq = 0; qq < 2; qq++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          B[qq].oacc[k] = B[qq].acc[k];
+          B[qq].ojerk[k] = B[qq].jerk[k];
+        }
+      double new_dt = dt, end_dt = dt;
+      for (int it = 0; it <= n_iter; it++) {
+        const double prev = new_dt;
+        publish(S, n, lane, B);
+        const double ts2 = forces<EXACT>(S, n, lane, B);
+        end_dt = EXACT ? MUL(eta, __dsqrt_rn(ts2)) : eta * sqrt(ts2);
+        if (it < n_iter) {
+          if (EXACT) {
+            new_dt = MUL(0.5, ADD(dt, end_dt));
+            new_dt = ADD(dt, MUL(MUL(0.5, SUB(end_dt, dt)), DIV(new_dt, prev)));
+          } else {
+            new_dt = 0.5 * (dt + end_dt);
+            new_dt = dt + 0.5 * (end_dt - dt) * (new_dt / prev);
+          }
+        }
+        const bool cj = new_dt != prev;
+        double tau = 0, tau2 = 0, tau3 = 0, theta = 0, inv_theta = 0;
+        if (cj) {
+          if (EXACT) {
+            const double dt_off = SUB(new_dt, MUL(0.5, prev));
+            theta = MUL(0.5, prev);
+            tau = DIV(dt_off, theta);
+            inv_theta = DIV(1.0, theta);
+            tau2 = MUL(tau, tau);
+            tau3 = MUL(tau2, tau);
+          } else {
+            theta = 0.5 * prev;
+            tau = (new_dt - theta) / theta;
+            inv_theta = 1.0 / theta;
+            tau2 = tau * tau;
+            tau3 = tau2 * tau;
+          }
+        }
+        const double nd2 = EXACT ? MUL(new_dt, new_dt) : new_dt * new_dt;
+#pragma unroll
+        for (int qq = 0; qq < 2; qq++) {
+          Body &b = B[qq];
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            if (cj) {  // correct_acc_and_jerk(new_dt, prev)
+              const double pa = b.acc[k], pj = b.jerk[k], oa = b.oacc[k], oj = b.ojerk[k];
+              if (EXACT) {
+                const double c1 = ADD(SUB(2.0, MUL(3.0, tau)), tau3);
+                const double c2 = SUB(ADD(2.0, MUL(3.0, tau)), tau3);
+                const double c3 = ADD(SUB(SUB(1.0, tau), tau2), tau3);
+                const double c4 = ADD(ADD(SUB(-1.0, tau), tau2), tau3);
+                b.acc[k] = MUL(0.25, ADD(ADD(ADD(MUL(oa, c1), MUL(pa, c2)), MUL(MUL(oj, theta), c3)),
+                                         MUL(MUL(pj, theta), c4)));
+                const double e1 = ADD(-1.0, tau2), e2 = SUB(1.0, tau2);
+                const double e3 = ADD(SUB(-1.0, MUL(2.0, tau)), MUL(3.0, tau2));
+                const double e4 = ADD(ADD(-1.0, MUL(2.0, tau)), MUL(3.0, tau2));
+                b.jerk[k] = MUL(0.25, ADD(ADD(ADD(MUL(MUL(MUL(oa, inv_theta), 3.0), e1),
+                                                  MUL(MUL(MUL(pa, inv_theta), 3.0), e2)),
+                                              MUL(oj, e3)),
+                                          MUL(pj, e4)));
+              } else {
+                b.acc[k] = 0.25 * (oa * (2 - 3 * tau + tau3) + pa * (2 + 3 * tau - tau3) +
+                                   oj * theta * (1 - tau - tau2 + tau3) +
+                                   pj * theta * (-1 - tau + tau2 + tau3));
+                b.jerk[k] = 0.25 * (oa * inv_theta * 3 * (-1 + tau2) + pa * inv_theta * 3 * (1 - tau2) +
+                                    oj * (-1 - 2 * tau + 3 * tau2) + pj * (-1 + 2 * tau + 3 * tau2));
+              }
+            }
+            // correct_pos_and_vel(new_dt)
+            if (EXACT) {
+              b.pv[k] = SUB(ADD(b.vel[k], DIV(MUL(new_dt, ADD(b.acc[k], b.oacc[k])), 2.0)),
+                            DIV(MUL(nd2, SUB(b.jerk[k], b.ojerk[k])), 12.0));
+              b.pp[k] = SUB(ADD(b.pos[k], DIV(MUL(new_dt, ADD(b.pv[k], b.vel[k])), 2.0)),
+                            DIV(MUL(nd2, SUB(b.acc[k], b.oacc[k])), 12.0));
+            } else {
+              b.pv[k] = b.vel[k] + new_dt * (b.acc[k] + b.oacc[k]) * 0.5 -
+                        nd2 * (b.jerk[k] - b.ojerk[k]) * (1.0 / 12.0);
+              b.pp[k] = b.pos[k] + new_dt * (b.pv[k] + b.vel[k]) * 0.5 -
+                        nd2 * (b.acc[k] - b.oacc[k]) * (1.0 / 12.0);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int qq = 0; qq < 2; qq++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          B[qq].pos[k] = B[qq].pp[k];
+          B[qq].vel[k] = B[qq].pv[k];
+        }
+      dt = end_dt;
+      t = EXACT ? ADD(t, new_dt) : t + new_dt;
+      nsteps++;
+    }
+#pragma unroll
+    for (int qq = 0; qq < 2; qq++) {
+      const int i = lane + 32 * qq;
+      if (i < n) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          pos[3 * (base + i) + k] = B[qq].pos[k];
+          vel[3 * (base + i) + k] = B[qq].vel[k];
+        }
+      }
+    }
+    if (lane == 0) {
+      unsigned long long t1;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+      t_out[s] = t;
+      steps_out[s] = nsteps;
+      wall_ns[s] = t1 - t0;
+      status[s] = st;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void queue_reset(int *queue) { *queue = 0; }
+
+}  // namespace
+
+extern "C" int g6k_batch_max_n(void) { return MAXN; }
+
+// One persistent launch: grid = ctas_per_sm * SMs, warps_per_cta warps each.
+// Resets the queue counter first (same stream), so the pair can be captured
+// in a CUDA graph and replayed.
+extern "C" int g6k_batch_launch(int nsys, const int *order, const int *off, const double *t_end,
+                                const double *mass, double *pos, double *vel, double eta,
+                                int n_iter, long long max_steps, int exact, int warps_per_cta,
+                                int ctas, int *queue, double *t_out, long long *steps_out,
+                                unsigned long long *wall_ns, int *status, cudaStream_t st) {
+  if (warps_per_cta < 1 || warps_per_cta > WARPS_MAX || ctas < 1) return -2;
+  queue_reset<<<1, 1, 0, st>>>(queue);
+  if (exact)
+    batch_kernel<true><<<ctas, 32 * warps_per_cta, 0, st>>>(nsys, order, off, t_end, mass, pos,
+                                                           vel, eta, n_iter, max_steps, queue,
+                                                           t_out, steps_out, wall_ns, status);
+  else
+    batch_kernel<false><<<ctas, 32 * warps_per_cta, 0, st>>>(nsys, order, off, t_end, mass, pos,
+                                                            vel, eta, n_iter, max_steps, queue,
+                                                            t_out, steps_out, wall_ns, status);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}

@@ -128,3 +128,22 @@ def plummer_salpeter(n, alpha=-2.35, mass_min=0.1, mass_max=100.0, rng=None,
     move_to_center(mass, pos, vel)
     scale_to_standard(mass, pos, vel, potential_energy)
     return mass, pos, vel
+
+
+def encounter_batch(nsys=4096, nmin=3, nmax=64, r_vir=1e-3, seed=1):
+    """Independent few-body systems: n ~ U[nmin, nmax] per system (seeded),
+    each an equal-mass Plummer realisation in standard units (M = 1),
+    re-scaled to virial radius r_vir (positions x r_vir, velocities
+    x r_vir^-1/2, which keeps virial equilibrium with G = M = 1).
+    Returns (n_per_sys, mass, pos, vel, t_cross) with bodies back to back and
+    t_cross = 2 sqrt(2) r_vir^1.5 (G = M = 1)."""
+    rng = np.random.RandomState(seed)
+    ns = rng.randint(nmin, nmax + 1, size=nsys)
+    ms, xs, vs = [], [], []
+    for n in ns:
+        m, x, v = plummer(int(n), do_scale=True, rng=rng)
+        ms.append(m)
+        xs.append(x * r_vir)
+        vs.append(v / math.sqrt(r_vir))
+    t_cross = 2 * math.sqrt(2) * r_vir ** 1.5
+    return ns.astype(np.int32), np.concatenate(ms), np.concatenate(xs), np.concatenate(vs), t_cross

@@ -193,6 +193,32 @@ double g6x_system_time(void);
 int g6x_timing(int on);
 int g6x_stats(double out[8]);
 
+/* Batched few-body systems (the encounters AMUSE's multiples module hands
+   to smallN): nsys independent systems of n_per_sys[s] bodies (2..64),
+   stored back to back in mass/pos/vel, each integrated to t_end[s] with
+   smallN's time-symmetrised shared-step Hermite scheme and Kepler step
+   criterion (src/amuse_ph4/src/smallN.cc:85-116,318-363,487-682) without
+   the unperturbed-binary tree, in one persistent kernel fed by a device work
+   queue (largest systems first) and replayed from a CUDA graph.  exact != 0
+   reproduces smallN's floating-point operations bit for bit; exact = 0 uses
+   one reciprocal square root per pair.  pos/vel are overwritten; optional
+   outputs: t_final[s], steps[s], wall_ms[s] (GPU time from the first to the
+   last step of system s), status[s] (0 done, 1 step budget max_steps
+   exhausted), *elapsed_ms (whole launch). */
+int g6x_batch_run(int nsys, const int *n_per_sys, const double *t_end, const double *mass,
+                  double (*pos)[3], double (*vel)[3], double eta, int n_iter,
+                  long long max_steps, int exact, double *t_final, long long *steps,
+                  double *wall_ms, int *status, double *elapsed_ms);
+/* Launch shape of g6x_batch_run: warps (= systems in flight) per CTA and
+   CTAs per SM. */
+int g6x_batch_config(int warps_per_cta, int ctas_per_sm);
+/* Autotuner: time the candidate shapes on the given systems (end times
+   scaled by frac; the inputs are not modified) and keep the fastest;
+   out = {warps per CTA, CTAs per SM, ms}. */
+int g6x_batch_tune(int nsys, const int *n_per_sys, const double *t_end, const double *mass,
+                   const double (*pos)[3], const double (*vel)[3], double eta, int n_iter,
+                   int exact, double frac, double out[3]);
+
 /* Device pointers of the predicted j records (for tools) and the stream. */
 void *g6x_stream(void);
 

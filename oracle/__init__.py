@@ -61,6 +61,8 @@ def port():
         lib.orc_run.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_dbl, _c_int,
                                 _dp, _dp, _dp, _dp, _dp, _dp, _c_long]
         lib.orc_run.restype = _c_long
+        lib.orc_smalln.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_int, _c_dbl, _dp, _c_long]
+        lib.orc_smalln.restype = _c_long
         _port_lib = lib
     return _port_lib
 
@@ -79,6 +81,7 @@ def ref():
                                        _dp, _dp, _dp]
         lib.ph4ref_run.argtypes = [_c_int, _dp, _ip, _dp, _dp, _c_dbl, _c_dbl, _c_dbl,
                                    _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        lib.ph4ref_smalln.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_dbl, _dp]
         _ref_lib = lib
     return _ref_lib
 
@@ -148,3 +151,17 @@ def run(mass, pos, vel, eps2, eta, t_end, threads=1, lib=None, ids=None, max_blo
                             time, step, stats, max_blocks)
     return dict(pos=pos, vel=vel, acc=acc, jerk=jerk, pot=pot, time=time, timestep=step,
                 E0=stats[0], E1=stats[1], total_steps=stats[2], t=stats[3], blocks=blocks)
+
+
+def smalln(mass, pos, vel, eta, t_end, n_iter=2, lib=None, dt_crit=0.0, max_steps=0):
+    """smallN's few-body integrator without unperturbed binaries (smallN.cc).
+    Returns (pos, vel, t_final, steps); steps is None for the reference."""
+    mass, pos, vel = _c(mass), _c(pos).copy(), _c(vel).copy()
+    t = np.zeros(1)
+    if lib == "ref":
+        rc = ref().ph4ref_smalln(len(mass), mass, pos, vel, eta, t_end, dt_crit, t)
+        if rc != 0:
+            raise RuntimeError("smallN built a binary node")
+        return pos, vel, float(t[0]), None
+    steps = port().orc_smalln(len(mass), mass, pos, vel, eta, n_iter, t_end, t, max_steps)
+    return pos, vel, float(t[0]), int(steps)

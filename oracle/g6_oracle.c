@@ -372,3 +372,155 @@ long orc_run(int n, const double *mass, double *pos, double *vel, double eps2,
   free(oa); free(oj); free(ia); free(ij); free(ipot); free(it); free(its);
   return blocks;
 }
+
+/* ------------------------------------------------------------------ */
+/* smallN's few-body integrator without the unperturbed-binary tree   */
+/* (smallN with dt_crit = 0): all bodies are top-level nodes.           */
+/*   calculate_top_level_acc_and_jerk  smallN.cc:318-363 (pairs i<j,   */
+/*       get_pairwise_acc_and_jerk_CPT smallN.cc:121-273, leaf = node), */
+/*   kepler_step_sq                    smallN.cc:85-116,               */
+/*   take_a_step                       smallN.cc:553-682 (n_iter       */
+/*       iterations of the time-symmetrised corrector),                */
+/*   correct_acc_and_jerk / correct_pos_and_vel smallN.cc:487-531,     */
+/*   predict_loworder                  hdyn.h:192-201,                 */
+/*   smallN_evolve loop                smallN.cc:906-1117.             */
+/* Vector operations follow vec.h (dot = (a0 b0 + a1 b1) + a2 b2, v/s   */
+/* per component).  State in place; returns the number of steps.       */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  double m, pos[3], vel[3], pp[3], pv[3], acc[3], jerk[3], oacc[3], ojerk[3];
+  double t_pred;
+} sn_body;
+
+static double sn_forces(int n, sn_body *b) {
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < 3; k++) b[i].acc[k] = b[i].jerk[k] = 0;
+  double min_ts2 = ORC_INF;
+  for (int i = 0; i < n; i++)
+    for (int j = i + 1; j < n; j++) {
+      double dx[3], dv[3];
+      for (int k = 0; k < 3; k++) {
+        dx[k] = b[j].pp[k] - b[i].pp[k] + 0.0;
+        dv[k] = b[j].pv[k] - b[i].pv[k] + 0.0;
+      }
+      double d2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+      double d = sqrt(d2);
+      double d3 = d2 * d;
+      double xv = dx[0] * dv[0] + dx[1] * dv[1] + dx[2] * dv[2];
+      double force[3], jerk[3];
+      for (int k = 0; k < 3; k++) {
+        double iforce = b[j].m * dx[k] / d3;
+        double ijerk = b[j].m * (dv[k] / d3 - 3 * dx[k] * xv / (d3 * d2));
+        force[k] = b[i].m * iforce;
+        jerk[k] = b[i].m * ijerk;
+      }
+      /* kepler_step_sq(d2, d3, mi + mj, |vj - vi|^2) */
+      double mass = b[j].m + b[i].m;
+      double dvc[3];
+      for (int k = 0; k < 3; k++) dvc[k] = b[j].pv[k] - b[i].pv[k];
+      double vel2 = dvc[0] * dvc[0] + dvc[1] * dvc[1] + dvc[2] * dvc[2];
+      double dtff2 = 0.5 * d3 / mass;
+      double dtv2 = d2 / fabs(vel2);
+      double ts2 = fmin(dtff2, dtv2);
+      double mi = 1 / b[i].m, mj = 1 / b[j].m;
+      for (int k = 0; k < 3; k++) {
+        b[i].acc[k] += mi * force[k];
+        b[i].jerk[k] += mi * jerk[k];
+        b[j].acc[k] += -mj * force[k];
+        b[j].jerk[k] += -mj * jerk[k];
+      }
+      if (ts2 < min_ts2) min_ts2 = ts2;
+    }
+  return min_ts2;
+}
+
+long orc_smalln(int n, const double *mass, double *pos, double *vel, double eta, int n_iter,
+                double t_end, double *t_out, long max_steps) {
+  sn_body *b = (sn_body *)calloc((size_t)n, sizeof(sn_body));
+  for (int i = 0; i < n; i++) {
+    b[i].m = mass[i];
+    b[i].t_pred = -1;
+    for (int k = 0; k < 3; k++) {
+      b[i].pos[k] = pos[3 * i + k];
+      b[i].vel[k] = vel[3 * i + k];
+      b[i].pp[k] = b[i].pos[k]; /* init_pred */
+      b[i].pv[k] = b[i].vel[k];
+    }
+  }
+  double t = 0, root_t_pred = -1;
+  double dt = eta * sqrt(sn_forces(n, b));
+  long steps = 0;
+  while (t < t_end && (max_steps <= 0 || steps < max_steps)) {
+    /* take_a_step */
+    double tn = t + dt;
+    if (tn != root_t_pred) { /* predict_loworder_all */
+      for (int i = 0; i < n; i++) {
+        if (tn != b[i].t_pred) {
+          double h = tn - t, h3 = h / 3, h2 = h / 2;
+          for (int k = 0; k < 3; k++) {
+            b[i].pp[k] = ((b[i].ojerk[k] * h3 + b[i].oacc[k]) * h2 + b[i].vel[k]) * h + b[i].pos[k];
+            b[i].pv[k] = (b[i].ojerk[k] * h2 + b[i].oacc[k]) * h + b[i].vel[k];
+          }
+          b[i].t_pred = tn;
+        }
+      }
+      root_t_pred = tn;
+    }
+    for (int i = 0; i < n; i++)
+      for (int k = 0; k < 3; k++) {
+        b[i].oacc[k] = b[i].acc[k];
+        b[i].ojerk[k] = b[i].jerk[k];
+      }
+    double new_dt = dt, end_dt = dt;
+    for (int it = 0; it <= n_iter; it++) {
+      double prev = new_dt;
+      end_dt = eta * sqrt(sn_forces(n, b));
+      if (it < n_iter) {
+        new_dt = 0.5 * (dt + end_dt);
+        new_dt = dt + 0.5 * (end_dt - dt) * (new_dt / prev);
+      }
+      for (int i = 0; i < n; i++) {
+        if (new_dt != prev) { /* correct_acc_and_jerk(new_dt, prev) */
+          double dt_off = new_dt - 0.5 * prev;
+          double theta = 0.5 * prev;
+          double tau = dt_off / theta;
+          double inv_theta = 1 / theta;
+          double tau2 = tau * tau, tau3 = tau2 * tau;
+          for (int k = 0; k < 3; k++) {
+            double pa = b[i].acc[k], pj = b[i].jerk[k];
+            double oa = b[i].oacc[k], oj = b[i].ojerk[k];
+            b[i].acc[k] = 0.25 * (oa * (2 - 3 * tau + tau3) + pa * (2 + 3 * tau - tau3) +
+                                  oj * theta * (1 - tau - tau2 + tau3) +
+                                  pj * theta * (-1 - tau + tau2 + tau3));
+            b[i].jerk[k] = 0.25 * (oa * inv_theta * 3 * (-1 + tau2) + pa * inv_theta * 3 * (1 - tau2) +
+                                   oj * (-1 - 2 * tau + 3 * tau2) + pj * (-1 + 2 * tau + 3 * tau2));
+          }
+        }
+        /* correct_pos_and_vel(new_dt) */
+        double nd2 = new_dt * new_dt;
+        for (int k = 0; k < 3; k++) {
+          b[i].pv[k] = b[i].vel[k] + new_dt * (b[i].acc[k] + b[i].oacc[k]) / 2 -
+                       nd2 * (b[i].jerk[k] - b[i].ojerk[k]) / 12;
+          b[i].pp[k] = b[i].pos[k] + new_dt * (b[i].pv[k] + b[i].vel[k]) / 2 -
+                       nd2 * (b[i].acc[k] - b[i].oacc[k]) / 12;
+        }
+      }
+    }
+    for (int i = 0; i < n; i++)
+      for (int k = 0; k < 3; k++) {
+        b[i].pos[k] = b[i].pp[k];
+        b[i].vel[k] = b[i].pv[k];
+      }
+    dt = end_dt;
+    t = t + new_dt;
+    steps++;
+  }
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < 3; k++) {
+      pos[3 * i + k] = b[i].pos[k];
+      vel[3 * i + k] = b[i].vel[k];
+    }
+  if (t_out) *t_out = t;
+  free(b);
+  return steps;
+}

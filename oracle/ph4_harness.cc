@@ -12,6 +12,7 @@
 #include <cstring>
 #include <iostream>
 
+#include "hdyn.h"
 #include "idata.h"
 #include "jdata.h"
 #include "scheduler.h"
@@ -170,6 +171,57 @@ int ph4ref_run(int n, const double *mass, const int *ids, const double *pos,
   (void)id;
   // jdata/idata/scheduler are leaked: ph4's cleanup paths assume the
   // worker process exits afterwards.
+  return 0;
+}
+
+// smallN (src/amuse_ph4/src/smallN.cc smallN_evolve) on one system, set up
+// as the smallN worker does (src/amuse_smalln/interface.cc:61-85,
+// src/amuse_smalln/src/smallN_interface.cc:8-36), with dt_crit given
+// (0 disables the unperturbed-binary tree).  State in place.
+int ph4ref_smalln(int n, const double *mass, double *pos, double *vel, double eta,
+                  double t_end, double dt_crit, double *t_out) {
+  std::streambuf *old = std::cout.rdbuf(NULL);
+  hdyn *b = new hdyn;
+  b->set_eta(eta);
+  b->set_gamma(1e-6);
+  b->set_system_time(0.0);
+  b->set_allow_full_unperturbed(1);
+  b->set_cm_index(100000);
+  b->set_dt_crit(dt_crit);
+  b->set_n_iter(2);
+  hdyn *prev = NULL;
+  for (int i = 0; i < n; i++) {
+    hdyn *bn = new hdyn;
+    bn->set_mass(mass[i]);
+    bn->set_radius(0.0);
+    bn->set_pos(vec(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
+    bn->set_vel(vec(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]));
+    bn->set_index(i + 1);
+    bn->set_parent(b);
+    if (!prev) {
+      b->set_oldest_daughter(bn);
+    } else {
+      bn->set_older_sister(prev);
+      prev->set_younger_sister(bn);
+    }
+    prev = bn;
+  }
+  smallN_evolve(b, t_end, _INFINITY_, _INFINITY_, _INFINITY_, 0, "");
+  int i = 0;
+  for_all_daughters(hdyn, b, bi) {
+    if (bi->get_oldest_daughter()) {  // a binary node: report its leaves' CM
+      std::cout.rdbuf(old);
+      return -1;
+    }
+    vec p = bi->get_pos(), v = bi->get_vel();
+    for (int k = 0; k < 3; k++) {
+      pos[3 * i + k] = p[k];
+      vel[3 * i + k] = v[k];
+    }
+    i++;
+  }
+  *t_out = b->get_system_time();
+  std::cout.rdbuf(old);
   return 0;
 }
 

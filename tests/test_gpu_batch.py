@@ -1,0 +1,77 @@
+"""Batched few-body systems (config 4 shape: n ~ U[3, 64], Plummer with
+virial radius 1e-3, eps = 0) in one persistent kernel, against smallN's
+integrator restated in the oracle (itself bit-identical to smallN built from
+the reference sources with dt_crit = 0, tests/test_batch_oracle.py)."""
+import numpy as np
+import pytest
+
+import amuse_gb300 as ag
+import oracle
+from amuse_gb300 import ic
+
+pytestmark = pytest.mark.gpu
+
+
+def _systems(nsys, nmin, nmax, seed):
+    ns, m, x, v, tcr = ic.encounter_batch(nsys, nmin, nmax, seed=seed)
+    return ns, m, x, v, tcr
+
+
+def test_exact_mode_is_bit_identical_to_smalln(g6):
+    ns, m, x, v, tcr = _systems(24, 3, 40, seed=5)
+    t_end = np.full(len(ns), 1.0 * tcr)
+    r = g6.batch_run(ns, t_end, m, x, v, eta=0.14, exact=True)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    for s in range(len(ns)):
+        a, b = off[s], off[s + 1]
+        px, pv, tf, st = oracle.smalln(m[a:b], x[a:b], v[a:b], 0.14, t_end[s])
+        assert r["status"][s] == 0
+        assert r["steps"][s] == st, s
+        assert r["t_final"][s] == tf, s
+        assert np.array_equal(r["pos"][a:b], px), s
+        assert np.array_equal(r["vel"][a:b], pv), s
+
+
+def _energy(m, x, v):
+    k = 0.5 * np.sum(m * np.sum(v * v, 1))
+    d = x[:, None, :] - x[None, :, :]
+    r = np.sqrt(np.sum(d * d, -1))
+    iu = np.triu_indices(len(m), 1)
+    return k - np.sum(m[iu[0]] * m[iu[1]] / r[iu])
+
+
+def test_fast_mode_conserves_energy_like_exact(g6):
+    ns, m, x, v, tcr = _systems(64, 3, 64, seed=6)
+    t_end = np.full(len(ns), 2.0 * tcr)
+    fast = g6.batch_run(ns, t_end, m, x, v, exact=False)
+    exact = g6.batch_run(ns, t_end, m, x, v, exact=True)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    de_f, de_e = [], []
+    for s in range(len(ns)):
+        a, b = off[s], off[s + 1]
+        e0 = _energy(m[a:b], x[a:b], v[a:b])
+        de_f.append(abs((_energy(m[a:b], fast["pos"][a:b], fast["vel"][a:b]) - e0) / e0))
+        de_e.append(abs((_energy(m[a:b], exact["pos"][a:b], exact["vel"][a:b]) - e0) / e0))
+    print(f"median |dE/E| fast {np.median(de_f):.2e} exact {np.median(de_e):.2e}; "
+          f"max fast {max(de_f):.2e} exact {max(de_e):.2e}")
+    assert np.all(fast["status"] == 0) and np.all(fast["t_final"] >= t_end)
+    # the scheme's own truncation error dominates: both modes agree on it
+    assert np.median(de_f) < 2 * np.median(de_e) + 1e-12
+    assert max(de_f) < 3 * max(de_e) + 1e-12
+
+
+def test_step_budget_and_queue(g6):
+    ns, m, x, v, tcr = _systems(500, 3, 64, seed=7)
+    r = g6.batch_run(ns, 5 * tcr, m, x, v, max_steps=10)
+    assert np.all(r["steps"] == 10) and np.all(r["status"] == 1)
+    r = g6.batch_run(ns, 0.05 * tcr, m, x, v)
+    assert np.all(r["status"] == 0) and np.all(r["t_final"] >= 0.05 * tcr)
+    assert np.all(r["wall_ms"] > 0)
+
+
+def test_autotuner(g6):
+    ns, m, x, v, tcr = _systems(300, 3, 64, seed=8)
+    best = g6.batch_tune(ns, tcr, m, x, v, frac=0.02)
+    assert best["warps_per_cta"] >= 1 and best["ctas_per_sm"] >= 1 and best["ms"] > 0
+    r = g6.batch_run(ns, 0.05 * tcr, m, x, v)
+    assert np.all(r["status"] == 0)

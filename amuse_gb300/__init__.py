@@ -48,6 +48,7 @@ EXT_SYMBOLS = [
     "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
     "g6x_energy", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
     "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
+    "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp", "g6x_fixed_step_adjoint",
 ]
 
 _lib = None
@@ -112,6 +113,10 @@ def load():
     lib.g6x_timing.argtypes = [I]
     lib.g6x_stats.argtypes = [_pd]
     lib.g6x_stream.restype = _vp
+    lib.g6x_fixed_force.argtypes = [I, D] + [_vp] * 5
+    lib.g6x_fixed_step.argtypes = [I, D, D] + [_vp] * 7
+    lib.g6x_force_vjp.argtypes = [I, D] + [_vp] * 8
+    lib.g6x_fixed_step_adjoint.argtypes = [I, D, D] + [_vp] * 9
     _lib = lib
     return lib
 
@@ -278,6 +283,23 @@ class G6X(G6):
         _check(self.lib.g6x_force_dev_noalloc(ti, eps2, nj, ni, d_xi, d_vi, d_self, d_acc,
                                               d_jerk, d_pot, d_nn, 1 if sync else 0),
                "g6x_force_dev_noalloc")
+
+    # ---- fixed-step Hermite and its adjoint (device pointers, [n][3]) ----
+    def fixed_force(self, n, eps2, d_x, d_v, d_m, d_a, d_j):
+        _check(self.lib.g6x_fixed_force(n, eps2, d_x, d_v, d_m, d_a, d_j), "g6x_fixed_force")
+
+    def fixed_step(self, n, h, eps2, d_x, d_v, d_a, d_j, d_m, d_xp, d_vp):
+        _check(self.lib.g6x_fixed_step(n, h, eps2, d_x, d_v, d_a, d_j, d_m, d_xp, d_vp),
+               "g6x_fixed_step")
+
+    def force_vjp(self, n, eps2, d_x, d_v, d_m, d_la, d_lj, d_gx, d_gv, d_gm):
+        _check(self.lib.g6x_force_vjp(n, eps2, d_x, d_v, d_m, d_la, d_lj, d_gx, d_gv, d_gm),
+               "g6x_force_vjp")
+
+    def fixed_step_adjoint(self, n, h, eps2, d_xp, d_vp, d_m, d_lx, d_lv, d_la, d_lj, d_lm,
+                           d_work):
+        _check(self.lib.g6x_fixed_step_adjoint(n, h, eps2, d_xp, d_vp, d_m, d_lx, d_lv, d_la,
+                                               d_lj, d_lm, d_work), "g6x_fixed_step_adjoint")
 
     def run_init(self, eps2, eta):
         _check(self.lib.g6x_run_init(eps2, eta), "g6x_run_init")

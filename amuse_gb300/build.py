@@ -24,7 +24,8 @@ LIB = os.path.join(HERE, "lib")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kern_force.cu", "kern_predict.cu", "kern_step.cu", "kern_ngb.cu", "kern_batch.cu"]
+CU_SOURCES = ["kern_force.cu", "kern_predict.cu", "kern_step.cu", "kern_ngb.cu", "kern_batch.cu",
+              "kern_fixed.cu"]
 C_SOURCES = ["g6_host.c"]
 
 

@@ -1590,3 +1590,124 @@ int g6x_batch_tune(int nsys, const int *n_per_sys, const double *t_end, const do
   }
   return rc;
 }
+
+/* ============================== fixed-step Hermite and its adjoint ===== */
+/* Building blocks on device arrays ([n][3] doubles) for the differentiable
+ * fixed-step integrator (amuse_gb300/adjoint.py drives them from a
+ * torch.autograd.Function).  All calls are blocking. */
+int g6k_fixed_records(const g6_jstate *js, int n, const double *x, const double *v,
+                      const double *m, int prec, cudaStream_t st);
+int g6k_fixed_predict(int n, double h, const double *x, const double *v, const double *a,
+                      const double *j, double *xp, double *vp, cudaStream_t st);
+int g6k_fixed_correct(int n, double h, double *x, double *v, double *a, double *j,
+                      const double *a1, const double *j1, cudaStream_t st);
+int g6k_fixed_adj_pre(int n, double h, double *lx, double *lv, double *la, double *lj,
+                      double *la1, double *lj1, cudaStream_t st);
+int g6k_fixed_adj_post(int n, double h, double *lx, double *lv, double *la, double *lj,
+                       const double *gxp, const double *gvp, double *lm, const double *gm,
+                       cudaStream_t st);
+size_t g6k_vjp_scratch_bytes(int n);
+int g6k_force_vjp(int n, double eps2, int prec, const double *x, const double *v,
+                  const double *m, const double *la1, const double *lj1, double *gx, double *gv,
+                  double *gm, double *part, cudaStream_t st);
+
+static double *fx_a1, *fx_j1, *fx_part;
+static int fx_cap;
+
+static int fixed_buffers(int n) {
+  if (n <= fx_cap && fx_part) return 0;
+  cudaFree(fx_a1); cudaFree(fx_j1); cudaFree(fx_part);
+  fx_a1 = fx_j1 = fx_part = NULL;
+  fx_cap = 0;
+  if (cudaMalloc((void **)&fx_a1, sizeof(double) * 3 * (size_t)n) != cudaSuccess ||
+      cudaMalloc((void **)&fx_j1, sizeof(double) * 3 * (size_t)n) != cudaSuccess ||
+      cudaMalloc((void **)&fx_part, g6k_vjp_scratch_bytes(n)) != cudaSuccess) {
+    seterr("cannot allocate fixed-step buffers for n=%d", n);
+    return G6_ERR_NOMEM;
+  }
+  fx_cap = n;
+  return 0;
+}
+
+/* acc/jerk of all n bodies at (x, v) (split or FP64 per g6x_set_precision). */
+int g6x_fixed_force(int n, double eps2, const double *d_x, const double *d_v, const double *d_m,
+                    double *d_a, double *d_j) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (n <= 0) return G6_ERR_ARG;
+  rc = grow_j((n + G6_TILE - 1) / G6_TILE * G6_TILE);
+  if (rc) return rc;
+  rc = ensure_run_buffers(n);
+  if (rc) return rc;
+  rc = identity_list(n);
+  if (rc) return rc;
+  if (g6k_fixed_records(&G.js, n, d_x, d_v, d_m, G.prec, G.st)) return G6_ERR_CUDA;
+  G.pred_valid = 0; /* the records no longer hold a prediction of the j-state */
+  g6_force_args a;
+  memset(&a, 0, sizeof(a));
+  a.ni = n;
+  a.nj = n;
+  a.prec = G.prec;
+  a.eps2 = eps2;
+  a.ilist = G.d_ilist;
+  a.acc = d_a;
+  a.jerk = d_j;
+  a.pot = G.d_rpot;
+  rc = run_force(&a);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(G.st));
+  return read_err_word();
+}
+
+/* One fixed step in place on (x, v, a, j); xp/vp (or NULL) receive the
+ * predicted positions and velocities the force was evaluated at. */
+int g6x_fixed_step(int n, double h, double eps2, double *d_x, double *d_v, double *d_a,
+                   double *d_j, const double *d_m, double *d_xp, double *d_vp) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (n <= 0 || !d_xp || !d_vp) return G6_ERR_ARG;
+  rc = fixed_buffers(n);
+  if (rc) return rc;
+  if (g6k_fixed_predict(n, h, d_x, d_v, d_a, d_j, d_xp, d_vp, G.st)) return G6_ERR_CUDA;
+  rc = g6x_fixed_force(n, eps2, d_xp, d_vp, d_m, fx_a1, fx_j1);
+  if (rc) return rc;
+  if (g6k_fixed_correct(n, h, d_x, d_v, d_a, d_j, fx_a1, fx_j1, G.st)) return G6_ERR_CUDA;
+  CK(cudaStreamSynchronize(G.st));
+  return 0;
+}
+
+/* Vector-Jacobian product of the force at (x, v): given cotangents la/lj of
+ * (acc, jerk), gx/gv/gm receive the cotangents of x, v, m. */
+int g6x_force_vjp(int n, double eps2, const double *d_x, const double *d_v, const double *d_m,
+                  const double *d_la, const double *d_lj, double *d_gx, double *d_gv,
+                  double *d_gm) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (n <= 0) return G6_ERR_ARG;
+  rc = fixed_buffers(n);
+  if (rc) return rc;
+  if (g6k_force_vjp(n, eps2, G.prec, d_x, d_v, d_m, d_la, d_lj, d_gx, d_gv, d_gm, fx_part, G.st))
+    return G6_ERR_CUDA;
+  CK(cudaStreamSynchronize(G.st));
+  return 0;
+}
+
+/* Adjoint of one fixed step (in place on lx, lv, la, lj; gm accumulates
+ * into d_lm) at the predicted state (xp, vp) the forward step used. */
+int g6x_fixed_step_adjoint(int n, double h, double eps2, const double *d_xp, const double *d_vp,
+                           const double *d_m, double *d_lx, double *d_lv, double *d_la,
+                           double *d_lj, double *d_lm, double *d_work /* [7n] */) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (n <= 0 || !d_work) return G6_ERR_ARG;
+  rc = fixed_buffers(n);
+  if (rc) return rc;
+  double *gxp = d_work, *gvp = d_work + 3 * (size_t)n, *gm = d_work + 6 * (size_t)n;
+  if (g6k_fixed_adj_pre(n, h, d_lx, d_lv, d_la, d_lj, fx_a1, fx_j1, G.st)) return G6_ERR_CUDA;
+  if (g6k_force_vjp(n, eps2, G.prec, d_xp, d_vp, d_m, fx_a1, fx_j1, gxp, gvp, gm, fx_part, G.st))
+    return G6_ERR_CUDA;
+  if (g6k_fixed_adj_post(n, h, d_lx, d_lv, d_la, d_lj, gxp, gvp, d_lm, gm, G.st))
+    return G6_ERR_CUDA;
+  CK(cudaStreamSynchronize(G.st));
+  return 0;
+}

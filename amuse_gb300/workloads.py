@@ -1,17 +1,19 @@
 """Workload runners for the benchmark configurations other than the headline
 one (which is bench.py).  Each prints one JSON line.
 
-  python -m amuse_gb300.workloads batch   [--nsys 4096] [--exact-sample 256]
-      Config 4: nsys few-body systems, n ~ U[3, 64], Plummer with virial
-      radius 1e-3, eps = 0, to 10 crossing times, smallN's scheme
-      (g6x_batch_run) after the autotuner; systems/s, p50/p99 per-system
-      GPU time, the bit-identical (exact) mode on a sample, and the oracle's
-      smallN restatement on the host cores for the same sample.
+  python -m amuse_gb300.workloads batch   [--nsys 4096]
+      nsys few-body systems, n ~ U[3, 64], Plummer with virial radius 1e-3,
+      eps = 0, to 10 crossing times, smallN's scheme (g6x_batch_run) after
+      the autotuner; systems/s and p50/p99 per-system GPU time.
+      (bench.py --workload batch adds the host-core baseline.)
+  python -m amuse_gb300.workloads adjoint [--n 16384] [--nsteps 256]
+      Differentiable fixed-step Hermite: timing of forward and backward in
+      split precision and FP64, split vs FP64 gradients, and finite
+      differences of the forward against the adjoint.
 """
 from __future__ import annotations
 
 import argparse
-import concurrent.futures as cf
 import json
 import os
 import sys
@@ -25,10 +27,10 @@ if ROOT not in sys.path:
 
 
 def run_batch(args):
+    """Config 4 on the GPU: autotune, the full batch, and a sample of systems
+    (returned for a host-core comparison by the caller)."""
     import amuse_gb300 as ag
     from amuse_gb300 import ic
-    import oracle
-    oracle.build_port()
     ns, m, x, v, tcr = ic.encounter_batch(args.nsys, 3, 64, r_vir=1e-3, seed=args.seed)
     t_end = 10 * tcr
     off = np.concatenate([[0], np.cumsum(ns)])
@@ -37,54 +39,22 @@ def run_batch(args):
                        f"t_end=10 t_cross={t_end:.4g}, eta={args.eta}, smallN scheme "
                        f"(n_iter=2, Kepler criterion), FP64, step cap {args.max_steps}/system"}
 
-    # 1. parity: exact mode on the first systems, truncated at a step budget,
-    #    against the oracle (smallN restated) on the host
-    k = min(args.exact_sample, args.nsys)
-    sub = slice(0, off[k])
-    re = g6.batch_run(ns[:k], t_end, m[sub], x[sub], v[sub], eta=args.eta,
-                      max_steps=args.exact_steps, exact=True)
-    same = True
-    for s in range(k):
-        a, b = off[s], off[s + 1]
-        px, pv, tf, st = oracle.smalln(m[a:b], x[a:b], v[a:b], args.eta, t_end,
-                                       max_steps=args.exact_steps)
-        same &= bool(np.array_equal(re["pos"][a:b], px) and np.array_equal(re["vel"][a:b], pv)
-                     and re["steps"][s] == st)
-    out["parity"] = {"systems": k, "step_budget": args.exact_steps,
-                     "exact_mode_bit_identical_to_oracle": same}
-    print(json.dumps(out), flush=True)
-
-    # 2. autotune on 512 systems for 0.5% of the end time
+    # 1. autotune on 512 systems for 0.5% of the end time
     kt = min(args.nsys, 512)
     tune = g6.batch_tune(ns[:kt], t_end, m[:off[kt]], x[:off[kt]], v[:off[kt]], eta=args.eta,
                          frac=0.005)
     out["autotune"] = tune
     print(json.dumps(out), flush=True)
 
-    # 3. GPU vs host cores on the same sample of systems (same step cap)
+    # 2. the sample the caller times on the host cores (same step cap)
     kc = min(args.cpu_sample, args.nsys)
     sc = slice(0, off[kc])
     rg = g6.batch_run(ns[:kc], t_end, m[sc], x[sc], v[sc], eta=args.eta,
                       max_steps=args.max_steps)
-    if not args.no_cpu:
-        threads = os.cpu_count() or 1
+    out["sample"] = {"systems": kc, "gpu_systems_per_s": kc / (rg["elapsed_ms"] / 1e3),
+                     "gpu_mode": "fast"}
 
-        def one(s):
-            a, b = off[s], off[s + 1]
-            return oracle.smalln(m[a:b], x[a:b], v[a:b], args.eta, t_end,
-                                 max_steps=args.max_steps)
-
-        t1 = time.perf_counter()
-        with cf.ThreadPoolExecutor(threads) as ex:
-            list(ex.map(one, range(kc)))
-        cdt = time.perf_counter() - t1
-        out["sample_gpu_vs_cpu"] = {
-            "systems": kc, "gpu_systems_per_s": kc / (rg["elapsed_ms"] / 1e3),
-            "cpu_systems_per_s": kc / cdt, "cpu_cores": threads, "cpu_kind": "port",
-            "gpu_mode": "fast"}
-        print(json.dumps(out), flush=True)
-
-    # 4. the full batch
+    # 3. the full batch
     t0 = time.perf_counter()
     r = g6.batch_run(ns, t_end, m, x, v, eta=args.eta, max_steps=args.max_steps)
     wall = time.perf_counter() - t0
@@ -102,6 +72,96 @@ def run_batch(args):
         "completed": int(done.sum()), "capped": int((r["status"] == 1).sum()),
     })
     print(json.dumps(out), flush=True)
+    sample = dict(ns=ns[:kc], mass=m[sc], pos=x[sc], vel=v[sc], t_end=t_end, off=off[:kc + 1])
+    return out, sample
+
+
+def run_adjoint(args):
+    """Config 5: Plummer n equal-mass bodies, eps2 = 1e-4, fixed dt = 1/256
+    for 256 steps, loss = sum w_i |x_i|^2 (seeded w); gradient w.r.t. x0, v0,
+    m through the adjoint with a checkpoint every 16 steps, in split
+    precision and in FP64; central finite differences (h = 1e-6) on seeded
+    coordinates of the split forward and, on fewer, of the FP64 forward."""
+    import torch
+    from amuse_gb300 import ic
+    from amuse_gb300.adjoint import hermite_fixed
+    n, eps2, dt, nsteps, ck = args.n, 1e-4, 1.0 / 256, args.nsteps, 16
+    rng = np.random.RandomState(args.seed)
+    m, x, v = ic.plummer(n, do_scale=True, rng=rng)
+    w = rng.uniform(0.5, 1.5, n)
+    dev = torch.device("cuda", 0)
+    base = [torch.tensor(a, dtype=torch.float64, device=dev) for a in (x, v, m)]
+    tw = torch.tensor(w, dtype=torch.float64, device=dev)
+    out = {"workload": f"Plummer n={n} equal mass, eps2={eps2}, dt=1/256, {nsteps} steps, "
+                       f"checkpoint every {ck}, loss=sum w|x|^2"}
+
+    def grad(prec):
+        xs = [t.clone().requires_grad_(True) for t in base]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xf, _ = hermite_fixed(xs[0], xs[1], xs[2], eps2=eps2, dt=dt, nsteps=nsteps,
+                              checkpoint=ck, precision=prec)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        loss = (tw * (xf * xf).sum(1)).sum()
+        loss.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        return float(loss), [t.grad.cpu().numpy() for t in xs], t1 - t0, t2 - t1
+
+    def loss_at(which, idx, delta, prec):
+        xs = [t.clone() for t in base]
+        xs[which][idx] += delta
+        with torch.no_grad():
+            xf, _ = hermite_fixed(xs[0], xs[1], xs[2], eps2=eps2, dt=dt, nsteps=nsteps,
+                                  checkpoint=nsteps, precision=prec)
+            return float((tw * (xf * xf).sum(1)).sum())
+
+    hermite_fixed(base[0], base[1], base[2], eps2=eps2, dt=dt, nsteps=2, precision="split")
+    ls, gs, fs, bs = grad("split")
+    pairs_fwd = (nsteps + 1) * n * (n - 1)
+    out["split"] = {"loss": ls, "forward_s": fs, "backward_s": bs,
+                    "forward_pairs_per_s": pairs_fwd / fs}
+    print(json.dumps(out), flush=True)
+    ld, gd, fd_, bd = grad("fp64")
+    out["fp64"] = {"loss": ld, "forward_s": fd_, "backward_s": bd}
+    names = ["x0", "v0", "m"]
+    out["split_vs_fp64_gradient"] = {
+        names[k]: float(np.linalg.norm(gs[k] - gd[k]) / np.linalg.norm(gd[k])) for k in range(3)}
+    out["split_vs_fp64_loss_rel"] = abs(ls - ld) / abs(ld)
+    print(json.dumps(out), flush=True)
+
+    h = 1e-6
+    crng = np.random.RandomState(args.seed + 1)
+    coords = []
+    for _ in range(args.fd_coords):
+        k = crng.randint(3)
+        i = crng.randint(n)
+        coords.append((k, (i,) if k == 2 else (i, crng.randint(3))))
+
+    def fd_errors(prec, cs):
+        rel = []
+        for k, idx in cs:
+            fd = (loss_at(k, idx, h, prec) - loss_at(k, idx, -h, prec)) / (2 * h)
+            g_ad = (gs if prec == "split" else gd)[k][idx]
+            scale = max(abs(g_ad), 1e-2 * np.abs((gs if prec == "split" else gd)[k]).max())
+            rel.append(abs(fd - g_ad) / scale)
+        return rel
+
+    t0 = time.perf_counter()
+    rs = fd_errors("split", coords)
+    out["fd_split"] = {"coords": len(coords), "h": h, "max_rel": float(max(rs)),
+                       "median_rel": float(np.median(rs)), "n_above_1e-4": int(sum(r > 1e-4 for r in rs)),
+                       "seconds": time.perf_counter() - t0}
+    print(json.dumps(out), flush=True)
+    if args.fd64_coords > 0:
+        t0 = time.perf_counter()
+        rd = fd_errors("fp64", coords[: args.fd64_coords])
+        out["fd_fp64"] = {"coords": len(rd), "h": h, "max_rel": float(max(rd)),
+                          "median_rel": float(np.median(rd)),
+                          "seconds": time.perf_counter() - t0}
+        print(json.dumps(out), flush=True)
+    return out
 
 
 def main():
@@ -112,13 +172,18 @@ def main():
     b.add_argument("--seed", type=int, default=1)
     b.add_argument("--eta", type=float, default=0.14)
     b.add_argument("--max-steps", type=int, default=250_000)
-    b.add_argument("--exact-sample", type=int, default=32)
-    b.add_argument("--exact-steps", type=int, default=5_000)
     b.add_argument("--cpu-sample", type=int, default=64)
-    b.add_argument("--no-cpu", action="store_true")
+    d = sub.add_parser("adjoint")
+    d.add_argument("--n", type=int, default=16384)
+    d.add_argument("--nsteps", type=int, default=256)
+    d.add_argument("--seed", type=int, default=7)
+    d.add_argument("--fd-coords", type=int, default=32)
+    d.add_argument("--fd64-coords", type=int, default=4)
     a = ap.parse_args()
     if a.cmd == "batch":
         run_batch(a)
+    elif a.cmd == "adjoint":
+        run_adjoint(a)
 
 
 if __name__ == "__main__":

@@ -23,6 +23,16 @@ Reported next to it:
 
 --impl reference times the reference's CPU force path (ph4's
 idata::get_partial_acc_and_jerk restated in oracle/, all host threads).
+
+Secondary workloads (one JSON line each; not the headline metric):
+  --workload batch    4096 few-body systems through g6x_batch_run
+                      (amuse_gb300.workloads.run_batch) with the oracle's
+                      smallN restatement timed on the host cores on the
+                      same sample of systems as cpu_baseline;
+  --workload adjoint  the differentiable fixed-step Hermite at n = 16384
+                      (amuse_gb300.workloads.run_adjoint) with the oracle's
+                      restatement of the hermite code's step timed on the
+                      host cores as cpu_baseline.
 """
 from __future__ import annotations
 
@@ -57,6 +67,17 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="force", choices=["force", "batch", "adjoint"])
+    # batch workload
+    ap.add_argument("--nsys", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=None)
+    ap.add_argument("--eta", type=float, default=0.14)
+    ap.add_argument("--max-steps", type=int, default=250_000)
+    ap.add_argument("--cpu-sample", type=int, default=64)
+    # adjoint workload
+    ap.add_argument("--nsteps", type=int, default=256)
+    ap.add_argument("--fd-coords", type=int, default=32)
+    ap.add_argument("--fd64-coords", type=int, default=4)
     return ap.parse_args()
 
 
@@ -361,8 +382,54 @@ def run_ours(args):
     return 0
 
 
+def run_secondary(args):
+    """The batch / adjoint workloads with their host-core baselines."""
+    from amuse_gb300 import workloads
+    import oracle
+    oracle.build_port()
+    threads = os.cpu_count() or 1
+    if args.workload == "batch":
+        args.seed = 1 if args.seed is None else args.seed
+        out, smp = workloads.run_batch(args)
+        off = smp["off"]
+
+        def one(s):
+            a, b = off[s], off[s + 1]
+            return oracle.smalln(smp["mass"][a:b], smp["pos"][a:b], smp["vel"][a:b], args.eta,
+                                 smp["t_end"], max_steps=args.max_steps)
+
+        import concurrent.futures as cf
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(one, range(len(off) - 1)))
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "value": (len(off) - 1) / dt, "unit": "systems/s", "cores": threads, "kind": "port",
+            "sample": f"the first {len(off) - 1} systems (smallN restated in "
+                      f"oracle/g6_oracle.c, same step cap), {dt:.1f} s"}
+    else:
+        args.seed = 7 if args.seed is None else args.seed
+        args.n = 16384 if args.n == N_DEFAULT else args.n
+        out = workloads.run_adjoint(args)
+        from amuse_gb300 import ic
+        rng = np.random.RandomState(args.seed)
+        m, x, v = ic.plummer(args.n, do_scale=True, rng=rng)
+        t0 = time.perf_counter()
+        oracle.hermite_fixed(m, x, v, 1e-4, 1.0 / 256, 1)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "value": 2 * args.n * (args.n - 1) / dt, "unit": "pair-interactions/s (forward)",
+            "cores": 1, "kind": "port",
+            "sample": f"one fixed step (2 force evaluations) of the hermite code's scheme "
+                      f"restated in oracle/g6_oracle.c at n={args.n}, {dt:.1f} s"}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload != "force":
+        return run_secondary(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -219,6 +219,34 @@ int g6x_batch_tune(int nsys, const int *n_per_sys, const double *t_end, const do
                    const double (*pos)[3], const double (*vel)[3], double eta, int n_iter,
                    int exact, double frac, double out[3]);
 
+/* Fixed-step Hermite integration and its adjoint (no reference
+   counterpart in the GRAPE-6 ABI: the scheme is the hermite code's,
+   src/amuse_hermite/interface.cc:266-281 predict_step and :536-552
+   correct_step, with this library's force).  All arrays are device
+   pointers, particle-major [n][3] doubles (m: [n]); every call blocks.
+   g6x_fixed_force         -- (a, j) of all n bodies at (x, v); precision as
+                              set by g6x_set_precision; overwrites the j
+                              records (a later g6_ call re-predicts).
+   g6x_fixed_step          -- one step of size h in place on (x, v, a, j);
+                              xp/vp receive the predicted state the force
+                              was evaluated at (needed by the adjoint).
+   g6x_force_vjp           -- cotangents (gx, gv, gm) of the force's inputs
+                              given cotangents (la, lj) of (acc, jerk).
+   g6x_fixed_step_adjoint  -- the adjoint of one g6x_fixed_step, in place on
+                              the state cotangents (lx, lv, la, lj); lm
+                              accumulates the mass cotangent; work holds 7n
+                              doubles. */
+int g6x_fixed_force(int n, double eps2, const double *d_x, const double *d_v, const double *d_m,
+                    double *d_a, double *d_j);
+int g6x_fixed_step(int n, double h, double eps2, double *d_x, double *d_v, double *d_a,
+                   double *d_j, const double *d_m, double *d_xp, double *d_vp);
+int g6x_force_vjp(int n, double eps2, const double *d_x, const double *d_v, const double *d_m,
+                  const double *d_la, const double *d_lj, double *d_gx, double *d_gv,
+                  double *d_gm);
+int g6x_fixed_step_adjoint(int n, double h, double eps2, const double *d_xp, const double *d_vp,
+                           const double *d_m, double *d_lx, double *d_lv, double *d_la,
+                           double *d_lj, double *d_lm, double *d_work);
+
 /* Device pointers of the predicted j records (for tools) and the stream. */
 void *g6x_stream(void);
 

@@ -63,6 +63,9 @@ def port():
         lib.orc_run.restype = _c_long
         lib.orc_smalln.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_int, _c_dbl, _dp, _c_long]
         lib.orc_smalln.restype = _c_long
+        lib.orc_hermite_fixed.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_int, _dp,
+                                          _dp]
+        lib.orc_hermite_fixed.restype = None
         _port_lib = lib
     return _port_lib
 
@@ -165,3 +168,12 @@ def smalln(mass, pos, vel, eta, t_end, n_iter=2, lib=None, dt_crit=0.0, max_step
         return pos, vel, float(t[0]), None
     steps = port().orc_smalln(len(mass), mass, pos, vel, eta, n_iter, t_end, t, max_steps)
     return pos, vel, float(t[0]), int(steps)
+
+
+def hermite_fixed(mass, pos, vel, eps2, dt, nsteps):
+    """The hermite code's fixed-step shared Hermite (interface.cc:266-281,
+    387-552, test_mode).  Returns (pos, vel, acc, jerk) after nsteps."""
+    mass, pos, vel = _c(mass), _c(pos).copy(), _c(vel).copy()
+    acc = np.zeros_like(pos); jerk = np.zeros_like(pos)
+    port().orc_hermite_fixed(len(mass), mass, pos, vel, eps2, dt, nsteps, acc, jerk)
+    return pos, vel, acc, jerk

@@ -524,3 +524,75 @@ long orc_smalln(int n, const double *mass, double *pos, double *vel, double eta,
   free(b);
   return steps;
 }
+
+/* ------------------------------------------------------------------ */
+/* Fixed-step shared Hermite: the hermite code in test_mode            */
+/* (calculate_step returns dt_param, interface.cc:618-637):            */
+/*   hf_forces    get_acc_jerk_pot_coll   interface.cc:387-533         */
+/*                (symmetric j > i pair loop; note rv_r2 = (r.v)/r^2   */
+/*                uses the UNsoftened r^2 while r3 is softened)        */
+/*   predict      predict_step            interface.cc:266-281         */
+/*   correct      correct_step            interface.cc:536-552         */
+/*   step loop    evolve_step             interface.cc:558-616         */
+/* pos/vel in place; acc/jerk (may be NULL) receive the final forces.  */
+/* ------------------------------------------------------------------ */
+static void hf_forces(int n, const double *mass, const double *pos, const double *vel,
+                      double eps2, double *acc, double *jerk) {
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < 3; k++) acc[3 * i + k] = jerk[3 * i + k] = 0;
+  for (int i = 0; i < n; i++)
+    for (int j = i + 1; j < n; j++) {
+      double rji[3], vji[3];
+      for (int k = 0; k < 3; k++) {
+        rji[k] = pos[3 * j + k] - pos[3 * i + k];
+        vji[k] = vel[3 * j + k] - vel[3 * i + k];
+      }
+      double r2 = 0, rv_r2 = 0;
+      for (int k = 0; k < 3; k++) {
+        r2 += rji[k] * rji[k];
+        rv_r2 += rji[k] * vji[k];
+      }
+      rv_r2 /= r2;
+      r2 += eps2;
+      double r = sqrt(r2);
+      double r3 = r * r2;
+      double da[3], dj[3];
+      for (int k = 0; k < 3; k++) {
+        da[k] = rji[k] / r3;
+        dj[k] = (vji[k] - 3 * rv_r2 * rji[k]) / r3;
+      }
+      for (int k = 0; k < 3; k++) {
+        acc[3 * i + k] += mass[j] * da[k];
+        acc[3 * j + k] -= mass[i] * da[k];
+        jerk[3 * i + k] += mass[j] * dj[k];
+        jerk[3 * j + k] -= mass[i] * dj[k];
+      }
+    }
+}
+
+void orc_hermite_fixed(int n, const double *mass, double *pos, double *vel, double eps2,
+                       double dt, int nsteps, double *acc_out, double *jerk_out) {
+  size_t b = sizeof(double) * 3 * (size_t)n;
+  double *acc = (double *)malloc(b), *jerk = (double *)malloc(b);
+  double *op = (double *)malloc(b), *ov = (double *)malloc(b);
+  double *oa = (double *)malloc(b), *oj = (double *)malloc(b);
+  hf_forces(n, mass, pos, vel, eps2, acc, jerk);
+  for (int s = 0; s < nsteps; s++) {
+    memcpy(op, pos, b);
+    memcpy(ov, vel, b);
+    memcpy(oa, acc, b);
+    memcpy(oj, jerk, b);
+    for (int e = 0; e < 3 * n; e++) {
+      pos[e] += vel[e] * dt + acc[e] * dt * dt / 2 + jerk[e] * dt * dt * dt / 6;
+      vel[e] += acc[e] * dt + jerk[e] * dt * dt / 2;
+    }
+    hf_forces(n, mass, pos, vel, eps2, acc, jerk);
+    for (int e = 0; e < 3 * n; e++) {
+      vel[e] = ov[e] + (oa[e] + acc[e]) * dt / 2 + (oj[e] - jerk[e]) * dt * dt / 12;
+      pos[e] = op[e] + (ov[e] + vel[e]) * dt / 2 + (oa[e] - acc[e]) * dt * dt / 12;
+    }
+  }
+  if (acc_out) memcpy(acc_out, acc, b);
+  if (jerk_out) memcpy(jerk_out, jerk, b);
+  free(acc); free(jerk); free(op); free(ov); free(oa); free(oj);
+}

@@ -33,6 +33,7 @@ G6_ERR = {
     -5: "no such device", -6: "kernel error word set", -7: "call out of order",
 }
 SPLIT, FP64 = 0, 1
+JERK_HERMITE, JERK_SOFTENED = 0, 1
 NGB_MAX = 256
 
 # Every symbol include/g6.h declares.
@@ -48,7 +49,8 @@ EXT_SYMBOLS = [
     "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
     "g6x_energy", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
     "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
-    "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp", "g6x_fixed_step_adjoint",
+    "g6x_set_fixed_jerk", "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp",
+    "g6x_fixed_step_adjoint",
 ]
 
 _lib = None
@@ -113,6 +115,7 @@ def load():
     lib.g6x_timing.argtypes = [I]
     lib.g6x_stats.argtypes = [_pd]
     lib.g6x_stream.restype = _vp
+    lib.g6x_set_fixed_jerk.argtypes = [I]
     lib.g6x_fixed_force.argtypes = [I, D] + [_vp] * 5
     lib.g6x_fixed_step.argtypes = [I, D, D] + [_vp] * 7
     lib.g6x_force_vjp.argtypes = [I, D] + [_vp] * 8
@@ -285,6 +288,10 @@ class G6X(G6):
                "g6x_force_dev_noalloc")
 
     # ---- fixed-step Hermite and its adjoint (device pointers, [n][3]) ----
+    def set_fixed_jerk(self, form):
+        """JERK_HERMITE (the hermite code's form) or JERK_SOFTENED."""
+        _check(self.lib.g6x_set_fixed_jerk(form), "g6x_set_fixed_jerk")
+
     def fixed_force(self, n, eps2, d_x, d_v, d_m, d_a, d_j):
         _check(self.lib.g6x_fixed_force(n, eps2, d_x, d_v, d_m, d_a, d_j), "g6x_fixed_force")
 

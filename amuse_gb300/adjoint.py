@@ -26,7 +26,7 @@ from __future__ import annotations
 
 import torch
 
-from . import FP64, G6X, SPLIT
+from . import FP64, G6X, JERK_HERMITE, JERK_SOFTENED, SPLIT
 
 _ctx = {}
 
@@ -45,13 +45,15 @@ def _p(t):
 class _Run:
     """Fixed-step runner bound to one library context and precision."""
 
-    def __init__(self, g6, n, eps2, dt, precision):
+    def __init__(self, g6, n, eps2, dt, precision, jerk):
         self.g6, self.n, self.eps2, self.dt = g6, n, float(eps2), float(dt)
         self.prec = FP64 if precision == "fp64" else SPLIT
+        self.jerk = JERK_SOFTENED if jerk == "softened" else JERK_HERMITE
 
     def __enter__(self):
         self.old = self.g6.get_precision()
         self.g6.set_precision(self.prec)
+        self.g6.set_fixed_jerk(self.jerk)
         return self
 
     def __exit__(self, *exc):
@@ -82,13 +84,13 @@ class HermiteFixedFunction(torch.autograd.Function):
     """(x0, v0, m) -> (x, v) after ``nsteps`` fixed Hermite steps."""
 
     @staticmethod
-    def forward(ctx, x0, v0, m, eps2, dt, nsteps, checkpoint, precision, device):
+    def forward(ctx, x0, v0, m, eps2, dt, nsteps, checkpoint, precision, jerk, device):
         _check_inputs(x0, v0, m)
         g6 = context(device)
         n = x0.shape[0]
         stream = torch.cuda.ExternalStream(g6.stream(), device=x0.device)
         stream.wait_stream(torch.cuda.current_stream(x0.device))
-        with torch.cuda.stream(stream), _Run(g6, n, eps2, dt, precision) as r:
+        with torch.cuda.stream(stream), _Run(g6, n, eps2, dt, precision, jerk) as r:
             x, v, mm = x0.detach().clone(), v0.detach().clone(), m.detach().contiguous()
             a, j = r.force(x, v, mm)
             xp, vp = torch.empty_like(x), torch.empty_like(x)
@@ -99,18 +101,18 @@ class HermiteFixedFunction(torch.autograd.Function):
                 r.step(x, v, a, j, mm, xp, vp)
         torch.cuda.current_stream(x0.device).wait_stream(stream)
         ctx.save_for_backward(x0, v0, mm, *ckpt)
-        ctx.cfg = (eps2, dt, nsteps, checkpoint, precision, device)
+        ctx.cfg = (eps2, dt, nsteps, checkpoint, precision, jerk, device)
         return x, v
 
     @staticmethod
     def backward(ctx, gx, gv):
         x0, v0, m, *ckpt = ctx.saved_tensors
-        eps2, dt, nsteps, checkpoint, precision, device = ctx.cfg
+        eps2, dt, nsteps, checkpoint, precision, jerk, device = ctx.cfg
         g6 = context(device)
         n = x0.shape[0]
         stream = torch.cuda.ExternalStream(g6.stream(), device=x0.device)
         stream.wait_stream(torch.cuda.current_stream(x0.device))
-        with torch.cuda.stream(stream), _Run(g6, n, eps2, dt, precision) as r:
+        with torch.cuda.stream(stream), _Run(g6, n, eps2, dt, precision, jerk) as r:
             lx = gx.clone() if gx is not None else torch.zeros_like(x0)
             lv = gv.clone() if gv is not None else torch.zeros_like(x0)
             la, lj = torch.zeros_like(x0), torch.zeros_like(x0)
@@ -136,27 +138,33 @@ class HermiteFixedFunction(torch.autograd.Function):
             lv += gv0
             lm += gm0
         torch.cuda.current_stream(x0.device).wait_stream(stream)
-        return lx, lv, lm, None, None, None, None, None, None
+        return lx, lv, lm, None, None, None, None, None, None, None
 
 
-def hermite_fixed(x0, v0, m, *, eps2, dt, nsteps, checkpoint=16, precision="split", device=0):
+def hermite_fixed(x0, v0, m, *, eps2, dt, nsteps, checkpoint=16, precision="split",
+                  jerk="hermite", device=0):
     """Integrate ``nsteps`` fixed Hermite steps of size dt; differentiable in
     (x0, v0, m) through the hand-written adjoint.  precision: "split"
-    (double-single positions, FP32 pair arithmetic) or "fp64"."""
+    (double-single positions, FP32 pair arithmetic) or "fp64".  jerk:
+    "hermite" (the hermite code's form, whose (r.v) factor uses the
+    unsoftened r^2) or "softened" (the exact derivative of the softened
+    acceleration, as ph4 and the g6 force); equal when eps2 = 0."""
     if precision not in ("split", "fp64"):
         raise ValueError("precision must be 'split' or 'fp64'")
+    if jerk not in ("hermite", "softened"):
+        raise ValueError("jerk must be 'hermite' or 'softened'")
     if nsteps < 1 or checkpoint < 1:
         raise ValueError("nsteps and checkpoint must be positive")
     return HermiteFixedFunction.apply(x0, v0, m, float(eps2), float(dt), int(nsteps),
-                                      int(checkpoint), precision, device)
+                                      int(checkpoint), precision, jerk, device)
 
 
-def final_forces(x, v, m, *, eps2, precision="split", device=0):
+def final_forces(x, v, m, *, eps2, precision="split", jerk="hermite", device=0):
     """(acc, jerk) of the state (x, v) (no gradient)."""
     g6 = context(device)
     stream = torch.cuda.ExternalStream(g6.stream(), device=x.device)
     stream.wait_stream(torch.cuda.current_stream(x.device))
-    with torch.cuda.stream(stream), _Run(g6, x.shape[0], eps2, 0.0, precision) as r:
+    with torch.cuda.stream(stream), _Run(g6, x.shape[0], eps2, 0.0, precision, jerk) as r:
         a, j = r.force(x.detach().contiguous(), v.detach().contiguous(), m.detach().contiguous())
     torch.cuda.current_stream(x.device).wait_stream(stream)
     return a, j

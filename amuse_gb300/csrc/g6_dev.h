@@ -67,6 +67,9 @@ typedef struct {
   /* launch shape override (0 = automatic) */
   int force_jl, force_nsplit;
   int want_nn; /* 0: nn[] = -1 (no nearest-neighbour search) */
+  int hjerk;   /* 1: jerk as the hermite code forms it, (r.v) / r^2 with the
+                  unsoftened r^2 (src/amuse_hermite/interface.cc:440-449,486);
+                  needs want_nn = 0 and force_jl 0 or 1 */
 } g6_force_args;
 
 /* Launch shape actually used (reported by g6k_force). */

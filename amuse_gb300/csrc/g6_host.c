@@ -363,7 +363,8 @@ static int predict_if_needed(int nj) {
 
 /* Run one force evaluation whose inputs are already on the device. */
 static int run_force(g6_force_args *a) {
-  size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, 0, 0);
+  size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->hjerk ? 1 : a->force_jl,
+                                  a->force_nsplit);
   int rc = ensure_scratch(need);
   if (rc) return rc;
   a->scratch = G.d_scratch;
@@ -1607,12 +1608,19 @@ int g6k_fixed_adj_post(int n, double h, double *lx, double *lv, double *la, doub
                        const double *gxp, const double *gvp, double *lm, const double *gm,
                        cudaStream_t st);
 size_t g6k_vjp_scratch_bytes(int n);
-int g6k_force_vjp(int n, double eps2, int prec, const double *x, const double *v,
+int g6k_force_vjp(int n, double eps2, int prec, int hjerk, const double *x, const double *v,
                   const double *m, const double *la1, const double *lj1, double *gx, double *gv,
                   double *gm, double *part, cudaStream_t st);
 
 static double *fx_a1, *fx_j1, *fx_part;
 static int fx_cap;
+static int fx_form = G6_JERK_HERMITE;
+
+int g6x_set_fixed_jerk(int form) {
+  if (form != G6_JERK_HERMITE && form != G6_JERK_SOFTENED) return G6_ERR_ARG;
+  fx_form = form;
+  return 0;
+}
 
 static int fixed_buffers(int n) {
   if (n <= fx_cap && fx_part) return 0;
@@ -1653,6 +1661,7 @@ int g6x_fixed_force(int n, double eps2, const double *d_x, const double *d_v, co
   a.acc = d_a;
   a.jerk = d_j;
   a.pot = G.d_rpot;
+  a.hjerk = fx_form == G6_JERK_HERMITE;
   rc = run_force(&a);
   if (rc) return rc;
   CK(cudaStreamSynchronize(G.st));
@@ -1686,7 +1695,8 @@ int g6x_force_vjp(int n, double eps2, const double *d_x, const double *d_v, cons
   if (n <= 0) return G6_ERR_ARG;
   rc = fixed_buffers(n);
   if (rc) return rc;
-  if (g6k_force_vjp(n, eps2, G.prec, d_x, d_v, d_m, d_la, d_lj, d_gx, d_gv, d_gm, fx_part, G.st))
+  if (g6k_force_vjp(n, eps2, G.prec, fx_form == G6_JERK_HERMITE, d_x, d_v, d_m, d_la, d_lj, d_gx,
+                    d_gv, d_gm, fx_part, G.st))
     return G6_ERR_CUDA;
   CK(cudaStreamSynchronize(G.st));
   return 0;
@@ -1704,7 +1714,8 @@ int g6x_fixed_step_adjoint(int n, double h, double eps2, const double *d_xp, con
   if (rc) return rc;
   double *gxp = d_work, *gvp = d_work + 3 * (size_t)n, *gm = d_work + 6 * (size_t)n;
   if (g6k_fixed_adj_pre(n, h, d_lx, d_lv, d_la, d_lj, fx_a1, fx_j1, G.st)) return G6_ERR_CUDA;
-  if (g6k_force_vjp(n, eps2, G.prec, d_xp, d_vp, d_m, fx_a1, fx_j1, gxp, gvp, gm, fx_part, G.st))
+  if (g6k_force_vjp(n, eps2, G.prec, fx_form == G6_JERK_HERMITE, d_xp, d_vp, d_m, fx_a1, fx_j1,
+                    gxp, gvp, gm, fx_part, G.st))
     return G6_ERR_CUDA;
   if (g6k_fixed_adj_post(n, h, d_lx, d_lv, d_la, d_lj, gxp, gvp, d_lm, gm, G.st))
     return G6_ERR_CUDA;

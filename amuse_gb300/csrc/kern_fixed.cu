@@ -25,6 +25,13 @@
 //   gv_k += mu s^-3/2 - 3 (r.mu) r s^-5/2
 //   gm_k -= La1_j . r s^-3/2 + Lj1_j . (v s^-3/2 - 3 (r.v) r s^-5/2)
 // (the pair Jacobians are even in (r, v), which gives the c combination).
+// With the hermite code's jerk form (r.v divided by the unsoftened q = r^2,
+// src/amuse_hermite/interface.cc:440-449,486) the jerk terms become
+//   gx_k += -3 (mu.v) r s^-5/2 - 3 [(mu.r) v + (r.v) mu] q^-1 s^-3/2
+//           + 3 (r.v)(mu.r) r (2 q^-2 s^-3/2 + 3 q^-1 s^-5/2)
+//   gv_k += mu s^-3/2 - 3 (r.mu) r q^-1 s^-3/2
+//   gm_k -= ... + Lj1_j . (v s^-3/2 - 3 (r.v) r q^-1 s^-3/2)
+// (q = s recovers the softened form).
 // The VJP runs in split precision (double-single r, FP32 pair math, per-tile
 // FP32 partials folded into FP64 totals) or in FP64.
 #include <cuda_runtime.h>
@@ -142,7 +149,7 @@ struct VRecD {
   double x[3], v[3], m, la[3], lj[3];
 };
 
-template <bool F64>
+template <bool F64, bool HJ>
 __global__ void __launch_bounds__(VT) vjp_kernel(int n, double eps2, const double *__restrict__ x,
                                                  const double *__restrict__ v,
                                                  const double *__restrict__ m,
@@ -233,15 +240,26 @@ __global__ void __launch_bounds__(VT) vjp_kernel(int n, double eps2, const doubl
         const double rm = R[0] * mu[0] + R[1] * mu[1] + R[2] * mu[2];
         const double vm = V[0] * mu[0] + V[1] * mu[1] + V[2] * mu[2];
         const double rv = R[0] * V[0] + R[1] * V[1] + R[2] * V[2];
-        const double cr = -3.0 * (rl + vm) * s5 + 15.0 * rv * rm * s7;
+        // qs = q^-1 s^-3/2 (s^-5/2 in the softened form), c7 = 15 s^-7/2 resp.
+        // 3 (2 q^-2 s^-3/2 + 3 q^-1 s^-5/2)
+        double qs, c7;
+        if (HJ) {
+          const double qi = 1.0 / (R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
+          qs = qi * s3;
+          c7 = 3.0 * (2.0 * qi * qs + 3.0 * qi * s5);
+        } else {
+          qs = s5;
+          c7 = 15.0 * s7;
+        }
+        const double cr = -3.0 * (rl * s5 + vm * s5) + rv * rm * c7;
         for (int c = 0; c < 3; c++) {
-          acc[c] += lam[c] * s3 + cr * R[c] - 3.0 * s5 * (rm * V[c] + rv * mu[c]);
-          acc[3 + c] += mu[c] * s3 - 3.0 * rm * s5 * R[c];
+          acc[c] += lam[c] * s3 + cr * R[c] - 3.0 * qs * (rm * V[c] + rv * mu[c]);
+          acc[3 + c] += mu[c] * s3 - 3.0 * rm * qs * R[c];
         }
         const double ga = (r.la[0] * R[0] + r.la[1] * R[1] + r.la[2] * R[2]) * s3;
         const double lv = r.lj[0] * V[0] + r.lj[1] * V[1] + r.lj[2] * V[2];
         const double lr = r.lj[0] * R[0] + r.lj[1] * R[1] + r.lj[2] * R[2];
-        acc[6] -= ga + lv * s3 - 3.0 * rv * lr * s5;
+        acc[6] -= ga + lv * s3 - 3.0 * rv * lr * qs;
       }
       for (int c = 0; c < 7; c++) tot[c] += acc[c];
     } else {
@@ -271,15 +289,24 @@ __global__ void __launch_bounds__(VT) vjp_kernel(int n, double eps2, const doubl
         const float rm = R[0] * mu[0] + R[1] * mu[1] + R[2] * mu[2];
         const float vm = V[0] * mu[0] + V[1] * mu[1] + V[2] * mu[2];
         const float rv = R[0] * V[0] + R[1] * V[1] + R[2] * V[2];
-        const float cr = -3.0f * (rl + vm) * s5 + 15.0f * rv * rm * s7;
+        float qs, c7;
+        if (HJ) {
+          const float qi = __frcp_rn(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
+          qs = qi * s3;
+          c7 = 3.0f * (2.0f * qi * qs + 3.0f * qi * s5);
+        } else {
+          qs = s5;
+          c7 = 15.0f * s7;
+        }
+        const float cr = -3.0f * (rl * s5 + vm * s5) + rv * rm * c7;
         for (int c = 0; c < 3; c++) {
-          acc[c] += lam[c] * s3 + cr * R[c] - 3.0f * s5 * (rm * V[c] + rv * mu[c]);
-          acc[3 + c] += mu[c] * s3 - 3.0f * rm * s5 * R[c];
+          acc[c] += lam[c] * s3 + cr * R[c] - 3.0f * qs * (rm * V[c] + rv * mu[c]);
+          acc[3 + c] += mu[c] * s3 - 3.0f * rm * qs * R[c];
         }
         const float ga = (r.la[0] * R[0] + r.la[1] * R[1] + r.la[2] * R[2]) * s3;
         const float lv = r.lj[0] * V[0] + r.lj[1] * V[1] + r.lj[2] * V[2];
         const float lr = r.lj[0] * R[0] + r.lj[1] * R[1] + r.lj[2] * R[2];
-        acc[6] -= ga + lv * s3 - 3.0f * rv * lr * s5;
+        acc[6] -= ga + lv * s3 - 3.0f * rv * lr * qs;
       }
       for (int c = 0; c < 7; c++) tot[c] += (double)acc[c];
     }
@@ -347,17 +374,25 @@ extern "C" size_t g6k_vjp_scratch_bytes(int n) {
   return (size_t)nsplit * (size_t)n * 7 * sizeof(double);
 }
 
-extern "C" int g6k_force_vjp(int n, double eps2, int prec, const double *x, const double *v,
-                             const double *m, const double *la1, const double *lj1, double *gx,
-                             double *gv, double *gm, double *part, cudaStream_t st) {
+// hjerk: differentiate the hermite code's jerk form instead of the softened
+// one (must match the force the forward step used).
+extern "C" int g6k_force_vjp(int n, double eps2, int prec, int hjerk, const double *x,
+                             const double *v, const double *m, const double *la1,
+                             const double *lj1, double *gx, double *gv, double *gm, double *part,
+                             cudaStream_t st) {
   if (n <= 0) return 0;
   const int nsplit = n >= 8192 ? 8 : (n >= 1024 ? 4 : 1);
   const int jsplit = (n + nsplit - 1) / nsplit;
   dim3 grid((n + VT - 1) / VT, nsplit);
-  if (prec == G6_PREC_FP64)
-    vjp_kernel<true><<<grid, VT, 0, st>>>(n, eps2, x, v, m, la1, lj1, jsplit, part);
-  else
-    vjp_kernel<false><<<grid, VT, 0, st>>>(n, eps2, x, v, m, la1, lj1, jsplit, part);
+#define G6_VJP(F, H) vjp_kernel<F, H><<<grid, VT, 0, st>>>(n, eps2, x, v, m, la1, lj1, jsplit, part)
+  if (prec == G6_PREC_FP64) {
+    if (hjerk) G6_VJP(true, true);
+    else G6_VJP(true, false);
+  } else {
+    if (hjerk) G6_VJP(false, true);
+    else G6_VJP(false, false);
+  }
+#undef G6_VJP
   vjp_reduce_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, nsplit, part, gx, gv, gm);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }

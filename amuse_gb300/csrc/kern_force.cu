@@ -155,6 +155,13 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
   return y;
 }
 
+// One MUFU.RCP, flush-to-zero.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // ------------------------------------------------------- float-float ---
 // Knuth TwoSum folded into a (hi, lo) accumulator.
 __device__ __forceinline__ void ff_acc(float &hi, float &lo, float p) {
@@ -244,7 +251,10 @@ struct SplitP {
     r2 = __fmaf_rn(dy, dy, r2);
     return __fmaf_rn(dz, dz, r2);
   }
-  template <bool CHECK, bool NN>
+  // HJ: the jerk as the hermite code forms it (src/amuse_hermite/interface.cc:440-449,
+  // 469-486):
+  // the (r.v) factor is divided by the UNsoftened r^2.
+  template <bool CHECK, bool NN, bool HJ = false>
   __device__ static __forceinline__ void pair(const I &s, const Rec &r, float eps2, Part &q,
                                               float &nnmin, bool is_self) {
     float dx, dy, dz;
@@ -261,7 +271,14 @@ struct SplitP {
     const float rinv2 = rinv * rinv;
     const float mri = r.ph.w * rinv;
     const float mr3i = mri * rinv2;
-    const float a3 = -3.0f * (rv * rinv2);
+    float a3;
+    if (HJ) {
+      const float r2u = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+      a3 = -3.0f * (rv * rcp_approx(r2u));
+      if (CHECK) a3 = is_self ? 0.f : a3;
+    } else {
+      a3 = -3.0f * (rv * rinv2);
+    }
     q.a[0] = fmaf(mr3i, dx, q.a[0]);
     q.a[1] = fmaf(mr3i, dy, q.a[1]);
     q.a[2] = fmaf(mr3i, dz, q.a[2]);
@@ -370,7 +387,7 @@ struct F64P {
     y = y * __fma_rn(-hx * y, y, 1.5);
     return y;
   }
-  template <bool CHECK, bool NN>
+  template <bool CHECK, bool NN, bool HJ = false>
   __device__ static __forceinline__ void pair(const I &s, const Rec &r, double eps2, Part &q,
                                               double &nnmin, bool is_self) {
     double dx, dy, dz;
@@ -387,7 +404,13 @@ struct F64P {
     const double rinv2 = rinv * rinv;
     const double mri = r.p.w * rinv;
     const double mr3i = mri * rinv2;
-    const double a3 = -3.0 * (rv * rinv2);
+    double a3;
+    if (HJ) {
+      const double r2u = dx * dx + dy * dy + dz * dz;
+      a3 = (CHECK && is_self) ? 0.0 : -3.0 * (rv / r2u);
+    } else {
+      a3 = -3.0 * (rv * rinv2);
+    }
     q.a[0] = fma(mr3i, dx, q.a[0]);
     q.a[1] = fma(mr3i, dy, q.a[1]);
     q.a[2] = fma(mr3i, dz, q.a[2]);
@@ -454,12 +477,13 @@ struct KParams {
   int ni_pad;
   int *err;
   int want_nn;
+  int hjerk;  // the hermite code's jerk form (JL = 1, no nn only)
 };
 
 // Number of j per thread between compensated folds.
 constexpr int FOLD_J = 64;
 
-template <class P, int JL, bool NN>
+template <class P, int JL, bool NN, bool HJ = false>
 __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   constexpr int NSTAGE = P::NSTAGE;
   using Rec = typename P::Rec;
@@ -570,7 +594,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
         const Rec r = tile[jl + JL * u];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
-          P::template pair<false, NN>(I[k], r, eps2, q[k], nnmin[k], false);
+          P::template pair<false, NN, HJ>(I[k], r, eps2, q[k], nnmin[k], false);
       }
     } else {
       for (int u = 0; u < JPT; u++) {
@@ -578,7 +602,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
         const Rec r = tile[jj];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
-          P::template pair<true, NN>(I[k], r, eps2, q[k], nnmin[k], tj0 + jj == self[k]);
+          P::template pair<true, NN, HJ>(I[k], r, eps2, q[k], nnmin[k], tj0 + jj == self[k]);
       }
     }
 
@@ -826,7 +850,10 @@ int launch(const KParams &kp, int jl, int gx, cudaStream_t st) {
   dim3 grid(gx, kp.nsplit), block(NT);
   // Without nearest neighbours only the large-block shape has its own
   // instantiation; small blocks are latency-bound and keep the nn code.
-  if (jl == 1 && !kp.want_nn) {
+  if (kp.hjerk) {
+    if (jl != 1 || kp.want_nn) return -2;
+    force_kernel<P, 1, false, true><<<grid, block, 0, st>>>(kp);
+  } else if (jl == 1 && !kp.want_nn) {
     force_kernel<P, 1, false><<<grid, block, 0, st>>>(kp);
   } else switch (jl) {
 #define G6_CASE(J)                                         \
@@ -868,8 +895,10 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
   if (a->ni <= 0) return 0;
   if (a->nj <= 0 || !a->acc || !a->jerk || !a->pot || !a->js || !a->err) return -1;
   if (!a->ilist && (!a->ipos || !a->ivel)) return -1;
+  if (a->hjerk && (a->want_nn || (a->force_jl != 0 && a->force_jl != 1))) return -2;
   int jl, nsplit, jsplit;
-  choose_shape(a->ni, a->nj, a->prec, a->force_jl, a->force_nsplit, &jl, &nsplit, &jsplit);
+  choose_shape(a->ni, a->nj, a->prec, a->hjerk ? 1 : a->force_jl, a->force_nsplit, &jl, &nsplit,
+               &jsplit);
   if (jl < 1 || jl > JLMAX || (jl & (jl - 1))) return -2;
   KParams kp;
   kp.ni = a->ni;
@@ -890,6 +919,7 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
   kp.ni_pad = a->ni;
   kp.err = a->err;
   kp.want_nn = a->want_nn;
+  kp.hjerk = a->hjerk;
   const size_t need = nsplit > 1 ? g6k_scratch_bytes(a->ni, a->nj, a->prec, jl, nsplit) : 0;
   if (need > a->scratch_bytes) return -4;
   const int islots = (NT / jl) * IPT;
@@ -940,7 +970,8 @@ extern "C" int g6k_force_static(const g6_force_args *a, g6_shape *shape, cudaStr
     addr[dev] = p;
     have[dev] = 1;
   }
-  const size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->force_jl, a->force_nsplit);
+  const size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->hjerk ? 1 : a->force_jl,
+                                        a->force_nsplit);
   if (need_out) *need_out = need;
   if (need > G6_STATIC_SCRATCH_BYTES) return -4;
   g6_force_args b = *a;

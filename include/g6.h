@@ -236,6 +236,14 @@ int g6x_batch_tune(int nsys, const int *n_per_sys, const double *t_end, const do
                               the state cotangents (lx, lv, la, lj); lm
                               accumulates the mass cotangent; work holds 7n
                               doubles. */
+/* Jerk form of the fixed-step force (and of its derivatives):
+   G6_JERK_HERMITE (default) -- the hermite code's, whose (r.v) factor is
+     divided by the unsoftened r^2 (interface.cc:440-449,486);
+   G6_JERK_SOFTENED          -- ph4's / this library's g6 force, the exact
+     time derivative of the softened acceleration.  Equal when eps2 = 0. */
+#define G6_JERK_HERMITE 0
+#define G6_JERK_SOFTENED 1
+int g6x_set_fixed_jerk(int form);
 int g6x_fixed_force(int n, double eps2, const double *d_x, const double *d_v, const double *d_m,
                     double *d_a, double *d_j);
 int g6x_fixed_step(int n, double h, double eps2, double *d_x, double *d_v, double *d_a,

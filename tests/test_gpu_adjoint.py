@@ -1,7 +1,7 @@
 """GPU: fixed-step Hermite forward and its hand-written adjoint.
 
-* forward (FP64 force) against the torch FP64 restatement and, at eps2 = 0,
-  against the oracle's restatement of the hermite code;
+* forward (FP64 force) against the torch FP64 restatement (both jerk forms)
+  and against the oracle's restatement of the hermite code;
 * adjoint (FP64) against torch autograd of the restatement (reference
   gradient), against central finite differences of the GPU forward
   (h = 1e-6, relative error <= 1e-4), and independent of the checkpoint
@@ -31,48 +31,52 @@ def _cuda(*arrays):
     return [torch.tensor(a, dtype=torch.float64, device="cuda") for a in arrays]
 
 
-def _grad(m, x, v, w, eps2, dt, nsteps, checkpoint, precision):
+def _grad(m, x, v, w, eps2, dt, nsteps, checkpoint, precision, jerk="hermite"):
     from amuse_gb300.adjoint import hermite_fixed
     tm, tx, tv, tw = _cuda(m, x, v, w)
     for t in (tm, tx, tv):
         t.requires_grad_(True)
     xf, vf = hermite_fixed(tx, tv, tm, eps2=eps2, dt=dt, nsteps=nsteps, checkpoint=checkpoint,
-                           precision=precision)
+                           precision=precision, jerk=jerk)
     loss = ht.loss(xf, tw)
     loss.backward()
     return (loss.item(), tx.grad.cpu().numpy(), tv.grad.cpu().numpy(), tm.grad.cpu().numpy(),
             xf.detach().cpu().numpy(), vf.detach().cpu().numpy())
 
 
-def test_forward_fp64_matches_torch(g6):
+@pytest.mark.parametrize("jerk", ["hermite", "softened"])
+def test_forward_fp64_matches_torch(g6, jerk):
     from amuse_gb300.adjoint import hermite_fixed
     m, x, v, _ = _system(96, 1)
     tm, tx, tv = _cuda(m, x, v)
-    xf, vf = hermite_fixed(tx, tv, tm, eps2=1e-4, dt=1 / 256, nsteps=24, precision="fp64")
-    rx, rv = ht.run(torch.tensor(x), torch.tensor(v), torch.tensor(m), 1e-4, 1 / 256, 24)
+    xf, vf = hermite_fixed(tx, tv, tm, eps2=1e-4, dt=1 / 256, nsteps=24, precision="fp64",
+                           jerk=jerk)
+    rx, rv = ht.run(torch.tensor(x), torch.tensor(v), torch.tensor(m), 1e-4, 1 / 256, 24, jerk)
     np.testing.assert_allclose(xf.cpu().numpy(), rx.numpy(), rtol=0, atol=1e-12)
     np.testing.assert_allclose(vf.cpu().numpy(), rv.numpy(), rtol=0, atol=1e-11)
 
 
-def test_forward_fp64_matches_hermite_oracle(g6):
+@pytest.mark.parametrize("eps2", [0.0, 1e-4])
+def test_forward_fp64_matches_hermite_oracle(g6, eps2):
     import oracle
     m, x, v, _ = _system(300, 2, eps_mass=False)
     tm, tx, tv = _cuda(m, x, v)
     from amuse_gb300.adjoint import hermite_fixed
-    xf, vf = hermite_fixed(tx, tv, tm, eps2=0.0, dt=1 / 1024, nsteps=16, precision="fp64")
-    p, vv, _, _ = oracle.hermite_fixed(m, x, v, 0.0, 1 / 1024, 16)
+    xf, vf = hermite_fixed(tx, tv, tm, eps2=eps2, dt=1 / 1024, nsteps=16, precision="fp64")
+    p, vv, _, _ = oracle.hermite_fixed(m, x, v, eps2, 1 / 1024, 16)
     np.testing.assert_allclose(xf.cpu().numpy(), p, rtol=0, atol=1e-11)
     np.testing.assert_allclose(vf.cpu().numpy(), vv, rtol=0, atol=1e-9)
 
 
-def test_adjoint_fp64_matches_autograd(g6):
+@pytest.mark.parametrize("jerk", ["hermite", "softened"])
+def test_adjoint_fp64_matches_autograd(g6, jerk):
     m, x, v, w = _system(64, 3)
     eps2, dt, nsteps = 1e-4, 1 / 256, 12
-    _, gx, gv, gm, _, _ = _grad(m, x, v, w, eps2, dt, nsteps, 5, "fp64")
+    _, gx, gv, gm, _, _ = _grad(m, x, v, w, eps2, dt, nsteps, 5, "fp64", jerk)
     tx = torch.tensor(x, requires_grad=True)
     tv = torch.tensor(v, requires_grad=True)
     tm = torch.tensor(m, requires_grad=True)
-    xf, _ = ht.run(tx, tv, tm, eps2, dt, nsteps)
+    xf, _ = ht.run(tx, tv, tm, eps2, dt, nsteps, jerk)
     ht.loss(xf, torch.tensor(w)).backward()
     for g, r in ((gx, tx.grad), (gv, tv.grad), (gm, tm.grad)):
         r = r.numpy()
@@ -133,3 +137,19 @@ def test_adjoint_split_close_to_fp64(g6):
 def test_force_vjp_rejects_empty(g6):
     with pytest.raises(Exception):
         g6.force_vjp(0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0)
+
+
+@pytest.mark.parametrize("precision", ["split", "fp64"])
+def test_fixed_force_matches_torch(g6, precision):
+    """The force alone, hermite jerk form, against the torch restatement."""
+    from amuse_gb300.adjoint import final_forces
+    m, x, v, _ = _system(1000, 8)
+    tm, tx, tv = _cuda(m, x, v)
+    a, j = final_forces(tx, tv, tm, eps2=1e-4, precision=precision)
+    ra, rj = ht.forces(torch.tensor(x), torch.tensor(v), torch.tensor(m), 1e-4)
+    for g, r, tol_split in ((a, ra, 1e-6), (j, rj, 1e-5)):
+        err = ((g.cpu() - r).norm(dim=1) / r.norm(dim=1)).numpy()
+        if precision == "fp64":
+            assert err.max() <= 1e-10, err.max()
+        else:
+            assert np.quantile(err, 0.99) <= tol_split, np.quantile(err, 0.99)

@@ -311,8 +311,9 @@ class G6X(G6):
     def run_init(self, eps2, eta):
         _check(self.lib.g6x_run_init(eps2, eta), "g6x_run_init")
 
-    def run(self, t_end):
-        nb = ctypes.c_longlong(0)
+    def run(self, t_end, max_blocks=0):
+        """Block steps to t_end (or max_blocks of them); -> (blocks, particle steps)."""
+        nb = ctypes.c_longlong(max_blocks)
         ns = ctypes.c_double(0)
         _check(self.lib.g6x_run(t_end, ctypes.byref(nb), ctypes.byref(ns)), "g6x_run")
         return nb.value, ns.value

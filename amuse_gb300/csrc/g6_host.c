@@ -1165,11 +1165,12 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
   if (rc) return rc;
   const int n = G.run_n;
   if (n <= 0 || G.run_cap < n) return G6_ERR_STATE;
+  const long long max_blocks = blocks && *blocks > 0 ? *blocks : -1;
   long long nb = 0;
   double ns = 0;
   int hbuf[2];
   double tn;
-  while (G.run_t < t_end) {
+  while (G.run_t < t_end && nb != max_blocks) {
     ilist_identity_n = 0;
     if (g6k_schedule(&G.js, n, G.d_ilist, G.d_ni, G.d_tnext, G.d_sched, 4, G.st))
       return G6_ERR_CUDA;

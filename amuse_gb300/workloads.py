@@ -6,6 +6,12 @@ one (which is bench.py).  Each prints one JSON line.
       eps = 0, to 10 crossing times, smallN's scheme (g6x_batch_run) after
       the autotuner; systems/s and p50/p99 per-system GPU time.
       (bench.py --workload batch adds the host-core baseline.)
+  python -m amuse_gb300.workloads precision [--n 1048576]
+      Split vs FP64 per-particle force errors on all N and the energy drift
+      over 64 block steps.
+  python -m amuse_gb300.workloads salpeter [--n 65536] [--t-end 0.25]
+      Salpeter-IMF Plummer block-step run on the device, then split vs FP64
+      forces at ni = 1 ... N.
   python -m amuse_gb300.workloads adjoint [--n 16384] [--nsteps 256]
       Differentiable fixed-step Hermite: timing of forward and backward in
       split precision and FP64, split vs FP64 gradients, and finite
@@ -164,6 +170,123 @@ def run_adjoint(args):
     return out
 
 
+def _stats(err):
+    err = np.asarray(err)
+    return {"min": float(err.min()), "p50": float(np.percentile(err, 50)),
+            "p99": float(np.percentile(err, 99)), "max": float(err.max()),
+            "frac_le_1e-6": float(np.mean(err <= 1e-6))}
+
+
+def _slot_forces(g6, torch, prec, n, ni, eps2, ilist):
+    """acc, jerk, pot of slots [0, ni) against slots [0, n) (device run)."""
+    g6.set_precision(prec)
+    dev = ilist.device
+    acc = torch.empty((ni, 3), dtype=torch.float64, device=dev)
+    jerk = torch.empty_like(acc)
+    pot = torch.empty(ni, dtype=torch.float64, device=dev)
+    t0 = time.perf_counter()
+    g6.force_slots(g6.system_time(), eps2, n, ilist.data_ptr(), ni, acc.data_ptr(),
+                   jerk.data_ptr(), pot.data_ptr(), None)
+    dt = time.perf_counter() - t0
+    return acc.cpu().numpy(), jerk.cpu().numpy(), pot.cpu().numpy(), dt
+
+
+def _errors(s, d):
+    a, j, p = s[:3]
+    ad, jd, pd = d[:3]
+    return {"acc": _stats(np.linalg.norm(a - ad, axis=1) / np.linalg.norm(ad, axis=1)),
+            "jerk": _stats(np.linalg.norm(j - jd, axis=1) / np.linalg.norm(jd, axis=1)),
+            "pot": _stats(np.abs(p - pd) / np.abs(pd))}
+
+
+def run_precision(args):
+    """Config 3: Plummer N = 2^20 equal mass, eps2 = 1e-6 (the benchmark's
+    particles).  Per-particle relative acc/jerk/pot errors of the split
+    kernel against the plain FP64 kernel on all N (min/p50/p99/max), and the
+    energy drift of the device block-step driver over 64 block steps."""
+    import torch
+    import amuse_gb300 as ag
+    from amuse_gb300 import ic
+    n, eps2 = args.n, 1e-6
+    np.random.seed(1)
+    m, x, v = ic.plummer(n, do_scale=False)
+    g6 = ag.G6X(0)
+    g6.load_particles(m, x, v)
+    ilist = torch.arange(n, dtype=torch.int32, device="cuda")
+    out = {"workload": f"plummer N={n} equal mass eps2={eps2} (numpy seed 1)"}
+    sp = _slot_forces(g6, torch, ag.SPLIT, n, n, eps2, ilist)
+    dp = _slot_forces(g6, torch, ag.FP64, n, n, eps2, ilist)
+    out["split_vs_fp64"] = _errors(sp, dp)
+    out["force_seconds"] = {"split": sp[3], "fp64": dp[3],
+                            "split_pairs_per_s": n * (n - 1) / sp[3],
+                            "fp64_pairs_per_s": n * (n - 1) / dp[3]}
+    print(json.dumps(out), flush=True)
+    g6.set_precision(ag.SPLIT)
+    g6.run_init(eps2, args.eta)
+    k0, p0 = g6.energy()
+    t0 = time.perf_counter()
+    nb, ns = g6.run(1e30, max_blocks=64)
+    wall = time.perf_counter() - t0
+    k1, p1 = g6.energy()
+    e0, e1 = k0 + p0, k1 + p1
+    out["block_steps"] = {"eta": args.eta, "precision": "split", "blocks": nb,
+                          "particle_steps": ns, "t_reached": g6.system_time(),
+                          "seconds": wall, "pairs_per_s": ns * (n - 1) / wall,
+                          "E0": e0, "E1": e1, "dE_over_E": abs(e1 - e0) / abs(e0)}
+    print(json.dumps(out), flush=True)
+    return out
+
+
+def run_salpeter(args):
+    """Config 2: Plummer N = 65536 with a Salpeter IMF (slope -2.35, mass
+    range 0.1-100, total mass 1, re-scaled to virial after the masses),
+    eps2 = 1e-6, block steps to t = 0.25 on the device; then split vs FP64
+    forces on blocks of ni = 1 ... N slots."""
+    import torch
+    import amuse_gb300 as ag
+    from amuse_gb300 import ic
+    n, eps2 = args.n, 1e-6
+    g6 = ag.G6X(0)
+    ilist = torch.arange(n, dtype=torch.int32, device="cuda")
+
+    def gpu_potential(mass, pos):
+        g6.load_particles(mass, pos, np.zeros_like(pos))
+        _, _, pot, _ = _slot_forces(g6, torch, ag.FP64, len(mass), len(mass), 0.0, ilist)
+        return 0.5 * float(np.sum(mass * pot))
+
+    rng = np.random.RandomState(args.seed)
+    m, x, v = ic.plummer_salpeter(n, mass_min=0.1, mass_max=100.0, rng=rng,
+                                  potential_energy=gpu_potential)
+    g6.load_particles(m, x, v)
+    out = {"workload": f"plummer N={n} Salpeter IMF (-2.35, 0.1-100) eps2={eps2}, "
+                       f"block steps to t={args.t_end}, eta={args.eta}, seed {args.seed}"}
+    prec = ag.FP64 if args.fp64 else ag.SPLIT
+    g6.set_precision(prec)
+    g6.run_init(eps2, args.eta)
+    k0, p0 = g6.energy()
+    t0 = time.perf_counter()
+    nb, ns = g6.run(args.t_end)
+    wall = time.perf_counter() - t0
+    k1, p1 = g6.energy()
+    e0, e1 = k0 + p0, k1 + p1
+    out["run"] = {"precision": "fp64" if args.fp64 else "split", "blocks": nb,
+                  "particle_steps": ns, "mean_ni": ns / max(nb, 1), "seconds": wall,
+                  "pairs_per_s": ns * (n - 1) / wall, "E0": e0, "E1": e1,
+                  "dE_over_E": abs(e1 - e0) / abs(e0)}
+    print(json.dumps(out), flush=True)
+    checks = {}
+    for ni in (1, 2, 3, 7, 31, 100, 1000, 4096, 10000, n):
+        ni = min(ni, n)
+        sp = _slot_forces(g6, torch, ag.SPLIT, n, ni, eps2, ilist)
+        dp = _slot_forces(g6, torch, ag.FP64, n, ni, eps2, ilist)
+        e = _errors(sp, dp)
+        checks[str(ni)] = {k: {"p99": e[k]["p99"], "max": e[k]["max"]} for k in e}
+    out["split_vs_fp64_by_ni"] = checks
+    g6.set_precision(ag.SPLIT)
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -179,11 +302,24 @@ def main():
     d.add_argument("--seed", type=int, default=7)
     d.add_argument("--fd-coords", type=int, default=32)
     d.add_argument("--fd64-coords", type=int, default=4)
+    pr = sub.add_parser("precision")
+    pr.add_argument("--n", type=int, default=1 << 20)
+    pr.add_argument("--eta", type=float, default=0.14)
+    sa = sub.add_parser("salpeter")
+    sa.add_argument("--n", type=int, default=65536)
+    sa.add_argument("--eta", type=float, default=0.14)
+    sa.add_argument("--t-end", type=float, default=0.25)
+    sa.add_argument("--seed", type=int, default=1)
+    sa.add_argument("--fp64", action="store_true")
     a = ap.parse_args()
     if a.cmd == "batch":
         run_batch(a)
     elif a.cmd == "adjoint":
         run_adjoint(a)
+    elif a.cmd == "precision":
+        run_precision(a)
+    elif a.cmd == "salpeter":
+        run_salpeter(a)
 
 
 if __name__ == "__main__":

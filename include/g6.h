@@ -170,7 +170,9 @@ int g6x_force_slots(double ti, double eps2, int nj, int ni, const int *d_ilist, 
 /* Device-resident ph4-style integration of the loaded particles:
    g6x_run_init  -- forces at t = 0 and initial steps (jdata.cc:503-580),
    g6x_run       -- block steps (predict all j, force on the block, FP64
-                    corrector + Aarseth step) until system time >= t_end,
+                    corrector + Aarseth step) until system time >= t_end
+                    or, if *blocks > 0 on entry, after *blocks block steps;
+                    *blocks returns the block steps taken,
    g6x_energy    -- kinetic and potential energy at the system time,
    g6x_step_all  -- one shared step of all particles to tnext (the
                     benchmark step: predict + force on all + correct). */

@@ -106,6 +106,22 @@ def test_force_block_sizes(g6, prec, ni):
     check_force(out, ref, prec, x, x[sel], label=f"ni={ni}")
 
 
+def test_force_1m_subset_vs_oracle(g6, prec):
+    """The precision configuration's particles (Plummer N = 2^20, eps2 = 1e-6):
+    a 1024-particle i-subset against all N j, GPU vs the oracle's ph4 loop
+    on the host cores.  This is the cross-check that makes the FP64 GPU kernel
+    the oracle for the all-N error distribution."""
+    import os
+    n = 1 << 20
+    np.random.seed(1)
+    m, x, v = ic.plummer(n)
+    sel = np.sort(np.random.RandomState(3).choice(n, 1024, replace=False))
+    g6.load_particles(m, x, v)
+    out = g6.force(0.0, 1e-6, n, x[sel], v[sel], self_slot=sel)
+    ref = oracle.force(m, x, v, 1e-6, x[sel], v[sel], threads=os.cpu_count() or 1)
+    check_force(out, ref, prec, x, x[sel], label="N=2^20")
+
+
 def test_chunking_by_npipes(g6):
     np.random.seed(12)
     m, x, v = ic.plummer(2048)

@@ -159,6 +159,15 @@ def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
+BATCH_MODES = {"fast": 0, "exact": 1, "split": 2}
+
+
+def _batch_mode(mode, exact):
+    if mode is None:
+        return BATCH_MODES["exact" if exact else "fast"]
+    return BATCH_MODES[mode]
+
+
 class G6:
     """The GRAPE-6 API of the library (one context per process)."""
 
@@ -327,9 +336,11 @@ class G6X(G6):
                "g6x_correct")
 
     def batch_run(self, n_per_sys, t_end, mass, pos, vel, eta=0.14, n_iter=2, max_steps=0,
-                  exact=False):
+                  exact=False, mode=None):
         """Integrate many few-body systems (smallN's scheme); returns a dict
-        with pos, vel (updated copies), t_final, steps, wall_ms, status, elapsed_ms."""
+        with pos, vel (updated copies), t_final, steps, wall_ms, status, elapsed_ms.
+        mode: "fast" (default), "exact" (bit-identical to smallN; also
+        exact=True) or "split" (FP32 pair terms from double-single positions)."""
         n_per_sys = _i32(n_per_sys)
         nsys = len(n_per_sys)
         t_end = _f64(np.broadcast_to(np.asarray(t_end, dtype=np.float64), (nsys,)))
@@ -342,7 +353,7 @@ class G6X(G6):
         P = lambda a: _ptr(a, ctypes.c_double)
         _check(self.lib.g6x_batch_run(nsys, _ptr(n_per_sys, ctypes.c_int), P(t_end), P(mass),
                                       P(pos), P(vel), eta, n_iter, int(max_steps),
-                                      1 if exact else 0, P(tf),
+                                      _batch_mode(mode, exact), P(tf),
                                       st.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
                                       P(wall), _ptr(status, ctypes.c_int), ctypes.byref(el)),
                "g6x_batch_run")
@@ -353,7 +364,7 @@ class G6X(G6):
         _check(self.lib.g6x_batch_config(warps_per_cta, ctas_per_sm), "g6x_batch_config")
 
     def batch_tune(self, n_per_sys, t_end, mass, pos, vel, eta=0.14, n_iter=2, exact=False,
-                   frac=0.1):
+                   frac=0.1, mode=None):
         n_per_sys = _i32(n_per_sys)
         nsys = len(n_per_sys)
         t_end = _f64(np.broadcast_to(np.asarray(t_end, dtype=np.float64), (nsys,)))
@@ -361,7 +372,8 @@ class G6X(G6):
         P = lambda a: _ptr(a, ctypes.c_double)
         _check(self.lib.g6x_batch_tune(nsys, _ptr(n_per_sys, ctypes.c_int), P(t_end),
                                        P(_f64(mass)), P(_f64(pos)), P(_f64(vel)), eta, n_iter,
-                                       1 if exact else 0, frac, P(out)), "g6x_batch_tune")
+                                       _batch_mode(mode, exact), frac, P(out)),
+               "g6x_batch_tune")
         return dict(warps_per_cta=int(out[0]), ctas_per_sm=int(out[1]), ms=out[2])
 
     def step_all(self, tnext):

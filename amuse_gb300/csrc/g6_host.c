@@ -1468,7 +1468,8 @@ int g6x_batch_run(int nsys, const int *n_per_sys, const double *t_end, const dou
                   double *wall_ms, int *status, double *elapsed_ms) {
   int rc = check_open();
   if (rc) return rc;
-  if (nsys <= 0 || !n_per_sys || !t_end || !mass || !pos || !vel || n_iter < 0 || eta <= 0)
+  if (nsys <= 0 || !n_per_sys || !t_end || !mass || !pos || !vel || n_iter < 0 || eta <= 0 ||
+      exact < G6_BATCH_FAST || exact > G6_BATCH_SPLIT)
     return G6_ERR_ARG;
   const int maxn = g6k_batch_max_n();
   int *off = (int *)malloc(sizeof(int) * (size_t)(nsys + 1));

@@ -19,9 +19,14 @@
 // the same order, as smallN on the CPU (each pair in its (i < j) orientation,
 // contributions accumulated in smallN's pair order, no fused multiply-adds,
 // IEEE divides and square roots), so results are bit-identical to smallN.
-// EXACT = false uses one reciprocal square root per pair and FMAs (about 7x
+// MODE_FAST uses one reciprocal square root per pair and FMAs (about 7x
 // fewer FP64 instructions; results differ from smallN at the last-bit
 // level, which chaotic systems amplify).
+// MODE_SPLIT keeps the state, the predictor and the corrector in FP64 but
+// evaluates the pair terms in FP32 from double-single positions (the
+// relative position is exact to FP32 precision of |r|, as in the g6 force
+// kernel) and FP32 velocities, with one rsqrt.approx per pair: GB300 runs
+// FP32 at 64x its FP64 rate, and the pair terms are the O(n^2) part.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -29,6 +34,7 @@ namespace {
 
 constexpr int MAXN = 64;
 constexpr int WARPS_MAX = 8;
+enum { MODE_FAST = 0, MODE_EXACT = 1, MODE_SPLIT = 2 };
 
 
 __device__ __forceinline__ double ADD(double a, double b) { return __dadd_rn(a, b); }
@@ -42,9 +48,19 @@ struct Body {
 };
 
 struct WarpSmem {
-  double pp[MAXN][3];
-  double pv[MAXN][3];
+  union {
+    struct {
+      double pp[MAXN][3];
+      double pv[MAXN][3];
+    } d;
+    struct {  // MODE_SPLIT: double-single positions, FP32 velocities
+      float ph[MAXN][3];
+      float pl[MAXN][3];
+      float vf[MAXN][3];
+    } f;
+  };
   double m[MAXN];
+  float mf[MAXN];
 };
 
 // 1/sqrt(x): FP32 MUFU seed, two Newton-Raphson steps.
@@ -65,8 +81,8 @@ __device__ __forceinline__ double pair_term(const WarpSmem &S, int a, int b, boo
   double dx[3], dv[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    dx[k] = SUB(S.pp[b][k], S.pp[a][k]);
-    dv[k] = SUB(S.pv[b][k], S.pv[a][k]);
+    dx[k] = SUB(S.d.pp[b][k], S.d.pp[a][k]);
+    dv[k] = SUB(S.d.pv[b][k], S.d.pv[a][k]);
   }
   if (EXACT) {
     const double d2 = ADD(ADD(MUL(dx[0], dx[0]), MUL(dx[1], dx[1])), MUL(dx[2], dx[2]));
@@ -112,10 +128,46 @@ __device__ __forceinline__ double pair_term(const WarpSmem &S, int a, int b, boo
   }
 }
 
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// MODE_SPLIT pair term: contribution of j to body i (FP32), and the pair's
+// Kepler step^2 (FP32; FP64 below d^2 = 1e-24, where d^3 would leave the
+// FP32 normal range).
+__device__ __forceinline__ float pair_split(const WarpSmem &S, int i, int j, float acc[3],
+                                            float jerk[3]) {
+  float dx[3], dv[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    dx[k] = __fadd_rn(__fsub_rn(S.f.ph[j][k], S.f.ph[i][k]), __fsub_rn(S.f.pl[j][k], S.f.pl[i][k]));
+    dv[k] = S.f.vf[j][k] - S.f.vf[i][k];
+  }
+  const float d2 = fmaf(dx[2], dx[2], fmaf(dx[1], dx[1], dx[0] * dx[0]));
+  const float rinv = rsqrt_approx(d2);
+  const float rinv2 = rinv * rinv;
+  const float f = S.mf[j] * rinv * rinv2;
+  const float xv = fmaf(dx[2], dv[2], fmaf(dx[1], dv[1], dx[0] * dv[0]));
+  const float a3 = -3.0f * xv * rinv2;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    acc[k] = fmaf(f, dx[k], acc[k]);
+    jerk[k] = fmaf(f, fmaf(a3, dx[k], dv[k]), jerk[k]);
+  }
+  const float v2 = fmaf(dv[2], dv[2], fmaf(dv[1], dv[1], dv[0] * dv[0]));
+  const float mt = S.mf[i] + S.mf[j];
+  if (d2 >= 1e-24f) return fminf(0.5f * d2 * (d2 * rinv) / mt, d2 / v2);
+  const double dd2 = (double)d2;
+  return (float)fmin(0.5 * dd2 * sqrt(dd2) / (double)mt, dd2 / (double)v2);
+}
+
 // acc/jerk of the lane's bodies from the predicted state in S; returns the
 // system's min Kepler step^2 (warp-uniform).
-template <bool EXACT>
+template <int MODE>
 __device__ double forces(const WarpSmem &S, int n, int lane, Body B[2]) {
+  constexpr bool EXACT = MODE == MODE_EXACT;
   double ts2 = __longlong_as_double(0x7ff0000000000000ll);
 #pragma unroll
   for (int q = 0; q < 2; q++) {
@@ -123,7 +175,20 @@ __device__ double forces(const WarpSmem &S, int n, int lane, Body B[2]) {
 #pragma unroll
     for (int k = 0; k < 3; k++) B[q].acc[k] = B[q].jerk[k] = 0.0;
     if (i >= n) continue;
-    if (EXACT) {
+    if (MODE == MODE_SPLIT) {
+      float a[3] = {0.f, 0.f, 0.f}, jk[3] = {0.f, 0.f, 0.f};
+      float m2 = __int_as_float(0x7f800000);
+      for (int j = 0; j < n; j++) {
+        if (j == i) continue;
+        m2 = fminf(m2, pair_split(S, i, j, a, jk));
+      }
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        B[q].acc[k] = (double)a[k];
+        B[q].jerk[k] = (double)jk[k];
+      }
+      ts2 = fmin(ts2, (double)m2);
+    } else if (EXACT) {
       // smallN's pair order: (j, i) for j < i first, then (i, j) for j > i,
       // each pair in its (i < j) orientation.
       for (int j = 0; j < i; j++)
@@ -143,6 +208,7 @@ __device__ double forces(const WarpSmem &S, int n, int lane, Body B[2]) {
   return ts2;
 }
 
+template <int MODE>
 __device__ __forceinline__ void publish(WarpSmem &S, int n, int lane, const Body B[2]) {
   __syncwarp();
 #pragma unroll
@@ -151,20 +217,28 @@ __device__ __forceinline__ void publish(WarpSmem &S, int n, int lane, const Body
     if (i < n) {
 #pragma unroll
       for (int k = 0; k < 3; k++) {
-        S.pp[i][k] = B[q].pp[k];
-        S.pv[i][k] = B[q].pv[k];
+        if (MODE == MODE_SPLIT) {
+          const float h = __double2float_rn(B[q].pp[k]);
+          S.f.ph[i][k] = h;
+          S.f.pl[i][k] = __double2float_rn(B[q].pp[k] - (double)h);
+          S.f.vf[i][k] = __double2float_rn(B[q].pv[k]);
+        } else {
+          S.d.pp[i][k] = B[q].pp[k];
+          S.d.pv[i][k] = B[q].pv[k];
+        }
       }
     }
   }
   __syncwarp();
 }
 
-template <bool EXACT>
+template <int MODE>
 __global__ void batch_kernel(int nsys, const int *__restrict__ order, const int *__restrict__ off,
                              const double *__restrict__ t_end_s, const double *__restrict__ mass,
                              double *pos, double *vel, double eta, int n_iter,
                              long long max_steps, int *queue, double *t_out, long long *steps_out,
                              unsigned long long *wall_ns, int *status) {
+  constexpr bool EXACT = MODE == MODE_EXACT;
   __shared__ WarpSmem smem[WARPS_MAX];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
@@ -203,12 +277,15 @@ __global__ void batch_kernel(int nsys, const int *__restrict__ order, const int 
         B[qq].pv[k] = B[qq].vel[k];
         B[qq].oacc[k] = B[qq].ojerk[k] = 0.0;  // hdyn() zeroes them
       }
-      if (i < n) S.m[i] = B[qq].m;
+      if (i < n) {
+        S.m[i] = B[qq].m;
+        S.mf[i] = __double2float_rn(B[qq].m);
+      }
     }
-    publish(S, n, lane, B);
+    publish<MODE>(S, n, lane, B);
     double t = 0.0, t_pred = -1.0;
-    double dt = EXACT ? MUL(eta, __dsqrt_rn(forces<EXACT>(S, n, lane, B)))
-                      : eta * sqrt(forces<EXACT>(S, n, lane, B));
+    double dt = EXACT ? MUL(eta, __dsqrt_rn(forces<MODE>(S, n, lane, B)))
+                      : eta * sqrt(forces<MODE>(S, n, lane, B));
     long long nsteps = 0;
     int st = 0;
     while (t < t_end) {
@@ -247,8 +324,8 @@ __global__ void batch_kernel(int nsys, const int *__restrict__ order, const int 
       double new_dt = dt, end_dt = dt;
       for (int it = 0; it <= n_iter; it++) {
         const double prev = new_dt;
-        publish(S, n, lane, B);
-        const double ts2 = forces<EXACT>(S, n, lane, B);
+        publish<MODE>(S, n, lane, B);
+        const double ts2 = forces<MODE>(S, n, lane, B);
         end_dt = EXACT ? MUL(eta, __dsqrt_rn(ts2)) : eta * sqrt(ts2);
         if (it < n_iter) {
           if (EXACT) {
@@ -371,14 +448,18 @@ extern "C" int g6k_batch_launch(int nsys, const int *order, const int *off, cons
                                 int ctas, int *queue, double *t_out, long long *steps_out,
                                 unsigned long long *wall_ns, int *status, cudaStream_t st) {
   if (warps_per_cta < 1 || warps_per_cta > WARPS_MAX || ctas < 1) return -2;
+  if (exact < MODE_FAST || exact > MODE_SPLIT) return -2;
   queue_reset<<<1, 1, 0, st>>>(queue);
-  if (exact)
-    batch_kernel<true><<<ctas, 32 * warps_per_cta, 0, st>>>(nsys, order, off, t_end, mass, pos,
-                                                           vel, eta, n_iter, max_steps, queue,
-                                                           t_out, steps_out, wall_ns, status);
+#define G6_BATCH(M)                                                                           \
+  batch_kernel<M><<<ctas, 32 * warps_per_cta, 0, st>>>(nsys, order, off, t_end, mass, pos, vel, \
+                                                       eta, n_iter, max_steps, queue, t_out,    \
+                                                       steps_out, wall_ns, status)
+  if (exact == MODE_EXACT)
+    G6_BATCH(MODE_EXACT);
+  else if (exact == MODE_SPLIT)
+    G6_BATCH(MODE_SPLIT);
   else
-    batch_kernel<false><<<ctas, 32 * warps_per_cta, 0, st>>>(nsys, order, off, t_end, mass, pos,
-                                                            vel, eta, n_iter, max_steps, queue,
-                                                            t_out, steps_out, wall_ns, status);
+    G6_BATCH(MODE_FAST);
+#undef G6_BATCH
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }

@@ -201,12 +201,18 @@ int g6x_stats(double out[8]);
    smallN's time-symmetrised shared-step Hermite scheme and Kepler step
    criterion (src/amuse_ph4/src/smallN.cc:85-116,318-363,487-682) without
    the unperturbed-binary tree, in one persistent kernel fed by a device work
-   queue (largest systems first) and replayed from a CUDA graph.  exact != 0
-   reproduces smallN's floating-point operations bit for bit; exact = 0 uses
-   one reciprocal square root per pair.  pos/vel are overwritten; optional
+   queue (largest systems first) and replayed from a CUDA graph.  mode
+   (argument `exact`): G6_BATCH_EXACT reproduces smallN's floating-point
+   operations bit for bit; G6_BATCH_FAST uses one FP64 reciprocal square
+   root per pair; G6_BATCH_SPLIT keeps state, predictor and corrector in
+   FP64 and evaluates the pair terms in FP32 from double-single positions
+   (relative force error ~1e-7).  pos/vel are overwritten; optional
    outputs: t_final[s], steps[s], wall_ms[s] (GPU time from the first to the
    last step of system s), status[s] (0 done, 1 step budget max_steps
    exhausted), *elapsed_ms (whole launch). */
+#define G6_BATCH_FAST 0
+#define G6_BATCH_EXACT 1
+#define G6_BATCH_SPLIT 2
 int g6x_batch_run(int nsys, const int *n_per_sys, const double *t_end, const double *mass,
                   double (*pos)[3], double (*vel)[3], double eta, int n_iter,
                   long long max_steps, int exact, double *t_final, long long *steps,

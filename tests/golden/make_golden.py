@@ -5,9 +5,10 @@ Runs in the development container only (it needs the reference checkout):
     imported from the reference tree, give the inputs;
   * the unmodified ph4 CPU objects, compiled by ``make -C oracle ref`` into
     oracle/_ref/libph4ref.so, give the outputs (force: idata.cc:147-237,
-    corrector: idata.cc:399-514, full block-step run: interface.cc:317-711).
+    corrector: idata.cc:399-514, full block-step run: interface.cc:317-711,
+    smallN few-body runs: smallN.cc:906-1117 with dt_crit = 0).
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+Usage:  python tests/golden/make_golden.py [--ref /root/reference] [--only smalln]
 """
 import argparse
 import os
@@ -46,10 +47,13 @@ def save(name, **arrays):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None, choices=[None, "smalln"])
     args = ap.parse_args()
     sys.path.insert(0, os.path.join(args.ref, "src"))
     import oracle
     oracle.build_ref(args.ref)
+    if args.only == "smalln":
+        return smalln_fixtures(oracle)
 
     # 1. IC generators (pins amuse_gb300/ic.py).
     np.random.seed(1)
@@ -125,6 +129,23 @@ def main():
     r = oracle.run(m, x, v, 1e-6, 0.01, 0.125, lib="ref")
     save("run_plummer256_eps1e-6.npz", mass=m, pos0=x, vel0=v, eps2=1e-6, eta=0.01,
          t_end=0.125, **{k: np.asarray(r[k]) for k in r})
+
+
+def smalln_fixtures(oracle):
+    """7. smallN on few-body systems like the batching configuration's
+    (equal-mass Plummer, virial radius 1e-3, eps = 0, eta = 0.14) to two
+    crossing times, through the unmodified smallN objects."""
+    from amuse_gb300 import ic
+    out = {}
+    tcr = 2 * np.sqrt(2) * 1e-3 ** 1.5
+    for k, (n, seed) in enumerate([(3, 11), (4, 12), (9, 13), (24, 14), (64, 15)]):
+        rng = np.random.RandomState(seed)
+        m, x, v = ic.plummer(n, do_scale=True, rng=rng)
+        x, v = x * 1e-3, v / np.sqrt(1e-3)
+        p, vv, t, _ = oracle.smalln(m, x, v, 0.14, 2 * tcr, lib="ref")
+        out.update({f"s{k}_mass": m, f"s{k}_pos0": x, f"s{k}_vel0": v, f"s{k}_pos": p,
+                    f"s{k}_vel": vv, f"s{k}_t": t})
+    save("smalln_systems.npz", nsys=len(out) // 6, eta=0.14, t_end=2 * tcr, **out)
 
 
 if __name__ == "__main__":

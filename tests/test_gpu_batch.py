@@ -32,6 +32,21 @@ def test_exact_mode_is_bit_identical_to_smalln(g6):
         assert np.array_equal(r["vel"][a:b], pv), s
 
 
+def test_exact_mode_matches_reference_smalln_fixtures(g6):
+    """Against smallN built from the reference sources (tests/golden/
+    smalln_systems.npz): n = 3 ... 64, two crossing times, bit for bit."""
+    from conftest import golden
+    g = golden("smalln_systems.npz")
+    k = int(g["nsys"])
+    ns = np.array([len(g[f"s{i}_mass"]) for i in range(k)], np.int32)
+    cat = lambda key: np.concatenate([g[f"s{i}_{key}"] for i in range(k)])
+    t_end = np.full(k, float(g["t_end"]))
+    r = g6.batch_run(ns, t_end, cat("mass"), cat("pos0"), cat("vel0"), eta=float(g["eta"]),
+                     exact=True)
+    assert np.array_equal(r["pos"], cat("pos")) and np.array_equal(r["vel"], cat("vel"))
+    assert np.array_equal(r["t_final"], np.array([float(g[f"s{i}_t"]) for i in range(k)]))
+
+
 def _energy(m, x, v):
     k = 0.5 * np.sum(m * np.sum(v * v, 1))
     d = x[:, None, :] - x[None, :, :]
@@ -58,6 +73,33 @@ def test_fast_mode_conserves_energy_like_exact(g6):
     # the scheme's own truncation error dominates: both modes agree on it
     assert np.median(de_f) < 2 * np.median(de_e) + 1e-12
     assert max(de_f) < 3 * max(de_e) + 1e-12
+
+
+def test_split_mode_energy_and_short_time_agreement(g6):
+    """Split mode (FP32 pair terms from double-single positions): over two
+    crossing times its energy error stays at the scheme's truncation level
+    (within 10x of exact mode, or 1e-7), and over a short time, before the
+    systems' chaos amplifies rounding, it tracks the exact mode closely."""
+    ns, m, x, v, tcr = _systems(64, 3, 64, seed=6)
+    t_end = np.full(len(ns), 2.0 * tcr)
+    split = g6.batch_run(ns, t_end, m, x, v, mode="split")
+    exact = g6.batch_run(ns, t_end, m, x, v, mode="exact")
+    off = np.concatenate([[0], np.cumsum(ns)])
+    de_s, de_e = [], []
+    for s in range(len(ns)):
+        a, b = off[s], off[s + 1]
+        e0 = _energy(m[a:b], x[a:b], v[a:b])
+        de_s.append(abs((_energy(m[a:b], split["pos"][a:b], split["vel"][a:b]) - e0) / e0))
+        de_e.append(abs((_energy(m[a:b], exact["pos"][a:b], exact["vel"][a:b]) - e0) / e0))
+    print(f"median |dE/E| split {np.median(de_s):.2e} exact {np.median(de_e):.2e}; "
+          f"max split {max(de_s):.2e} exact {max(de_e):.2e}")
+    assert np.all(split["status"] == 0) and np.all(split["t_final"] >= t_end)
+    assert np.median(de_s) < 10 * np.median(de_e) + 1e-7
+    short = np.full(len(ns), 0.02 * tcr)
+    rs = g6.batch_run(ns, short, m, x, v, mode="split")
+    re = g6.batch_run(ns, short, m, x, v, mode="exact")
+    scale = np.abs(re["pos"]).max()
+    assert np.abs(rs["pos"] - re["pos"]).max() <= 1e-5 * scale
 
 
 def test_step_budget_and_queue(g6):

@@ -50,7 +50,7 @@ EXT_SYMBOLS = [
     "g6x_energy", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
     "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
     "g6x_set_fixed_jerk", "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp",
-    "g6x_fixed_step_adjoint",
+    "g6x_fixed_step_adjoint", "g6x_fixed_run", "g6x_fixed_adjoint_run",
 ]
 
 _lib = None
@@ -120,6 +120,8 @@ def load():
     lib.g6x_fixed_step.argtypes = [I, D, D] + [_vp] * 7
     lib.g6x_force_vjp.argtypes = [I, D] + [_vp] * 8
     lib.g6x_fixed_step_adjoint.argtypes = [I, D, D] + [_vp] * 9
+    lib.g6x_fixed_run.argtypes = [I, D, D, I] + [_vp] * 7
+    lib.g6x_fixed_adjoint_run.argtypes = [I, D, D, I] + [_vp] * 9
     _lib = lib
     return lib
 
@@ -316,6 +318,17 @@ class G6X(G6):
                            d_work):
         _check(self.lib.g6x_fixed_step_adjoint(n, h, eps2, d_xp, d_vp, d_m, d_lx, d_lv, d_la,
                                                d_lj, d_lm, d_work), "g6x_fixed_step_adjoint")
+
+    def fixed_run(self, n, h, eps2, nsteps, d_x, d_v, d_a, d_j, d_m, d_xp_all=None,
+                  d_vp_all=None):
+        _check(self.lib.g6x_fixed_run(n, h, eps2, nsteps, d_x, d_v, d_a, d_j, d_m, d_xp_all,
+                                      d_vp_all), "g6x_fixed_run")
+
+    def fixed_adjoint_run(self, n, h, eps2, nsteps, d_xp_all, d_vp_all, d_m, d_lx, d_lv, d_la,
+                          d_lj, d_lm, d_work):
+        _check(self.lib.g6x_fixed_adjoint_run(n, h, eps2, nsteps, d_xp_all, d_vp_all, d_m, d_lx,
+                                              d_lv, d_la, d_lj, d_lm, d_work),
+               "g6x_fixed_adjoint_run")
 
     def run_init(self, eps2, eta):
         _check(self.lib.g6x_run_init(eps2, eta), "g6x_run_init")

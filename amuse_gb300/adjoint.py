@@ -65,9 +65,14 @@ class _Run:
         self.g6.fixed_force(self.n, self.eps2, _p(x), _p(v), _p(m), _p(a), _p(j))
         return a, j
 
-    def step(self, x, v, a, j, m, xp, vp):
-        self.g6.fixed_step(self.n, self.dt, self.eps2, _p(x), _p(v), _p(a), _p(j), _p(m),
-                           _p(xp), _p(vp))
+    def run(self, x, v, a, j, m, nsteps, xps=None, vps=None):
+        """nsteps steps in place; xps/vps ([nsteps, n, 3]) keep the predicted states."""
+        self.g6.fixed_run(self.n, self.dt, self.eps2, nsteps, _p(x), _p(v), _p(a), _p(j), _p(m),
+                          None if xps is None else _p(xps), None if vps is None else _p(vps))
+
+    def adjoint_run(self, xps, vps, m, lx, lv, la, lj, lm, work):
+        self.g6.fixed_adjoint_run(self.n, self.dt, self.eps2, xps.shape[0], _p(xps), _p(vps),
+                                  _p(m), _p(lx), _p(lv), _p(la), _p(lj), _p(lm), _p(work))
 
 
 def _check_inputs(x0, v0, m):
@@ -93,12 +98,10 @@ class HermiteFixedFunction(torch.autograd.Function):
         with torch.cuda.stream(stream), _Run(g6, n, eps2, dt, precision, jerk) as r:
             x, v, mm = x0.detach().clone(), v0.detach().clone(), m.detach().contiguous()
             a, j = r.force(x, v, mm)
-            xp, vp = torch.empty_like(x), torch.empty_like(x)
             ckpt = []
-            for s in range(nsteps):
-                if s % checkpoint == 0:
-                    ckpt.append(torch.stack((x, v, a, j)))
-                r.step(x, v, a, j, mm, xp, vp)
+            for s0 in range(0, nsteps, checkpoint):
+                ckpt.append(torch.stack((x, v, a, j)))
+                r.run(x, v, a, j, mm, min(checkpoint, nsteps - s0))
         torch.cuda.current_stream(x0.device).wait_stream(stream)
         ctx.save_for_backward(x0, v0, mm, *ckpt)
         ctx.cfg = (eps2, dt, nsteps, checkpoint, precision, jerk, device)
@@ -124,11 +127,8 @@ class HermiteFixedFunction(torch.autograd.Function):
                 x, v, a, j = (t.clone() for t in ckpt[c])
                 xps = torch.empty((k, n, 3), dtype=torch.float64, device=x0.device)
                 vps = torch.empty_like(xps)
-                for s in range(k):
-                    r.step(x, v, a, j, m, xps[s], vps[s])
-                for s in range(k - 1, -1, -1):
-                    g6.fixed_step_adjoint(n, float(dt), float(eps2), _p(xps[s]), _p(vps[s]), _p(m),
-                                          _p(lx), _p(lv), _p(la), _p(lj), _p(lm), _p(work))
+                r.run(x, v, a, j, m, k, xps, vps)
+                r.adjoint_run(xps, vps, m, lx, lv, la, lj, lm, work)
             # initial forces (a0, j0) = F(x0, v0, m)
             gx0, gv0 = torch.empty_like(x0), torch.empty_like(x0)
             gm0 = torch.empty_like(m)

@@ -127,6 +127,7 @@ typedef struct {
   double run_t, run_eps2, run_eta;
   int *d_ilist, *d_ni;
   double *d_tnext, *d_sched, *d_esum, *d_racc, *d_rjerk, *d_rpot;
+  void *d_mail, *h_mail; /* 16 B {tnext, ni}: device copy and pinned host copy */
   int *d_rnn;
   int run_cap;
   /* statistics */
@@ -445,7 +446,8 @@ int g6_close_(int *id) {
   if (G.h_in) cudaFreeHost(G.h_in);
   if (G.h_out) cudaFreeHost(G.h_out);
   cudaFree(G.d_upd); cudaFree(G.d_in); cudaFree(G.d_out); cudaFree(G.d_scratch);
-  cudaFree(G.d_ilist); cudaFree(G.d_ni); cudaFree(G.d_tnext); cudaFree(G.d_sched);
+  cudaFree(G.d_ilist); cudaFree(G.d_mail); cudaFree(G.d_sched);
+  if (G.h_mail) cudaFreeHost(G.h_mail);
   cudaFree(G.d_esum); cudaFree(G.d_racc); cudaFree(G.d_rjerk); cudaFree(G.d_rpot);
   cudaFree(G.d_rnn);
   cudaEventDestroy(G.ev_done); cudaEventDestroy(G.ev_upd);
@@ -1088,15 +1090,18 @@ int g6x_force_slots(double ti, double eps2, int nj, int ni, const int *d_ilist, 
 
 static int ensure_run_buffers(int n) {
   if (n <= G.run_cap) return 0;
-  cudaFree(G.d_ilist); cudaFree(G.d_ni); cudaFree(G.d_tnext); cudaFree(G.d_sched);
+  cudaFree(G.d_ilist); cudaFree(G.d_mail); cudaFree(G.d_sched);
   cudaFree(G.d_esum); cudaFree(G.d_racc); cudaFree(G.d_rjerk); cudaFree(G.d_rpot);
   cudaFree(G.d_rnn);
+  G.d_mail = NULL;
+  G.d_ni = NULL;
+  G.d_tnext = NULL;
   G.run_cap = 0;
   ilist_identity_n = 0;
   size_t nd = sizeof(double) * (size_t)n;
   int ok = cudaMalloc((void **)&G.d_ilist, sizeof(int) * (size_t)n) == cudaSuccess &&
-           cudaMalloc((void **)&G.d_ni, sizeof(int) * 2) == cudaSuccess &&
-           cudaMalloc((void **)&G.d_tnext, sizeof(double) * 2) == cudaSuccess &&
+           cudaMalloc(&G.d_mail, 16) == cudaSuccess &&
+           (G.h_mail || cudaHostAlloc(&G.h_mail, 16, cudaHostAllocDefault) == cudaSuccess) &&
            cudaMalloc((void **)&G.d_sched, sizeof(double) * 4) == cudaSuccess &&
            cudaMalloc((void **)&G.d_esum, sizeof(double) * (size_t)(4 + 2 * (n / 256 + 2))) ==
                cudaSuccess &&
@@ -1108,6 +1113,8 @@ static int ensure_run_buffers(int n) {
     seterr("cannot allocate run buffers");
     return G6_ERR_NOMEM;
   }
+  G.d_tnext = (double *)G.d_mail;
+  G.d_ni = (int *)((char *)G.d_mail + 8);
   G.run_cap = n;
   return 0;
 }
@@ -1174,9 +1181,11 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
     ilist_identity_n = 0;
     if (g6k_schedule(&G.js, n, G.d_ilist, G.d_ni, G.d_tnext, G.d_sched, 4, G.st))
       return G6_ERR_CUDA;
-    CK(cudaMemcpyAsync(hbuf, G.d_ni, sizeof(int), cudaMemcpyDeviceToHost, G.st));
-    CK(cudaMemcpyAsync(&tn, G.d_tnext, sizeof(double), cudaMemcpyDeviceToHost, G.st));
+    /* one 16-byte copy into pinned memory: the only host round trip per block */
+    CK(cudaMemcpyAsync(G.h_mail, G.d_mail, 16, cudaMemcpyDeviceToHost, G.st));
     CK(cudaStreamSynchronize(G.st));
+    memcpy(&tn, G.h_mail, sizeof(double));
+    memcpy(hbuf, (const char *)G.h_mail + 8, sizeof(int));
     const int ni = hbuf[0];
     if (ni <= 0 || ni > n || !(tn > G.run_t)) {
       seterr("scheduler produced ni=%d tnext=%.17g at t=%.17g", ni, tn, G.run_t);
@@ -1612,9 +1621,11 @@ int g6k_fixed_adj_post(int n, double h, double *lx, double *lv, double *la, doub
 size_t g6k_vjp_scratch_bytes(int n);
 int g6k_force_vjp(int n, double eps2, int prec, int hjerk, const double *x, const double *v,
                   const double *m, const double *la1, const double *lj1, double *gx, double *gv,
-                  double *gm, double *part, cudaStream_t st);
+                  double *gm, void *scratch, cudaStream_t st);
 
-static double *fx_a1, *fx_j1, *fx_part;
+static double *fx_a1, *fx_j1, *fx_xp, *fx_vp;
+static void *fx_part;
+static size_t fx_part_bytes;
 static int fx_cap;
 static int fx_form = G6_JERK_HERMITE;
 
@@ -1624,28 +1635,37 @@ int g6x_set_fixed_jerk(int form) {
   return 0;
 }
 
+/* a1/j1 hold n bodies; the VJP scratch is sized for this n's launch shape
+   (its split count depends on n, so a smaller n can need more). */
 static int fixed_buffers(int n) {
-  if (n <= fx_cap && fx_part) return 0;
-  cudaFree(fx_a1); cudaFree(fx_j1); cudaFree(fx_part);
-  fx_a1 = fx_j1 = fx_part = NULL;
+  const size_t need = g6k_vjp_scratch_bytes(n);
+  if (n <= fx_cap && fx_part && need <= fx_part_bytes) return 0;
+  const int cap = n > fx_cap ? n : fx_cap;
+  const size_t bytes = need > fx_part_bytes ? need : fx_part_bytes;
+  cudaFree(fx_a1); cudaFree(fx_j1); cudaFree(fx_xp); cudaFree(fx_vp); cudaFree(fx_part);
+  fx_a1 = fx_j1 = fx_xp = fx_vp = NULL;
+  fx_part = NULL;
   fx_cap = 0;
-  if (cudaMalloc((void **)&fx_a1, sizeof(double) * 3 * (size_t)n) != cudaSuccess ||
-      cudaMalloc((void **)&fx_j1, sizeof(double) * 3 * (size_t)n) != cudaSuccess ||
-      cudaMalloc((void **)&fx_part, g6k_vjp_scratch_bytes(n)) != cudaSuccess) {
+  fx_part_bytes = 0;
+  if (cudaMalloc((void **)&fx_a1, sizeof(double) * 3 * (size_t)cap) != cudaSuccess ||
+      cudaMalloc((void **)&fx_j1, sizeof(double) * 3 * (size_t)cap) != cudaSuccess ||
+      cudaMalloc((void **)&fx_xp, sizeof(double) * 3 * (size_t)cap) != cudaSuccess ||
+      cudaMalloc((void **)&fx_vp, sizeof(double) * 3 * (size_t)cap) != cudaSuccess ||
+      cudaMalloc(&fx_part, bytes) != cudaSuccess) {
     seterr("cannot allocate fixed-step buffers for n=%d", n);
     return G6_ERR_NOMEM;
   }
-  fx_cap = n;
+  fx_cap = cap;
+  fx_part_bytes = bytes;
   return 0;
 }
 
-/* acc/jerk of all n bodies at (x, v) (split or FP64 per g6x_set_precision). */
-int g6x_fixed_force(int n, double eps2, const double *d_x, const double *d_v, const double *d_m,
-                    double *d_a, double *d_j) {
-  int rc = check_open();
-  if (rc) return rc;
-  if (n <= 0) return G6_ERR_ARG;
-  rc = grow_j((n + G6_TILE - 1) / G6_TILE * G6_TILE);
+/* The fixed-step calls enqueue on the library stream; the public entry
+   points below synchronise once at their end and then check the force
+   kernel's error word. */
+static int fixed_force_async(int n, double eps2, const double *d_x, const double *d_v,
+                             const double *d_m, double *d_a, double *d_j) {
+  int rc = grow_j((n + G6_TILE - 1) / G6_TILE * G6_TILE);
   if (rc) return rc;
   rc = ensure_run_buffers(n);
   if (rc) return rc;
@@ -1664,14 +1684,49 @@ int g6x_fixed_force(int n, double eps2, const double *d_x, const double *d_v, co
   a.jerk = d_j;
   a.pot = G.d_rpot;
   a.hjerk = fx_form == G6_JERK_HERMITE;
-  rc = run_force(&a);
+  return run_force(&a);
+}
+
+static int fixed_step_async(int n, double h, double eps2, double *d_x, double *d_v, double *d_a,
+                            double *d_j, const double *d_m, double *d_xp, double *d_vp) {
+  if (g6k_fixed_predict(n, h, d_x, d_v, d_a, d_j, d_xp, d_vp, G.st)) return G6_ERR_CUDA;
+  int rc = fixed_force_async(n, eps2, d_xp, d_vp, d_m, fx_a1, fx_j1);
   if (rc) return rc;
+  if (g6k_fixed_correct(n, h, d_x, d_v, d_a, d_j, fx_a1, fx_j1, G.st)) return G6_ERR_CUDA;
+  return 0;
+}
+
+static int fixed_step_adjoint_async(int n, double h, double eps2, const double *d_xp,
+                                    const double *d_vp, const double *d_m, double *d_lx,
+                                    double *d_lv, double *d_la, double *d_lj, double *d_lm,
+                                    double *d_work) {
+  double *gxp = d_work, *gvp = d_work + 3 * (size_t)n, *gm = d_work + 6 * (size_t)n;
+  if (g6k_fixed_adj_pre(n, h, d_lx, d_lv, d_la, d_lj, fx_a1, fx_j1, G.st)) return G6_ERR_CUDA;
+  if (g6k_force_vjp(n, eps2, G.prec, fx_form == G6_JERK_HERMITE, d_xp, d_vp, d_m, fx_a1, fx_j1,
+                    gxp, gvp, gm, fx_part, G.st))
+    return G6_ERR_CUDA;
+  if (g6k_fixed_adj_post(n, h, d_lx, d_lv, d_la, d_lj, gxp, gvp, d_lm, gm, G.st))
+    return G6_ERR_CUDA;
+  return 0;
+}
+
+static int fixed_finish(void) {
   CK(cudaStreamSynchronize(G.st));
   return read_err_word();
 }
 
-/* One fixed step in place on (x, v, a, j); xp/vp (or NULL) receive the
- * predicted positions and velocities the force was evaluated at. */
+/* acc/jerk of all n bodies at (x, v) (split or FP64 per g6x_set_precision). */
+int g6x_fixed_force(int n, double eps2, const double *d_x, const double *d_v, const double *d_m,
+                    double *d_a, double *d_j) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (n <= 0) return G6_ERR_ARG;
+  rc = fixed_force_async(n, eps2, d_x, d_v, d_m, d_a, d_j);
+  return rc ? rc : fixed_finish();
+}
+
+/* One fixed step in place on (x, v, a, j); xp/vp receive the predicted
+ * positions and velocities the force was evaluated at. */
 int g6x_fixed_step(int n, double h, double eps2, double *d_x, double *d_v, double *d_a,
                    double *d_j, const double *d_m, double *d_xp, double *d_vp) {
   int rc = check_open();
@@ -1679,12 +1734,28 @@ int g6x_fixed_step(int n, double h, double eps2, double *d_x, double *d_v, doubl
   if (n <= 0 || !d_xp || !d_vp) return G6_ERR_ARG;
   rc = fixed_buffers(n);
   if (rc) return rc;
-  if (g6k_fixed_predict(n, h, d_x, d_v, d_a, d_j, d_xp, d_vp, G.st)) return G6_ERR_CUDA;
-  rc = g6x_fixed_force(n, eps2, d_xp, d_vp, d_m, fx_a1, fx_j1);
+  rc = fixed_step_async(n, h, eps2, d_x, d_v, d_a, d_j, d_m, d_xp, d_vp);
+  return rc ? rc : fixed_finish();
+}
+
+/* nsteps fixed steps in place, one host synchronisation at the end.  If
+ * d_xp_all/d_vp_all are not NULL they receive the predicted states of every
+ * step ([nsteps][n][3] each); otherwise library scratch is used. */
+int g6x_fixed_run(int n, double h, double eps2, int nsteps, double *d_x, double *d_v,
+                  double *d_a, double *d_j, const double *d_m, double *d_xp_all,
+                  double *d_vp_all) {
+  int rc = check_open();
   if (rc) return rc;
-  if (g6k_fixed_correct(n, h, d_x, d_v, d_a, d_j, fx_a1, fx_j1, G.st)) return G6_ERR_CUDA;
-  CK(cudaStreamSynchronize(G.st));
-  return 0;
+  if (n <= 0 || nsteps < 0 || (!d_xp_all) != (!d_vp_all)) return G6_ERR_ARG;
+  rc = fixed_buffers(n);
+  if (rc) return rc;
+  for (int s = 0; s < nsteps; s++) {
+    const size_t o = d_xp_all ? 3 * (size_t)n * (size_t)s : 0;
+    rc = fixed_step_async(n, h, eps2, d_x, d_v, d_a, d_j, d_m, d_xp_all ? d_xp_all + o : fx_xp,
+                          d_vp_all ? d_vp_all + o : fx_vp);
+    if (rc) return rc;
+  }
+  return fixed_finish();
 }
 
 /* Vector-Jacobian product of the force at (x, v): given cotangents la/lj of
@@ -1700,8 +1771,7 @@ int g6x_force_vjp(int n, double eps2, const double *d_x, const double *d_v, cons
   if (g6k_force_vjp(n, eps2, G.prec, fx_form == G6_JERK_HERMITE, d_x, d_v, d_m, d_la, d_lj, d_gx,
                     d_gv, d_gm, fx_part, G.st))
     return G6_ERR_CUDA;
-  CK(cudaStreamSynchronize(G.st));
-  return 0;
+  return fixed_finish();
 }
 
 /* Adjoint of one fixed step (in place on lx, lv, la, lj; gm accumulates
@@ -1714,13 +1784,27 @@ int g6x_fixed_step_adjoint(int n, double h, double eps2, const double *d_xp, con
   if (n <= 0 || !d_work) return G6_ERR_ARG;
   rc = fixed_buffers(n);
   if (rc) return rc;
-  double *gxp = d_work, *gvp = d_work + 3 * (size_t)n, *gm = d_work + 6 * (size_t)n;
-  if (g6k_fixed_adj_pre(n, h, d_lx, d_lv, d_la, d_lj, fx_a1, fx_j1, G.st)) return G6_ERR_CUDA;
-  if (g6k_force_vjp(n, eps2, G.prec, fx_form == G6_JERK_HERMITE, d_xp, d_vp, d_m, fx_a1, fx_j1,
-                    gxp, gvp, gm, fx_part, G.st))
-    return G6_ERR_CUDA;
-  if (g6k_fixed_adj_post(n, h, d_lx, d_lv, d_la, d_lj, gxp, gvp, d_lm, gm, G.st))
-    return G6_ERR_CUDA;
-  CK(cudaStreamSynchronize(G.st));
-  return 0;
+  rc = fixed_step_adjoint_async(n, h, eps2, d_xp, d_vp, d_m, d_lx, d_lv, d_la, d_lj, d_lm,
+                                d_work);
+  return rc ? rc : fixed_finish();
+}
+
+/* The adjoints of nsteps consecutive steps, last step first, at the
+ * predicted states d_xp_all/d_vp_all ([nsteps][n][3], as g6x_fixed_run
+ * wrote them); one host synchronisation at the end. */
+int g6x_fixed_adjoint_run(int n, double h, double eps2, int nsteps, const double *d_xp_all,
+                          const double *d_vp_all, const double *d_m, double *d_lx, double *d_lv,
+                          double *d_la, double *d_lj, double *d_lm, double *d_work) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (n <= 0 || nsteps < 0 || !d_work || !d_xp_all || !d_vp_all) return G6_ERR_ARG;
+  rc = fixed_buffers(n);
+  if (rc) return rc;
+  for (int s = nsteps - 1; s >= 0; s--) {
+    const size_t o = 3 * (size_t)n * (size_t)s;
+    rc = fixed_step_adjoint_async(n, h, eps2, d_xp_all + o, d_vp_all + o, d_m, d_lx, d_lv, d_la,
+                                  d_lj, d_lm, d_work);
+    if (rc) return rc;
+  }
+  return fixed_finish();
 }

@@ -134,11 +134,12 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
   return y;
 }
 
-// MODE_SPLIT pair term: contribution of j to body i (FP32), and the pair's
-// Kepler step^2 (FP32; FP64 below d^2 = 1e-24, where d^3 would leave the
-// FP32 normal range).
+// MODE_SPLIT pair term: contribution of j to body i, and the pair's Kepler
+// step^2.  FP32 unless the pair is closer than 1e-9 (d^2 < 1e-18): there
+// m / d^3 times a relative velocity ~ sqrt(M / d) can leave the FP32 range,
+// so such (rare) pairs are evaluated in FP64 into separate accumulators.
 __device__ __forceinline__ float pair_split(const WarpSmem &S, int i, int j, float acc[3],
-                                            float jerk[3]) {
+                                            float jerk[3], double accd[3], double jerkd[3]) {
   float dx[3], dv[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
@@ -146,21 +147,39 @@ __device__ __forceinline__ float pair_split(const WarpSmem &S, int i, int j, flo
     dv[k] = S.f.vf[j][k] - S.f.vf[i][k];
   }
   const float d2 = fmaf(dx[2], dx[2], fmaf(dx[1], dx[1], dx[0] * dx[0]));
-  const float rinv = rsqrt_approx(d2);
-  const float rinv2 = rinv * rinv;
-  const float f = S.mf[j] * rinv * rinv2;
-  const float xv = fmaf(dx[2], dv[2], fmaf(dx[1], dv[1], dx[0] * dv[0]));
-  const float a3 = -3.0f * xv * rinv2;
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    acc[k] = fmaf(f, dx[k], acc[k]);
-    jerk[k] = fmaf(f, fmaf(a3, dx[k], dv[k]), jerk[k]);
-  }
   const float v2 = fmaf(dv[2], dv[2], fmaf(dv[1], dv[1], dv[0] * dv[0]));
   const float mt = S.mf[i] + S.mf[j];
-  if (d2 >= 1e-24f) return fminf(0.5f * d2 * (d2 * rinv) / mt, d2 / v2);
-  const double dd2 = (double)d2;
-  return (float)fmin(0.5 * dd2 * sqrt(dd2) / (double)mt, dd2 / (double)v2);
+  if (d2 >= 1e-18f) {
+    const float rinv = rsqrt_approx(d2);
+    const float rinv2 = rinv * rinv;
+    const float f = S.mf[j] * rinv * rinv2;
+    const float xv = fmaf(dx[2], dv[2], fmaf(dx[1], dv[1], dx[0] * dv[0]));
+    const float a3 = -3.0f * xv * rinv2;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      acc[k] = fmaf(f, dx[k], acc[k]);
+      jerk[k] = fmaf(f, fmaf(a3, dx[k], dv[k]), jerk[k]);
+    }
+    return fminf(0.5f * d2 * (d2 * rinv) / mt, d2 / v2);
+  }
+  double X[3], W[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    X[k] = (double)dx[k];
+    W[k] = (double)dv[k];
+  }
+  const double dd2 = X[0] * X[0] + X[1] * X[1] + X[2] * X[2];
+  const double d = sqrt(dd2);
+  const double rinv2 = 1.0 / dd2;
+  const double f = (double)S.mf[j] * rinv2 / d;
+  const double a3 = -3.0 * (X[0] * W[0] + X[1] * W[1] + X[2] * W[2]) * rinv2;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    accd[k] += f * X[k];
+    jerkd[k] += f * (a3 * X[k] + W[k]);
+  }
+  const double vv = W[0] * W[0] + W[1] * W[1] + W[2] * W[2];
+  return (float)fmin(0.5 * dd2 * d / (double)mt, dd2 / vv);
 }
 
 // acc/jerk of the lane's bodies from the predicted state in S; returns the
@@ -177,15 +196,16 @@ __device__ double forces(const WarpSmem &S, int n, int lane, Body B[2]) {
     if (i >= n) continue;
     if (MODE == MODE_SPLIT) {
       float a[3] = {0.f, 0.f, 0.f}, jk[3] = {0.f, 0.f, 0.f};
+      double ad[3] = {0.0, 0.0, 0.0}, jd[3] = {0.0, 0.0, 0.0};
       float m2 = __int_as_float(0x7f800000);
       for (int j = 0; j < n; j++) {
         if (j == i) continue;
-        m2 = fminf(m2, pair_split(S, i, j, a, jk));
+        m2 = fminf(m2, pair_split(S, i, j, a, jk, ad, jd));
       }
 #pragma unroll
       for (int k = 0; k < 3; k++) {
-        B[q].acc[k] = (double)a[k];
-        B[q].jerk[k] = (double)jk[k];
+        B[q].acc[k] = (double)a[k] + ad[k];
+        B[q].jerk[k] = (double)jk[k] + jd[k];
       }
       ts2 = fmin(ts2, (double)m2);
     } else if (EXACT) {

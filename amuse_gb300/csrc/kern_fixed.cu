@@ -140,180 +140,247 @@ __global__ void adj_post_kernel(int n, double h, double *lx, double *lv, double 
   lj[e] += gx * h * h * h / 6 + gv * h * h / 2;
 }
 
-// ---- force VJP ----
-struct VRec {  // one j in shared memory
-  float xh, yh, zh, xl, yl, zl, vx, vy, vz, m;
-  float la[3], lj[3];
-};
+// ---- force VJP, FP64 ----
 struct VRecD {
   double x[3], v[3], m, la[3], lj[3];
 };
 
-template <bool F64, bool HJ>
-__global__ void __launch_bounds__(VT) vjp_kernel(int n, double eps2, const double *__restrict__ x,
-                                                 const double *__restrict__ v,
-                                                 const double *__restrict__ m,
-                                                 const double *__restrict__ la1,
-                                                 const double *__restrict__ lj1, int jsplit,
-                                                 double *part /* [nsplit][n][7] */) {
-  __shared__ VRec ts[F64 ? 1 : VTILE];
-  __shared__ VRecD td[F64 ? VTILE : 1];
+// One body k per thread, j in shared-memory tiles of VTILE, the j range
+// split over gridDim.y CTA rows; m < 0 marks padding.
+template <bool HJ>
+__global__ void __launch_bounds__(VT) vjp_f64_kernel(int n, double eps2,
+                                                     const double *__restrict__ x,
+                                                     const double *__restrict__ v,
+                                                     const double *__restrict__ m,
+                                                     const double *__restrict__ la1,
+                                                     const double *__restrict__ lj1, int jsplit,
+                                                     double *part /* [nsplit][n][7] */) {
+  __shared__ VRecD td[VTILE];
   eps2 += 1.0 / 4503599627370496.0;  // the force kernel's softening (+2^-52, as ph4)
   const int k = blockIdx.x * VT + threadIdx.x;
   const bool valid = k < n;
   const int kk = valid ? k : 0;
   const int j0 = blockIdx.y * jsplit;
   const int j1 = min(n, j0 + jsplit);
-  // own data
   const double xk[3] = {x[3 * kk], x[3 * kk + 1], x[3 * kk + 2]};
   const double vk[3] = {v[3 * kk], v[3 * kk + 1], v[3 * kk + 2]};
   const double mk = m[kk];
   const double lak[3] = {la1[3 * kk], la1[3 * kk + 1], la1[3 * kk + 2]};
   const double ljk[3] = {lj1[3 * kk], lj1[3 * kk + 1], lj1[3 * kk + 2]};
-  float xkh[3], xkl[3];
-  for (int q = 0; q < 3; q++) {
-    xkh[q] = __double2float_rn(xk[q]);
-    xkl[q] = __double2float_rn(xk[q] - (double)xkh[q]);
-  }
   double tot[7] = {0, 0, 0, 0, 0, 0, 0};  // gx[3], gv[3], gm
   for (int t0 = j0; t0 < j1; t0 += VTILE) {
     __syncthreads();
     for (int q = threadIdx.x; q < VTILE; q += VT) {
       const int jj = t0 + q;
-      if (F64) {
-        VRecD &r = td[q];
-        if (jj < j1) {
-          for (int c = 0; c < 3; c++) {
-            r.x[c] = x[3 * jj + c];
-            r.v[c] = v[3 * jj + c];
-            r.la[c] = la1[3 * jj + c];
-            r.lj[c] = lj1[3 * jj + c];
-          }
-          r.m = m[jj];
-        } else {
-          for (int c = 0; c < 3; c++) r.x[c] = r.v[c] = r.la[c] = r.lj[c] = 0.0;
-          r.m = -1.0;  // marks padding
+      VRecD &r = td[q];
+      if (jj < j1) {
+        for (int c = 0; c < 3; c++) {
+          r.x[c] = x[3 * jj + c];
+          r.v[c] = v[3 * jj + c];
+          r.la[c] = la1[3 * jj + c];
+          r.lj[c] = lj1[3 * jj + c];
         }
+        r.m = m[jj];
       } else {
-        VRec &r = ts[q];
-        if (jj < j1) {
-          const double X[3] = {x[3 * jj], x[3 * jj + 1], x[3 * jj + 2]};
-          r.xh = __double2float_rn(X[0]);
-          r.yh = __double2float_rn(X[1]);
-          r.zh = __double2float_rn(X[2]);
-          r.xl = __double2float_rn(X[0] - (double)r.xh);
-          r.yl = __double2float_rn(X[1] - (double)r.yh);
-          r.zl = __double2float_rn(X[2] - (double)r.zh);
-          r.vx = __double2float_rn(v[3 * jj]);
-          r.vy = __double2float_rn(v[3 * jj + 1]);
-          r.vz = __double2float_rn(v[3 * jj + 2]);
-          r.m = __double2float_rn(m[jj]);
-          for (int c = 0; c < 3; c++) {
-            r.la[c] = __double2float_rn(la1[3 * jj + c]);
-            r.lj[c] = __double2float_rn(lj1[3 * jj + c]);
-          }
-        } else {
-          r.xh = r.yh = r.zh = 1.0e18f;
-          r.xl = r.yl = r.zl = r.vx = r.vy = r.vz = 0.f;
-          r.m = -1.0f;
-          for (int c = 0; c < 3; c++) r.la[c] = r.lj[c] = 0.f;
-        }
+        for (int c = 0; c < 3; c++) r.x[c] = r.v[c] = r.la[c] = r.lj[c] = 0.0;
+        r.m = -1.0;
       }
     }
     __syncthreads();
-    if (F64) {
-      double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-      for (int q = 0; q < VTILE; q++) {
-        const VRecD &r = td[q];
-        if (r.m < 0.0 || t0 + q == k) continue;
-        double R[3], V[3], lam[3], mu[3];
-        for (int c = 0; c < 3; c++) {
-          R[c] = r.x[c] - xk[c];
-          V[c] = r.v[c] - vk[c];
-          lam[c] = mk * r.la[c] - r.m * lak[c];
-          mu[c] = mk * r.lj[c] - r.m * ljk[c];
-        }
-        const double s = R[0] * R[0] + R[1] * R[1] + R[2] * R[2] + eps2;
-        const double si = 1.0 / s, s1 = sqrt(si);
-        const double s3 = s1 * si, s5 = s3 * si, s7 = s5 * si;
-        const double rl = R[0] * lam[0] + R[1] * lam[1] + R[2] * lam[2];
-        const double rm = R[0] * mu[0] + R[1] * mu[1] + R[2] * mu[2];
-        const double vm = V[0] * mu[0] + V[1] * mu[1] + V[2] * mu[2];
-        const double rv = R[0] * V[0] + R[1] * V[1] + R[2] * V[2];
-        // qs = q^-1 s^-3/2 (s^-5/2 in the softened form), c7 = 15 s^-7/2 resp.
-        // 3 (2 q^-2 s^-3/2 + 3 q^-1 s^-5/2)
-        double qs, c7;
-        if (HJ) {
-          const double qi = 1.0 / (R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
-          qs = qi * s3;
-          c7 = 3.0 * (2.0 * qi * qs + 3.0 * qi * s5);
-        } else {
-          qs = s5;
-          c7 = 15.0 * s7;
-        }
-        const double cr = -3.0 * (rl * s5 + vm * s5) + rv * rm * c7;
-        for (int c = 0; c < 3; c++) {
-          acc[c] += lam[c] * s3 + cr * R[c] - 3.0 * qs * (rm * V[c] + rv * mu[c]);
-          acc[3 + c] += mu[c] * s3 - 3.0 * rm * qs * R[c];
-        }
-        const double ga = (r.la[0] * R[0] + r.la[1] * R[1] + r.la[2] * R[2]) * s3;
-        const double lv = r.lj[0] * V[0] + r.lj[1] * V[1] + r.lj[2] * V[2];
-        const double lr = r.lj[0] * R[0] + r.lj[1] * R[1] + r.lj[2] * R[2];
-        acc[6] -= ga + lv * s3 - 3.0 * rv * lr * qs;
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int q = 0; q < VTILE; q++) {
+      const VRecD &r = td[q];
+      if (r.m < 0.0 || t0 + q == k) continue;
+      double R[3], V[3], lam[3], mu[3];
+      for (int c = 0; c < 3; c++) {
+        R[c] = r.x[c] - xk[c];
+        V[c] = r.v[c] - vk[c];
+        lam[c] = mk * r.la[c] - r.m * lak[c];
+        mu[c] = mk * r.lj[c] - r.m * ljk[c];
       }
-      for (int c = 0; c < 7; c++) tot[c] += acc[c];
-    } else {
-      float acc[7] = {0, 0, 0, 0, 0, 0, 0};
-      const float lamk[3] = {(float)lak[0], (float)lak[1], (float)lak[2]};
-      const float muk[3] = {(float)ljk[0], (float)ljk[1], (float)ljk[2]};
-      const float mkf = (float)mk;
-      const float vkf[3] = {(float)vk[0], (float)vk[1], (float)vk[2]};
-      const float e2 = (float)eps2;
-      for (int q = 0; q < VTILE; q++) {
-        const VRec &r = ts[q];
-        if (r.m < 0.f || t0 + q == k) continue;
-        const float R[3] = {__fadd_rn(__fsub_rn(r.xh, xkh[0]), __fsub_rn(r.xl, xkl[0])),
-                            __fadd_rn(__fsub_rn(r.yh, xkh[1]), __fsub_rn(r.yl, xkl[1])),
-                            __fadd_rn(__fsub_rn(r.zh, xkh[2]), __fsub_rn(r.zl, xkl[2]))};
-        const float V[3] = {r.vx - vkf[0], r.vy - vkf[1], r.vz - vkf[2]};
-        float lam[3], mu[3];
-        for (int c = 0; c < 3; c++) {
-          lam[c] = mkf * r.la[c] - r.m * lamk[c];
-          mu[c] = mkf * r.lj[c] - r.m * muk[c];
-        }
-        const float s = fmaf(R[0], R[0], fmaf(R[1], R[1], fmaf(R[2], R[2], e2)));
-        const float s1 = rsqrtf(s);
-        const float si = s1 * s1;
-        const float s3 = s1 * si, s5 = s3 * si, s7 = s5 * si;
-        const float rl = R[0] * lam[0] + R[1] * lam[1] + R[2] * lam[2];
-        const float rm = R[0] * mu[0] + R[1] * mu[1] + R[2] * mu[2];
-        const float vm = V[0] * mu[0] + V[1] * mu[1] + V[2] * mu[2];
-        const float rv = R[0] * V[0] + R[1] * V[1] + R[2] * V[2];
-        float qs, c7;
-        if (HJ) {
-          const float qi = __frcp_rn(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
-          qs = qi * s3;
-          c7 = 3.0f * (2.0f * qi * qs + 3.0f * qi * s5);
-        } else {
-          qs = s5;
-          c7 = 15.0f * s7;
-        }
-        const float cr = -3.0f * (rl * s5 + vm * s5) + rv * rm * c7;
-        for (int c = 0; c < 3; c++) {
-          acc[c] += lam[c] * s3 + cr * R[c] - 3.0f * qs * (rm * V[c] + rv * mu[c]);
-          acc[3 + c] += mu[c] * s3 - 3.0f * rm * qs * R[c];
-        }
-        const float ga = (r.la[0] * R[0] + r.la[1] * R[1] + r.la[2] * R[2]) * s3;
-        const float lv = r.lj[0] * V[0] + r.lj[1] * V[1] + r.lj[2] * V[2];
-        const float lr = r.lj[0] * R[0] + r.lj[1] * R[1] + r.lj[2] * R[2];
-        acc[6] -= ga + lv * s3 - 3.0f * rv * lr * qs;
+      const double s = R[0] * R[0] + R[1] * R[1] + R[2] * R[2] + eps2;
+      const double si = 1.0 / s, s1 = sqrt(si);
+      const double s3 = s1 * si, s5 = s3 * si, s7 = s5 * si;
+      const double rl = R[0] * lam[0] + R[1] * lam[1] + R[2] * lam[2];
+      const double rm = R[0] * mu[0] + R[1] * mu[1] + R[2] * mu[2];
+      const double vm = V[0] * mu[0] + V[1] * mu[1] + V[2] * mu[2];
+      const double rv = R[0] * V[0] + R[1] * V[1] + R[2] * V[2];
+      // qs = q^-1 s^-3/2 (s^-5/2 in the softened form), c7 = 15 s^-7/2 resp.
+      // 3 (2 q^-2 s^-3/2 + 3 q^-1 s^-5/2)
+      double qs, c7;
+      if (HJ) {
+        const double qi = 1.0 / (R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
+        qs = qi * s3;
+        c7 = 3.0 * (2.0 * qi * qs + 3.0 * qi * s5);
+      } else {
+        qs = s5;
+        c7 = 15.0 * s7;
       }
-      for (int c = 0; c < 7; c++) tot[c] += (double)acc[c];
+      const double cr = -3.0 * (rl * s5 + vm * s5) + rv * rm * c7;
+      for (int c = 0; c < 3; c++) {
+        acc[c] += lam[c] * s3 + cr * R[c] - 3.0 * qs * (rm * V[c] + rv * mu[c]);
+        acc[3 + c] += mu[c] * s3 - 3.0 * rm * qs * R[c];
+      }
+      const double ga = (r.la[0] * R[0] + r.la[1] * R[1] + r.la[2] * R[2]) * s3;
+      const double lv = r.lj[0] * V[0] + r.lj[1] * V[1] + r.lj[2] * V[2];
+      const double lr = r.lj[0] * R[0] + r.lj[1] * R[1] + r.lj[2] * R[2];
+      acc[6] -= ga + lv * s3 - 3.0 * rv * lr * qs;
     }
+    for (int c = 0; c < 7; c++) tot[c] += acc[c];
   }
   if (valid) {
     double *p = part + ((size_t)blockIdx.y * n + k) * 7;
     for (int c = 0; c < 7; c++) p[c] = tot[c];
+  }
+}
+
+// ---- split-precision force VJP, register-blocked ----
+// One 64 B record per body: {xh,yh,zh,m} {xl,yl,zl,vx} {vy,vz,la0,la1}
+// {la2,lj0,lj1,lj2}; padding records (zero mass and cotangents, far away)
+// contribute exactly zero.  Each thread owns VIPT bodies, so every j record
+// read from shared memory serves VIPT pairs.  The self pair also contributes
+// exactly zero: r = v = 0 and lam = m_k La_j - m_j La_k cancels bit for bit
+// (two rounded products, no contraction); with the hermite jerk form the
+// 1/r^2 factor is set to 0 there.
+struct __align__(16) VJRec {
+  float4 a, b, c, d;
+};
+constexpr int VIPT = 4;
+constexpr int VT2 = 128;
+
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__global__ void vjp_records_kernel(int n, int n_pad, const double *__restrict__ x,
+                                   const double *__restrict__ v, const double *__restrict__ m,
+                                   const double *__restrict__ la1, const double *__restrict__ lj1,
+                                   VJRec *rec) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_pad) return;
+  VJRec r;
+  if (s < n) {
+    float h[3], l[3];
+    for (int k = 0; k < 3; k++) {
+      h[k] = __double2float_rn(x[3 * s + k]);
+      l[k] = __double2float_rn(x[3 * s + k] - (double)h[k]);
+    }
+    r.a = make_float4(h[0], h[1], h[2], __double2float_rn(m[s]));
+    r.b = make_float4(l[0], l[1], l[2], __double2float_rn(v[3 * s]));
+    r.c = make_float4(__double2float_rn(v[3 * s + 1]), __double2float_rn(v[3 * s + 2]),
+                      __double2float_rn(la1[3 * s]), __double2float_rn(la1[3 * s + 1]));
+    r.d = make_float4(__double2float_rn(la1[3 * s + 2]), __double2float_rn(lj1[3 * s]),
+                      __double2float_rn(lj1[3 * s + 1]), __double2float_rn(lj1[3 * s + 2]));
+  } else {
+    r.a = make_float4(1.0e18f, 1.0e18f, 1.0e18f, 0.f);
+    r.b = make_float4(0.f, 0.f, 0.f, 0.f);
+    r.c = r.b;
+    r.d = r.b;
+  }
+  rec[s] = r;
+}
+
+template <bool HJ>
+__global__ void __launch_bounds__(VT2) vjp_split_kernel(int n, float eps2, const VJRec *__restrict__ rec,
+                                                        int jsplit, int n_pad,
+                                                        double *part /* [nsplit][n][7] */) {
+  __shared__ VJRec tile[VTILE];
+  float xh[VIPT][3], xl[VIPT][3], vk[VIPT][3], mk[VIPT], lak[VIPT][3], ljk[VIPT][3];
+  int kk[VIPT];
+#pragma unroll
+  for (int q = 0; q < VIPT; q++) {
+    kk[q] = blockIdx.x * (VT2 * VIPT) + q * VT2 + threadIdx.x;
+    const VJRec r = rec[kk[q] < n_pad ? kk[q] : 0];
+    xh[q][0] = r.a.x; xh[q][1] = r.a.y; xh[q][2] = r.a.z; mk[q] = r.a.w;
+    xl[q][0] = r.b.x; xl[q][1] = r.b.y; xl[q][2] = r.b.z;
+    vk[q][0] = r.b.w; vk[q][1] = r.c.x; vk[q][2] = r.c.y;
+    lak[q][0] = r.c.z; lak[q][1] = r.c.w; lak[q][2] = r.d.x;
+    ljk[q][0] = r.d.y; ljk[q][1] = r.d.z; ljk[q][2] = r.d.w;
+  }
+  double tot[VIPT][7];
+#pragma unroll
+  for (int q = 0; q < VIPT; q++)
+#pragma unroll
+    for (int c = 0; c < 7; c++) tot[q][c] = 0.0;
+  const int j0 = blockIdx.y * jsplit;
+  const int j1 = min(n_pad, j0 + jsplit);
+  for (int t0 = j0; t0 < j1; t0 += VTILE) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < VTILE; q += VT2) tile[q] = rec[t0 + q];
+    __syncthreads();
+    float g[VIPT][7];
+#pragma unroll
+    for (int q = 0; q < VIPT; q++)
+#pragma unroll
+      for (int c = 0; c < 7; c++) g[q][c] = 0.f;
+#pragma unroll 2
+    for (int jj = 0; jj < VTILE; jj++) {
+      const VJRec r = tile[jj];
+      const float laj[3] = {r.c.z, r.c.w, r.d.x}, ljj[3] = {r.d.y, r.d.z, r.d.w};
+      const float vj[3] = {r.b.w, r.c.x, r.c.y};
+      const float xhj[3] = {r.a.x, r.a.y, r.a.z}, xlj[3] = {r.b.x, r.b.y, r.b.z};
+#pragma unroll
+      for (int q = 0; q < VIPT; q++) {
+        float R[3], V[3], lam[3], mu[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          R[c] = __fadd_rn(__fsub_rn(xhj[c], xh[q][c]), __fsub_rn(xlj[c], xl[q][c]));
+          V[c] = vj[c] - vk[q][c];
+          lam[c] = __fsub_rn(__fmul_rn(mk[q], laj[c]), __fmul_rn(r.a.w, lak[q][c]));
+          mu[c] = __fsub_rn(__fmul_rn(mk[q], ljj[c]), __fmul_rn(r.a.w, ljk[q][c]));
+        }
+        const float s = fmaf(R[2], R[2], fmaf(R[1], R[1], fmaf(R[0], R[0], eps2)));
+        const float s1 = rsqrt_approx(s);
+        const float si = s1 * s1;
+        const float s3 = s1 * si, s5 = s3 * si;
+        const float rl = fmaf(R[2], lam[2], fmaf(R[1], lam[1], R[0] * lam[0]));
+        const float rm = fmaf(R[2], mu[2], fmaf(R[1], mu[1], R[0] * mu[0]));
+        const float vm = fmaf(V[2], mu[2], fmaf(V[1], mu[1], V[0] * mu[0]));
+        const float rv = fmaf(R[2], V[2], fmaf(R[1], V[1], R[0] * V[0]));
+        float qs, c7;
+        if (HJ) {
+          const float r2u = fmaf(R[2], R[2], fmaf(R[1], R[1], R[0] * R[0]));
+          const float qi = r2u > 0.f ? rcp_approx(r2u) : 0.f;
+          qs = qi * s3;
+          c7 = qi * fmaf(6.0f, qs, 9.0f * s5);
+        } else {
+          qs = s5;
+          c7 = 15.0f * (s5 * si);
+        }
+        const float q3 = -3.0f * qs;
+        const float cr = fmaf(rv * rm, c7, -3.0f * (rl + vm) * s5);
+        const float w = q3 * rm;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const float u = fmaf(rm, V[c], rv * mu[c]);
+          g[q][c] = fmaf(q3, u, fmaf(cr, R[c], fmaf(lam[c], s3, g[q][c])));
+          g[q][3 + c] = fmaf(w, R[c], fmaf(mu[c], s3, g[q][3 + c]));
+        }
+        const float ga = fmaf(laj[2], R[2], fmaf(laj[1], R[1], laj[0] * R[0]));
+        const float lv = fmaf(ljj[2], V[2], fmaf(ljj[1], V[1], ljj[0] * V[0]));
+        const float lr = fmaf(ljj[2], R[2], fmaf(ljj[1], R[1], ljj[0] * R[0]));
+        g[q][6] -= fmaf(ga + lv, s3, q3 * rv * lr);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < VIPT; q++)
+#pragma unroll
+      for (int c = 0; c < 7; c++) tot[q][c] += (double)g[q][c];
+  }
+#pragma unroll
+  for (int q = 0; q < VIPT; q++) {
+    if (kk[q] < n) {
+      double *p = part + ((size_t)blockIdx.y * n + kk[q]) * 7;
+#pragma unroll
+      for (int c = 0; c < 7; c++) p[c] = tot[q][c];
+    }
   }
 }
 
@@ -368,31 +435,69 @@ extern "C" int g6k_fixed_adj_post(int n, double h, double *lx, double *lv, doubl
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
-// part must hold nsplit * n * 7 doubles; nsplit = ceil(n / jsplit).
+// Launch shapes.  FP64: one body per thread, j split over 1/4/8 CTA rows.
+// Split: VIPT bodies per thread, j split so that there are >= 4 CTAs per SM.
+static void vjp_shape(int n, int prec, int *nsplit, int *jsplit, int *n_pad) {
+  *n_pad = (n + VTILE - 1) / VTILE * VTILE;
+  if (prec == G6_PREC_FP64) {
+    *nsplit = n >= 8192 ? 8 : (n >= 1024 ? 4 : 1);
+    *jsplit = (n + *nsplit - 1) / *nsplit;
+    return;
+  }
+  int sms = 0, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+    sms = 152;
+  const int gx = (n + VT2 * VIPT - 1) / (VT2 * VIPT);
+  const int tiles = *n_pad / VTILE;
+  int ns = (4 * sms + gx - 1) / gx;
+  if (ns > tiles) ns = tiles;
+  if (ns < 1) ns = 1;
+  const int tp = (tiles + ns - 1) / ns;  // tiles per split
+  *jsplit = tp * VTILE;
+  *nsplit = (tiles + tp - 1) / tp;
+}
+
+// Scratch: the split records (n_pad x 64 B), then the partials
+// (nsplit x n x 7 doubles); the larger of the two precisions' needs.
 extern "C" size_t g6k_vjp_scratch_bytes(int n) {
-  const int nsplit = n >= 8192 ? 8 : (n >= 1024 ? 4 : 1);
-  return (size_t)nsplit * (size_t)n * 7 * sizeof(double);
+  size_t need = 0;
+  for (int prec = 0; prec < 2; prec++) {
+    int ns, js, np;
+    vjp_shape(n, prec, &ns, &js, &np);
+    const size_t b = (size_t)np * sizeof(VJRec) + (size_t)ns * (size_t)n * 7 * sizeof(double);
+    if (b > need) need = b;
+  }
+  return need;
 }
 
 // hjerk: differentiate the hermite code's jerk form instead of the softened
 // one (must match the force the forward step used).
 extern "C" int g6k_force_vjp(int n, double eps2, int prec, int hjerk, const double *x,
                              const double *v, const double *m, const double *la1,
-                             const double *lj1, double *gx, double *gv, double *gm, double *part,
+                             const double *lj1, double *gx, double *gv, double *gm, void *scratch,
                              cudaStream_t st) {
   if (n <= 0) return 0;
-  const int nsplit = n >= 8192 ? 8 : (n >= 1024 ? 4 : 1);
-  const int jsplit = (n + nsplit - 1) / nsplit;
-  dim3 grid((n + VT - 1) / VT, nsplit);
-#define G6_VJP(F, H) vjp_kernel<F, H><<<grid, VT, 0, st>>>(n, eps2, x, v, m, la1, lj1, jsplit, part)
+  int nsplit, jsplit, n_pad;
+  vjp_shape(n, prec, &nsplit, &jsplit, &n_pad);
+  VJRec *rec = reinterpret_cast<VJRec *>(scratch);
+  double *part = reinterpret_cast<double *>(reinterpret_cast<char *>(scratch) +
+                                            (size_t)n_pad * sizeof(VJRec));
   if (prec == G6_PREC_FP64) {
-    if (hjerk) G6_VJP(true, true);
-    else G6_VJP(true, false);
-  } else {
-    if (hjerk) G6_VJP(false, true);
-    else G6_VJP(false, false);
-  }
+    dim3 grid((n + VT - 1) / VT, nsplit);
+#define G6_VJP(H) vjp_f64_kernel<H><<<grid, VT, 0, st>>>(n, eps2, x, v, m, la1, lj1, jsplit, part)
+    if (hjerk) G6_VJP(true);
+    else G6_VJP(false);
 #undef G6_VJP
+  } else {
+    vjp_records_kernel<<<(n_pad + PT - 1) / PT, PT, 0, st>>>(n, n_pad, x, v, m, la1, lj1, rec);
+    const float e2 = (float)eps2 + (float)(1.0 / 4503599627370496.0);
+    dim3 grid((n + VT2 * VIPT - 1) / (VT2 * VIPT), nsplit);
+    if (hjerk)
+      vjp_split_kernel<true><<<grid, VT2, 0, st>>>(n, e2, rec, jsplit, n_pad, part);
+    else
+      vjp_split_kernel<false><<<grid, VT2, 0, st>>>(n, e2, rec, jsplit, n_pad, part);
+  }
   vjp_reduce_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, nsplit, part, gx, gv, gm);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }

@@ -853,12 +853,13 @@ int launch(const KParams &kp, int jl, int gx, cudaStream_t st) {
   if (kp.hjerk) {
     if (jl != 1 || kp.want_nn) return -2;
     force_kernel<P, 1, false, true><<<grid, block, 0, st>>>(kp);
-  } else if (jl == 1 && !kp.want_nn) {
-    force_kernel<P, 1, false><<<grid, block, 0, st>>>(kp);
   } else switch (jl) {
-#define G6_CASE(J)                                         \
-  case J:                                                  \
-    force_kernel<P, J, true><<<grid, block, 0, st>>>(kp); \
+#define G6_CASE(J)                                            \
+  case J:                                                     \
+    if (kp.want_nn)                                           \
+      force_kernel<P, J, true><<<grid, block, 0, st>>>(kp);  \
+    else                                                      \
+      force_kernel<P, J, false><<<grid, block, 0, st>>>(kp); \
     break;
     G6_CASE(1)
     G6_CASE(2)

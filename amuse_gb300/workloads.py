@@ -32,6 +32,13 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 
+def _few_body_energy(m, x, v):
+    d = x[:, None, :] - x[None, :, :]
+    r = np.sqrt(np.sum(d * d, -1))
+    iu = np.triu_indices(len(m), 1)
+    return 0.5 * np.sum(m * np.sum(v * v, 1)) - np.sum(m[iu[0]] * m[iu[1]] / r[iu])
+
+
 def run_batch(args):
     """Config 4 on the GPU: autotune, the full batch, and a sample of systems
     (returned for a host-core comparison by the caller)."""
@@ -41,14 +48,16 @@ def run_batch(args):
     t_end = 10 * tcr
     off = np.concatenate([[0], np.cumsum(ns)])
     g6 = ag.G6X(0)
+    mode = getattr(args, "batch_mode", "split")
     out = {"workload": f"{args.nsys} few-body systems, n~U[3,64], Plummer r_vir=1e-3, eps=0, "
                        f"t_end=10 t_cross={t_end:.4g}, eta={args.eta}, smallN scheme "
-                       f"(n_iter=2, Kepler criterion), FP64, step cap {args.max_steps}/system"}
+                       f"(n_iter=2, Kepler criterion), FP64 state, step cap "
+                       f"{args.max_steps}/system", "mode": mode}
 
     # 1. autotune on 512 systems for 0.5% of the end time
     kt = min(args.nsys, 512)
     tune = g6.batch_tune(ns[:kt], t_end, m[:off[kt]], x[:off[kt]], v[:off[kt]], eta=args.eta,
-                         frac=0.005)
+                         frac=0.005, mode=mode)
     out["autotune"] = tune
     print(json.dumps(out), flush=True)
 
@@ -56,15 +65,28 @@ def run_batch(args):
     kc = min(args.cpu_sample, args.nsys)
     sc = slice(0, off[kc])
     rg = g6.batch_run(ns[:kc], t_end, m[sc], x[sc], v[sc], eta=args.eta,
-                      max_steps=args.max_steps)
+                      max_steps=args.max_steps, mode=mode)
     out["sample"] = {"systems": kc, "gpu_systems_per_s": kc / (rg["elapsed_ms"] / 1e3),
-                     "gpu_mode": "fast"}
+                     "gpu_mode": mode}
 
     # 3. the full batch
     t0 = time.perf_counter()
-    r = g6.batch_run(ns, t_end, m, x, v, eta=args.eta, max_steps=args.max_steps)
+    r = g6.batch_run(ns, t_end, m, x, v, eta=args.eta, max_steps=args.max_steps, mode=mode)
     wall = time.perf_counter() - t0
     done = r["status"] == 0
+    de, bad = [], []
+    for s_ in range(args.nsys):
+        a, b = off[s_], off[s_ + 1]
+        e0 = _few_body_energy(m[a:b], x[a:b], v[a:b])
+        e1 = _few_body_energy(m[a:b], r["pos"][a:b], r["vel"][a:b])
+        if np.isfinite(e1):
+            de.append(abs((e1 - e0) / e0))
+        else:
+            bad.append(s_)
+    out["dE_over_E"] = {"p50": float(np.percentile(de, 50)), "p90": float(np.percentile(de, 90)),
+                        "p99": float(np.percentile(de, 99)), "max": float(np.max(de)),
+                        "systems": len(de), "nonfinite_systems": bad[:20],
+                        "n_nonfinite": len(bad)}
     out.update({
         "systems_per_s": args.nsys / (r["elapsed_ms"] / 1e3),
         "completed_systems_per_s": int(done.sum()) / (r["elapsed_ms"] / 1e3),
@@ -296,6 +318,7 @@ def main():
     b.add_argument("--eta", type=float, default=0.14)
     b.add_argument("--max-steps", type=int, default=250_000)
     b.add_argument("--cpu-sample", type=int, default=64)
+    b.add_argument("--batch-mode", default="split", choices=["fast", "exact", "split"])
     d = sub.add_parser("adjoint")
     d.add_argument("--n", type=int, default=16384)
     d.add_argument("--nsteps", type=int, default=256)

@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--eta", type=float, default=0.14)
     ap.add_argument("--max-steps", type=int, default=250_000)
     ap.add_argument("--cpu-sample", type=int, default=64)
+    ap.add_argument("--batch-mode", default="split", choices=["fast", "exact", "split"])
     # adjoint workload
     ap.add_argument("--nsteps", type=int, default=256)
     ap.add_argument("--fd-coords", type=int, default=32)

@@ -243,7 +243,12 @@ int g6x_batch_tune(int nsys, const int *n_per_sys, const double *t_end, const do
    g6x_fixed_step_adjoint  -- the adjoint of one g6x_fixed_step, in place on
                               the state cotangents (lx, lv, la, lj); lm
                               accumulates the mass cotangent; work holds 7n
-                              doubles. */
+                              doubles.
+   g6x_fixed_run           -- nsteps steps with one host synchronisation;
+                              optionally keeps every step's predicted state
+                              (xp_all/vp_all: [nsteps][n][3], or both NULL).
+   g6x_fixed_adjoint_run   -- the adjoints of nsteps steps, last first, at
+                              the predicted states g6x_fixed_run kept. */
 /* Jerk form of the fixed-step force (and of its derivatives):
    G6_JERK_HERMITE (default) -- the hermite code's, whose (r.v) factor is
      divided by the unsoftened r^2 (interface.cc:440-449,486);
@@ -262,6 +267,12 @@ int g6x_force_vjp(int n, double eps2, const double *d_x, const double *d_v, cons
 int g6x_fixed_step_adjoint(int n, double h, double eps2, const double *d_xp, const double *d_vp,
                            const double *d_m, double *d_lx, double *d_lv, double *d_la,
                            double *d_lj, double *d_lm, double *d_work);
+int g6x_fixed_run(int n, double h, double eps2, int nsteps, double *d_x, double *d_v,
+                  double *d_a, double *d_j, const double *d_m, double *d_xp_all,
+                  double *d_vp_all);
+int g6x_fixed_adjoint_run(int n, double h, double eps2, int nsteps, const double *d_xp_all,
+                          const double *d_vp_all, const double *d_m, double *d_lx, double *d_lv,
+                          double *d_la, double *d_lj, double *d_lm, double *d_work);
 
 /* Device pointers of the predicted j records (for tools) and the stream. */
 void *g6x_stream(void);

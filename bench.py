@@ -326,19 +326,20 @@ def run_ours(args):
         out = dict(acc=np.zeros((n, 3)), jerk=np.zeros((n, 3)), pot=np.zeros(n),
                    nn=np.zeros(n, np.int32))
         # warm (pinned buffers, capacities)
+        # ph4's common path: g6calc_lasthalf (no neighbour), as in the timed step
         ag.drive_load(mass, x, v, ids=ids)
-        ag.drive_force(n, 0.0, EPS2, ids, x, v, want_nn=True, out=out)
+        ag.drive_force(n, 0.0, EPS2, ids, x, v, want_nn=False, out=out)
         e2e_t = []
         for _ in range(max(1, min(args.steps, 2))):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             ag.drive_load(mass, x, v, ids=ids)          # j updates for all N (ph4 update_gpu)
-            ag.drive_force(n, 0.0, EPS2, ids, x, v, want_nn=True, out=out)
+            ag.drive_force(n, 0.0, EPS2, ids, x, v, want_nn=False, out=out)
             e2e_t.append(time.perf_counter() - t0)
         e2e = {"value": pairs_step / statistics.median(e2e_t), "unit": "pair-interactions/s",
                "h2d_bytes_per_step": n * (128 + 6 * 8 + 8 + 4),
-               "d2h_bytes_per_step": n * (7 * 8 + 4 + 4) + 16 * ((n + 16383) // 16384),
-               "path": "g6_set_j_particle x N + g6_set_ti + g6calc_firsthalf/lasthalf2 "
+               "d2h_bytes_per_step": n * 7 * 8 + 16 * ((n + 16383) // 16384),
+               "path": "g6_set_j_particle x N + g6_set_ti + g6calc_firsthalf/lasthalf "
                        "chunks of g6_npipes()=16384 (libg6drive.so, ph4 gpu.cc order)"}
 
     cpu = None

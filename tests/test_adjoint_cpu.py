@@ -30,6 +30,21 @@ def test_oracle_hermite_binary_known_answer(lib_built):
     np.testing.assert_allclose(p2, [[0.5, 0, 0], [-0.5, 0, 0]], atol=5e-4)
 
 
+def test_oracle_hermite_force_matches_ph4_force_unsoftened(lib_built):
+    """At eps2 = 0 the hermite code's pair force (symmetric j > i loop) equals
+    ph4's (idata.cc:147-237, pinned bit-exact against the reference build)
+    up to summation order."""
+    import oracle
+    from amuse_gb300 import ic
+    rng = np.random.RandomState(8)
+    m, x, v = ic.plummer(200, do_scale=True, rng=rng)
+    _, _, a, j = oracle.hermite_fixed(m, x, v, 0.0, 1 / 256, 0)
+    ref = oracle.force(m, x, v, 0.0, x, v)
+    for got, want in ((a, ref["acc"]), (j, ref["jerk"])):
+        err = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+        assert err.max() <= 1e-12, err.max()
+
+
 @pytest.mark.parametrize("eps2", [0.0, 1e-4])
 def test_oracle_hermite_matches_torch(lib_built, eps2):
     """The oracle's hermite step and the torch restatement (hermite jerk)."""

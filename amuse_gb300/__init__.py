@@ -47,7 +47,7 @@ BYVALUE_SYMBOLS = [s[:-1] for s in ABI_SYMBOLS]
 EXT_SYMBOLS = [
     "g6x_set_precision", "g6x_get_precision", "g6x_set_npipes", "g6x_last_error", "g6x_load",
     "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
-    "g6x_energy", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
+    "g6x_energy", "g6x_run_stats", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
     "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
     "g6x_set_fixed_jerk", "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp",
     "g6x_fixed_step_adjoint", "g6x_fixed_run", "g6x_fixed_adjoint_run",
@@ -104,6 +104,7 @@ def load():
     lib.g6x_run_init.argtypes = [D, D]
     lib.g6x_run.argtypes = [D, ctypes.POINTER(ctypes.c_longlong), _pd]
     lib.g6x_energy.argtypes = [_pd, _pd]
+    lib.g6x_run_stats.argtypes = [_pd]
     lib.g6x_step_all.argtypes = [D]
     lib.g6x_correct.argtypes = [I, _pi, D, D, _pd, _pd]
     _pll = ctypes.POINTER(ctypes.c_longlong)
@@ -339,6 +340,12 @@ class G6X(G6):
         ns = ctypes.c_double(0)
         _check(self.lib.g6x_run(t_end, ctypes.byref(nb), ctypes.byref(ns)), "g6x_run")
         return nb.value, ns.value
+
+    def run_stats(self):
+        """Host-side account of the last run(): blocks, wall_ms, sync_ms, steps."""
+        out = np.zeros(4)
+        _check(self.lib.g6x_run_stats(_ptr(out, ctypes.c_double)), "g6x_run_stats")
+        return dict(blocks=out[0], wall_ms=out[1], sync_ms=out[2], particle_steps=out[3])
 
     def correct(self, slots, tnext, eta, acc, jerk):
         slots = _i32(slots)

@@ -12,11 +12,13 @@
  *   - errors return negative codes instead of exit(-1).
  * There is no CPU force path: every force is computed by the CUDA kernels.
  */
+#define _POSIX_C_SOURCE 200112L /* clock_gettime */
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include <cuda_runtime_api.h>
 
@@ -1167,9 +1169,25 @@ int g6x_run_init(double eps2, double eta) {
   return read_err_word();
 }
 
+static double run_stats[4]; /* last g6x_run: blocks, wall ms, ms waiting in syncs, steps */
+
+static double now_ms(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec * 1e3 + ts.tv_nsec * 1e-6;
+}
+
+int g6x_run_stats(double out[4]) {
+  if (!out) return G6_ERR_ARG;
+  memcpy(out, run_stats, sizeof(run_stats));
+  return 0;
+}
+
 int g6x_run(double t_end, long long *blocks, double *particle_steps) {
   int rc = check_open();
   if (rc) return rc;
+  const double w0 = now_ms();
+  double wsync = 0;
   const int n = G.run_n;
   if (n <= 0 || G.run_cap < n) return G6_ERR_STATE;
   const long long max_blocks = blocks && *blocks > 0 ? *blocks : -1;
@@ -1183,7 +1201,9 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
       return G6_ERR_CUDA;
     /* one 16-byte copy into pinned memory: the only host round trip per block */
     CK(cudaMemcpyAsync(G.h_mail, G.d_mail, 16, cudaMemcpyDeviceToHost, G.st));
+    const double s0 = now_ms();
     CK(cudaStreamSynchronize(G.st));
+    wsync += now_ms() - s0;
     memcpy(&tn, G.h_mail, sizeof(double));
     memcpy(hbuf, (const char *)G.h_mail + 8, sizeof(int));
     const int ni = hbuf[0];
@@ -1203,6 +1223,10 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
     ns += ni;
   }
   CK(cudaStreamSynchronize(G.st));
+  run_stats[0] = (double)nb;
+  run_stats[1] = now_ms() - w0;
+  run_stats[2] = wsync;
+  run_stats[3] = ns;
   if (blocks) *blocks = nb;
   if (particle_steps) *particle_steps = ns;
   return read_err_word();

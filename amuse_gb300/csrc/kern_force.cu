@@ -774,11 +774,11 @@ struct ShapeKey {
   int ni, nj, prec, fjl, fns;
   int jl, nsplit, jsplit;
 };
-ShapeKey g_shape_cache[64];
+ShapeKey g_shape_cache[256];
 
 void choose_shape(int ni, int nj, int prec, int force_jl, int force_nsplit, int *jl_out,
                   int *nsplit_out, int *jsplit_out) {
-  const unsigned h = ((unsigned)ni * 2654435761u ^ (unsigned)nj * 40503u ^ (unsigned)prec) & 63u;
+  const unsigned h = ((unsigned)ni * 2654435761u ^ (unsigned)nj * 40503u ^ (unsigned)prec) & 255u;
   ShapeKey &c = g_shape_cache[h];
   if (c.ni == ni && c.nj == nj && c.prec == prec && c.fjl == force_jl && c.fns == force_nsplit &&
       c.jl > 0) {
@@ -798,28 +798,40 @@ void choose_shape(int ni, int nj, int prec, int force_jl, int force_nsplit, int 
   if (force_jl > 0) jl_lo = jl_hi = force_jl;
   else if (jl0 == 1 && (ni + (NT * IPT) - 1) / (NT * IPT) >= slots) jl_hi = 1;
   const int max_ns = ntiles < 4 * slots ? ntiles : 4 * slots;
+  // Split counts: all small ones, then those from small tiles_per; each is
+  // normalised to (tiles per split, splits), and repeats are dropped (a
+  // repeat has the same cost and cannot win the strict comparison below).
+  int cand_tp[512], cand_ns[512];
+  int nc = 0;
+  {
+    int raw[512];
+    int nr = 0;
+    if (force_nsplit > 0) {
+      raw[nr++] = force_nsplit;
+    } else {
+      for (int q = 1; q <= 128 && q <= max_ns; q++) raw[nr++] = q;
+      for (int tp = 1; tp <= 256 && nr < 512; tp++) {
+        const int q = (ntiles + tp - 1) / tp;
+        if (q > 128 && q <= max_ns) raw[nr++] = q;
+      }
+    }
+    for (int k = 0; k < nr; k++) {
+      int ns = raw[k] < 1 ? 1 : raw[k];
+      if (ns > ntiles) ns = ntiles;
+      const int tp = (ntiles + ns - 1) / ns;
+      if (nc > 0 && cand_tp[nc - 1] == tp) continue;
+      cand_tp[nc] = tp;
+      cand_ns[nc] = (ntiles + tp - 1) / tp;
+      nc++;
+    }
+  }
   double best = 1e300;
   int bjl = jl_lo, bns = 1;
   for (int jl = jl_lo; jl <= jl_hi; jl *= 2) {
     const int islots = (NT / jl) * IPT;
     const long long gx = (ni + islots - 1) / islots;
-    // distinct split counts: all small ones, then those from small tiles_per
-    int cand[512];
-    int nc = 0;
-    if (force_nsplit > 0) {
-      cand[nc++] = force_nsplit;
-    } else {
-      for (int q = 1; q <= 128 && q <= max_ns; q++) cand[nc++] = q;
-      for (int tp = 1; tp <= 256 && nc < 512; tp++) {
-        const int q = (ntiles + tp - 1) / tp;
-        if (q > 128 && q <= max_ns) cand[nc++] = q;
-      }
-    }
     for (int k = 0; k < nc; k++) {
-      int ns = cand[k] < 1 ? 1 : cand[k];
-      if (ns > ntiles) ns = ntiles;
-      const int tp = (ntiles + ns - 1) / ns;
-      ns = (ntiles + tp - 1) / tp;
+      const int tp = cand_tp[k], ns = cand_ns[k];
       const long long ctas = gx * ns;
       const long long waves = (ctas + slots - 1) / slots;
       const double cost =

@@ -291,7 +291,9 @@ def run_salpeter(args):
     wall = time.perf_counter() - t0
     k1, p1 = g6.energy()
     e0, e1 = k0 + p0, k1 + p1
+    rs = g6.run_stats()
     out["run"] = {"precision": "fp64" if args.fp64 else "split", "blocks": nb,
+                  "host_wall_ms": rs["wall_ms"], "host_sync_wait_ms": rs["sync_ms"],
                   "particle_steps": ns, "mean_ni": ns / max(nb, 1), "seconds": wall,
                   "pairs_per_s": ns * (n - 1) / wall, "E0": e0, "E1": e1,
                   "dE_over_E": abs(e1 - e0) / abs(e0)}

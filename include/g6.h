@@ -178,6 +178,9 @@ int g6x_force_slots(double ti, double eps2, int nj, int ni, const int *d_ilist, 
                     benchmark step: predict + force on all + correct). */
 int g6x_run_init(double eps2, double eta);
 int g6x_run(double t_end, long long *blocks, double *particle_steps);
+/* Host-side account of the last g6x_run: out = {block steps, wall ms, ms
+   spent waiting in the per-block synchronisation, particle steps}. */
+int g6x_run_stats(double out[4]);
 int g6x_energy(double *kinetic, double *potential);
 int g6x_step_all(double tnext);
 /* FP64 corrector + Aarseth step (idata.cc:399-514) applied on the device to

@@ -731,7 +731,8 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   }
 }
 
-// Second pass: merge the nsplit partial records of each i in split order.
+// Second pass: merge the nsplit partial records of each i in split order
+// (one thread per i; for large blocks).
 template <class P>
 __global__ void reduce_kernel(KParams kp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -742,6 +743,36 @@ __global__ void reduce_kernel(KParams kp) {
   P::write_final(o, i, kp.acc, kp.jerk, kp.pot);
   if (kp.nn) kp.nn[i] = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
   if (kp.nn_r2) kp.nn_r2[i] = (float)o.nnr2;
+}
+
+// The same merge with one warp per i, for small blocks, where the splits are
+// many and the i few (a thread walking 128 splits alone took ~90 us): lane l
+// merges splits l, l+32, ... in order, then the lanes merge in a fixed
+// shuffle-down tree.  Deterministic for a given (ni, nsplit).
+template <class P>
+__global__ void reduce_warp_kernel(KParams kp) {
+  const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= kp.ni) return;  // whole warps exit together
+  const typename P::Out *part = reinterpret_cast<const typename P::Out *>(kp.part);
+  typename P::Out o = part[(size_t)(lane < kp.nsplit ? lane : 0) * kp.ni_pad + i];
+  for (int s = lane + 32; s < kp.nsplit; s += 32) P::merge(o, part[(size_t)s * kp.ni_pad + i]);
+  const int have = kp.nsplit < 32 ? kp.nsplit : 32;  // lanes holding a partial
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    typename P::Out b;
+    const int *src = reinterpret_cast<const int *>(&o);
+    int *dst = reinterpret_cast<int *>(&b);
+#pragma unroll
+    for (int w = 0; w < (int)(sizeof(b) / 4); w++)
+      dst[w] = __shfl_down_sync(0xffffffffu, src[w], off);
+    if (lane < off && lane + off < have) P::merge(o, b);
+  }
+  if (lane == 0) {
+    P::write_final(o, i, kp.acc, kp.jerk, kp.pot);
+    if (kp.nn) kp.nn[i] = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
+    if (kp.nn_r2) kp.nn_r2[i] = (float)o.nnr2;
+  }
 }
 
 int g_sms = 0;
@@ -888,7 +919,12 @@ int launch(const KParams &kp, int jl, int gx, cudaStream_t st) {
     default:
       return -2;
   }
-  if (kp.nsplit > 1) reduce_kernel<P><<<(kp.ni + 127) / 128, 128, 0, st>>>(kp);
+  if (kp.nsplit > 1) {
+    if (kp.ni < 4096)
+      reduce_warp_kernel<P><<<(kp.ni + 3) / 4, 128, 0, st>>>(kp);
+    else
+      reduce_kernel<P><<<(kp.ni + 127) / 128, 128, 0, st>>>(kp);
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

@@ -26,6 +26,31 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 
+// fmod(t, p) == 0 for p a positive normal power of two, without the
+// iterative double-precision fmod: t = m * 2^e (m an integer) is a multiple
+// of p = 2^k exactly when e + (trailing zero bits of m) >= k.  Any other p
+// goes to fmod.  Infinite or NaN t: fmod is NaN, so "not a multiple".
+__device__ __forceinline__ bool multiple_of_pow2(double t, double p) {
+  const unsigned long long pb = (unsigned long long)__double_as_longlong(p);
+  const int pe = (int)((pb >> 52) & 0x7ff);
+  if (pe == 0 || pe == 0x7ff || (pb & 0x000fffffffffffffull) || (pb >> 63))
+    return fmod(t, p) == 0;
+  const unsigned long long tb = (unsigned long long)__double_as_longlong(t) & 0x7fffffffffffffffull;
+  if (tb == 0) return true;
+  const int te = (int)(tb >> 52);
+  if (te == 0x7ff) return false;
+  unsigned long long m = tb & 0x000fffffffffffffull;
+  int e;
+  if (te == 0) {
+    e = -1074;
+  } else {
+    m |= 1ull << 52;
+    e = te - 1075;
+  }
+  const int tz = __ffsll((long long)m) - 1;
+  return e + tz >= pe - 1023;
+}
+
 __global__ void correct_kernel(g6_jstate js, int ni, const int *__restrict__ ilist, double tnext,
                                double eta, const double *__restrict__ acc,
                                const double *__restrict__ jerk, const double *__restrict__ pot,
@@ -72,12 +97,13 @@ __global__ void correct_kernel(g6_jstate js, int ni, const int *__restrict__ ili
   const double olds = js.dt[s];
   int expo;
   double oldstep2 = ddiv(olds, dmul(2.0, frexp(olds, &expo)));
-  for (int guard = 0; guard < 1100 && fmod(tnext, oldstep2) != 0; guard++) oldstep2 = ddiv(oldstep2, 2.0);
+  for (int guard = 0; guard < 1100 && !multiple_of_pow2(tnext, oldstep2); guard++)
+    oldstep2 = ddiv(oldstep2, 2.0);
   if (newstep < oldstep2) {
     newstep = ddiv(oldstep2, 2.0);
   } else {
     const double t2 = dmul(2.0, oldstep2);
-    if (newstep >= t2 && fmod(tnext, t2) == 0)
+    if (newstep >= t2 && multiple_of_pow2(tnext, t2))
       newstep = t2;
     else
       newstep = oldstep2;
@@ -170,7 +196,7 @@ __global__ void initial_step_kernel(g6_jstate js, int nj, double eta, double fac
   if (isnan(fs)) fs = dmul(fac, eta);
   int expo;
   fs = ddiv(fs, dmul(2.0, frexp(fs, &expo)));
-  for (int g = 0; g < 1100 && fmod(system_time, fs) != 0; g++) fs = ddiv(fs, 2.0);
+  for (int g = 0; g < 1100 && !multiple_of_pow2(system_time, fs); g++) fs = ddiv(fs, 2.0);
   for (int g = 0; g < 1100 && fs > limit; g++) fs = ddiv(fs, 2.0);
   js.dt[s] = fs;
   js.t[s] = system_time;

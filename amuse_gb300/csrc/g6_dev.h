@@ -9,7 +9,11 @@
  *   jp                      predicted records, one per slot, padded to the
  *                           next multiple of G6_TILE with zero-mass records
  *                           far away:
- *                             split: 48 B {xh,yh,zh,m}{xl,yl,zl,0}{vx,vy,vz,0}
+ *                             split: 48 B per slot, stored in pairs of slots
+ *                                    (2p, 2p+1) with every field a float2
+ *                                    {slot 2p, slot 2p+1}, 96 B per pair:
+ *                                    [xh yh zh m][xl yl zl 0][vx vy vz 0]
+ *                                    (the force kernel's packed f32x2 loads)
  *                             fp64 : 64 B {x,y,z,m}{vx,vy,vz,0}
  * Accelerations and jerks are stored unscaled (the GRAPE-6 a/2, j/6 inputs
  * are rescaled on the host), so the device predictor evaluates exactly
@@ -107,6 +111,25 @@ int g6k_store_forces(const g6_jstate *js, int ni, const int *ilist,
                      const int *nn, cudaStream_t st);
 
 #ifdef __cplusplus
+}
+#endif
+
+#ifdef __CUDACC__
+/* Split-record field f of slot s (f: 0 xh, 1 yh, 2 zh, 3 m, 4 xl, 5 yl,
+   6 zl, 7 pad, 8 vx, 9 vy, 10 vz, 11 pad) in the pair layout above. */
+__device__ __forceinline__ float *g6_split_field(void *base, int s, int f) {
+  return (float *)base + (size_t)(s >> 1) * 24 + (f >> 2) * 8 + (f & 3) * 2 + (s & 1);
+}
+__device__ __forceinline__ float g6_split_get(const void *base, int s, int f) {
+  return *g6_split_field((void *)base, s, f);
+}
+__device__ __forceinline__ void g6_split_store(void *base, int s, float xh, float yh, float zh,
+                                               float m, float xl, float yl, float zl, float vx,
+                                               float vy, float vz) {
+  float *p = (float *)base + (size_t)(s >> 1) * 24 + (s & 1);
+  p[0] = xh; p[2] = yh; p[4] = zh; p[6] = m;
+  p[8] = xl; p[10] = yl; p[12] = zl; p[14] = 0.f;
+  p[16] = vx; p[18] = vy; p[20] = vz; p[22] = 0.f;
 }
 #endif
 #endif

@@ -77,11 +77,8 @@ __global__ void records_kernel(int n, int n_pad, const double *__restrict__ x,
       h[k] = __double2float_rn(xp[k]);
       l[k] = __double2float_rn(xp[k] - (double)h[k]);
     }
-    float4 *r = reinterpret_cast<float4 *>(jp_split) + 3 * (size_t)s;
-    r[0] = make_float4(h[0], h[1], h[2], __double2float_rn(mm));
-    r[1] = make_float4(l[0], l[1], l[2], 0.f);
-    r[2] = make_float4(__double2float_rn(vp[0]), __double2float_rn(vp[1]),
-                       __double2float_rn(vp[2]), 0.f);
+    g6_split_store(jp_split, s, h[0], h[1], h[2], __double2float_rn(mm), l[0], l[1], l[2],
+                   __double2float_rn(vp[0]), __double2float_rn(vp[1]), __double2float_rn(vp[2]));
   }
 }
 

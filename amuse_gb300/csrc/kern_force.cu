@@ -56,30 +56,39 @@ namespace {
 #define G6_NT 128
 #endif
 #ifndef G6_IPT
-#define G6_IPT 4
+#define G6_IPT 2
 #endif
 #ifndef G6_UNROLL
 #define G6_UNROLL 4
 #endif
 #ifndef G6_MINB
-#define G6_MINB 2
+#define G6_MINB 3
+#endif
+#ifndef G6_IPT_F64
+#define G6_IPT_F64 4
 #endif
 constexpr int NT = G6_NT;    // threads per CTA
 constexpr int TJ = G6_TILE;  // j records per tile
-constexpr int IPT = G6_IPT;  // i-particles per thread
+// i-particles per thread: the split kernel's packed f32x2 pair terms need
+// twice the registers per i, so it holds fewer i than the FP64 kernel.
+constexpr int IPT_SPLIT = G6_IPT;
+constexpr int IPT_F64 = G6_IPT_F64;
 constexpr int UNROLL = G6_UNROLL;  // j-loop unroll factor
 constexpr int JLMAX = TJ < NT ? TJ : NT;  // j-lanes per i at most
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound per wait
 
 enum { ERR_TMA_TIMEOUT = 1, ERR_SHAPE = 2 };
 
+// Split records come in pairs of consecutive j slots, every field a float2
+// {j even, j odd} (the global layout the predictor writes, g6_dev.h), so a
+// packed f32x2 instruction evaluates two j at once.
 struct __align__(16) RecS {
-  float4 ph, pl, v;
+  float2 xh, yh, zh, m, xl, yl, zl, pad0, vx, vy, vz, pad1;
 };
 struct __align__(16) RecD {
   G6D4 p, v;
 };
-static_assert(sizeof(RecS) == 48, "split record");
+static_assert(sizeof(RecS) == 96, "split record pair");
 static_assert(sizeof(RecD) == 64, "fp64 record");
 
 // ---------------------------------------------------------------- PTX ---
@@ -162,6 +171,49 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return y;
 }
 
+// ------------------------------------------------------ packed f32x2 ---
+// Two floats in one 64-bit register pair; each op is the IEEE
+// round-to-nearest scalar op on both halves (no contraction).
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x f2_add(f2x a, f2x b) {
+  f2x d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
+  f2x d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2x f2_mul(f2x a, f2x b) {
+  f2x d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c) {
+  f2x d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2x f2_pack(float lo, float hi) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float f2_lo(f2x v) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+  return lo;
+}
+__device__ __forceinline__ float f2_hi(f2x v) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+  return hi;
+}
+__device__ __forceinline__ f2x f2_of(const float2 &v) {
+  return *reinterpret_cast<const f2x *>(&v);
+}
+
 // ------------------------------------------------------- float-float ---
 // Knuth TwoSum folded into a (hi, lo) accumulator.
 __device__ __forceinline__ void ff_acc(float &hi, float &lo, float p) {
@@ -185,13 +237,15 @@ __device__ __forceinline__ void ff_add(float &ah, float &al, float bh, float bl)
 struct SplitP {
   using Rec = RecS;
   using R = float;
+  static constexpr int JPR = 2;     // j per record (packed pair)
+  static constexpr int IPT = IPT_SPLIT;
   static constexpr int NSTAGE = 3;  // TMA ring depth (3 x 12 KB)
   static constexpr int MINB = G6_MINB;  // resident CTAs per SM
-  struct I {
-    float xh, yh, zh, xl, yl, zl, vx, vy, vz;
+  struct I {  // i values duplicated into both halves
+    f2x xh, yh, zh, xl, yl, zl, vx, vy, vz;
   };
-  struct Part {  // per-fold-period partial sums
-    float a[3], j[3], p;
+  struct Part {  // per-fold-period partial sums, one per half
+    f2x a[3], j[3], p;
   };
   struct Tot {  // compensated totals
     float ah[3], al[3], jh[3], jl[3], ph, pl;
@@ -205,27 +259,33 @@ struct SplitP {
     h = __double2float_rn(d);
     l = __double2float_rn(d - (double)h);
   }
-  __device__ static I load_i_explicit(const double *p, const double *v) {
+  __device__ static I dup(float xh, float yh, float zh, float xl, float yl, float zl, float vx,
+                          float vy, float vz) {
     I s;
-    split(p[0], s.xh, s.xl);
-    split(p[1], s.yh, s.yl);
-    split(p[2], s.zh, s.zl);
-    s.vx = __double2float_rn(v[0]);
-    s.vy = __double2float_rn(v[1]);
-    s.vz = __double2float_rn(v[2]);
+    s.xh = f2_pack(xh, xh); s.yh = f2_pack(yh, yh); s.zh = f2_pack(zh, zh);
+    s.xl = f2_pack(xl, xl); s.yl = f2_pack(yl, yl); s.zl = f2_pack(zl, zl);
+    s.vx = f2_pack(vx, vx); s.vy = f2_pack(vy, vy); s.vz = f2_pack(vz, vz);
     return s;
   }
-  __device__ static I load_i_rec(const Rec &r) {
-    I s;
-    s.xh = r.ph.x; s.yh = r.ph.y; s.zh = r.ph.z;
-    s.xl = r.pl.x; s.yl = r.pl.y; s.zl = r.pl.z;
-    s.vx = r.v.x; s.vy = r.v.y; s.vz = r.v.z;
-    return s;
+  __device__ static I load_i_explicit(const double *p, const double *v) {
+    float xh, yh, zh, xl, yl, zl;
+    split(p[0], xh, xl);
+    split(p[1], yh, yl);
+    split(p[2], zh, zl);
+    return dup(xh, yh, zh, xl, yl, zl, __double2float_rn(v[0]), __double2float_rn(v[1]),
+               __double2float_rn(v[2]));
+  }
+  __device__ static I load_i_slot(const void *recs, int slot) {
+    return dup(g6_split_get(recs, slot, 0), g6_split_get(recs, slot, 1),
+               g6_split_get(recs, slot, 2), g6_split_get(recs, slot, 4),
+               g6_split_get(recs, slot, 5), g6_split_get(recs, slot, 6),
+               g6_split_get(recs, slot, 8), g6_split_get(recs, slot, 9),
+               g6_split_get(recs, slot, 10));
   }
   __device__ static void zero(Part &q) {
 #pragma unroll
-    for (int k = 0; k < 3; k++) q.a[k] = q.j[k] = 0.f;
-    q.p = 0.f;
+    for (int k = 0; k < 3; k++) q.a[k] = q.j[k] = 0ull;
+    q.p = 0ull;
   }
   __device__ static void zero(Tot &t) {
 #pragma unroll
@@ -235,57 +295,94 @@ struct SplitP {
   __device__ static void fold(Tot &t, const Part &q) {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      ff_acc(t.ah[k], t.al[k], q.a[k]);
-      ff_acc(t.jh[k], t.jl[k], q.j[k]);
+      ff_acc(t.ah[k], t.al[k], f2_lo(q.a[k]));
+      ff_acc(t.ah[k], t.al[k], f2_hi(q.a[k]));
+      ff_acc(t.jh[k], t.jl[k], f2_lo(q.j[k]));
+      ff_acc(t.jh[k], t.jl[k], f2_hi(q.j[k]));
     }
-    ff_acc(t.ph, t.pl, q.p);
+    ff_acc(t.ph, t.pl, f2_lo(q.p));
+    ff_acc(t.ph, t.pl, f2_hi(q.p));
   }
-  // r^2 + eps^2 for the nearest-neighbour key: must be bit-identical in the
-  // main loop and in the re-scan.
-  __device__ static __forceinline__ float r2e(const I &s, const Rec &r, float eps2,
-                                              float &dx, float &dy, float &dz) {
-    dx = __fadd_rn(__fsub_rn(r.ph.x, s.xh), __fsub_rn(r.pl.x, s.xl));
-    dy = __fadd_rn(__fsub_rn(r.ph.y, s.yh), __fsub_rn(r.pl.y, s.yl));
-    dz = __fadd_rn(__fsub_rn(r.ph.z, s.zh), __fsub_rn(r.pl.z, s.zl));
-    float r2 = __fmaf_rn(dx, dx, eps2);
-    r2 = __fmaf_rn(dy, dy, r2);
-    return __fmaf_rn(dz, dz, r2);
+  // r^2 + eps^2 of both j of a record (the nearest-neighbour key): the main
+  // loop and the re-scan use this same arithmetic, so the keys are
+  // bit-identical.
+  __device__ static __forceinline__ f2x r2e(const I &s, const Rec &r, f2x eps2, f2x &dx, f2x &dy,
+                                            f2x &dz) {
+    dx = f2_add(f2_sub(f2_of(r.xh), s.xh), f2_sub(f2_of(r.xl), s.xl));
+    dy = f2_add(f2_sub(f2_of(r.yh), s.yh), f2_sub(f2_of(r.yl), s.yl));
+    dz = f2_add(f2_sub(f2_of(r.zh), s.zh), f2_sub(f2_of(r.zl), s.zl));
+    return f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, eps2)));
   }
-  // HJ: the jerk as the hermite code forms it (src/amuse_hermite/interface.cc:440-449,
-  // 469-486):
-  // the (r.v) factor is divided by the UNsoftened r^2.
+  // Both j of record r on one i.  selfrel = (self slot) - (slot of the
+  // record's first j): half h is the i itself when selfrel == h (CHECK only).
+  // HJ: the jerk as the hermite code forms it (src/amuse_hermite/
+  // interface.cc:440-449,469-486): the (r.v) factor divided by the
+  // UNsoftened r^2.
   template <bool CHECK, bool NN, bool HJ = false>
-  __device__ static __forceinline__ void pair(const I &s, const Rec &r, float eps2, Part &q,
-                                              float &nnmin, bool is_self) {
-    float dx, dy, dz;
-    const float r2 = r2e(s, r, eps2, dx, dy, dz);
-    float rinv = rsqrt_approx(r2);
+  __device__ static __forceinline__ void pair(const I &s, const Rec &r, f2x eps2, Part &q,
+                                              float &nnmin, int selfrel) {
+    f2x dx, dy, dz;
+    const f2x r2 = r2e(s, r, eps2, dx, dy, dz);
+    const float r2a = f2_lo(r2), r2b = f2_hi(r2);
+    float ra = rsqrt_approx(r2a), rb = rsqrt_approx(r2b);
     if (CHECK) {
-      rinv = is_self ? 0.f : rinv;
-      if (NN) nnmin = fminf(nnmin, is_self ? __int_as_float(0x7f800000) : r2);
+      ra = selfrel == 0 ? 0.f : ra;
+      rb = selfrel == 1 ? 0.f : rb;
+      if (NN) {
+        const float inf = __int_as_float(0x7f800000);
+        nnmin = fminf(nnmin, fminf(selfrel == 0 ? inf : r2a, selfrel == 1 ? inf : r2b));
+      }
     } else if (NN) {
-      nnmin = fminf(nnmin, r2);
+      nnmin = fminf(nnmin, fminf(r2a, r2b));
     }
-    const float dvx = r.v.x - s.vx, dvy = r.v.y - s.vy, dvz = r.v.z - s.vz;
-    const float rv = dx * dvx + dy * dvy + dz * dvz;
-    const float rinv2 = rinv * rinv;
-    const float mri = r.ph.w * rinv;
-    const float mr3i = mri * rinv2;
-    float a3;
+    const f2x rinv = f2_pack(ra, rb);
+    const f2x dvx = f2_sub(f2_of(r.vx), s.vx);
+    const f2x dvy = f2_sub(f2_of(r.vy), s.vy);
+    const f2x dvz = f2_sub(f2_of(r.vz), s.vz);
+    const f2x rv = f2_fma(dz, dvz, f2_fma(dy, dvy, f2_mul(dx, dvx)));
+    const f2x rinv2 = f2_mul(rinv, rinv);
+    const f2x mri = f2_mul(f2_of(r.m), rinv);
+    const f2x mr3i = f2_mul(mri, rinv2);
+    const f2x m3 = f2_pack(-3.0f, -3.0f);
+    f2x a3;
     if (HJ) {
-      const float r2u = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-      a3 = -3.0f * (rv * rcp_approx(r2u));
-      if (CHECK) a3 = is_self ? 0.f : a3;
+      const f2x r2u = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+      float ia = rcp_approx(f2_lo(r2u)), ib = rcp_approx(f2_hi(r2u));
+      if (CHECK) {
+        ia = selfrel == 0 ? 0.f : ia;
+        ib = selfrel == 1 ? 0.f : ib;
+      }
+      a3 = f2_mul(m3, f2_mul(rv, f2_pack(ia, ib)));
     } else {
-      a3 = -3.0f * (rv * rinv2);
+      a3 = f2_mul(m3, f2_mul(rv, rinv2));
     }
-    q.a[0] = fmaf(mr3i, dx, q.a[0]);
-    q.a[1] = fmaf(mr3i, dy, q.a[1]);
-    q.a[2] = fmaf(mr3i, dz, q.a[2]);
-    q.j[0] = fmaf(mr3i, fmaf(a3, dx, dvx), q.j[0]);
-    q.j[1] = fmaf(mr3i, fmaf(a3, dy, dvy), q.j[1]);
-    q.j[2] = fmaf(mr3i, fmaf(a3, dz, dvz), q.j[2]);
-    q.p += mri;
+    q.a[0] = f2_fma(mr3i, dx, q.a[0]);
+    q.a[1] = f2_fma(mr3i, dy, q.a[1]);
+    q.a[2] = f2_fma(mr3i, dz, q.a[2]);
+    q.j[0] = f2_fma(mr3i, f2_fma(a3, dx, dvx), q.j[0]);
+    q.j[1] = f2_fma(mr3i, f2_fma(a3, dy, dvy), q.j[1]);
+    q.j[2] = f2_fma(mr3i, f2_fma(a3, dz, dvz), q.j[2]);
+    q.p = f2_add(q.p, mri);
+  }
+  // Nearest-neighbour re-scan of one record: the first of its j (in slot
+  // order) whose key equals best and that is not the i itself.
+  __device__ static __forceinline__ bool rescan(const I &s, const Rec &r, f2x eps2, float best,
+                                                int slot0, int self, int &idx) {
+    f2x dx, dy, dz;
+    const f2x r2 = r2e(s, r, eps2, dx, dy, dz);
+    if (f2_lo(r2) == best && slot0 != self) {
+      idx = slot0;
+      return true;
+    }
+    if (f2_hi(r2) == best && slot0 + 1 != self) {
+      idx = slot0 + 1;
+      return true;
+    }
+    return false;
+  }
+  __device__ static f2x eps(double eps2) {
+    const float e = (float)eps2 + (float)(1.0 / 4503599627370496.0);  // + 2^-52 (ph4)
+    return f2_pack(e, e);
   }
   __device__ static void to_out(const Tot &t, float nnr2, int nn, Out &o) {
 #pragma unroll
@@ -323,6 +420,8 @@ struct SplitP {
 struct F64P {
   using Rec = RecD;
   using R = double;
+  static constexpr int JPR = 1;     // j per record
+  static constexpr int IPT = IPT_F64;
   static constexpr int NSTAGE = 2;  // TMA ring depth (2 x 16 KB)
   static constexpr int MINB = 1;
   struct I {
@@ -345,12 +444,14 @@ struct F64P {
     s.vx = v[0]; s.vy = v[1]; s.vz = v[2];
     return s;
   }
-  __device__ static I load_i_rec(const Rec &r) {
+  __device__ static I load_i_slot(const void *recs, int slot) {
+    const Rec &r = reinterpret_cast<const Rec *>(recs)[slot];
     I s;
     s.x = r.p.x; s.y = r.p.y; s.z = r.p.z;
     s.vx = r.v.x; s.vy = r.v.y; s.vz = r.v.z;
     return s;
   }
+  __device__ static double eps(double eps2) { return eps2 + 1.0 / 4503599627370496.0; }
   __device__ static void zero(Part &q) {
 #pragma unroll
     for (int k = 0; k < 3; k++) q.a[k] = q.j[k] = 0.0;
@@ -389,7 +490,8 @@ struct F64P {
   }
   template <bool CHECK, bool NN, bool HJ = false>
   __device__ static __forceinline__ void pair(const I &s, const Rec &r, double eps2, Part &q,
-                                              double &nnmin, bool is_self) {
+                                              double &nnmin, int selfrel) {
+    const bool is_self = CHECK && selfrel == 0;
     double dx, dy, dz;
     const double r2 = r2e(s, r, eps2, dx, dy, dz);
     double rinv = rsqrt64(r2);
@@ -418,6 +520,15 @@ struct F64P {
     q.j[1] = fma(mr3i, fma(a3, dy, dvy), q.j[1]);
     q.j[2] = fma(mr3i, fma(a3, dz, dvz), q.j[2]);
     q.p += mri;
+  }
+  __device__ static __forceinline__ bool rescan(const I &s, const Rec &r, double eps2,
+                                                double best, int slot0, int self, int &idx) {
+    double dx, dy, dz;
+    if (r2e(s, r, eps2, dx, dy, dz) == best && slot0 != self) {
+      idx = slot0;
+      return true;
+    }
+    return false;
   }
   __device__ static void to_out(const Tot &t, double nnr2, int nn, Out &o) {
 #pragma unroll
@@ -488,13 +599,16 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   constexpr int NSTAGE = P::NSTAGE;
   using Rec = typename P::Rec;
   using R = typename P::R;
+  constexpr int JPR = P::JPR;            // j per record
+  constexpr int IPT = P::IPT;            // i-particles per thread
+  constexpr int RPT = TJ / JPR;          // records per tile
   constexpr int NIL = NT / JL;           // i-lanes per CTA
   constexpr int ISLOTS = NIL * IPT;      // i-particles per CTA
-  constexpr int JPT = TJ / JL;           // j per thread per tile
-  constexpr int FOLD_TILES = (FOLD_J / JPT) > 0 ? (FOLD_J / JPT) : 1;
-  static_assert(JL >= 1 && JL <= JLMAX && (TJ % JL) == 0, "JL");
+  constexpr int JPT = RPT / JL;          // records per thread per tile
+  constexpr int FOLD_TILES = (FOLD_J / (JPT * JPR)) > 0 ? (FOLD_J / (JPT * JPR)) : 1;
+  static_assert(JL >= 1 && JL <= JLMAX && JL <= RPT && (RPT % JL) == 0, "JL");
 
-  __shared__ __align__(128) Rec tiles[NSTAGE][TJ];
+  __shared__ __align__(128) Rec tiles[NSTAGE][RPT];
   __shared__ __align__(8) uint64_t full[NSTAGE];
   __shared__ int released[NSTAGE];
   __shared__ int issued_s;
@@ -516,7 +630,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
     const int ii = valid[k] ? i : 0;
     if (kp.ilist) {
       const int slot = kp.ilist[ii];
-      I[k] = P::load_i_rec(reinterpret_cast<const Rec *>(kp.jrec)[slot]);
+      I[k] = P::load_i_slot(kp.jrec, slot);
       self[k] = valid[k] ? (kp.iself ? kp.iself[ii] : slot) : -1;
     } else {
       I[k] = P::load_i_explicit(kp.ipos + 3 * ii, kp.ivel + 3 * ii);
@@ -530,7 +644,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   const int nj_pad = (kp.nj + TJ - 1) / TJ * TJ;
   if (je > nj_pad) je = nj_pad;
   const int ntiles = je > js ? (je - js) / TJ : 0;
-  const Rec *gj = reinterpret_cast<const Rec *>(kp.jrec) + js;
+  const Rec *gj = reinterpret_cast<const Rec *>(kp.jrec) + js / JPR;
 
   constexpr int NWARP = NT / 32;
   if (tid == 0) {
@@ -546,12 +660,12 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   __syncthreads();
   if (tid == 0) {
     for (int s = 0; s < NSTAGE && s < ntiles; s++) {
-      mbar_expect_tx(&full[s], TJ * sizeof(Rec));
-      tma_load_1d(&tiles[s][0], gj + s * TJ, TJ * sizeof(Rec), &full[s]);
+      mbar_expect_tx(&full[s], RPT * sizeof(Rec));
+      tma_load_1d(&tiles[s][0], gj + s * RPT, RPT * sizeof(Rec), &full[s]);
     }
   }
 
-  const R eps2 = (R)kp.eps2 + (R)(1.0 / 4503599627370496.0);  // + 2^-52 (ph4)
+  const auto eps2 = P::eps(kp.eps2);  // eps^2 + 2^-52 (ph4)
   typename P::Part q[IPT];
   typename P::Tot T[IPT];
   R nnmin[IPT], nnbest[IPT];
@@ -594,7 +708,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
         const Rec r = tile[jl + JL * u];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
-          P::template pair<false, NN, HJ>(I[k], r, eps2, q[k], nnmin[k], false);
+          P::template pair<false, NN, HJ>(I[k], r, eps2, q[k], nnmin[k], 0);
       }
     } else {
       for (int u = 0; u < JPT; u++) {
@@ -602,7 +716,8 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
         const Rec r = tile[jj];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
-          P::template pair<true, NN, HJ>(I[k], r, eps2, q[k], nnmin[k], tj0 + jj == self[k]);
+          P::template pair<true, NN, HJ>(I[k], r, eps2, q[k], nnmin[k],
+                                         self[k] - (tj0 + JPR * jj));
       }
     }
 
@@ -632,8 +747,8 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
       const int c = atomicAdd(&released[s], 1);
       if (c == (t / NSTAGE + 1) * NWARP - 1 && t + NSTAGE < ntiles) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(&full[s], TJ * sizeof(Rec));
-        tma_load_1d(&tiles[s][0], gj + (t + NSTAGE) * TJ, TJ * sizeof(Rec), &full[s]);
+        mbar_expect_tx(&full[s], RPT * sizeof(Rec));
+        tma_load_1d(&tiles[s][0], gj + (t + NSTAGE) * RPT, RPT * sizeof(Rec), &full[s]);
         atomicMax(&issued_s, t + NSTAGE + 1);
       }
     }
@@ -656,18 +771,12 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
 #pragma unroll
   for (int k = 0; k < IPT; k++) {
     if (!NN || besttile[k] < 0) continue;
-    const Rec *g = gj + besttile[k] * TJ;
+    const Rec *g = gj + besttile[k] * RPT;
     const int tj0 = js + besttile[k] * TJ;
     bool found = false;
     for (int u = 0; u < JPT && !found; u++) {
       const int jj = jl + JL * u;
-      const Rec r = g[jj];
-      R dx, dy, dz;
-      const R r2 = P::r2e(I[k], r, eps2, dx, dy, dz);
-      if (r2 == nnbest[k] && tj0 + jj != self[k]) {
-        nnidx[k] = tj0 + jj;
-        found = true;
-      }
+      found = P::rescan(I[k], g[jj], eps2, nnbest[k], tj0 + JPR * jj, self[k], nnidx[k]);
     }
   }
 
@@ -699,7 +808,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
     // Cross-warp: warps w0..w0+JL/32-1 own one i-lane group.
     __syncthreads();
     typename P::Out *buf = reinterpret_cast<typename P::Out *>(&tiles[0][0]);
-    static_assert(sizeof(typename P::Out) * IPT * (NT / 32) <= sizeof(Rec) * TJ * NSTAGE, "smem");
+    static_assert(sizeof(typename P::Out) * IPT * (NT / 32) <= sizeof(Rec) * RPT * NSTAGE, "smem");
     const int warp = tid >> 5;
     if (lane == 0) {
 #pragma unroll
@@ -822,7 +931,9 @@ void choose_shape(int ni, int nj, int prec, int force_jl, int force_nsplit, int 
   const int minb = prec == G6_PREC_FP64 ? F64P::MINB : SplitP::MINB;
   const int slots = minb * sm_count();
   const double A = 150.0, F = 3000.0;
-  const double B = (prec == G6_PREC_FP64 ? 32.0 : 1.0) * 37.0 * IPT;
+  // per j and i: ~20 issue slots split (packed j pairs), ~37 x 32 FP64
+  const int IPT = prec == G6_PREC_FP64 ? IPT_F64 : IPT_SPLIT;
+  const double B = (prec == G6_PREC_FP64 ? 32.0 * 37.0 : 20.0) * IPT;
   int jl0 = 1;
   while (jl0 < JLMAX && (NT / (jl0 * 2)) * IPT >= ni && ni > 0) jl0 *= 2;
   int jl_lo = jl0, jl_hi = JLMAX;
@@ -971,7 +1082,7 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
   kp.hjerk = a->hjerk;
   const size_t need = nsplit > 1 ? g6k_scratch_bytes(a->ni, a->nj, a->prec, jl, nsplit) : 0;
   if (need > a->scratch_bytes) return -4;
-  const int islots = (NT / jl) * IPT;
+  const int islots = (NT / jl) * (a->prec == G6_PREC_FP64 ? IPT_F64 : IPT_SPLIT);
   const int gx = (a->ni + islots - 1) / islots;
   if (shape) {
     shape->jl = jl;

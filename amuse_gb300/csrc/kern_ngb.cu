@@ -40,11 +40,10 @@ __global__ void __launch_bounds__(NB) ngb_kernel(g6_jstate js, int nj, const dou
   for (int j = threadIdx.x; j < nj; j += NB) {
     double dx, dy, dz;
     if (PREC == G6_PREC_SPLIT) {
-      const float4 *r = reinterpret_cast<const float4 *>(js.jp_split) + 3 * (size_t)j;
-      const float4 h = r[0], l = r[1];
-      dx = ((double)h.x + (double)l.x) - xi;
-      dy = ((double)h.y + (double)l.y) - yi;
-      dz = ((double)h.z + (double)l.z) - zi;
+      const void *b = js.jp_split;
+      dx = ((double)g6_split_get(b, j, 0) + (double)g6_split_get(b, j, 4)) - xi;
+      dy = ((double)g6_split_get(b, j, 1) + (double)g6_split_get(b, j, 5)) - yi;
+      dz = ((double)g6_split_get(b, j, 2) + (double)g6_split_get(b, j, 6)) - zi;
     } else {
       const G6D4 p = reinterpret_cast<const G6D4 *>(js.jp_f64)[2 * (size_t)j];
       dx = p.x - xi;

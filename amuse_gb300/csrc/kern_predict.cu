@@ -91,11 +91,8 @@ __global__ void __launch_bounds__(PT) predict_kernel(g6_jstate js, int nj, int n
       h[k] = __double2float_rn(xp[k]);
       l[k] = __double2float_rn(xp[k] - (double)h[k]);
     }
-    float4 *rec = reinterpret_cast<float4 *>(js.jp_split) + 3 * (size_t)s;
-    rec[0] = make_float4(h[0], h[1], h[2], __double2float_rn(m));
-    rec[1] = make_float4(l[0], l[1], l[2], 0.f);
-    rec[2] = make_float4(__double2float_rn(vp[0]), __double2float_rn(vp[1]),
-                         __double2float_rn(vp[2]), 0.f);
+    g6_split_store(js.jp_split, s, h[0], h[1], h[2], __double2float_rn(m), l[0], l[1], l[2],
+                   __double2float_rn(vp[0]), __double2float_rn(vp[1]), __double2float_rn(vp[2]));
   } else {
     G6D4 *rec = reinterpret_cast<G6D4 *>(js.jp_f64) + 2 * (size_t)s;
     rec[0] = g6d4(xp[0], xp[1], xp[2], m);

@@ -5,6 +5,10 @@
 //          position formed by (xj_hi - xi_hi) + (xj_lo - xi_lo), all pair
 //          arithmetic in FP32 (one MUFU rsqrt per pair), per-tile FP32
 //          partial sums folded into compensated (TwoSum) hi/lo totals.
+//          The j records are stored in pairs (every field a float2 of two
+//          consecutive j), so each packed f32x2 instruction (add/sub/mul/fma
+//          .rn.f32x2) evaluates one i against two j: half the issue slots of
+//          scalar code for the same FP32 work.
 //   fp64:  the same pair formula in plain FP64 (the "plain FP64 GPU"
 //          kernel; also the GPU-side oracle at N=2^20).
 //
@@ -18,7 +22,8 @@
 // here the host resolves id -> j slot once per call and the kernel skips
 // that slot.
 //
-// Structure (one CTA = 128 threads = 4 warps, 4 i-particles per thread):
+// Structure (one CTA = 128 threads = 4 warps; 2 i-particles per thread in
+// split precision, 3 CTAs per SM; 4 in FP64):
 //   * j-tiles of 256 records are streamed HBM/L2 -> shared memory with
 //     cp.async.bulk (TMA, non-tensor) completing on an mbarrier; warps
 //     consume the ring independently (no CTA barrier in the loop).

@@ -231,19 +231,57 @@ __global__ void __launch_bounds__(VT) vjp_f64_kernel(int n, double eps2,
   }
 }
 
-// ---- split-precision force VJP, register-blocked ----
-// One 64 B record per body: {xh,yh,zh,m} {xl,yl,zl,vx} {vy,vz,la0,la1}
-// {la2,lj0,lj1,lj2}; padding records (zero mass and cotangents, far away)
-// contribute exactly zero.  Each thread owns VIPT bodies, so every j record
-// read from shared memory serves VIPT pairs.  The self pair also contributes
-// exactly zero: r = v = 0 and lam = m_k La_j - m_j La_k cancels bit for bit
-// (two rounded products, no contraction); with the hermite jerk form the
-// 1/r^2 factor is set to 0 there.
-struct __align__(16) VJRec {
-  float4 a, b, c, d;
+// ---- split-precision force VJP, packed f32x2, register-blocked ----
+// Records come in pairs of consecutive bodies, every field a float2 (body
+// 2p, body 2p+1), 128 B per pair: xh yh zh m xl yl zl vx vy vz la0 la1 la2
+// lj0 lj1 lj2.  Each add/sub/mul/fma.rn.f32x2 evaluates one body k against
+// two bodies j; each thread owns VIPT bodies k (values duplicated into both
+// halves), so every shared-memory record pair serves 2 x VIPT pairs.
+// Padding records (zero mass and cotangents, far away) contribute exactly
+// zero.  The self pair also contributes exactly zero: r = v = 0 and
+// lam = m_k La_j - m_j La_k cancels bit for bit (two rounded products, no
+// contraction); with the hermite jerk form the 1/r^2 factor is set to 0
+// there.
+constexpr int VF = 16;  // fields per body
+struct __align__(16) VJPair {
+  float2 f[VF];
 };
-constexpr int VIPT = 4;
+constexpr int VIPT = 2;
 constexpr int VT2 = 128;
+
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x f2_add(f2x a, f2x b) {
+  f2x d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
+  f2x d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2x f2_mul(f2x a, f2x b) {
+  f2x d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c) {
+  f2x d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2x f2_pack(float lo, float hi) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f2x v, float &lo, float &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2x f2_of(const float2 &v) {
+  return *reinterpret_cast<const f2x *>(&v);
+}
+__device__ __forceinline__ f2x f2_dup(float v) { return f2_pack(v, v); }
 
 __device__ __forceinline__ float rsqrt_approx(float x) {
   float y;
@@ -259,117 +297,135 @@ __device__ __forceinline__ float rcp_approx(float x) {
 __global__ void vjp_records_kernel(int n, int n_pad, const double *__restrict__ x,
                                    const double *__restrict__ v, const double *__restrict__ m,
                                    const double *__restrict__ la1, const double *__restrict__ lj1,
-                                   VJRec *rec) {
+                                   VJPair *rec) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_pad) return;
-  VJRec r;
+  float f[VF];
   if (s < n) {
-    float h[3], l[3];
     for (int k = 0; k < 3; k++) {
-      h[k] = __double2float_rn(x[3 * s + k]);
-      l[k] = __double2float_rn(x[3 * s + k] - (double)h[k]);
+      f[k] = __double2float_rn(x[3 * s + k]);
+      f[4 + k] = __double2float_rn(x[3 * s + k] - (double)f[k]);
+      f[7 + k] = __double2float_rn(v[3 * s + k]);
+      f[10 + k] = __double2float_rn(la1[3 * s + k]);
+      f[13 + k] = __double2float_rn(lj1[3 * s + k]);
     }
-    r.a = make_float4(h[0], h[1], h[2], __double2float_rn(m[s]));
-    r.b = make_float4(l[0], l[1], l[2], __double2float_rn(v[3 * s]));
-    r.c = make_float4(__double2float_rn(v[3 * s + 1]), __double2float_rn(v[3 * s + 2]),
-                      __double2float_rn(la1[3 * s]), __double2float_rn(la1[3 * s + 1]));
-    r.d = make_float4(__double2float_rn(la1[3 * s + 2]), __double2float_rn(lj1[3 * s]),
-                      __double2float_rn(lj1[3 * s + 1]), __double2float_rn(lj1[3 * s + 2]));
+    f[3] = __double2float_rn(m[s]);
   } else {
-    r.a = make_float4(1.0e18f, 1.0e18f, 1.0e18f, 0.f);
-    r.b = make_float4(0.f, 0.f, 0.f, 0.f);
-    r.c = r.b;
-    r.d = r.b;
+    for (int k = 0; k < VF; k++) f[k] = 0.f;
+    f[0] = f[1] = f[2] = 1.0e18f;
   }
-  rec[s] = r;
+  float *dst = reinterpret_cast<float *>(rec + (s >> 1)) + (s & 1);
+  for (int k = 0; k < VF; k++) dst[2 * k] = f[k];
 }
 
 template <bool HJ>
-__global__ void __launch_bounds__(VT2) vjp_split_kernel(int n, float eps2, const VJRec *__restrict__ rec,
+__global__ void __launch_bounds__(VT2) vjp_split_kernel(int n, float eps2, const VJPair *__restrict__ rec,
                                                         int jsplit, int n_pad,
                                                         double *part /* [nsplit][n][7] */) {
-  __shared__ VJRec tile[VTILE];
-  float xh[VIPT][3], xl[VIPT][3], vk[VIPT][3], mk[VIPT], lak[VIPT][3], ljk[VIPT][3];
+  __shared__ VJPair tile[VTILE / 2];
+  f2x xh[VIPT][3], xl[VIPT][3], vk[VIPT][3], mk[VIPT], lak[VIPT][3], ljk[VIPT][3];
   int kk[VIPT];
 #pragma unroll
   for (int q = 0; q < VIPT; q++) {
     kk[q] = blockIdx.x * (VT2 * VIPT) + q * VT2 + threadIdx.x;
-    const VJRec r = rec[kk[q] < n_pad ? kk[q] : 0];
-    xh[q][0] = r.a.x; xh[q][1] = r.a.y; xh[q][2] = r.a.z; mk[q] = r.a.w;
-    xl[q][0] = r.b.x; xl[q][1] = r.b.y; xl[q][2] = r.b.z;
-    vk[q][0] = r.b.w; vk[q][1] = r.c.x; vk[q][2] = r.c.y;
-    lak[q][0] = r.c.z; lak[q][1] = r.c.w; lak[q][2] = r.d.x;
-    ljk[q][0] = r.d.y; ljk[q][1] = r.d.z; ljk[q][2] = r.d.w;
+    const int k = kk[q] < n_pad ? kk[q] : 0;
+    const float *src = reinterpret_cast<const float *>(rec + (k >> 1)) + (k & 1);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      xh[q][c] = f2_dup(src[2 * c]);
+      xl[q][c] = f2_dup(src[2 * (4 + c)]);
+      vk[q][c] = f2_dup(src[2 * (7 + c)]);
+      lak[q][c] = f2_dup(src[2 * (10 + c)]);
+      ljk[q][c] = f2_dup(src[2 * (13 + c)]);
+    }
+    mk[q] = f2_dup(src[2 * 3]);
   }
   double tot[VIPT][7];
 #pragma unroll
   for (int q = 0; q < VIPT; q++)
 #pragma unroll
     for (int c = 0; c < 7; c++) tot[q][c] = 0.0;
+  const f2x e2 = f2_dup(eps2);
+  const f2x m3 = f2_dup(-3.0f);
   const int j0 = blockIdx.y * jsplit;
   const int j1 = min(n_pad, j0 + jsplit);
   for (int t0 = j0; t0 < j1; t0 += VTILE) {
     __syncthreads();
-    for (int q = threadIdx.x; q < VTILE; q += VT2) tile[q] = rec[t0 + q];
+    for (int q = threadIdx.x; q < VTILE / 2; q += VT2) tile[q] = rec[t0 / 2 + q];
     __syncthreads();
-    float g[VIPT][7];
+    f2x g[VIPT][7];
 #pragma unroll
     for (int q = 0; q < VIPT; q++)
 #pragma unroll
-      for (int c = 0; c < 7; c++) g[q][c] = 0.f;
+      for (int c = 0; c < 7; c++) g[q][c] = 0ull;
 #pragma unroll 2
-    for (int jj = 0; jj < VTILE; jj++) {
-      const VJRec r = tile[jj];
-      const float laj[3] = {r.c.z, r.c.w, r.d.x}, ljj[3] = {r.d.y, r.d.z, r.d.w};
-      const float vj[3] = {r.b.w, r.c.x, r.c.y};
-      const float xhj[3] = {r.a.x, r.a.y, r.a.z}, xlj[3] = {r.b.x, r.b.y, r.b.z};
+    for (int jj = 0; jj < VTILE / 2; jj++) {
+      const VJPair &r = tile[jj];
+      f2x xhj[3], xlj[3], vj[3], laj[3], ljj[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        xhj[c] = f2_of(r.f[c]);
+        xlj[c] = f2_of(r.f[4 + c]);
+        vj[c] = f2_of(r.f[7 + c]);
+        laj[c] = f2_of(r.f[10 + c]);
+        ljj[c] = f2_of(r.f[13 + c]);
+      }
+      const f2x mj = f2_of(r.f[3]);
 #pragma unroll
       for (int q = 0; q < VIPT; q++) {
-        float R[3], V[3], lam[3], mu[3];
+        f2x R[3], V[3], lam[3], mu[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          R[c] = __fadd_rn(__fsub_rn(xhj[c], xh[q][c]), __fsub_rn(xlj[c], xl[q][c]));
-          V[c] = vj[c] - vk[q][c];
-          lam[c] = __fsub_rn(__fmul_rn(mk[q], laj[c]), __fmul_rn(r.a.w, lak[q][c]));
-          mu[c] = __fsub_rn(__fmul_rn(mk[q], ljj[c]), __fmul_rn(r.a.w, ljk[q][c]));
+          R[c] = f2_add(f2_sub(xhj[c], xh[q][c]), f2_sub(xlj[c], xl[q][c]));
+          V[c] = f2_sub(vj[c], vk[q][c]);
+          lam[c] = f2_sub(f2_mul(mk[q], laj[c]), f2_mul(mj, lak[q][c]));
+          mu[c] = f2_sub(f2_mul(mk[q], ljj[c]), f2_mul(mj, ljk[q][c]));
         }
-        const float s = fmaf(R[2], R[2], fmaf(R[1], R[1], fmaf(R[0], R[0], eps2)));
-        const float s1 = rsqrt_approx(s);
-        const float si = s1 * s1;
-        const float s3 = s1 * si, s5 = s3 * si;
-        const float rl = fmaf(R[2], lam[2], fmaf(R[1], lam[1], R[0] * lam[0]));
-        const float rm = fmaf(R[2], mu[2], fmaf(R[1], mu[1], R[0] * mu[0]));
-        const float vm = fmaf(V[2], mu[2], fmaf(V[1], mu[1], V[0] * mu[0]));
-        const float rv = fmaf(R[2], V[2], fmaf(R[1], V[1], R[0] * V[0]));
-        float qs, c7;
+        const f2x s = f2_fma(R[2], R[2], f2_fma(R[1], R[1], f2_fma(R[0], R[0], e2)));
+        float sa, sb;
+        f2_unpack(s, sa, sb);
+        const f2x s1 = f2_pack(rsqrt_approx(sa), rsqrt_approx(sb));
+        const f2x si = f2_mul(s1, s1);
+        const f2x s3 = f2_mul(s1, si), s5 = f2_mul(s3, si);
+        const f2x rl = f2_fma(R[2], lam[2], f2_fma(R[1], lam[1], f2_mul(R[0], lam[0])));
+        const f2x rm = f2_fma(R[2], mu[2], f2_fma(R[1], mu[1], f2_mul(R[0], mu[0])));
+        const f2x vm = f2_fma(V[2], mu[2], f2_fma(V[1], mu[1], f2_mul(V[0], mu[0])));
+        const f2x rv = f2_fma(R[2], V[2], f2_fma(R[1], V[1], f2_mul(R[0], V[0])));
+        f2x qs, c7;
         if (HJ) {
-          const float r2u = fmaf(R[2], R[2], fmaf(R[1], R[1], R[0] * R[0]));
-          const float qi = r2u > 0.f ? rcp_approx(r2u) : 0.f;
-          qs = qi * s3;
-          c7 = qi * fmaf(6.0f, qs, 9.0f * s5);
+          const f2x r2u = f2_fma(R[2], R[2], f2_fma(R[1], R[1], f2_mul(R[0], R[0])));
+          float ua, ub;
+          f2_unpack(r2u, ua, ub);
+          const f2x qi = f2_pack(ua > 0.f ? rcp_approx(ua) : 0.f, ub > 0.f ? rcp_approx(ub) : 0.f);
+          qs = f2_mul(qi, s3);
+          c7 = f2_mul(qi, f2_fma(f2_dup(6.0f), qs, f2_mul(f2_dup(9.0f), s5)));
         } else {
           qs = s5;
-          c7 = 15.0f * (s5 * si);
+          c7 = f2_mul(f2_dup(15.0f), f2_mul(s5, si));
         }
-        const float q3 = -3.0f * qs;
-        const float cr = fmaf(rv * rm, c7, -3.0f * (rl + vm) * s5);
-        const float w = q3 * rm;
+        const f2x q3 = f2_mul(m3, qs);
+        const f2x cr = f2_fma(f2_mul(rv, rm), c7, f2_mul(m3, f2_mul(f2_add(rl, vm), s5)));
+        const f2x w = f2_mul(q3, rm);
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          const float u = fmaf(rm, V[c], rv * mu[c]);
-          g[q][c] = fmaf(q3, u, fmaf(cr, R[c], fmaf(lam[c], s3, g[q][c])));
-          g[q][3 + c] = fmaf(w, R[c], fmaf(mu[c], s3, g[q][3 + c]));
+          const f2x u = f2_fma(rm, V[c], f2_mul(rv, mu[c]));
+          g[q][c] = f2_fma(q3, u, f2_fma(cr, R[c], f2_fma(lam[c], s3, g[q][c])));
+          g[q][3 + c] = f2_fma(w, R[c], f2_fma(mu[c], s3, g[q][3 + c]));
         }
-        const float ga = fmaf(laj[2], R[2], fmaf(laj[1], R[1], laj[0] * R[0]));
-        const float lv = fmaf(ljj[2], V[2], fmaf(ljj[1], V[1], ljj[0] * V[0]));
-        const float lr = fmaf(ljj[2], R[2], fmaf(ljj[1], R[1], ljj[0] * R[0]));
-        g[q][6] -= fmaf(ga + lv, s3, q3 * rv * lr);
+        const f2x ga = f2_fma(laj[2], R[2], f2_fma(laj[1], R[1], f2_mul(laj[0], R[0])));
+        const f2x lv = f2_fma(ljj[2], V[2], f2_fma(ljj[1], V[1], f2_mul(ljj[0], V[0])));
+        const f2x lr = f2_fma(ljj[2], R[2], f2_fma(ljj[1], R[1], f2_mul(ljj[0], R[0])));
+        g[q][6] = f2_sub(g[q][6], f2_fma(f2_add(ga, lv), s3, f2_mul(f2_mul(q3, rv), lr)));
       }
     }
 #pragma unroll
     for (int q = 0; q < VIPT; q++)
 #pragma unroll
-      for (int c = 0; c < 7; c++) tot[q][c] += (double)g[q][c];
+      for (int c = 0; c < 7; c++) {
+        float lo, hi;
+        f2_unpack(g[q][c], lo, hi);
+        tot[q][c] += (double)lo + (double)hi;
+      }
   }
 #pragma unroll
   for (int q = 0; q < VIPT; q++) {
@@ -462,7 +518,7 @@ extern "C" size_t g6k_vjp_scratch_bytes(int n) {
   for (int prec = 0; prec < 2; prec++) {
     int ns, js, np;
     vjp_shape(n, prec, &ns, &js, &np);
-    const size_t b = (size_t)np * sizeof(VJRec) + (size_t)ns * (size_t)n * 7 * sizeof(double);
+    const size_t b = (size_t)np * (sizeof(VJPair) / 2) + (size_t)ns * (size_t)n * 7 * sizeof(double);
     if (b > need) need = b;
   }
   return need;
@@ -477,9 +533,9 @@ extern "C" int g6k_force_vjp(int n, double eps2, int prec, int hjerk, const doub
   if (n <= 0) return 0;
   int nsplit, jsplit, n_pad;
   vjp_shape(n, prec, &nsplit, &jsplit, &n_pad);
-  VJRec *rec = reinterpret_cast<VJRec *>(scratch);
+  VJPair *rec = reinterpret_cast<VJPair *>(scratch);
   double *part = reinterpret_cast<double *>(reinterpret_cast<char *>(scratch) +
-                                            (size_t)n_pad * sizeof(VJRec));
+                                            (size_t)n_pad * (sizeof(VJPair) / 2));
   if (prec == G6_PREC_FP64) {
     dim3 grid((n + VT - 1) / VT, nsplit);
 #define G6_VJP(H) vjp_f64_kernel<H><<<grid, VT, 0, st>>>(n, eps2, x, v, m, la1, lj1, jsplit, part)

@@ -176,13 +176,15 @@ def run_adjoint(args):
             rel.append(abs(fd - g_ad) / scale)
         return rel
 
-    t0 = time.perf_counter()
-    rs = fd_errors("split", coords)
-    out["fd_split"] = {"coords": len(coords), "h": h, "max_rel": float(max(rs)),
-                       "median_rel": float(np.median(rs)), "n_above_1e-4": int(sum(r > 1e-4 for r in rs)),
-                       "seconds": time.perf_counter() - t0}
-    print(json.dumps(out), flush=True)
-    if args.fd64_coords > 0:
+    if coords:
+        t0 = time.perf_counter()
+        rs = fd_errors("split", coords)
+        out["fd_split"] = {"coords": len(coords), "h": h, "max_rel": float(max(rs)),
+                           "median_rel": float(np.median(rs)),
+                           "n_above_1e-4": int(sum(r > 1e-4 for r in rs)),
+                           "seconds": time.perf_counter() - t0}
+        print(json.dumps(out), flush=True)
+    if args.fd64_coords > 0 and coords:
         t0 = time.perf_counter()
         rd = fd_errors("fp64", coords[: args.fd64_coords])
         out["fd_fp64"] = {"coords": len(rd), "h": h, "max_rel": float(max(rd)),

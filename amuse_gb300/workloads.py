@@ -145,7 +145,14 @@ def run_adjoint(args):
                                   checkpoint=nsteps, precision=prec)
             return float((tw * (xf * xf).sum(1)).sum())
 
-    hermite_fixed(base[0], base[1], base[2], eps2=eps2, dt=dt, nsteps=2, precision="split")
+    # warm-up: first forward and backward (library buffers, autograd's device
+    # threads), outside the timed calls
+    for prec in ("split", "fp64"):
+        w0 = [t[:256].clone().requires_grad_(True) for t in base]
+        xw, _ = hermite_fixed(w0[0], w0[1], w0[2], eps2=eps2, dt=dt, nsteps=2, checkpoint=1,
+                              precision=prec)
+        (xw * xw).sum().backward()
+    torch.cuda.synchronize()
     ls, gs, fs, bs = grad("split")
     pairs_fwd = (nsteps + 1) * n * (n - 1)
     out["split"] = {"loss": ls, "forward_s": fs, "backward_s": bs,

@@ -82,9 +82,6 @@ def parse():
     return ap.parse_args()
 
 
-def dist_env():
-    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
-            int(os.environ.get("LOCAL_RANK", 0)))
 
 
 def workload(n):
@@ -179,7 +176,8 @@ def cpu_baseline(mass, pos, vel, seconds, threads):
 
 
 def run_reference(args):
-    rank, world, _ = dist_env()
+    from amuse_gb300 import replicas
+    rank, world, _ = replicas.env()
     if rank != 0:
         return 0
     mass, pos, vel = workload(args.n)
@@ -212,10 +210,9 @@ def run_ours(args):
     import amuse_gb300 as ag
     from amuse_gb300 import build as b
 
-    rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    from amuse_gb300 import replicas
+    rank, world, local = replicas.env()
+    replicas.init("nccl")
     torch.cuda.set_device(local)
     b.build()
     n = args.n
@@ -238,8 +235,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         one_step()
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     sampler = ClockSampler(local)
     sampler.start()
     g6.timing(True)
@@ -262,16 +258,11 @@ def run_ours(args):
     torch.cuda.synchronize()
     g6.timing(False)
     clocks = sampler.stop()
-    if world > 1:
-        tt = torch.tensor([sum(times)], device=f"cuda:{local}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total = float(tt.item())
-    else:
-        total = sum(times)
+    total = replicas.max_over_ranks(sum(times), device=f"cuda:{local}")
     k1, u1 = g6.energy()
     e1 = k1 + u1
     pairs_step = n * (n - 1)
-    value = world * args.steps * pairs_step / total
+    value = replicas.whole_job_rate(args.steps * pairs_step, world, total)
     force_s = statistics.mean(fms) / 1e3
     achieved = FLOP_PER_PAIR * pairs_step / force_s / 1e12
     pk = peaks()
@@ -379,8 +370,7 @@ def run_ours(args):
             "gpu_launches": launches,
         }
         print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finalize()
     return 0
 
 

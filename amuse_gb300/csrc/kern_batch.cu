@@ -138,8 +138,13 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 // step^2.  FP32 unless the pair is closer than 1e-9 (d^2 < 1e-18): there
 // m / d^3 times a relative velocity ~ sqrt(M / d) can leave the FP32 range,
 // so such (rare) pairs are evaluated in FP64 into separate accumulators.
+// The pair j == i (self) is evaluated too, with its contribution masked to
+// zero and its step to +inf, so the j loop has no divergent skip.  The step
+// quotients use the approximate division (split mode is not bit-exact with
+// anything, and the step only has to follow the criterion closely).
 __device__ __forceinline__ float pair_split(const WarpSmem &S, int i, int j, float acc[3],
                                             float jerk[3], double accd[3], double jerkd[3]) {
+  const bool self = j == i;
   float dx[3], dv[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
@@ -149,8 +154,8 @@ __device__ __forceinline__ float pair_split(const WarpSmem &S, int i, int j, flo
   const float d2 = fmaf(dx[2], dx[2], fmaf(dx[1], dx[1], dx[0] * dx[0]));
   const float v2 = fmaf(dv[2], dv[2], fmaf(dv[1], dv[1], dv[0] * dv[0]));
   const float mt = S.mf[i] + S.mf[j];
-  if (d2 >= 1e-18f) {
-    const float rinv = rsqrt_approx(d2);
+  if (self || d2 >= 1e-18f) {
+    const float rinv = self ? 0.f : rsqrt_approx(d2);
     const float rinv2 = rinv * rinv;
     const float f = S.mf[j] * rinv * rinv2;
     const float xv = fmaf(dx[2], dv[2], fmaf(dx[1], dv[1], dx[0] * dv[0]));
@@ -160,7 +165,8 @@ __device__ __forceinline__ float pair_split(const WarpSmem &S, int i, int j, flo
       acc[k] = fmaf(f, dx[k], acc[k]);
       jerk[k] = fmaf(f, fmaf(a3, dx[k], dv[k]), jerk[k]);
     }
-    return fminf(0.5f * d2 * (d2 * rinv) / mt, d2 / v2);
+    const float ts = fminf(__fdividef(0.5f * d2 * (d2 * rinv), mt), __fdividef(d2, v2));
+    return self ? __int_as_float(0x7f800000) : ts;
   }
   double X[3], W[3];
 #pragma unroll
@@ -198,10 +204,7 @@ __device__ double forces(const WarpSmem &S, int n, int lane, Body B[2]) {
       float a[3] = {0.f, 0.f, 0.f}, jk[3] = {0.f, 0.f, 0.f};
       double ad[3] = {0.0, 0.0, 0.0}, jd[3] = {0.0, 0.0, 0.0};
       float m2 = __int_as_float(0x7f800000);
-      for (int j = 0; j < n; j++) {
-        if (j == i) continue;
-        m2 = fminf(m2, pair_split(S, i, j, a, jk, ad, jd));
-      }
+      for (int j = 0; j < n; j++) m2 = fminf(m2, pair_split(S, i, j, a, jk, ad, jd));
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         B[q].acc[k] = (double)a[k] + ad[k];

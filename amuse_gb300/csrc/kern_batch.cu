@@ -53,16 +53,14 @@ struct WarpSmem {
       double pp[MAXN][3];
       double pv[MAXN][3];
     } d;
-    struct {  // MODE_SPLIT: double-single positions, FP32 velocities,
-              // component-major so that bodies j, j+1 load as one float2;
-              // index n of an odd-n system is a massless body far away
-      float ph[3][MAXN + 2];
-      float pl[3][MAXN + 2];
-      float vf[3][MAXN + 2];
+    struct {  // MODE_SPLIT: double-single positions, FP32 velocities
+      float ph[MAXN][3];
+      float pl[MAXN][3];
+      float vf[MAXN][3];
     } f;
   };
   double m[MAXN];
-  float mf[MAXN + 2];
+  float mf[MAXN];
 };
 
 // 1/sqrt(x): FP32 MUFU seed, two Newton-Raphson steps.
@@ -136,41 +134,6 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
   return y;
 }
 
-// Packed f32x2: two floats in one 64-bit register pair, each op the IEEE
-// round-to-nearest scalar op on both halves.
-typedef unsigned long long f2x;
-__device__ __forceinline__ f2x f2_add(f2x a, f2x b) {
-  f2x d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
-  f2x d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2x f2_mul(f2x a, f2x b) {
-  f2x d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c) {
-  f2x d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ f2x f2_pack(float lo, float hi) {
-  f2x r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void f2_unpack(f2x v, float &lo, float &hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f2x f2_ld(const float *p) {  // p 8-byte aligned
-  return *reinterpret_cast<const f2x *>(p);
-}
-
 // MODE_SPLIT pair term: contribution of j to body i, and the pair's Kepler
 // step^2.  FP32 unless the pair is closer than 1e-9 (d^2 < 1e-18): there
 // m / d^3 times a relative velocity ~ sqrt(M / d) can leave the FP32 range,
@@ -185,8 +148,8 @@ __device__ __forceinline__ float pair_split(const WarpSmem &S, int i, int j, flo
   float dx[3], dv[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    dx[k] = __fadd_rn(__fsub_rn(S.f.ph[k][j], S.f.ph[k][i]), __fsub_rn(S.f.pl[k][j], S.f.pl[k][i]));
-    dv[k] = S.f.vf[k][j] - S.f.vf[k][i];
+    dx[k] = __fadd_rn(__fsub_rn(S.f.ph[j][k], S.f.ph[i][k]), __fsub_rn(S.f.pl[j][k], S.f.pl[i][k]));
+    dv[k] = S.f.vf[j][k] - S.f.vf[i][k];
   }
   const float d2 = fmaf(dx[2], dx[2], fmaf(dx[1], dx[1], dx[0] * dx[0]));
   const float v2 = fmaf(dv[2], dv[2], fmaf(dv[1], dv[1], dv[0] * dv[0]));
@@ -238,69 +201,14 @@ __device__ double forces(const WarpSmem &S, int n, int lane, Body B[2]) {
     for (int k = 0; k < 3; k++) B[q].acc[k] = B[q].jerk[k] = 0.0;
     if (i >= n) continue;
     if (MODE == MODE_SPLIT) {
-      // bodies j, j+1 per packed instruction; a pair with a close member
-      // (d^2 < 1e-18, see pair_split) goes through the scalar path instead
       float a[3] = {0.f, 0.f, 0.f}, jk[3] = {0.f, 0.f, 0.f};
       double ad[3] = {0.0, 0.0, 0.0}, jd[3] = {0.0, 0.0, 0.0};
-      f2x pa[3] = {0ull, 0ull, 0ull}, pj[3] = {0ull, 0ull, 0ull};
-      f2x phi[3], pli[3], vfi[3];
+      float m2 = __int_as_float(0x7f800000);
+      for (int j = 0; j < n; j++) m2 = fminf(m2, pair_split(S, i, j, a, jk, ad, jd));
 #pragma unroll
       for (int k = 0; k < 3; k++) {
-        phi[k] = f2_pack(S.f.ph[k][i], S.f.ph[k][i]);
-        pli[k] = f2_pack(S.f.pl[k][i], S.f.pl[k][i]);
-        vfi[k] = f2_pack(S.f.vf[k][i], S.f.vf[k][i]);
-      }
-      const f2x mfi = f2_pack(S.mf[i], S.mf[i]);
-      const f2x m3 = f2_pack(-3.0f, -3.0f), half = f2_pack(0.5f, 0.5f);
-      const float inf = __int_as_float(0x7f800000);
-      float m2 = inf;
-      for (int jp = 0; jp < n; jp += 2) {
-        f2x dx[3], dv[3];
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          dx[k] = f2_add(f2_sub(f2_ld(&S.f.ph[k][jp]), phi[k]),
-                         f2_sub(f2_ld(&S.f.pl[k][jp]), pli[k]));
-          dv[k] = f2_sub(f2_ld(&S.f.vf[k][jp]), vfi[k]);
-        }
-        const f2x d2 = f2_fma(dx[2], dx[2], f2_fma(dx[1], dx[1], f2_mul(dx[0], dx[0])));
-        float d2a, d2b;
-        f2_unpack(d2, d2a, d2b);
-        const bool sa = jp == i, sb = jp + 1 == i;
-        if ((!sa && d2a < 1e-18f) || (!sb && d2b < 1e-18f)) {
-          m2 = fminf(m2, pair_split(S, i, jp, a, jk, ad, jd));
-          m2 = fminf(m2, pair_split(S, i, jp + 1, a, jk, ad, jd));
-          continue;
-        }
-        const float ra = sa ? 0.f : rsqrt_approx(d2a), rb = sb ? 0.f : rsqrt_approx(d2b);
-        const f2x rinv = f2_pack(ra, rb);
-        const f2x rinv2 = f2_mul(rinv, rinv);
-        const f2x mfj = f2_ld(&S.mf[jp]);
-        const f2x f = f2_mul(f2_mul(mfj, rinv), rinv2);
-        const f2x xv = f2_fma(dx[2], dv[2], f2_fma(dx[1], dv[1], f2_mul(dx[0], dv[0])));
-        const f2x a3 = f2_mul(m3, f2_mul(xv, rinv2));
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          pa[k] = f2_fma(f, dx[k], pa[k]);
-          pj[k] = f2_fma(f, f2_fma(a3, dx[k], dv[k]), pj[k]);
-        }
-        const f2x v2 = f2_fma(dv[2], dv[2], f2_fma(dv[1], dv[1], f2_mul(dv[0], dv[0])));
-        const f2x mt = f2_add(mfi, mfj);
-        const f2x d3h = f2_mul(f2_mul(half, d2), f2_mul(d2, rinv));  // d^3 / 2
-        float na, nb, ma, mb, va, vb;
-        f2_unpack(d3h, na, nb);
-        f2_unpack(mt, ma, mb);
-        f2_unpack(v2, va, vb);
-        const float ta = sa ? inf : fminf(__fdividef(na, ma), __fdividef(d2a, va));
-        const float tb = sb ? inf : fminf(__fdividef(nb, mb), __fdividef(d2b, vb));
-        m2 = fminf(m2, fminf(ta, tb));
-      }
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        float lo, hi, jlo, jhi;
-        f2_unpack(pa[k], lo, hi);
-        f2_unpack(pj[k], jlo, jhi);
-        B[q].acc[k] = ((double)a[k] + (double)lo + (double)hi) + ad[k];
-        B[q].jerk[k] = ((double)jk[k] + (double)jlo + (double)jhi) + jd[k];
+        B[q].acc[k] = (double)a[k] + ad[k];
+        B[q].jerk[k] = (double)jk[k] + jd[k];
       }
       ts2 = fmin(ts2, (double)m2);
     } else if (EXACT) {
@@ -334,9 +242,9 @@ __device__ __forceinline__ void publish(WarpSmem &S, int n, int lane, const Body
       for (int k = 0; k < 3; k++) {
         if (MODE == MODE_SPLIT) {
           const float h = __double2float_rn(B[q].pp[k]);
-          S.f.ph[k][i] = h;
-          S.f.pl[k][i] = __double2float_rn(B[q].pp[k] - (double)h);
-          S.f.vf[k][i] = __double2float_rn(B[q].pv[k]);
+          S.f.ph[i][k] = h;
+          S.f.pl[i][k] = __double2float_rn(B[q].pp[k] - (double)h);
+          S.f.vf[i][k] = __double2float_rn(B[q].pv[k]);
         } else {
           S.d.pp[i][k] = B[q].pp[k];
           S.d.pv[i][k] = B[q].pv[k];
@@ -396,15 +304,6 @@ __global__ void batch_kernel(int nsys, const int *__restrict__ order, const int 
         S.m[i] = B[qq].m;
         S.mf[i] = __double2float_rn(B[qq].m);
       }
-    }
-    if (MODE == MODE_SPLIT && lane == 0 && (n & 1)) {  // the pad body of an odd n
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        S.f.ph[k][n] = 1.0e18f;
-        S.f.pl[k][n] = 0.f;
-        S.f.vf[k][n] = 0.f;
-      }
-      S.mf[n] = 0.f;
     }
     publish<MODE>(S, n, lane, B);
     double t = 0.0, t_pred = -1.0;

@@ -51,46 +51,73 @@ __device__ __forceinline__ bool multiple_of_pow2(double t, double p) {
   return e + tz >= pe - 1023;
 }
 
+// Four lanes per particle: lane k < 3 corrects component k (the divides of
+// the three components run in parallel, which is what bounds a small block's
+// latency), and the squared norms are summed in component order after a
+// shuffle, exactly as the scalar loop adds them, so the result stays
+// bit-identical with ph4.  Lane 3 only takes part in the shuffles.
 __global__ void correct_kernel(g6_jstate js, int ni, const int *__restrict__ ilist, double tnext,
                                double eta, const double *__restrict__ acc,
                                const double *__restrict__ jerk, const double *__restrict__ pot,
                                const int *__restrict__ nn) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ni) return;
-  const int s = ilist[i];
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = g >> 2;
+  const int k = g & 3;
+  const int lane = threadIdx.x & 31;
+  const int base = lane & ~3;
+  const bool active = i < ni;  // whole groups of 4 agree
+  const int ii = active ? i : 0;
+  const int s = ilist[ii];
   const int cap = js.cap;
   const double t0 = js.t[s];
   const double dt = dsub(tnext, t0);
   const double dt2 = dmul(dt, dt);
-  double xp[3], vp[3];
-  double a2 = 0, j2 = 0, k2 = 0, l2 = 0;
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const double x = js.x[k * cap + s], v = js.v[k * cap + s];
-    const double oa = js.a[k * cap + s], oj = js.j[k * cap + s];
+  const int kc = k < 3 ? k : 2;
+  double xp, vp, pa2 = 0, pj2 = 0, pk2 = 0, pl2 = 0;
+  {
+    const double x = js.x[kc * cap + s], v = js.v[kc * cap + s];
+    const double oa = js.a[kc * cap + s], oj = js.j[kc * cap + s];
     if (dt == 0) {
-      xp[k] = x;
-      vp[k] = v;
+      xp = x;
+      vp = v;
     } else {
       // x + dt*(v + 0.5*dt*(a + dt*j/3)),  v + dt*(a + 0.5*dt*j)
       const double hdt = dmul(0.5, dt);
-      xp[k] = dadd(x, dmul(dt, dadd(v, dmul(hdt, dadd(oa, ddiv(dmul(dt, oj), 3.0))))));
-      vp[k] = dadd(v, dmul(dt, dadd(oa, dmul(hdt, oj))));
+      xp = dadd(x, dmul(dt, dadd(v, dmul(hdt, dadd(oa, ddiv(dmul(dt, oj), 3.0))))));
+      vp = dadd(v, dmul(dt, dadd(oa, dmul(hdt, oj))));
     }
-    const double ia = acc[3 * i + k], ij = jerk[3 * i + k];
+    const double ia = acc[3 * ii + kc], ij = jerk[3 * ii + kc];
     const double da = dsub(oa, ia);
     const double alpha = dsub(dmul(-3.0, da), dmul(dt, dadd(dmul(2.0, oj), ij)));
     const double beta = dadd(dmul(2.0, da), dmul(dt, dadd(oj, ij)));
-    xp[k] = dadd(xp[k], dmul(dadd(ddiv(alpha, 12.0), ddiv(beta, 20.0)), dt2));
-    vp[k] = dadd(vp[k], dmul(dadd(ddiv(alpha, 3.0), ddiv(beta, 4.0)), dt));
-    a2 = dadd(a2, dmul(ia, ia));
+    xp = dadd(xp, dmul(dadd(ddiv(alpha, 12.0), ddiv(beta, 20.0)), dt2));
+    vp = dadd(vp, dmul(dadd(ddiv(alpha, 3.0), ddiv(beta, 4.0)), dt));
+    pa2 = dmul(ia, ia);
     const double dj = dmul(dt, ij);
-    j2 = dadd(j2, dmul(dj, dj));
+    pj2 = dmul(dj, dj);
     const double ak = dmul(2.0, alpha);
-    k2 = dadd(k2, dmul(ak, ak));
+    pk2 = dmul(ak, ak);
     const double bl = dmul(6.0, beta);
-    l2 = dadd(l2, dmul(bl, bl));
+    pl2 = dmul(bl, bl);
   }
+  // a2 = ((0 + p0) + p1) + p2, as the scalar component loop accumulates
+  double a2 = 0, j2 = 0, k2 = 0, l2 = 0;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    a2 = dadd(a2, __shfl_sync(0xffffffffu, pa2, base + c));
+    j2 = dadd(j2, __shfl_sync(0xffffffffu, pj2, base + c));
+    k2 = dadd(k2, __shfl_sync(0xffffffffu, pk2, base + c));
+    l2 = dadd(l2, __shfl_sync(0xffffffffu, pl2, base + c));
+  }
+  if (!active) return;
+  if (k < 3) {
+    js.x[k * cap + s] = xp;
+    js.v[k * cap + s] = vp;
+    js.a[k * cap + s] = acc[3 * i + k];
+    js.j[k * cap + s] = jerk[3 * i + k];
+    return;
+  }
+  // lane 3: the Aarseth step with power-of-two quantisation
   double newstep = dmul(dmul(eta, dt),
                         __dsqrt_rn(ddiv(dadd(__dsqrt_rn(dmul(a2, k2)), j2),
                                         dadd(__dsqrt_rn(dmul(j2, l2)), k2))));
@@ -107,13 +134,6 @@ __global__ void correct_kernel(g6_jstate js, int ni, const int *__restrict__ ili
       newstep = t2;
     else
       newstep = oldstep2;
-  }
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    js.x[k * cap + s] = xp[k];
-    js.v[k * cap + s] = vp[k];
-    js.a[k * cap + s] = acc[3 * i + k];
-    js.j[k * cap + s] = jerk[3 * i + k];
   }
   js.t[s] = tnext;
   js.dt[s] = newstep;
@@ -265,7 +285,8 @@ extern "C" int g6k_correct(const g6_jstate *js, int ni, const int *ilist, double
                            double eta, const double *acc, const double *jerk, const double *pot,
                            const int *nn, cudaStream_t st) {
   if (ni <= 0) return 0;
-  correct_kernel<<<(ni + 127) / 128, 128, 0, st>>>(*js, ni, ilist, tnext, eta, acc, jerk, pot, nn);
+  // 4 lanes per particle, 32 particles per 128-thread block
+  correct_kernel<<<(ni + 31) / 32, 128, 0, st>>>(*js, ni, ilist, tnext, eta, acc, jerk, pot, nn);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

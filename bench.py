@@ -51,6 +51,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FLOP_PER_PAIR = 60.0
+# DRAM bytes (read + write) of one force launch at the default N = 2^20, from
+# one ncu capture of this benchmark (profiles/force_kernel_dram_n1048576.md).
+FORCE_TRAFFIC_N = 1 << 20
+FORCE_TRAFFIC_BYTES = 75132672 + 47213568
 N_DEFAULT = 1 << 20
 EPS2 = 1e-6
 ETA = 0.01
@@ -356,8 +360,11 @@ def run_ours(args):
                         "sample": f"{nsub2} i x {n} j, nearest neighbour on (g6calc_lasthalf2)",
                         "frac_fp32": FLOP_PER_PAIR * nn_rate / 1e12 / fp32_peak},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
-                         "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
-                         "kernel": "force_kernel<SplitP,1,false>",
+                         "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                         "traffic": FORCE_TRAFFIC_BYTES if n == FORCE_TRAFFIC_N else None,
+                         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + "
+                                         "dram__bytes_write.sum, one capture at N = 2^20)",
+                         "kernel": "force_kernel<SplitP,1,false> (packed f32x2)",
                          "peak_source": f"{nsm} SMs x 128 FP32 lanes x 2 flop x {sm_max:.0f} MHz "
                                         "(sm_max_mhz, MEASURED_PEAKS.json; it holds no FP32 figure)",
                          "flop_per_pair": FLOP_PER_PAIR, "force_ms": 1e3 * force_s},

@@ -439,10 +439,17 @@ int g6_open_(int *id) {
   return 0;
 }
 
+static void ngb_free(void);
+static void batch_free(void);
+static void fixed_free(void);
+
 int g6_close_(int *id) {
   (void)id;
   if (!G.is_open) return 0;
   cudaStreamSynchronize(G.st);
+  ngb_free();
+  batch_free();
+  fixed_free();
   free_jstate(&G.js);
   if (G.h_upd) cudaFreeHost(G.h_upd);
   if (G.h_in) cudaFreeHost(G.h_in);
@@ -752,6 +759,14 @@ int g6_reset_fofpga_(int *cluster_id) { (void)cluster_id; return 0; }
    excluded), so the force kernel carries no list logic. */
 static int *h_ngb, *d_ngb;
 static int ngb_cap, ngb_ni, ngb_valid;
+
+static void ngb_free(void) {
+  if (h_ngb) cudaFreeHost(h_ngb);
+  cudaFree(d_ngb);
+  h_ngb = NULL;
+  d_ngb = NULL;
+  ngb_cap = ngb_ni = ngb_valid = 0;
+}
 
 int g6_read_neighbour_list_(int *cluster_id) {
   (void)cluster_id;
@@ -1406,6 +1421,17 @@ static struct {
 } BT = {0, 0, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, 4, 2,
         NULL, 0, 0, 0, 0, 0, 0.0, 0, NULL};
 
+static void batch_free(void) {
+  cudaFree(BT.d_order); cudaFree(BT.d_off); cudaFree(BT.d_queue); cudaFree(BT.d_status);
+  cudaFree(BT.d_tend); cudaFree(BT.d_mass); cudaFree(BT.d_pos); cudaFree(BT.d_vel);
+  cudaFree(BT.d_tout); cudaFree(BT.d_steps); cudaFree(BT.d_wall);
+  if (BT.gexec) cudaGraphExecDestroy(BT.gexec);
+  const int wpc = BT.wpc, cps = BT.cps;
+  memset(&BT, 0, sizeof(BT));
+  BT.wpc = wpc;
+  BT.cps = cps;
+}
+
 static int batch_ensure(int nsys, int nbody) {
   if (nsys > BT.cap_sys) {
     cudaFree(BT.d_order); cudaFree(BT.d_off); cudaFree(BT.d_tend); cudaFree(BT.d_tout);
@@ -1652,6 +1678,14 @@ static void *fx_part;
 static size_t fx_part_bytes;
 static int fx_cap;
 static int fx_form = G6_JERK_HERMITE;
+
+static void fixed_free(void) {
+  cudaFree(fx_a1); cudaFree(fx_j1); cudaFree(fx_xp); cudaFree(fx_vp); cudaFree(fx_part);
+  fx_a1 = fx_j1 = fx_xp = fx_vp = NULL;
+  fx_part = NULL;
+  fx_cap = 0;
+  fx_part_bytes = 0;
+}
 
 int g6x_set_fixed_jerk(int form) {
   if (form != G6_JERK_HERMITE && form != G6_JERK_SOFTENED) return G6_ERR_ARG;

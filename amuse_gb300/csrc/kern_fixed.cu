@@ -497,10 +497,14 @@ static void vjp_shape(int n, int prec, int *nsplit, int *jsplit, int *n_pad) {
     *jsplit = (n + *nsplit - 1) / *nsplit;
     return;
   }
-  int sms = 0, dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
-    sms = 152;
+  static int sms = 0;  // SM count of the (single) device, looked up once
+  if (sms <= 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms <= 0)
+      sms = 152;
+  }
   const int gx = (n + VT2 * VIPT - 1) / (VT2 * VIPT);
   const int tiles = *n_pad / VTILE;
   int ns = (4 * sms + gx - 1) / gx;

@@ -124,3 +124,24 @@ def test_fixed_step_rejects_bad_inputs(g6):
     with pytest.raises(ValueError):
         hermite_fixed(xd, xd, torch.ones(4, device="cuda", dtype=torch.float64), eps2=0.0,
                       dt=0.1, nsteps=0)
+
+
+def test_close_and_reopen(g6):
+    """g6_close_ releases every buffer (j-store, batch, fixed-step,
+    neighbour lists); a new g6_open_ gives a working context again."""
+    from amuse_gb300.adjoint import hermite_fixed
+    rng = np.random.RandomState(31)
+    m, x, v = ic.plummer(64, do_scale=True, rng=rng)
+    ids = np.arange(1, 65)
+    ag.drive_load(m, x, v, ids=ids)
+    before = ag.drive_force(64, 0.0, 1e-4, ids, x, v)
+    g6.close()
+    ag.G6X(0)  # g6_open_ again
+    ag.drive_load(m, x, v, ids=ids)
+    after = ag.drive_force(64, 0.0, 1e-4, ids, x, v)
+    np.testing.assert_array_equal(before["acc"], after["acc"])
+    r = g6.batch_run([5], 1e-5, m[:5], x[:5] * 1e-3, v[:5] / np.sqrt(1e-3), exact=True)
+    assert r["status"][0] == 0
+    t = [torch.tensor(a, device="cuda") for a in (x, v, m)]
+    xf, _ = hermite_fixed(t[0], t[1], t[2], eps2=1e-4, dt=1 / 256, nsteps=2)
+    assert torch.isfinite(xf).all()

@@ -218,7 +218,9 @@ def run_ours(args):
     rank, world, local = replicas.env()
     replicas.init("nccl")
     torch.cuda.set_device(local)
-    b.build()
+    if local == 0:
+        b.build()  # one builder per node; the other ranks wait for it
+    replicas.barrier()
     n = args.n
     mass, pos, vel = workload(n)
     g6 = ag.G6X(local)

@@ -603,16 +603,6 @@ struct KParams {
   int dev_slots;  // resident CTAs of the whole GPU (the split target)
 };
 
-// Device-shaped launches come in three j-lane classes, all launched for each
-// block step; the CTAs of the two classes that do not fit ni exit at once.
-// JL = 128 for tiny blocks (ni <= 4 CTA i-slots), JL = 16 for small ones
-// (ni <= 16 CTA i-slots), JL = 1 otherwise.
-__host__ __device__ __forceinline__ int dev_jl(int ni, int ipt) {
-  if (ni <= 4 * ipt) return 128;
-  if (ni <= 16 * (128 / 16) * ipt) return 16;
-  return 1;
-}
-
 // The device-shaped launch's shape for ni i-particles in CTAs of islots:
 // gx i-chunks times nsplit j-ranges of jsplit j, about dev_slots CTAs in all.
 __device__ __forceinline__ void dev_shape(const KParams &kp, int islots, int ni, int &gx,
@@ -656,7 +646,6 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   if (kp.d_ni) {
     ni = *kp.d_ni;
     ni_pad = ni;
-    if (dev_jl(ni, IPT) != JL) return;  // another class runs this block (uniform for the CTA)
     int gx;
     dev_shape(kp, ISLOTS, ni, gx, nsplit, jsplit);
     if ((int)blockIdx.x >= gx * nsplit) return;  // uniform for the CTA, before any barrier
@@ -938,9 +927,8 @@ __global__ void reduce_warp_kernel(KParams kp) {
 // on the device as in the force kernel; one warp per i, grid-stride (the
 // grid is fixed), nothing to do when the launch needed a single split.
 template <class P>
-__global__ void reduce_dev_kernel(KParams kp) {
+__global__ void reduce_dev_kernel(KParams kp, int islots) {
   const int ni = *kp.d_ni;
-  const int islots = (NT / dev_jl(ni, P::IPT)) * P::IPT;
   int gx, nsplit, jsplit;
   dev_shape(kp, islots, ni, gx, nsplit, jsplit);
   if (nsplit <= 1) return;
@@ -1170,23 +1158,17 @@ extern "C" int g6k_force_dev_shaped(const g6_force_args *a, const int *d_ni, int
   kp.err = a->err;
   kp.d_ni = d_ni;
   kp.dev_slots = dev_slots(a->prec);
-  // grids: JL = 1 covers up to ni_max; the small classes' work items never
-  // exceed dev_slots (their i-chunks are few)
   const int islots = dev_islots(a->prec);
   const int chunks = (ni_max + islots - 1) / islots;
-  const int grid1 = chunks > kp.dev_slots ? chunks : kp.dev_slots;
+  const int grid = chunks > kp.dev_slots ? chunks : kp.dev_slots;
   if (a->prec == G6_PREC_FP64) {
     kp.jrec = a->js->jp_f64;
-    force_kernel<F64P, 128, false><<<kp.dev_slots, NT, 0, st>>>(kp);
-    force_kernel<F64P, 16, false><<<kp.dev_slots, NT, 0, st>>>(kp);
-    force_kernel<F64P, 1, false><<<grid1, NT, 0, st>>>(kp);
-    reduce_dev_kernel<F64P><<<kp.dev_slots, 128, 0, st>>>(kp);
+    force_kernel<F64P, 1, false><<<grid, NT, 0, st>>>(kp);
+    reduce_dev_kernel<F64P><<<kp.dev_slots, 128, 0, st>>>(kp, islots);
   } else {
     kp.jrec = a->js->jp_split;
-    force_kernel<SplitP, 128, false><<<kp.dev_slots, NT, 0, st>>>(kp);
-    force_kernel<SplitP, 16, false><<<kp.dev_slots, NT, 0, st>>>(kp);
-    force_kernel<SplitP, 1, false><<<grid1, NT, 0, st>>>(kp);
-    reduce_dev_kernel<SplitP><<<kp.dev_slots, 128, 0, st>>>(kp);
+    force_kernel<SplitP, 1, false><<<grid, NT, 0, st>>>(kp);
+    reduce_dev_kernel<SplitP><<<kp.dev_slots, 128, 0, st>>>(kp, islots);
   }
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }

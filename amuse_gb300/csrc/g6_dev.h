@@ -81,27 +81,7 @@ typedef struct {
   int jl, nsplit, grid_x, grid_y, threads;
 } g6_shape;
 
-/* State of a device-driven block-step run (g6x_run): the system time, the
-   end time, the counters and the stop flags, kept on the device so that
-   many block steps are enqueued per host synchronisation. */
-typedef struct {
-  double t, t_end, steps;
-  long long blocks, max_blocks;
-  int done, err;
-} g6_runstate;
-
 size_t g6k_scratch_bytes(int ni, int nj, int prec, int force_jl, int force_nsplit);
-/* Device-shaped force for block steps: ni read from *d_ni (<= ni_max),
-   i-particles from a->ilist, no nearest neighbour; scratch of at least
-   g6k_scratch_bytes_dev(prec). */
-size_t g6k_scratch_bytes_dev(int prec);
-int g6k_force_dev_shaped(const g6_force_args *a, const int *d_ni, int ni_max, cudaStream_t st);
-int g6k_predict_dev(const g6_jstate *js, int nj, const double *d_ti, const int *d_ni, int prec,
-                    cudaStream_t st);
-int g6k_correct_dev(const g6_jstate *js, const int *d_ni, int ni_max, const int *ilist,
-                    const double *d_tnext, double eta, const double *acc, const double *jerk,
-                    const double *pot, cudaStream_t st);
-int g6k_run_step(g6_runstate *rs, int *d_ni, const double *d_tnext, cudaStream_t st);
 int g6k_sm_count(void);
 
 int g6k_scatter(const g6_jstate *js, const g6_jupd *d_upd, int n, cudaStream_t st);

@@ -13,7 +13,6 @@
  * There is no CPU force path: every force is computed by the CUDA kernels.
  */
 #define _POSIX_C_SOURCE 200112L /* clock_gettime */
-#include <limits.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -131,7 +130,6 @@ typedef struct {
   int *d_ilist, *d_ni;
   double *d_tnext, *d_sched, *d_esum, *d_racc, *d_rjerk, *d_rpot;
   void *d_mail, *h_mail; /* 16 B {tnext, ni}: device copy and pinned host copy */
-  void *d_run, *h_run;   /* g6_runstate of a device-driven run: device and pinned host */
   int *d_rnn;
   int run_cap;
   /* statistics */
@@ -457,9 +455,8 @@ int g6_close_(int *id) {
   if (G.h_in) cudaFreeHost(G.h_in);
   if (G.h_out) cudaFreeHost(G.h_out);
   cudaFree(G.d_upd); cudaFree(G.d_in); cudaFree(G.d_out); cudaFree(G.d_scratch);
-  cudaFree(G.d_ilist); cudaFree(G.d_mail); cudaFree(G.d_sched); cudaFree(G.d_run);
+  cudaFree(G.d_ilist); cudaFree(G.d_mail); cudaFree(G.d_sched);
   if (G.h_mail) cudaFreeHost(G.h_mail);
-  if (G.h_run) cudaFreeHost(G.h_run);
   cudaFree(G.d_esum); cudaFree(G.d_racc); cudaFree(G.d_rjerk); cudaFree(G.d_rpot);
   cudaFree(G.d_rnn);
   cudaEventDestroy(G.ev_done); cudaEventDestroy(G.ev_upd);
@@ -1122,9 +1119,6 @@ static int ensure_run_buffers(int n) {
   int ok = cudaMalloc((void **)&G.d_ilist, sizeof(int) * (size_t)n) == cudaSuccess &&
            cudaMalloc(&G.d_mail, 16) == cudaSuccess &&
            (G.h_mail || cudaHostAlloc(&G.h_mail, 16, cudaHostAllocDefault) == cudaSuccess) &&
-           (G.d_run || cudaMalloc(&G.d_run, sizeof(g6_runstate)) == cudaSuccess) &&
-           (G.h_run ||
-            cudaHostAlloc(&G.h_run, sizeof(g6_runstate), cudaHostAllocDefault) == cudaSuccess) &&
            cudaMalloc((void **)&G.d_sched, sizeof(double) * 4) == cudaSuccess &&
            cudaMalloc((void **)&G.d_esum, sizeof(double) * (size_t)(4 + 2 * (n / 256 + 2))) ==
                cudaSuccess &&
@@ -1204,76 +1198,52 @@ int g6x_run_stats(double out[4]) {
   return 0;
 }
 
-/* Block steps enqueued per host synchronisation.  Each step's kernels read
-   ni and tnext from the device (the scheduler writes them), so the host
-   only learns at the end of a batch whether the run ended; the steps
-   enqueued after the end do nothing. */
-#define G6_RUN_BATCH 16
-
 int g6x_run(double t_end, long long *blocks, double *particle_steps) {
   int rc = check_open();
   if (rc) return rc;
   const double w0 = now_ms();
   double wsync = 0;
   const int n = G.run_n;
-  if (n <= 0 || G.run_cap < n || !G.d_run || !G.h_run) return G6_ERR_STATE;
-  rc = flush_updates();
-  if (rc) return rc;
-  rc = ensure_scratch(g6k_scratch_bytes_dev(G.prec));
-  if (rc) return rc;
-  g6_runstate *hs = (g6_runstate *)G.h_run;
-  memset(hs, 0, sizeof(*hs));
-  hs->t = G.run_t;
-  hs->t_end = t_end;
-  hs->max_blocks = blocks && *blocks > 0 ? *blocks : LLONG_MAX;
-  CK(cudaMemcpyAsync(G.d_run, hs, sizeof(*hs), cudaMemcpyHostToDevice, G.st));
-  ilist_identity_n = 0;
-  g6_force_args a;
-  memset(&a, 0, sizeof(a));
-  a.ni = n;
-  a.nj = n;
-  a.prec = G.prec;
-  a.eps2 = G.run_eps2;
-  a.ilist = G.d_ilist;
-  a.acc = G.d_racc;
-  a.jerk = G.d_rjerk;
-  a.pot = G.d_rpot;
-  a.js = &G.js;
-  a.err = G.d_err;
-  a.scratch = G.d_scratch;
-  a.scratch_bytes = G.scratch_bytes;
-  while (1) {
-    for (int b = 0; b < G6_RUN_BATCH; b++) {
-      if (g6k_schedule(&G.js, n, G.d_ilist, G.d_ni, G.d_tnext, G.d_sched, 4, G.st) ||
-          g6k_run_step((g6_runstate *)G.d_run, G.d_ni, G.d_tnext, G.st) ||
-          g6k_predict_dev(&G.js, n, G.d_tnext, G.d_ni, G.prec, G.st) ||
-          g6k_force_dev_shaped(&a, G.d_ni, n, G.st) ||
-          g6k_correct_dev(&G.js, G.d_ni, n, G.d_ilist, G.d_tnext, G.run_eta, G.d_racc,
-                          G.d_rjerk, G.d_rpot, G.st)) {
-        seterr("block-step launch failed");
-        return G6_ERR_CUDA;
-      }
-    }
-    CK(cudaMemcpyAsync(hs, G.d_run, sizeof(*hs), cudaMemcpyDeviceToHost, G.st));
+  if (n <= 0 || G.run_cap < n) return G6_ERR_STATE;
+  const long long max_blocks = blocks && *blocks > 0 ? *blocks : -1;
+  long long nb = 0;
+  double ns = 0;
+  int hbuf[2];
+  double tn;
+  while (G.run_t < t_end && nb != max_blocks) {
+    ilist_identity_n = 0;
+    if (g6k_schedule(&G.js, n, G.d_ilist, G.d_ni, G.d_tnext, G.d_sched, 4, G.st))
+      return G6_ERR_CUDA;
+    /* one 16-byte copy into pinned memory: the only host round trip per block */
+    CK(cudaMemcpyAsync(G.h_mail, G.d_mail, 16, cudaMemcpyDeviceToHost, G.st));
     const double s0 = now_ms();
     CK(cudaStreamSynchronize(G.st));
     wsync += now_ms() - s0;
-    if (hs->done) break;
+    memcpy(&tn, G.h_mail, sizeof(double));
+    memcpy(hbuf, (const char *)G.h_mail + 8, sizeof(int));
+    const int ni = hbuf[0];
+    if (ni <= 0 || ni > n || !(tn > G.run_t)) {
+      seterr("scheduler produced ni=%d tnext=%.17g at t=%.17g", ni, tn, G.run_t);
+      return G6_ERR_STATE;
+    }
+    rc = g6x_force_slots(tn, G.run_eps2, n, ni, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot,
+                         NULL, 0);
+    if (rc) return rc;
+    if (g6k_correct(&G.js, ni, G.d_ilist, tn, G.run_eta, G.d_racc, G.d_rjerk, G.d_rpot,
+                    NULL, G.st))
+      return G6_ERR_CUDA;
+    G.pred_valid = 0; /* j-state changed */
+    G.run_t = tn;
+    nb++;
+    ns += ni;
   }
-  G.pred_valid = 0; /* j-state changed */
-  G.run_t = hs->t;
-  const long long nb = hs->blocks;
-  const double ns = hs->steps;
+  CK(cudaStreamSynchronize(G.st));
   run_stats[0] = (double)nb;
   run_stats[1] = now_ms() - w0;
   run_stats[2] = wsync;
   run_stats[3] = ns;
   if (blocks) *blocks = nb;
   if (particle_steps) *particle_steps = ns;
-  if (hs->err) {
-    seterr("scheduler produced an unusable block at t=%.17g", hs->t);
-    return G6_ERR_STATE;
-  }
   return read_err_word();
 }
 

@@ -41,7 +41,6 @@
 //     a checked copy of the loop (rinv = 0, r2 -> +inf for self).
 #include <cuda_runtime.h>
 #include <stdint.h>
-#include <string.h>
 
 #include "g6_dev.h"
 
@@ -595,27 +594,7 @@ struct KParams {
   int *err;
   int want_nn;
   int hjerk;  // the hermite code's jerk form (JL = 1, no nn only)
-  // Device-shaped launch (block steps enqueued without a host round trip):
-  // when d_ni is set, ni is read from *d_ni and the launch shape (JL = 1,
-  // j-splits) is derived on the device from it; the grid is 1-D and CTAs
-  // beyond the derived work exit at once.
-  const int *d_ni;
-  int dev_slots;  // resident CTAs of the whole GPU (the split target)
 };
-
-// The device-shaped launch's shape for ni i-particles in CTAs of islots:
-// gx i-chunks times nsplit j-ranges of jsplit j, about dev_slots CTAs in all.
-__device__ __forceinline__ void dev_shape(const KParams &kp, int islots, int ni, int &gx,
-                                          int &nsplit, int &jsplit) {
-  gx = (ni + islots - 1) / islots;
-  const int tiles = (kp.nj + G6_TILE - 1) / G6_TILE;
-  int ns = gx > 0 ? kp.dev_slots / gx : 1;
-  if (ns > tiles) ns = tiles;
-  if (ns < 1) ns = 1;
-  const int tp = (tiles + ns - 1) / ns;
-  nsplit = (tiles + tp - 1) / tp;
-  jsplit = tp * G6_TILE;
-}
 
 // Number of j per thread between compensated folds.
 constexpr int FOLD_J = 64;
@@ -640,19 +619,6 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   __shared__ int issued_s;
   __shared__ volatile int abort_s;
 
-  // effective launch parameters (host-shaped, or derived on the device)
-  int ni = kp.ni, nsplit = kp.nsplit, jsplit = kp.jsplit, ni_pad = kp.ni_pad;
-  int bx = blockIdx.x, by = blockIdx.y;
-  if (kp.d_ni) {
-    ni = *kp.d_ni;
-    ni_pad = ni;
-    int gx;
-    dev_shape(kp, ISLOTS, ni, gx, nsplit, jsplit);
-    if ((int)blockIdx.x >= gx * nsplit) return;  // uniform for the CTA, before any barrier
-    bx = blockIdx.x % gx;
-    by = blockIdx.x / gx;
-  }
-
   const int tid = threadIdx.x;
   const int jl = tid % JL;
   const int il = tid / JL;
@@ -664,8 +630,8 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   bool valid[IPT];
 #pragma unroll
   for (int k = 0; k < IPT; k++) {
-    const int i = bx * ISLOTS + k * NIL + il;
-    valid[k] = i < ni;
+    const int i = blockIdx.x * ISLOTS + k * NIL + il;
+    valid[k] = i < kp.ni;
     const int ii = valid[k] ? i : 0;
     if (kp.ilist) {
       const int slot = kp.ilist[ii];
@@ -678,8 +644,8 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   }
 
   // ---- j-range of this CTA ----
-  const int js = by * jsplit;
-  int je = js + jsplit;
+  const int js = blockIdx.y * kp.jsplit;
+  int je = js + kp.jsplit;
   const int nj_pad = (kp.nj + TJ - 1) / TJ * TJ;
   if (je > nj_pad) je = nj_pad;
   const int ntiles = je > js ? (je - js) / TJ : 0;
@@ -868,13 +834,13 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
 #pragma unroll
   for (int k = 0; k < IPT; k++) {
     if (!valid[k]) continue;
-    const int i = bx * ISLOTS + k * NIL + il;
-    if (nsplit == 1) {
+    const int i = blockIdx.x * ISLOTS + k * NIL + il;
+    if (kp.nsplit == 1) {
       P::write_final(o[k], i, kp.acc, kp.jerk, kp.pot);
       if (kp.nn) kp.nn[i] = (o[k].nn >= 0 && o[k].nn < kp.nj) ? o[k].nn : -1;
       if (kp.nn_r2) kp.nn_r2[i] = (float)o[k].nnr2;
     } else {
-      reinterpret_cast<typename P::Out *>(kp.part)[(size_t)by * ni_pad + i] = o[k];
+      reinterpret_cast<typename P::Out *>(kp.part)[(size_t)blockIdx.y * kp.ni_pad + i] = o[k];
     }
   }
 }
@@ -920,36 +886,6 @@ __global__ void reduce_warp_kernel(KParams kp) {
     P::write_final(o, i, kp.acc, kp.jerk, kp.pot);
     if (kp.nn) kp.nn[i] = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
     if (kp.nn_r2) kp.nn_r2[i] = (float)o.nnr2;
-  }
-}
-
-// Second pass of a device-shaped launch: ni and the split count are derived
-// on the device as in the force kernel; one warp per i, grid-stride (the
-// grid is fixed), nothing to do when the launch needed a single split.
-template <class P>
-__global__ void reduce_dev_kernel(KParams kp, int islots) {
-  const int ni = *kp.d_ni;
-  int gx, nsplit, jsplit;
-  dev_shape(kp, islots, ni, gx, nsplit, jsplit);
-  if (nsplit <= 1) return;
-  const int lane = threadIdx.x & 31;
-  const int warps = (gridDim.x * blockDim.x) >> 5;
-  const typename P::Out *part = reinterpret_cast<const typename P::Out *>(kp.part);
-  for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < ni; i += warps) {
-    typename P::Out o = part[(size_t)(lane < nsplit ? lane : 0) * ni + i];
-    for (int s = lane + 32; s < nsplit; s += 32) P::merge(o, part[(size_t)s * ni + i]);
-    const int have = nsplit < 32 ? nsplit : 32;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      typename P::Out b;
-      const int *src = reinterpret_cast<const int *>(&o);
-      int *dst = reinterpret_cast<int *>(&b);
-#pragma unroll
-      for (int w = 0; w < (int)(sizeof(b) / 4); w++)
-        dst[w] = __shfl_down_sync(0xffffffffu, src[w], off);
-      if (lane < off && lane + off < have) P::merge(o, b);
-    }
-    if (lane == 0) P::write_final(o, i, kp.acc, kp.jerk, kp.pot);
   }
 }
 
@@ -1120,59 +1056,6 @@ extern "C" size_t g6k_scratch_bytes(int ni, int nj, int prec, int force_jl, int 
   return (size_t)nsplit * (size_t)ni * rec;
 }
 
-// Device-shaped launches: resident CTAs of the GPU (the split target) and
-// the largest partial-sum buffer one can need (nsplit > 1 only when the
-// i-chunks are fewer than dev_slots, so nsplit x ni <= dev_slots x islots).
-static int dev_slots(int prec) {
-  return (prec == G6_PREC_FP64 ? F64P::MINB : SplitP::MINB) * sm_count();
-}
-static int dev_islots(int prec) { return NT * (prec == G6_PREC_FP64 ? IPT_F64 : IPT_SPLIT); }
-extern "C" size_t g6k_scratch_bytes_dev(int prec) {
-  const size_t rec = prec == G6_PREC_FP64 ? sizeof(F64P::Out) : sizeof(SplitP::Out);
-  return (size_t)dev_slots(prec) * (size_t)dev_islots(prec) * rec;
-}
-
-// ni_max bounds *d_ni (the grid covers it); i-particles from ilist only, no
-// nearest neighbour, the softened jerk.
-extern "C" int g6k_force_dev_shaped(const g6_force_args *a, const int *d_ni, int ni_max,
-                                    cudaStream_t st) {
-  if (ni_max <= 0) return 0;
-  if (a->nj <= 0 || !a->acc || !a->jerk || !a->pot || !a->js || !a->err || !a->ilist || !d_ni)
-    return -1;
-  if (a->want_nn || a->hjerk) return -2;
-  if (a->scratch_bytes < g6k_scratch_bytes_dev(a->prec)) return -4;
-  KParams kp;
-  memset(&kp, 0, sizeof(kp));
-  kp.ni = ni_max;
-  kp.nj = a->nj;
-  kp.nsplit = 1;
-  kp.jsplit = 0;
-  kp.eps2 = a->eps2;
-  kp.ilist = a->ilist;
-  kp.iself = a->iself;
-  kp.acc = a->acc;
-  kp.jerk = a->jerk;
-  kp.pot = a->pot;
-  kp.part = a->scratch;
-  kp.ni_pad = ni_max;
-  kp.err = a->err;
-  kp.d_ni = d_ni;
-  kp.dev_slots = dev_slots(a->prec);
-  const int islots = dev_islots(a->prec);
-  const int chunks = (ni_max + islots - 1) / islots;
-  const int grid = chunks > kp.dev_slots ? chunks : kp.dev_slots;
-  if (a->prec == G6_PREC_FP64) {
-    kp.jrec = a->js->jp_f64;
-    force_kernel<F64P, 1, false><<<grid, NT, 0, st>>>(kp);
-    reduce_dev_kernel<F64P><<<kp.dev_slots, 128, 0, st>>>(kp, islots);
-  } else {
-    kp.jrec = a->js->jp_split;
-    force_kernel<SplitP, 1, false><<<grid, NT, 0, st>>>(kp);
-    reduce_dev_kernel<SplitP><<<kp.dev_slots, 128, 0, st>>>(kp, islots);
-  }
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
-}
-
 extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t st) {
   if (a->ni <= 0) return 0;
   if (a->nj <= 0 || !a->acc || !a->jerk || !a->pot || !a->js || !a->err) return -1;
@@ -1183,7 +1066,6 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
                &jsplit);
   if (jl < 1 || jl > JLMAX || (jl & (jl - 1))) return -2;
   KParams kp;
-  memset(&kp, 0, sizeof(kp));
   kp.ni = a->ni;
   kp.nj = a->nj;
   kp.nsplit = nsplit;

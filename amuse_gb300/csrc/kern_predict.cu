@@ -52,17 +52,10 @@ __global__ void scatter_kernel(g6_jstate js, const g6_jupd *__restrict__ upd, in
   }
 }
 
-// d_ti / d_ni (device-driven block steps): when d_ti is set the prediction
-// time is *d_ti, and nothing is done while *d_ni == 0 (the run has ended).
 template <int PREC>
-__global__ void __launch_bounds__(PT) predict_kernel(g6_jstate js, int nj, int nj_pad, double ti,
-                                                     const double *d_ti, const int *d_ni) {
+__global__ void __launch_bounds__(PT) predict_kernel(g6_jstate js, int nj, int nj_pad, double ti) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nj_pad) return;
-  if (d_ti) {
-    if (*d_ni == 0) return;
-    ti = *d_ti;
-  }
   const int cap = js.cap;
   double xp[3], vp[3], m;
   if (s < nj) {
@@ -115,26 +108,14 @@ extern "C" int g6k_scatter(const g6_jstate *js, const g6_jupd *d_upd, int n, cud
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
-static int predict_launch(const g6_jstate *js, int nj, double ti, const double *d_ti,
-                          const int *d_ni, int prec, cudaStream_t st) {
+extern "C" int g6k_predict(const g6_jstate *js, int nj, double ti, int prec, cudaStream_t st) {
   if (nj <= 0) return 0;
   const int nj_pad = (nj + G6_TILE - 1) / G6_TILE * G6_TILE;
   if (nj_pad > js->cap) return -1;
   const int grid = (nj_pad + PT - 1) / PT;
   if (prec == G6_PREC_FP64)
-    predict_kernel<G6_PREC_FP64><<<grid, PT, 0, st>>>(*js, nj, nj_pad, ti, d_ti, d_ni);
+    predict_kernel<G6_PREC_FP64><<<grid, PT, 0, st>>>(*js, nj, nj_pad, ti);
   else
-    predict_kernel<G6_PREC_SPLIT><<<grid, PT, 0, st>>>(*js, nj, nj_pad, ti, d_ti, d_ni);
+    predict_kernel<G6_PREC_SPLIT><<<grid, PT, 0, st>>>(*js, nj, nj_pad, ti);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
-}
-
-extern "C" int g6k_predict(const g6_jstate *js, int nj, double ti, int prec, cudaStream_t st) {
-  return predict_launch(js, nj, ti, NULL, NULL, prec, st);
-}
-
-// The same prediction to the time *d_ti, skipped while *d_ni == 0.
-extern "C" int g6k_predict_dev(const g6_jstate *js, int nj, const double *d_ti, const int *d_ni,
-                               int prec, cudaStream_t st) {
-  if (!d_ti || !d_ni) return -1;
-  return predict_launch(js, nj, 0.0, d_ti, d_ni, prec, st);
 }

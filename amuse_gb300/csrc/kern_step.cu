@@ -56,14 +56,15 @@ __device__ __forceinline__ bool multiple_of_pow2(double t, double p) {
 // latency), and the squared norms are summed in component order after a
 // shuffle, exactly as the scalar loop adds them, so the result stays
 // bit-identical with ph4.  Lane 3 only takes part in the shuffles.
-__device__ __forceinline__ void correct_one(g6_jstate &js, int ni, int i, int k, int lane,
-                                            int base, const int *__restrict__ ilist,
-                                            double tnext, double eta,
-                                            const double *__restrict__ acc,
-                                            const double *__restrict__ jerk,
-                                            const double *__restrict__ pot,
-                                            const int *__restrict__ nn) {
-  (void)lane;
+__global__ void correct_kernel(g6_jstate js, int ni, const int *__restrict__ ilist, double tnext,
+                               double eta, const double *__restrict__ acc,
+                               const double *__restrict__ jerk, const double *__restrict__ pot,
+                               const int *__restrict__ nn) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = g >> 2;
+  const int k = g & 3;
+  const int lane = threadIdx.x & 31;
+  const int base = lane & ~3;
   const bool active = i < ni;  // whole groups of 4 agree
   const int ii = active ? i : 0;
   const int s = ilist[ii];
@@ -139,29 +140,6 @@ __device__ __forceinline__ void correct_one(g6_jstate &js, int ni, int i, int k,
   if (pot) js.pot[s] = pot[i];
   if (nn) js.nn[s] = nn[i];
 }
-
-// d_ni / d_tnext (device-driven block steps): when set, ni and tnext are
-// read from the device, and the grid strides over the particles in rounds of
-// 8 per warp (the round condition is warp-uniform, so the shuffles below see
-// every lane).
-__global__ void correct_kernel(g6_jstate js, int ni, const int *__restrict__ ilist, double tnext,
-                               double eta, const double *__restrict__ acc,
-                               const double *__restrict__ jerk, const double *__restrict__ pot,
-                               const int *__restrict__ nn, const int *d_ni,
-                               const double *d_tnext) {
-  if (d_ni) {
-    ni = *d_ni;
-    tnext = *d_tnext;
-  }
-  const int lane = threadIdx.x & 31;
-  const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  const int warps = (int)((gridDim.x * (size_t)blockDim.x) >> 5);
-  for (int r0 = warp * 8; r0 < ni; r0 += warps * 8) {
-    correct_one(js, ni, r0 + (lane >> 2), lane & 3, lane, lane & ~3, ilist, tnext, eta, acc,
-                jerk, pot, nn);
-  }
-}
-
 
 __global__ void store_kernel(g6_jstate js, int ni, const int *__restrict__ ilist,
                              const double *__restrict__ acc, const double *__restrict__ jerk,
@@ -308,53 +286,7 @@ extern "C" int g6k_correct(const g6_jstate *js, int ni, const int *ilist, double
                            const int *nn, cudaStream_t st) {
   if (ni <= 0) return 0;
   // 4 lanes per particle, 32 particles per 128-thread block
-  correct_kernel<<<(ni + 31) / 32, 128, 0, st>>>(*js, ni, ilist, tnext, eta, acc, jerk, pot, nn,
-                                                 NULL, NULL);
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
-}
-
-// The corrector with ni and tnext read from the device (device-driven block
-// steps); a fixed grid strides over up to ni_max particles.
-extern "C" int g6k_correct_dev(const g6_jstate *js, const int *d_ni, int ni_max,
-                               const int *ilist, const double *d_tnext, double eta,
-                               const double *acc, const double *jerk, const double *pot,
-                               cudaStream_t st) {
-  if (ni_max <= 0) return 0;
-  if (!d_ni || !d_tnext) return -1;
-  int grid = (ni_max + 31) / 32;
-  const int cap_grid = 4 * g6k_sm_count();
-  if (grid > cap_grid) grid = cap_grid;
-  correct_kernel<<<grid, 128, 0, st>>>(*js, 0, ilist, 0.0, eta, acc, jerk, pot, NULL, d_ni,
-                                       d_tnext);
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
-}
-
-// One block step's bookkeeping for device-driven runs (single thread), after
-// the scheduler wrote tnext and ni: end the run (ni := 0, so the block's
-// kernels do nothing) once the system time reached t_end or the block
-// budget is used up, or when the schedule is not usable; otherwise advance
-// the system time and the counters.
-__global__ void run_step_kernel(g6_runstate *rs, int *d_ni, const double *d_tnext) {
-  const int ni = *d_ni;
-  const double tn = *d_tnext;
-  if (rs->done || !(rs->t < rs->t_end) || rs->blocks >= rs->max_blocks) {
-    rs->done = 1;
-    *d_ni = 0;
-    return;
-  }
-  if (ni <= 0 || !(tn > rs->t)) {
-    rs->done = 1;
-    rs->err = 1;
-    *d_ni = 0;
-    return;
-  }
-  rs->t = tn;
-  rs->blocks += 1;
-  rs->steps += (double)ni;
-}
-
-extern "C" int g6k_run_step(g6_runstate *rs, int *d_ni, const double *d_tnext, cudaStream_t st) {
-  run_step_kernel<<<1, 1, 0, st>>>(rs, d_ni, d_tnext);
+  correct_kernel<<<(ni + 31) / 32, 128, 0, st>>>(*js, ni, ilist, tnext, eta, acc, jerk, pot, nn);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

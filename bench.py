@@ -51,6 +51,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FLOP_PER_PAIR = 60.0
+PRED_FP64_OPS = 36  # FP64-pipe operations per j of the split-record predictor
 # DRAM bytes (read + write) of one force launch at the default N = 2^20, from
 # one ncu capture of this benchmark (profiles/force_kernel_dram_n1048576.md).
 FORCE_TRAFFIC_N = 1 << 20
@@ -372,7 +373,15 @@ def run_ours(args):
                          "flop_per_pair": FLOP_PER_PAIR, "force_ms": 1e3 * force_s},
             "predictor": {"ms": statistics.mean(pms), "GB_s": pred_gbs,
                           "bytes_per_j": 15 * 8 + 4 + 48,
-                          "hbm_peak_gbs": pk.get("hbm_gbs")},
+                          "hbm_peak_gbs": pk.get("hbm_gbs"),
+                          # ph4's FP64 expression: ~20 FP64 ops per j for x and v,
+                          # plus ~16 conversions for the double-single record
+                          "bound": "fp64",
+                          "fp64_ops_per_j": PRED_FP64_OPS,
+                          "fp64_frac": (PRED_FP64_OPS * n / (statistics.mean(pms) / 1e3)
+                                        / (nsm * 2 * sm_max * 1e6)) if pms[0] > 0 else None,
+                          "fp64_peak_source": f"{nsm} SMs x 2 FP64 lanes x {sm_max:.0f} MHz "
+                                              "(GB300 FP64 = 1/64 of FP32)"},
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": clocks,

@@ -257,13 +257,24 @@ def run_precision(args):
     g6.run_init(eps2, args.eta)
     k0, p0 = g6.energy()
     t0 = time.perf_counter()
+    e0 = k0 + p0
     if args.t_end:
-        nb, ns = g6.run(args.t_end)  # to a system time (e.g. one N-body time unit)
+        # to a system time (e.g. one N-body time unit) in 8 segments, with the
+        # energy printed after each, so that partial results survive a time limit
+        nb = ns = 0
+        for seg in range(1, 9):
+            b, st = g6.run(args.t_end * seg / 8)
+            nb += b
+            ns += st
+            ks, ps = g6.energy()
+            print(json.dumps({"segment": seg, "t": g6.system_time(), "blocks": nb,
+                              "particle_steps": ns, "seconds": time.perf_counter() - t0,
+                              "dE_over_E": abs(ks + ps - e0) / abs(e0)}), flush=True)
     else:
         nb, ns = g6.run(1e30, max_blocks=64)
     wall = time.perf_counter() - t0
     k1, p1 = g6.energy()
-    e0, e1 = k0 + p0, k1 + p1
+    e1 = k1 + p1
     out["block_steps"] = {"eta": args.eta, "precision": "split", "blocks": nb,
                           "particle_steps": ns, "t_reached": g6.system_time(),
                           "seconds": wall, "pairs_per_s": ns * (n - 1) / wall,

@@ -13,7 +13,9 @@ resident in HBM; L2 is flushed (256 MB write) between timed steps.
 Reported next to it:
   e2e          the same metric through the GRAPE-6 C ABI with host buffers
                (g6_set_j_particle for all N, g6_set_ti, g6calc_firsthalf /
-               lasthalf2 chunked by npipes, as ph4's gpu.cc calls it);
+               lasthalf chunked by npipes, as ph4's gpu.cc calls it);
+  predictor    the FP64 j-predictor's time, HBM GB/s and FP64-pipe fraction
+               (on GB300 its FP64 arithmetic, not HBM, bounds it);
   fp64         the plain FP64 GPU kernel's pairs/s (on a 16384-particle
                i-subset against all N j) and the speed-up over it;
   roofline     the force kernel against the FP32 peak, 60 flop/pair (ph4's

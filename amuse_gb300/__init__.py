@@ -51,7 +51,11 @@ EXT_SYMBOLS = [
     "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
     "g6x_set_fixed_jerk", "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp",
     "g6x_fixed_step_adjoint", "g6x_fixed_run", "g6x_fixed_adjoint_run",
+    "g6x_set_encounters", "g6x_set_radius", "g6x_encounter",
 ]
+
+# Encounter-check modes of g6x_set_encounters (bits).
+ENC_CHECK, ENC_STOP_COLLISION, ENC_STOP_CLOSE = 1, 2, 4
 
 _lib = None
 _drv = None
@@ -105,6 +109,9 @@ def load():
     lib.g6x_run.argtypes = [D, ctypes.POINTER(ctypes.c_longlong), _pd]
     lib.g6x_energy.argtypes = [_pd, _pd]
     lib.g6x_run_stats.argtypes = [_pd]
+    lib.g6x_set_encounters.argtypes = [I, D]
+    lib.g6x_set_radius.argtypes = [I, _pd]
+    lib.g6x_encounter.argtypes = [_pi, _pd]
     lib.g6x_step_all.argtypes = [D]
     lib.g6x_correct.argtypes = [I, _pi, D, D, _pd, _pd]
     _pll = ctypes.POINTER(ctypes.c_longlong)
@@ -346,6 +353,28 @@ class G6X(G6):
         out = np.zeros(4)
         _check(self.lib.g6x_run_stats(_ptr(out, ctypes.c_double)), "g6x_run_stats")
         return dict(blocks=out[0], wall_ms=out[1], sync_ms=out[2], particle_steps=out[3])
+
+    def set_encounters(self, mode, rmin=0.0):
+        """Encounter check in run(): ENC_CHECK, ENC_STOP_COLLISION and
+        ENC_STOP_CLOSE bits (0 turns it off); rmin <= 0 is ph4's 2/n."""
+        _check(self.lib.g6x_set_encounters(int(mode), float(rmin)), "g6x_set_encounters")
+
+    def set_radius(self, radius):
+        """Particle radii by slot (the collision criterion's R)."""
+        radius = _f64(radius)
+        _check(self.lib.g6x_set_radius(len(radius), _ptr(radius, ctypes.c_double)),
+               "g6x_set_radius")
+
+    def encounter(self):
+        """The last checked block: close / coll (id pairs or None), stopped
+        (1 collision, 2 close, 0 none), t, rmax_close, rmax_coll."""
+        ids = np.zeros(4, np.int32)
+        out = np.zeros(4)
+        _check(self.lib.g6x_encounter(_ptr(ids, ctypes.c_int), _ptr(out, ctypes.c_double)),
+               "g6x_encounter")
+        pair = lambda a, b: None if a < 0 else (int(a), int(b))
+        return dict(close=pair(ids[0], ids[1]), coll=pair(ids[2], ids[3]), stopped=int(out[0]),
+                    t=float(out[1]), rmax_close=float(out[2]), rmax_coll=float(out[3]))
 
     def correct(self, slots, tnext, eta, acc, jerk):
         slots = _i32(slots)

@@ -98,6 +98,27 @@ int g6k_correct(const g6_jstate *js, int ni, const int *ilist, double tnext,
 int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni,
                  double *d_tnext, double *d_scratch, int scratch_len,
                  cudaStream_t st);
+/* Encounter check of one block (idata::check_encounters, idata.cc:620-700)
+ * and the stopping decision after its corrector (jdata.cc:797-850).         */
+typedef struct {
+  double rmax_close, rmax_coll; /* largest rmin/dnn and (R_i + R_nn)/dnn */
+  double t;                     /* time of the block */
+  int close_slot[2], coll_slot[2];
+  int close_id[2], coll_id[2];  /* -1: no pair */
+  int stopped;                  /* 1 collision, 2 close pair (bits) */
+  int pad;
+} g6_enc;
+/* Pre-corrector pass over the block: nn[i] is the nearest j slot of ilist[i]
+ * from the force; distances are recomputed in FP64 from both particles
+ * predicted to tnext.  part_d >= 2 * ceil(ni/256), part_i >= 4 * ceil(ni/256),
+ * *counter == 0 on entry (left 0).                                           */
+int g6k_enc_check(const g6_jstate *js, const double *rad, int ni, const int *ilist,
+                  const int *nn, double tnext, double rmin, double *part_d, int *part_i,
+                  unsigned *counter, g6_enc *enc, cudaStream_t st);
+/* Post-corrector: ids of the pairs, the collision test on the corrected
+ * state, stop bits into enc->stopped and *flag.                              */
+int g6k_enc_verdict(const g6_jstate *js, g6_enc *enc, int mode, double tnext, int *flag,
+                    cudaStream_t st);
 /* Initial time steps (jdata.cc:503-564 without the median limit). */
 int g6k_initial_step(const g6_jstate *js, int nj, double eta, double fac,
                      double limit, double system_time, cudaStream_t st);

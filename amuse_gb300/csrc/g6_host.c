@@ -129,9 +129,19 @@ typedef struct {
   double run_t, run_eps2, run_eta;
   int *d_ilist, *d_ni;
   double *d_tnext, *d_sched, *d_esum, *d_racc, *d_rjerk, *d_rpot;
-  void *d_mail, *h_mail; /* 16 B {tnext, ni}: device copy and pinned host copy */
+  void *d_mail, *h_mail; /* 16 B {tnext, ni, stop}: device copy and pinned host copy */
   int *d_rnn;
   int run_cap;
+  /* encounter check in g6x_run (idata::check_encounters) */
+  int enc_mode;
+  double enc_rmin;
+  double *d_rad; /* particle radii by slot, rad_cap entries */
+  int rad_cap;
+  g6_enc *d_enc;
+  double *d_encp_d;
+  int *d_encp_i;
+  unsigned *d_enc_ctr;
+  int enc_cap; /* CTAs the partial buffers hold */
   /* statistics */
   int timing;
   double st_predict_ms, st_force_ms, st_pairs, st_pred_bytes, st_nj;
@@ -459,6 +469,8 @@ int g6_close_(int *id) {
   if (G.h_mail) cudaFreeHost(G.h_mail);
   cudaFree(G.d_esum); cudaFree(G.d_racc); cudaFree(G.d_rjerk); cudaFree(G.d_rpot);
   cudaFree(G.d_rnn);
+  cudaFree(G.d_rad); cudaFree(G.d_enc); cudaFree(G.d_encp_d); cudaFree(G.d_encp_i);
+  cudaFree(G.d_enc_ctr);
   cudaEventDestroy(G.ev_done); cudaEventDestroy(G.ev_upd);
   cudaEventDestroy(G.ev_t0); cudaEventDestroy(G.ev_t1); cudaEventDestroy(G.ev_t2);
   cudaStreamDestroy(G.st);
@@ -1132,7 +1144,105 @@ static int ensure_run_buffers(int n) {
   }
   G.d_tnext = (double *)G.d_mail;
   G.d_ni = (int *)((char *)G.d_mail + 8);
+  CK(cudaMemset(G.d_mail, 0, 16));
   G.run_cap = n;
+  return 0;
+}
+
+/* ---- encounter check (extension API) ---- */
+
+/* Radii by slot, at least n entries; entries added are zero. */
+static int ensure_radius(int n) {
+  if (n <= G.rad_cap) return 0;
+  double *r = NULL;
+  CK(cudaMalloc((void **)&r, sizeof(double) * (size_t)n));
+  CK(cudaMemset(r, 0, sizeof(double) * (size_t)n));
+  if (G.d_rad) {
+    CK(cudaMemcpy(r, G.d_rad, sizeof(double) * (size_t)G.rad_cap, cudaMemcpyDeviceToDevice));
+    cudaFree(G.d_rad);
+  }
+  G.d_rad = r;
+  G.rad_cap = n;
+  return 0;
+}
+
+static int ensure_enc_buffers(int n) {
+  const int grid = (n + 255) / 256;
+  int rc = ensure_radius(n);
+  if (rc) return rc;
+  if (!G.d_enc) {
+    g6_enc e;
+    memset(&e, 0, sizeof(e));
+    e.close_slot[0] = e.close_slot[1] = e.coll_slot[0] = e.coll_slot[1] = -1;
+    e.close_id[0] = e.close_id[1] = e.coll_id[0] = e.coll_id[1] = -1;
+    CK(cudaMalloc((void **)&G.d_enc, sizeof(g6_enc)));
+    CK(cudaMemcpy(G.d_enc, &e, sizeof(e), cudaMemcpyHostToDevice));
+    CK(cudaMalloc((void **)&G.d_enc_ctr, sizeof(unsigned)));
+    CK(cudaMemset(G.d_enc_ctr, 0, sizeof(unsigned)));
+  }
+  if (grid > G.enc_cap) {
+    cudaFree(G.d_encp_d);
+    cudaFree(G.d_encp_i);
+    G.d_encp_d = NULL;
+    G.d_encp_i = NULL;
+    G.enc_cap = 0;
+    CK(cudaMalloc((void **)&G.d_encp_d, sizeof(double) * 2 * (size_t)grid));
+    CK(cudaMalloc((void **)&G.d_encp_i, sizeof(int) * 4 * (size_t)grid));
+    G.enc_cap = grid;
+  }
+  return 0;
+}
+
+int g6x_set_encounters(int mode, double rmin) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (mode & ~(G6_ENC_CHECK | G6_ENC_STOP_COLLISION | G6_ENC_STOP_CLOSE)) {
+    seterr("g6x_set_encounters: unknown mode bits %#x", mode);
+    return G6_ERR_ARG;
+  }
+  if (mode & (G6_ENC_STOP_COLLISION | G6_ENC_STOP_CLOSE)) mode |= G6_ENC_CHECK;
+  if (!(rmin >= 0)) {
+    seterr("g6x_set_encounters: rmin %g", rmin);
+    return G6_ERR_ARG;
+  }
+  G.enc_mode = mode;
+  G.enc_rmin = rmin;
+  return 0;
+}
+
+int g6x_set_radius(int n, const double *radius) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && !radius)) return G6_ERR_ARG;
+  if (n == 0) return 0;
+  rc = ensure_radius(n);
+  if (rc) return rc;
+  CK(cudaMemcpy(G.d_rad, radius, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int g6x_encounter(int ids[4], double out[4]) {
+  int rc = check_open();
+  if (rc) return rc;
+  g6_enc e;
+  memset(&e, 0, sizeof(e));
+  e.close_id[0] = e.close_id[1] = e.coll_id[0] = e.coll_id[1] = -1;
+  if (G.d_enc) {
+    CK(cudaStreamSynchronize(G.st));
+    CK(cudaMemcpy(&e, G.d_enc, sizeof(e), cudaMemcpyDeviceToHost));
+  }
+  if (ids) {
+    ids[0] = e.close_id[0];
+    ids[1] = e.close_id[1];
+    ids[2] = e.coll_id[0];
+    ids[3] = e.coll_id[1];
+  }
+  if (out) {
+    out[0] = e.stopped;
+    out[1] = e.t;
+    out[2] = e.rmax_close;
+    out[3] = e.rmax_coll;
+  }
   return 0;
 }
 
@@ -1210,6 +1320,18 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
   double ns = 0;
   int hbuf[2];
   double tn;
+  /* Encounter check: the force also finds each block particle's nearest
+     neighbour, a pass before the corrector evaluates ph4's criteria, one
+     after it the stopping test; its stop bits reach the host in the next
+     block's mailbox copy, before that block's force is launched. */
+  const int enc = G.enc_mode;
+  const double rmin = G.enc_rmin > 0 ? G.enc_rmin : 2.0 / n; /* jdata.cc:426 */
+  int *d_stop = (int *)((char *)G.d_mail + 12);
+  if (enc) {
+    rc = ensure_enc_buffers(n);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(d_stop, 0, sizeof(int), G.st));
+  }
   while (G.run_t < t_end && nb != max_blocks) {
     ilist_identity_n = 0;
     if (g6k_schedule(&G.js, n, G.d_ilist, G.d_ni, G.d_tnext, G.d_sched, 4, G.st))
@@ -1220,18 +1342,23 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
     CK(cudaStreamSynchronize(G.st));
     wsync += now_ms() - s0;
     memcpy(&tn, G.h_mail, sizeof(double));
-    memcpy(hbuf, (const char *)G.h_mail + 8, sizeof(int));
+    memcpy(hbuf, (const char *)G.h_mail + 8, 2 * sizeof(int));
+    if (enc && hbuf[1]) break; /* the previous block met a stopping condition */
     const int ni = hbuf[0];
     if (ni <= 0 || ni > n || !(tn > G.run_t)) {
       seterr("scheduler produced ni=%d tnext=%.17g at t=%.17g", ni, tn, G.run_t);
       return G6_ERR_STATE;
     }
     rc = g6x_force_slots(tn, G.run_eps2, n, ni, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot,
-                         NULL, 0);
+                         enc ? G.d_rnn : NULL, 0);
     if (rc) return rc;
-    if (g6k_correct(&G.js, ni, G.d_ilist, tn, G.run_eta, G.d_racc, G.d_rjerk, G.d_rpot,
-                    NULL, G.st))
+    if (enc && g6k_enc_check(&G.js, G.d_rad, ni, G.d_ilist, G.d_rnn, tn, rmin, G.d_encp_d,
+                             G.d_encp_i, G.d_enc_ctr, G.d_enc, G.st))
       return G6_ERR_CUDA;
+    if (g6k_correct(&G.js, ni, G.d_ilist, tn, G.run_eta, G.d_racc, G.d_rjerk, G.d_rpot,
+                    enc ? G.d_rnn : NULL, G.st))
+      return G6_ERR_CUDA;
+    if (enc && g6k_enc_verdict(&G.js, G.d_enc, enc, tn, d_stop, G.st)) return G6_ERR_CUDA;
     G.pred_valid = 0; /* j-state changed */
     G.run_t = tn;
     nb++;

@@ -12,7 +12,11 @@
 //                    src/amuse_ph4/src/scheduler.cc:66-79).
 //   initial_step     jdata::set_initial_timestep (jdata.cc:503-564).
 //   energy sums      sum m |v_p|^2 and sum m pot (jdata.cc:582-680).
+//   encounter check  idata::check_encounters (idata.cc:620-700) over a
+//                    block, and the COLLISION_DETECTION test of
+//                    jdata::advance_and_check_encounter (jdata.cc:797-850).
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <stdint.h>
 
 #include "g6_dev.h"
@@ -139,6 +143,162 @@ __global__ void correct_kernel(g6_jstate js, int ni, const int *__restrict__ ili
   js.dt[s] = newstep;
   if (pot) js.pot[s] = pot[i];
   if (nn) js.nn[s] = nn[i];
+}
+
+// ph4's prediction of one position component (predict_all, jdata.cc:736-744;
+// the same expression as the host i-prediction, idata.cc:346-365).
+__device__ __forceinline__ double predict_x(double x, double v, double a, double j, double dt) {
+  if (dt == 0) return x;
+  const double hdt = dmul(0.5, dt);
+  return dadd(x, dmul(dt, dadd(v, dmul(hdt, dadd(a, ddiv(dmul(dt, j), 3.0))))));
+}
+
+// ---- encounter check ----
+// A candidate pair (i slot s, its nearest neighbour j) with its ratio r.
+// ph4 keeps the first i of its list with the largest r (strict >); the
+// block list here has no fixed order, so ties go to the smaller slot, which
+// is the first in slot order.
+struct EncC {
+  double r;
+  int s, j;
+};
+
+__device__ __forceinline__ void enc_take(EncC &a, const EncC &b) {
+  if (b.r > a.r || (b.r == a.r && b.s < a.s)) a = b;
+}
+
+__device__ __forceinline__ EncC enc_shfl(const EncC &c, int o) {
+  EncC d;
+  d.r = __shfl_xor_sync(0xffffffffu, c.r, o);
+  d.s = __shfl_xor_sync(0xffffffffu, c.s, o);
+  d.j = __shfl_xor_sync(0xffffffffu, c.j, o);
+  return d;
+}
+
+// Both candidates reduced over the CTA; the result is valid in thread 0.
+__device__ void enc_block_reduce(EncC &c0, EncC &c1) {
+  __shared__ EncC sh[2][PT / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    enc_take(c0, enc_shfl(c0, o));
+    enc_take(c1, enc_shfl(c1, o));
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][w] = c0;
+    sh[1][w] = c1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 1; k < PT / 32; k++) {
+      enc_take(c0, sh[0][k]);
+      enc_take(c1, sh[1][k]);
+    }
+  __syncthreads();
+}
+
+// One thread per block particle: dnn = |x_nn - x_i| with both predicted to
+// tnext in FP64 (ph4 CPU mode: sqrt of the force loop's min r^2 over the
+// predicted j-system), then r_close = rmin / dnn and r_coll =
+// (R_i + R_nn) / dnn for pairs with at least one massive member.  Each CTA
+// leaves its best two candidates in part_*; the last CTA to finish (atomic
+// ticket) reduces them and writes the block's result.
+__global__ void enc_check_kernel(g6_jstate js, const double *__restrict__ rad, int ni,
+                                 const int *__restrict__ ilist, const int *__restrict__ nn,
+                                 double tnext, double rmin, double *part_d, int *part_i,
+                                 unsigned *counter, g6_enc *enc) {
+  const double tiny = 1.0 / 4503599627370496.0;  // 2^-52 (stdinc.h)
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  EncC cc = {0.0, INT_MAX, -1}, cl = {0.0, INT_MAX, -1};
+  if (i < ni) {
+    const int s = ilist[i];
+    const int jn = nn[i];
+    if (jn >= 0 && (js.m[jn] > tiny || js.m[s] > tiny)) {
+      const int cap = js.cap;
+      const double dti = dsub(tnext, js.t[s]), dtj = dsub(tnext, js.t[jn]);
+      double r2 = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const int a = k * cap + s, b = k * cap + jn;
+        const double xi = predict_x(js.x[a], js.v[a], js.a[a], js.j[a], dti);
+        const double xj = predict_x(js.x[b], js.v[b], js.a[b], js.j[b], dtj);
+        const double dx = dsub(xj, xi);
+        r2 = dadd(r2, dmul(dx, dx));
+      }
+      const double dnn = __dsqrt_rn(r2);
+      cc.r = ddiv(rmin, dnn);
+      cc.s = s;
+      cc.j = jn;
+      cl.r = ddiv(dadd(rad[s], rad[jn]), dnn);
+      cl.s = s;
+      cl.j = jn;
+    }
+  }
+  enc_block_reduce(cc, cl);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    part_d[2 * blockIdx.x] = cc.r;
+    part_d[2 * blockIdx.x + 1] = cl.r;
+    part_i[4 * blockIdx.x] = cc.s;
+    part_i[4 * blockIdx.x + 1] = cc.j;
+    part_i[4 * blockIdx.x + 2] = cl.s;
+    part_i[4 * blockIdx.x + 3] = cl.j;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  EncC a = {0.0, INT_MAX, -1}, b = {0.0, INT_MAX, -1};
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    const EncC ka = {__ldcg(part_d + 2 * k), __ldcg(part_i + 4 * k), __ldcg(part_i + 4 * k + 1)};
+    const EncC kb = {__ldcg(part_d + 2 * k + 1), __ldcg(part_i + 4 * k + 2),
+                     __ldcg(part_i + 4 * k + 3)};
+    enc_take(a, ka);
+    enc_take(b, kb);
+  }
+  enc_block_reduce(a, b);
+  if (threadIdx.x == 0) {
+    enc->rmax_close = a.r;
+    enc->rmax_coll = b.r;
+    const bool close = a.r >= 1.0, coll = b.r >= 1.0;
+    enc->close_slot[0] = close ? a.s : -1;
+    enc->close_slot[1] = close ? a.j : -1;
+    enc->coll_slot[0] = coll ? b.s : -1;
+    enc->coll_slot[1] = coll ? b.j : -1;
+    *counter = 0;
+  }
+}
+
+// After the corrector: the pair ids, and ph4's COLLISION_DETECTION test on
+// the current state of the pair, vr < EPS r v with EPS = 0.001
+// (jdata.cc:797,822-848).  mode bits: 2 stop on an approaching collision
+// pair, 4 stop on any close pair.
+__global__ void enc_verdict_kernel(g6_jstate js, g6_enc *enc, int mode, double tnext, int *flag) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int cap = js.cap;
+  for (int p = 0; p < 2; p++) {
+    enc->close_id[p] = enc->close_slot[p] >= 0 ? js.id[enc->close_slot[p]] : -1;
+    enc->coll_id[p] = enc->coll_slot[p] >= 0 ? js.id[enc->coll_slot[p]] : -1;
+  }
+  int stop = 0;
+  if ((mode & 2) && enc->coll_slot[0] >= 0) {
+    const int j1 = enc->coll_slot[0], j2 = enc->coll_slot[1];
+    double r = 0, v = 0, vr = 0;
+    for (int k = 0; k < 3; k++) {
+      const double dx = dsub(js.x[k * cap + j1], js.x[k * cap + j2]);
+      const double dv = dsub(js.v[k * cap + j1], js.v[k * cap + j2]);
+      r = dadd(r, dmul(dx, dx));
+      v = dadd(v, dmul(dv, dv));
+      vr = dadd(vr, dmul(dx, dv));
+    }
+    r = __dsqrt_rn(r);
+    v = __dsqrt_rn(v);
+    if (vr < dmul(dmul(0.001, r), v)) stop |= 1;
+  }
+  if ((mode & 4) && enc->close_slot[0] >= 0) stop |= 2;
+  enc->stopped = stop;
+  enc->t = tnext;
+  *flag = stop;
 }
 
 __global__ void store_kernel(g6_jstate js, int ni, const int *__restrict__ ilist,
@@ -308,6 +468,21 @@ extern "C" int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni
   sched_init<<<1, 1, 0, st>>>(dmin, d_ni);
   sched_min<<<grid, PT, 0, st>>>(*js, nj, dmin);
   sched_list<<<grid, PT, 0, st>>>(*js, nj, dmin, d_ilist, d_ni, d_tnext);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+extern "C" int g6k_enc_check(const g6_jstate *js, const double *rad, int ni, const int *ilist,
+                             const int *nn, double tnext, double rmin, double *part_d,
+                             int *part_i, unsigned *counter, g6_enc *enc, cudaStream_t st) {
+  if (ni <= 0) return 0;
+  enc_check_kernel<<<(ni + PT - 1) / PT, PT, 0, st>>>(*js, rad, ni, ilist, nn, tnext, rmin,
+                                                      part_d, part_i, counter, enc);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+extern "C" int g6k_enc_verdict(const g6_jstate *js, g6_enc *enc, int mode, double tnext,
+                               int *flag, cudaStream_t st) {
+  enc_verdict_kernel<<<1, 32, 0, st>>>(*js, enc, mode, tnext, flag);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

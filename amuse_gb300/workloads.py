@@ -322,6 +322,26 @@ def run_salpeter(args):
                   "pairs_per_s": ns * (n - 1) / wall, "E0": e0, "E1": e1,
                   "dE_over_E": abs(e1 - e0) / abs(e0)}
     print(json.dumps(out), flush=True)
+    if args.encounters:
+        # The same run with ph4's encounter check after every block (nearest
+        # neighbours in the force, the criteria before and the stopping test
+        # after the corrector; radius 0, so nothing stops).  The forces are
+        # the same arithmetic with or without the neighbour search, so the
+        # block sequence must repeat exactly.
+        g6.load_particles(m, x, v)
+        g6.set_encounters(ag.ENC_CHECK)
+        g6.run_init(eps2, args.eta)
+        t0 = time.perf_counter()
+        nb2, ns2 = g6.run(args.t_end)
+        wall2 = time.perf_counter() - t0
+        enc = g6.encounter()
+        g6.set_encounters(0)
+        k2, p2 = g6.energy()
+        out["run_with_encounter_check"] = {
+            "blocks": nb2, "seconds": wall2, "overhead": wall2 / wall - 1.0,
+            "same_blocks": nb2 == nb and ns2 == ns, "same_energy": (k2 + p2) == e1,
+            "rmin": 2.0 / n, "last_block": enc}
+        print(json.dumps(out), flush=True)
     checks = {}
     for ni in (1, 2, 3, 7, 31, 100, 1000, 4096, 10000, n):
         ni = min(ni, n)
@@ -364,6 +384,8 @@ def main():
     sa.add_argument("--t-end", type=float, default=0.25)
     sa.add_argument("--seed", type=int, default=1)
     sa.add_argument("--fp64", action="store_true")
+    sa.add_argument("--encounters", action="store_true",
+                    help="repeat the run with the encounter check on and report its cost")
     a = ap.parse_args()
     if a.cmd == "batch":
         run_batch(a)

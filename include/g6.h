@@ -181,6 +181,29 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps);
 /* Host-side account of the last g6x_run: out = {block steps, wall ms, ms
    spent waiting in the per-block synchronisation, particle steps}. */
 int g6x_run_stats(double out[4]);
+/* Encounter check in g6x_run (replaces ph4's idata::check_encounters,
+   src/amuse_ph4/src/idata.cc:620-700, and the COLLISION_DETECTION stopping
+   condition of jdata::advance_and_check_encounter, jdata.cc:797-850).
+   With G6_ENC_CHECK the force of every block also finds each particle's
+   nearest neighbour; over the block, the particle with the largest
+   rmin/dnn gives the close pair and the one with the largest
+   (R_i + R_nn)/dnn the collision pair, each when that ratio is >= 1 (dnn in
+   FP64 from both particles predicted to the block time; ties go to the
+   smaller slot, where ph4 takes the first in its scheduler's list).
+   G6_ENC_STOP_COLLISION ends g6x_run after a block whose collision pair is
+   approaching (vr < 0.001 r v on the corrected state), as ph4's worker
+   ends evolve_model; G6_ENC_STOP_CLOSE after any block with a close pair
+   (for a caller that resolves encounters itself).  Stop bits imply CHECK.
+   rmin <= 0 selects ph4's default 2/n (jdata.cc:426).  Radii are set by
+   slot (default 0).  g6x_encounter reports the last checked block: ids =
+   {close1, close2, coll1, coll2} (particle ids, -1 none), out = {stop bits
+   (1 collision, 2 close), block time, rmax_close, rmax_coll}. */
+#define G6_ENC_CHECK 1
+#define G6_ENC_STOP_COLLISION 2
+#define G6_ENC_STOP_CLOSE 4
+int g6x_set_encounters(int mode, double rmin);
+int g6x_set_radius(int n, const double *radius);
+int g6x_encounter(int ids[4], double out[4]);
 int g6x_energy(double *kinetic, double *potential);
 int g6x_step_all(double tnext);
 /* FP64 corrector + Aarseth step (idata.cc:399-514) applied on the device to

@@ -61,6 +61,10 @@ def port():
         lib.orc_run.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_dbl, _c_int,
                                 _dp, _dp, _dp, _dp, _dp, _dp, _c_long]
         lib.orc_run.restype = _c_long
+        lib.orc_run_enc.argtypes = [_c_int, _dp, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_dbl,
+                                    _c_int, _dp, _dp, _dp, _dp, _dp, _dp, _c_long, _c_int,
+                                    _c_dbl, _dp]
+        lib.orc_run_enc.restype = _c_long
         lib.orc_smalln.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_int, _c_dbl, _dp, _c_long]
         lib.orc_smalln.restype = _c_long
         lib.orc_hermite_fixed.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_int, _dp,
@@ -85,6 +89,8 @@ def ref():
         lib.ph4ref_run.argtypes = [_c_int, _dp, _ip, _dp, _dp, _c_dbl, _c_dbl, _c_dbl,
                                    _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         lib.ph4ref_smalln.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_dbl, _dp]
+        lib.ph4ref_run_coll.argtypes = [_c_int, _dp, _dp, _ip, _dp, _dp, _c_dbl, _c_dbl,
+                                        _c_dbl, _c_int, _dp, _dp, _dp, _dp, _dp, _dp]
         _ref_lib = lib
     return _ref_lib
 
@@ -154,6 +160,58 @@ def run(mass, pos, vel, eps2, eta, t_end, threads=1, lib=None, ids=None, max_blo
                             time, step, stats, max_blocks)
     return dict(pos=pos, vel=vel, acc=acc, jerk=jerk, pot=pot, time=time, timestep=step,
                 E0=stats[0], E1=stats[1], total_steps=stats[2], t=stats[3], blocks=blocks)
+
+
+ENC_CHECK, ENC_STOP_COLL, ENC_STOP_CLOSE = 1, 2, 4
+
+
+def run_enc(mass, radius, pos, vel, eps2, eta, t_end, mode=ENC_CHECK | ENC_STOP_COLL, rmin=0.0,
+            threads=1, lib=None, max_blocks=0):
+    """Block-step ph4 run with idata::check_encounters after every block
+    (idata.cc:620-700) and the COLLISION_DETECTION stopping condition
+    (jdata.cc:797-850).  Particle ids are 1..n (slot + 1).  Returns the
+    final state plus: close / coll (id pairs of the last block, None if
+    none), stopped (0 none, 1 collision, 2 close), t, blocks, rmin.  The
+    reference build supports only mode = CHECK | STOP_COLL with the default
+    rmin; its pair order follows ph4's scheduler list, the port's slot
+    order.  With lib="ref", mode CHECK | STOP_CLOSE ends the harness loop
+    after the first block with a close pair (the pair ph4 would hand to
+    resolve_encounter)."""
+    mass, radius = _c(mass), _c(radius)
+    pos, vel = _c(pos).copy(), _c(vel).copy()
+    n = len(mass)
+    time = np.zeros(n); step = np.zeros(n)
+    enc = np.zeros(8)
+
+    def pair(a, b):
+        return None if a < 0 else (int(a), int(b))
+
+    if lib == "ref":
+        if mode not in (ENC_CHECK | ENC_STOP_COLL, ENC_CHECK | ENC_STOP_CLOSE,
+                        ENC_CHECK | ENC_STOP_COLL | ENC_STOP_CLOSE) or rmin > 0:
+            raise ValueError("the reference harness needs CHECK and the default rmin")
+        ids = _c(np.arange(1, n + 1), np.int32)
+        stats = np.zeros(5)
+        pos_o = np.zeros_like(pos); vel_o = np.zeros_like(vel)
+        ref().ph4ref_run_coll(n, mass, radius, ids, pos, vel, eps2, eta, t_end,
+                              1 if mode & ENC_STOP_CLOSE else 0, pos_o, vel_o, time, step, stats,
+                              enc)
+        stop_pair = pair(enc[5], enc[6]) if enc[4] else None
+        return dict(pos=pos_o, vel=vel_o, time=time, timestep=step, E0=stats[0], E1=stats[1],
+                    total_steps=stats[2], t=stats[3], blocks=int(stats[4]),
+                    close=pair(enc[0], enc[1]), coll=pair(enc[2], enc[3]),
+                    stopped=int(enc[4]), stop_pair=stop_pair, rmin=enc[7])
+    acc = np.zeros((n, 3)); jerk = np.zeros((n, 3)); pot = np.zeros(n)
+    stats = np.zeros(4)
+    blocks = port().orc_run_enc(n, mass, radius, pos, vel, eps2, eta, t_end, threads, acc, jerk,
+                                pot, time, step, stats, max_blocks, mode, rmin, enc)
+    ids = lambda a, b: None if a < 0 else (int(a) + 1, int(b) + 1)
+    stopped = int(enc[6])
+    coll = ids(enc[2], enc[3])
+    return dict(pos=pos, vel=vel, acc=acc, jerk=jerk, pot=pot, time=time, timestep=step,
+                E0=stats[0], E1=stats[1], total_steps=stats[2], t=stats[3], blocks=int(blocks),
+                close=ids(enc[0], enc[1]), coll=coll, rmax_close=enc[4], rmax_coll=enc[5],
+                stopped=stopped, stop_pair=coll if stopped & 1 else None, rmin=enc[7])
 
 
 def smalln(mass, pos, vel, eta, t_end, n_iter=2, lib=None, dt_crit=0.0, max_steps=0):

@@ -18,6 +18,10 @@
  *   orc_run            src/amuse_ph4/src/jdata.cc:752-795 + idata.cc:832-881
  *                      (block-step loop of interface.cc:614-711, CPU mode,
  *                      manage_encounters = 0)
+ *   orc_run_enc        the same loop with idata::check_encounters
+ *                      (idata.cc:620-700) after every block and the
+ *                      COLLISION_DETECTION stopping condition of
+ *                      jdata::advance_and_check_encounter (jdata.cc:797-850)
  *   orc_hermite_fixed  src/amuse_hermite/interface.cc:266-281,387-552
  *                      (shared fixed-step Hermite, test_mode)
  */
@@ -287,10 +291,77 @@ static double energy_at(int n, double t, const double *mass, const double *time,
 /* State arrays are updated in place; returns block steps taken.        */
 /* stats (optional, length 4): E0, E1, total particle steps, t_final.   */
 /* ------------------------------------------------------------------ */
-long orc_run(int n, const double *mass, double *pos, double *vel, double eps2,
-             double eta, double t_end, int nthreads, double *acc, double *jerk,
-             double *pot, double *time, double *timestep, double *stats,
-             long max_blocks) {
+/* Encounter check modes (bits), shared with the library's g6x_set_encounters. */
+#define ORC_ENC_CHECK 1     /* run idata::check_encounters after every block */
+#define ORC_ENC_STOP_COLL 2 /* stop as COLLISION_DETECTION does (vr test) */
+#define ORC_ENC_STOP_CLOSE 4 /* stop when a close pair (rmin) is found */
+#define ORC_ENC_EPS 0.001   /* jdata.cc:797 (from couple/multiples.py) */
+
+/* idata::check_encounters (idata.cc:620-700) in CPU mode for one block:
+   nn/dnn are the block's nearest neighbours (j indices) and distances from
+   the force loop.  The first i (block order = slot order here) with the
+   largest rmin/dnn, resp. (R_i + R_nn)/dnn, wins; a pair is reported when
+   that ratio is >= 1.  ph4 tests the mass of i as imass[i], which CPU mode
+   never fills; the nn of a CPU-mode force always has mass > 2^-52, so the
+   test passes either way.  enc[0..5]: close pair (slots), collision pair
+   (slots), rmax_close, rmax_coll. */
+static void check_encounters(int ni, const int *ilist, const int *inn,
+                             const double *idnn, const double *mass,
+                             const double *radius, double rmin, double *enc) {
+  double rmax_close = 0, rmax_coll = 0;
+  int imax_close = -1, imax_coll = -1;
+  for (int i = 0; i < ni; i++) {
+    int jnn = inn[i];
+    if (jnn < 0) continue;
+    if (mass[jnn] > ORC_TINY || mass[ilist[i]] > ORC_TINY) {
+      double r = rmin / idnn[i];
+      if (r > rmax_close) {
+        rmax_close = r;
+        imax_close = i;
+      }
+      r = (radius[ilist[i]] + radius[jnn]) / idnn[i];
+      if (r > rmax_coll) {
+        rmax_coll = r;
+        imax_coll = i;
+      }
+    }
+  }
+  enc[0] = enc[1] = enc[2] = enc[3] = -1;
+  if (rmax_close >= 1) {
+    enc[0] = ilist[imax_close];
+    enc[1] = inn[imax_close];
+  }
+  if (rmax_coll >= 1) {
+    enc[2] = ilist[imax_coll];
+    enc[3] = inn[imax_coll];
+  }
+  enc[4] = rmax_close;
+  enc[5] = rmax_coll;
+}
+
+/* The COLLISION_DETECTION test of jdata::advance_and_check_encounter
+   (jdata.cc:822-848) on the current (corrected) state of the pair. */
+static int collision_approaching(const double *pos, const double *vel, int j1,
+                                 int j2) {
+  double r = 0, v = 0, vr = 0;
+  for (int k = 0; k < 3; k++) {
+    double dx = pos[3 * j1 + k] - pos[3 * j2 + k];
+    double dv = vel[3 * j1 + k] - vel[3 * j2 + k];
+    r += dx * dx;
+    v += dv * dv;
+    vr += dx * dv;
+  }
+  r = sqrt(r);
+  v = sqrt(v);
+  return vr < ORC_ENC_EPS * r * v;
+}
+
+static long run_impl(int n, const double *mass, double *pos, double *vel,
+                     double eps2, double eta, double t_end, int nthreads,
+                     double *acc, double *jerk, double *pot, double *time,
+                     double *timestep, double *stats, long max_blocks,
+                     const double *radius, int enc_mode, double rmin,
+                     double *enc_out) {
   double *pp = (double *)malloc(sizeof(double) * 3 * n);
   double *pv = (double *)malloc(sizeof(double) * 3 * n);
   double *scratch = (double *)malloc(sizeof(double) * 13 * n);
@@ -304,6 +375,12 @@ long orc_run(int n, const double *mass, double *pos, double *vel, double eps2,
   double *ipot = (double *)malloc(sizeof(double) * n);
   double *it = (double *)malloc(sizeof(double) * n);
   double *its = (double *)malloc(sizeof(double) * n);
+  int *inn = (int *)malloc(sizeof(int) * n);
+  double *idnn = (double *)malloc(sizeof(double) * n);
+  double enc[6] = {-1, -1, -1, -1, 0, 0};
+  int stopped = 0;
+  /* jdata::initialize_arrays (jdata.cc:426): rmin = 2/nj by default. */
+  if (rmin <= 0 && n > 0) rmin = 2. / n;
   double system_time = 0;
   /* commit_particles: initialize_arrays (time = 0, acc = jerk = 0),
      predict_all(0, true), idata::setup -> forces on all, scatter. */
@@ -342,7 +419,7 @@ long orc_run(int n, const double *mass, double *pos, double *vel, double eps2,
       }
     }
     orc_force_mt(nthreads, n, mass, pp, pv, eps2, ni, ip, iv, ia, ij, ipot,
-                 NULL, NULL);
+                 enc_mode ? inn : NULL, enc_mode ? idnn : NULL);
     orc_correct(ni, tnext, eta, it, its, ip, iv, oa, oj, ia, ij);
     for (int i = 0; i < ni; i++) {
       int j = ilist[i];
@@ -359,6 +436,14 @@ long orc_run(int n, const double *mass, double *pos, double *vel, double eps2,
     blocks++;
     steps += ni;
     system_time = tnext;
+    if (enc_mode) {
+      check_encounters(ni, ilist, inn, idnn, mass, radius, rmin, enc);
+      if ((enc_mode & ORC_ENC_STOP_COLL) && enc[2] >= 0 &&
+          collision_approaching(pos, vel, (int)enc[2], (int)enc[3]))
+        stopped = 1;
+      if ((enc_mode & ORC_ENC_STOP_CLOSE) && enc[0] >= 0) stopped |= 2;
+      if (stopped) break;
+    }
   }
   double e1 = energy_at(n, system_time, mass, time, pos, vel, acc, jerk, eps2,
                         scratch, nthreads);
@@ -368,9 +453,39 @@ long orc_run(int n, const double *mass, double *pos, double *vel, double eps2,
     stats[2] = steps;
     stats[3] = system_time;
   }
+  if (enc_out) {
+    for (int k = 0; k < 6; k++) enc_out[k] = enc[k];
+    enc_out[6] = stopped;
+    enc_out[7] = rmin;
+  }
   free(pp); free(pv); free(scratch); free(ilist); free(ip); free(iv);
   free(oa); free(oj); free(ia); free(ij); free(ipot); free(it); free(its);
+  free(inn); free(idnn);
   return blocks;
+}
+
+long orc_run(int n, const double *mass, double *pos, double *vel, double eps2,
+             double eta, double t_end, int nthreads, double *acc, double *jerk,
+             double *pot, double *time, double *timestep, double *stats,
+             long max_blocks) {
+  return run_impl(n, mass, pos, vel, eps2, eta, t_end, nthreads, acc, jerk,
+                  pot, time, timestep, stats, max_blocks, NULL, 0, 0.0, NULL);
+}
+
+/* orc_run with the encounter check after every block.  radius[n] (ph4's
+   particle radius), enc_mode (ORC_ENC_* bits), rmin (<= 0: 2/n).
+   enc_out[8]: close pair (slots, -1 none), collision pair (slots),
+   rmax_close, rmax_coll of the last block, stopped (1 collision, 2 close),
+   rmin used.  A stop ends the run after that block, as the ph4 worker's
+   evolve_model does (interface.cc:667-668). */
+long orc_run_enc(int n, const double *mass, const double *radius, double *pos,
+                 double *vel, double eps2, double eta, double t_end,
+                 int nthreads, double *acc, double *jerk, double *pot,
+                 double *time, double *timestep, double *stats,
+                 long max_blocks, int enc_mode, double rmin, double *enc_out) {
+  return run_impl(n, mass, pos, vel, eps2, eta, t_end, nthreads, acc, jerk,
+                  pot, time, timestep, stats, max_blocks, radius, enc_mode,
+                  rmin, enc_out);
 }
 
 /* ------------------------------------------------------------------ */

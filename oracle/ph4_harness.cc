@@ -174,6 +174,83 @@ int ph4ref_run(int n, const double *mass, const int *ids, const double *pos,
   return 0;
 }
 
+// Full run with the COLLISION_DETECTION stopping condition enabled, as the
+// ph4 worker sets it up (interface.cc:106 set_support_for_condition, :629
+// reset_stopping_conditions, :667-668 the evolve loop): particles carry a
+// radius; after every block idata::check_encounters (idata.cc:620-700) runs
+// and jdata::advance_and_check_encounter (jdata.cc:797-850) stops the run
+// when the collision pair is approaching.  enc_out: close1, close2, coll1,
+// coll2 (ids from the last block, -1 none), stopping condition set (0/1),
+// its two particle ids, rmin.  stats as ph4ref_run.  stop_on_close also ends
+// the loop after the first block that reports a close pair (jd->close1, the
+// pair ph4 hands to resolve_encounter when it manages encounters itself).
+int ph4ref_run_coll(int n, const double *mass, const double *radius, const int *ids,
+                    const double *pos, const double *vel, double eps2, double eta,
+                    double t_end, int stop_on_close, double *pos_out, double *vel_out,
+                    double *time_out, double *step_out, double *stats, double *enc_out) {
+  std::streambuf *old = std::cout.rdbuf(NULL);
+  set_support_for_condition(COLLISION_DETECTION);
+  enable_stopping_condition(COLLISION_DETECTION);
+  reset_stopping_conditions();
+  jdata *jd = new jdata;
+  jd->setup_gpu();
+  jd->system_time = 0;
+  jd->sync_time = 0;
+  jd->set_manage_encounters(0);
+  jd->eps2 = eps2;
+  jd->eta = eta;
+  for (int j = 0; j < n; j++) {
+    vec p(pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]);
+    vec v(vel[3 * j], vel[3 * j + 1], vel[3 * j + 2]);
+    jd->add_particle(mass[j], radius[j], p, v, ids[j]);
+  }
+  jd->initialize_arrays();
+  idata *id = new idata(jd);
+  jd->force_initial_timestep(0.0625, 0.03125, 8.0);
+  scheduler *s = new scheduler(jd);
+  double e0 = jd->get_energy();
+  jd->coll1 = jd->coll2 = -1;
+  jd->close1 = jd->close2 = -1;
+  while (jd->system_time < t_end) {
+    if (jd->advance_and_check_encounter()) break;
+    if (stop_on_close && jd->close1 >= 0) break;
+  }
+  int set = 0, p0 = -1, p1 = -1;
+  is_stopping_condition_set(COLLISION_DETECTION, &set);
+  if (set) {
+    get_stopping_condition_particle_index(0, 0, &p0);
+    get_stopping_condition_particle_index(0, 1, &p1);
+  }
+  enc_out[0] = jd->close1;
+  enc_out[1] = jd->close2;
+  enc_out[2] = jd->coll1;
+  enc_out[3] = jd->coll2;
+  enc_out[4] = set;
+  enc_out[5] = p0;
+  enc_out[6] = p1;
+  enc_out[7] = jd->rmin;
+  double e1 = jd->get_energy();
+  disable_stopping_condition(COLLISION_DETECTION);
+  reset_stopping_conditions();
+  std::cout.rdbuf(old);
+  for (int j = 0; j < n; j++) {
+    time_out[j] = jd->time[j];
+    step_out[j] = jd->timestep[j];
+    for (int k = 0; k < 3; k++) {
+      pos_out[3 * j + k] = jd->pos[j][k];
+      vel_out[3 * j + k] = jd->vel[j][k];
+    }
+  }
+  stats[0] = e0;
+  stats[1] = e1;
+  stats[2] = jd->total_steps;
+  stats[3] = jd->system_time;
+  stats[4] = jd->block_steps;
+  (void)s;
+  (void)id;
+  return 0;
+}
+
 // smallN (src/amuse_ph4/src/smallN.cc smallN_evolve) on one system, set up
 // as the smallN worker does (src/amuse_smalln/interface.cc:61-85,
 // src/amuse_smalln/src/smallN_interface.cc:8-36), with dt_crit given

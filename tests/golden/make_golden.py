@@ -6,9 +6,11 @@ Runs in the development container only (it needs the reference checkout):
   * the unmodified ph4 CPU objects, compiled by ``make -C oracle ref`` into
     oracle/_ref/libph4ref.so, give the outputs (force: idata.cc:147-237,
     corrector: idata.cc:399-514, full block-step run: interface.cc:317-711,
-    smallN few-body runs: smallN.cc:906-1117 with dt_crit = 0).
+    smallN few-body runs: smallN.cc:906-1117 with dt_crit = 0, block-step
+    runs with the encounter check: idata.cc:620-700, jdata.cc:797-850).
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference] [--only smalln]
+Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+                                          [--only smalln|encounters]
 """
 import argparse
 import os
@@ -47,13 +49,15 @@ def save(name, **arrays):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, choices=[None, "smalln"])
+    ap.add_argument("--only", default=None, choices=[None, "smalln", "encounters"])
     args = ap.parse_args()
     sys.path.insert(0, os.path.join(args.ref, "src"))
     import oracle
     oracle.build_ref(args.ref)
     if args.only == "smalln":
         return smalln_fixtures(oracle)
+    if args.only == "encounters":
+        return encounter_fixtures(oracle)
 
     # 1. IC generators (pins amuse_gb300/ic.py).
     np.random.seed(1)
@@ -146,6 +150,37 @@ def smalln_fixtures(oracle):
         out.update({f"s{k}_mass": m, f"s{k}_pos0": x, f"s{k}_vel0": v, f"s{k}_pos": p,
                     f"s{k}_vel": vv, f"s{k}_t": t})
     save("smalln_systems.npz", nsys=len(out) // 6, eta=0.14, t_end=2 * tcr, **out)
+
+
+# (n, seed, radius, mode): collision stops (radius R for all particles) and
+# close-pair stops (radius 0, ph4's rmin = 2/n).
+ENCOUNTER_CASES = [(64, 1, 0.02, "coll"), (128, 3, 0.01, "coll"), (256, 4, 0.005, "coll"),
+                   (64, 5, 0.0, "close"), (256, 4, 0.0, "close")]
+
+
+def encounter_fixtures(oracle):
+    """8. ph4 block-step runs with the encounter check: AMUSE's Plummer
+    spheres (eps2 = 1e-4, eta = 0.14, to t = 1 or 2) run through the
+    unmodified ph4 objects with the COLLISION_DETECTION stopping condition
+    enabled (idata.cc:620-700, jdata.cc:797-850), or until the first block
+    that reports a close pair.  Ids are slot + 1."""
+    from amuse_gb300 import ic
+    out = {}
+    for k, (n, seed, rad, kind) in enumerate(ENCOUNTER_CASES):
+        np.random.seed(seed)
+        m, x, v = ic.plummer(n)
+        radius = np.full(n, rad)
+        mode = oracle.ENC_CHECK | (oracle.ENC_STOP_COLL if kind == "coll"
+                                   else oracle.ENC_STOP_CLOSE)
+        t_end = 1.0 if kind == "coll" else 2.0
+        r = oracle.run_enc(m, radius, x, v, 1e-4, 0.14, t_end, mode=mode, lib="ref")
+        pair = r["stop_pair"] if kind == "coll" else r["close"]
+        assert pair is not None, (n, seed, kind)
+        out.update({f"c{k}_mass": m, f"c{k}_pos0": x, f"c{k}_vel0": v, f"c{k}_radius": radius,
+                    f"c{k}_mode": mode, f"c{k}_t_end": t_end, f"c{k}_t": r["t"],
+                    f"c{k}_blocks": r["blocks"], f"c{k}_pair": np.array(pair),
+                    f"c{k}_pos": r["pos"], f"c{k}_vel": r["vel"], f"c{k}_rmin": r["rmin"]})
+    save("encounter_runs.npz", ncase=len(ENCOUNTER_CASES), eps2=1e-4, eta=0.14, **out)
 
 
 if __name__ == "__main__":

@@ -93,11 +93,6 @@ int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t st);
 int g6k_correct(const g6_jstate *js, int ni, const int *ilist, double tnext,
                 double eta, const double *acc, const double *jerk,
                 const double *pot, const int *nn, cudaStream_t st);
-/* Block scheduler: tnext = min(t+dt); ilist = slots with t+dt == tnext.
- * Writes tnext to *d_tnext and the count to *d_ni. scratch >= 2*grid. */
-int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni,
-                 double *d_tnext, double *d_scratch, int scratch_len,
-                 cudaStream_t st);
 /* Encounter check of one block (idata::check_encounters, idata.cc:620-700)
  * and the stopping decision after its corrector (jdata.cc:797-850).         */
 typedef struct {
@@ -108,9 +103,16 @@ typedef struct {
   int stopped;                  /* 1 collision, 2 close pair (bits) */
   int pad;
 } g6_enc;
+/* A block whose stopping decision (g6k_enc_verdict) is still to be taken. */
+typedef struct {
+  g6_enc *enc; /* NULL: none */
+  int mode;
+  double t;
+  int *flag;
+} g6_enc_verdict_args;
 /* Pre-corrector pass over the block: nn[i] is the nearest j slot of ilist[i]
  * from the force; distances are recomputed in FP64 from both particles
- * predicted to tnext.  part_d >= 2 * ceil(ni/256), part_i >= 4 * ceil(ni/256),
+ * predicted to tnext.  part_d >= 2 * ceil(ni/32), part_i >= 4 * ceil(ni/32),
  * *counter == 0 on entry (left 0).                                           */
 int g6k_enc_check(const g6_jstate *js, const double *rad, int ni, const int *ilist,
                   const int *nn, double tnext, double rmin, double *part_d, int *part_i,
@@ -119,6 +121,13 @@ int g6k_enc_check(const g6_jstate *js, const double *rad, int ni, const int *ili
  * state, stop bits into enc->stopped and *flag.                              */
 int g6k_enc_verdict(const g6_jstate *js, g6_enc *enc, int mode, double tnext, int *flag,
                     cudaStream_t st);
+/* Block scheduler: tnext = min(t+dt); ilist = slots with t+dt == tnext.
+ * Writes tnext to *d_tnext and the count to *d_ni. scratch >= 2*grid.
+ * verdict (or NULL): the previous block's pending encounter verdict, taken
+ * by the scheduler's first kernel (after that block's corrector). */
+int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni,
+                 double *d_tnext, double *d_scratch, int scratch_len,
+                 const g6_enc_verdict_args *verdict, cudaStream_t st);
 /* Initial time steps (jdata.cc:503-564 without the median limit). */
 int g6k_initial_step(const g6_jstate *js, int nj, double eta, double fac,
                      double limit, double system_time, cudaStream_t st);

@@ -1167,7 +1167,7 @@ static int ensure_radius(int n) {
 }
 
 static int ensure_enc_buffers(int n) {
-  const int grid = (n + 255) / 256;
+  const int grid = (n + 31) / 32; /* enc_check_kernel: 32 particles per CTA */
   int rc = ensure_radius(n);
   if (rc) return rc;
   if (!G.d_enc) {
@@ -1321,9 +1321,10 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
   int hbuf[2];
   double tn;
   /* Encounter check: the force also finds each block particle's nearest
-     neighbour, a pass before the corrector evaluates ph4's criteria, one
-     after it the stopping test; its stop bits reach the host in the next
-     block's mailbox copy, before that block's force is launched. */
+     neighbour and a pass before the corrector evaluates ph4's criteria.  The
+     stopping test on the corrected pair runs in the first kernel of the next
+     block's scheduler (or after the loop), and its stop bits reach the host
+     in that block's mailbox copy, before that block's force is launched. */
   const int enc = G.enc_mode;
   const double rmin = G.enc_rmin > 0 ? G.enc_rmin : 2.0 / n; /* jdata.cc:426 */
   int *d_stop = (int *)((char *)G.d_mail + 12);
@@ -1332,10 +1333,14 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
     if (rc) return rc;
     CK(cudaMemsetAsync(d_stop, 0, sizeof(int), G.st));
   }
+  g6_enc_verdict_args pend; /* the last block's verdict, taken by the next schedule */
+  memset(&pend, 0, sizeof(pend));
   while (G.run_t < t_end && nb != max_blocks) {
     ilist_identity_n = 0;
-    if (g6k_schedule(&G.js, n, G.d_ilist, G.d_ni, G.d_tnext, G.d_sched, 4, G.st))
+    if (g6k_schedule(&G.js, n, G.d_ilist, G.d_ni, G.d_tnext, G.d_sched, 4,
+                     pend.enc ? &pend : NULL, G.st))
       return G6_ERR_CUDA;
+    pend.enc = NULL;
     /* one 16-byte copy into pinned memory: the only host round trip per block */
     CK(cudaMemcpyAsync(G.h_mail, G.d_mail, 16, cudaMemcpyDeviceToHost, G.st));
     const double s0 = now_ms();
@@ -1358,12 +1363,20 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
     if (g6k_correct(&G.js, ni, G.d_ilist, tn, G.run_eta, G.d_racc, G.d_rjerk, G.d_rpot,
                     enc ? G.d_rnn : NULL, G.st))
       return G6_ERR_CUDA;
-    if (enc && g6k_enc_verdict(&G.js, G.d_enc, enc, tn, d_stop, G.st)) return G6_ERR_CUDA;
+    if (enc) {
+      pend.enc = G.d_enc;
+      pend.mode = enc;
+      pend.t = tn;
+      pend.flag = d_stop;
+    }
     G.pred_valid = 0; /* j-state changed */
     G.run_t = tn;
     nb++;
     ns += ni;
   }
+  /* the loop ended on time or block count: the last block's verdict */
+  if (pend.enc && g6k_enc_verdict(&G.js, pend.enc, pend.mode, pend.t, pend.flag, G.st))
+    return G6_ERR_CUDA;
   CK(cudaStreamSynchronize(G.st));
   run_stats[0] = (double)nb;
   run_stats[1] = now_ms() - w0;

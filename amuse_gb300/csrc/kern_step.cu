@@ -175,9 +175,10 @@ __device__ __forceinline__ EncC enc_shfl(const EncC &c, int o) {
   return d;
 }
 
-// Both candidates reduced over the CTA; the result is valid in thread 0.
+// Both candidates reduced over the CTA (at most 8 warps); the result is
+// valid in thread 0.
 __device__ void enc_block_reduce(EncC &c0, EncC &c1) {
-  __shared__ EncC sh[2][PT / 32];
+  __shared__ EncC sh[2][8];
   for (int o = 16; o > 0; o >>= 1) {
     enc_take(c0, enc_shfl(c0, o));
     enc_take(c1, enc_shfl(c1, o));
@@ -189,49 +190,56 @@ __device__ void enc_block_reduce(EncC &c0, EncC &c1) {
   }
   __syncthreads();
   if (threadIdx.x == 0)
-    for (int k = 1; k < PT / 32; k++) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
       enc_take(c0, sh[0][k]);
       enc_take(c1, sh[1][k]);
     }
   __syncthreads();
 }
 
-// One thread per block particle: dnn = |x_nn - x_i| with both predicted to
-// tnext in FP64 (ph4 CPU mode: sqrt of the force loop's min r^2 over the
-// predicted j-system), then r_close = rmin / dnn and r_coll =
-// (R_i + R_nn) / dnn for pairs with at least one massive member.  Each CTA
-// leaves its best two candidates in part_*; the last CTA to finish (atomic
-// ticket) reduces them and writes the block's result.
+// Four lanes per block particle, as in the corrector (FP64 runs at 2 lanes
+// per SM here, so a block's FP64 work has to spread over many SMs): lane
+// k < 3 predicts component k of the particle and of its nearest neighbour
+// to tnext and forms dx_k^2; the group sums them in component order (ph4
+// CPU mode: idnn = sqrt of the force loop's min r^2 over the predicted
+// j-system).  The group's first lane forms r_close = rmin / dnn and r_coll
+// = (R_i + R_nn) / dnn for pairs with at least one massive member.  Each
+// CTA leaves its best two candidates in part_*; the last CTA to finish
+// (atomic ticket) reduces them and writes the block's result.
 __global__ void enc_check_kernel(g6_jstate js, const double *__restrict__ rad, int ni,
                                  const int *__restrict__ ilist, const int *__restrict__ nn,
                                  double tnext, double rmin, double *part_d, int *part_i,
                                  unsigned *counter, g6_enc *enc) {
   const double tiny = 1.0 / 4503599627370496.0;  // 2^-52 (stdinc.h)
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  EncC cc = {0.0, INT_MAX, -1}, cl = {0.0, INT_MAX, -1};
-  if (i < ni) {
-    const int s = ilist[i];
-    const int jn = nn[i];
-    if (jn >= 0 && (js.m[jn] > tiny || js.m[s] > tiny)) {
-      const int cap = js.cap;
-      const double dti = dsub(tnext, js.t[s]), dtj = dsub(tnext, js.t[jn]);
-      double r2 = 0;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = g >> 2;
+  const int k = g & 3;
+  const int base = (threadIdx.x & 31) & ~3;
+  const int ii = i < ni ? i : 0;
+  const int s = ilist[ii];
+  const int jn = nn[ii];
+  const bool valid = i < ni && jn >= 0 && (js.m[jn] > tiny || js.m[s] > tiny);
+  double p = 0;
+  if (valid && k < 3) {
+    const int cap = js.cap;
+    const int a = k * cap + s, b = k * cap + jn;
+    const double xi = predict_x(js.x[a], js.v[a], js.a[a], js.j[a], dsub(tnext, js.t[s]));
+    const double xj = predict_x(js.x[b], js.v[b], js.a[b], js.j[b], dsub(tnext, js.t[jn]));
+    const double dx = dsub(xj, xi);
+    p = dmul(dx, dx);
+  }
+  double r2 = 0;
 #pragma unroll
-      for (int k = 0; k < 3; k++) {
-        const int a = k * cap + s, b = k * cap + jn;
-        const double xi = predict_x(js.x[a], js.v[a], js.a[a], js.j[a], dti);
-        const double xj = predict_x(js.x[b], js.v[b], js.a[b], js.j[b], dtj);
-        const double dx = dsub(xj, xi);
-        r2 = dadd(r2, dmul(dx, dx));
-      }
-      const double dnn = __dsqrt_rn(r2);
-      cc.r = ddiv(rmin, dnn);
-      cc.s = s;
-      cc.j = jn;
-      cl.r = ddiv(dadd(rad[s], rad[jn]), dnn);
-      cl.s = s;
-      cl.j = jn;
-    }
+  for (int c = 0; c < 3; c++) r2 = dadd(r2, __shfl_sync(0xffffffffu, p, base + c));
+  EncC cc = {0.0, INT_MAX, -1}, cl = {0.0, INT_MAX, -1};
+  if (valid && k == 0) {
+    const double dnn = __dsqrt_rn(r2);
+    cc.r = ddiv(rmin, dnn);
+    cc.s = s;
+    cc.j = jn;
+    cl.r = ddiv(dadd(rad[s], rad[jn]), dnn);
+    cl.s = s;
+    cl.j = jn;
   }
   enc_block_reduce(cc, cl);
   __shared__ bool last;
@@ -249,10 +257,10 @@ __global__ void enc_check_kernel(g6_jstate js, const double *__restrict__ rad, i
   if (!last) return;
   __threadfence();
   EncC a = {0.0, INT_MAX, -1}, b = {0.0, INT_MAX, -1};
-  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
-    const EncC ka = {__ldcg(part_d + 2 * k), __ldcg(part_i + 4 * k), __ldcg(part_i + 4 * k + 1)};
-    const EncC kb = {__ldcg(part_d + 2 * k + 1), __ldcg(part_i + 4 * k + 2),
-                     __ldcg(part_i + 4 * k + 3)};
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
+    const EncC ka = {__ldcg(part_d + 2 * q), __ldcg(part_i + 4 * q), __ldcg(part_i + 4 * q + 1)};
+    const EncC kb = {__ldcg(part_d + 2 * q + 1), __ldcg(part_i + 4 * q + 2),
+                     __ldcg(part_i + 4 * q + 3)};
     enc_take(a, ka);
     enc_take(b, kb);
   }
@@ -272,9 +280,8 @@ __global__ void enc_check_kernel(g6_jstate js, const double *__restrict__ rad, i
 // After the corrector: the pair ids, and ph4's COLLISION_DETECTION test on
 // the current state of the pair, vr < EPS r v with EPS = 0.001
 // (jdata.cc:797,822-848).  mode bits: 2 stop on an approaching collision
-// pair, 4 stop on any close pair.
-__global__ void enc_verdict_kernel(g6_jstate js, g6_enc *enc, int mode, double tnext, int *flag) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// pair, 4 stop on any close pair.  One thread.
+__device__ void enc_verdict(const g6_jstate &js, g6_enc *enc, int mode, double t, int *flag) {
   const int cap = js.cap;
   for (int p = 0; p < 2; p++) {
     enc->close_id[p] = enc->close_slot[p] >= 0 ? js.id[enc->close_slot[p]] : -1;
@@ -297,8 +304,12 @@ __global__ void enc_verdict_kernel(g6_jstate js, g6_enc *enc, int mode, double t
   }
   if ((mode & 4) && enc->close_slot[0] >= 0) stop |= 2;
   enc->stopped = stop;
-  enc->t = tnext;
+  enc->t = t;
   *flag = stop;
+}
+
+__global__ void enc_verdict_kernel(g6_jstate js, g6_enc *enc, int mode, double t, int *flag) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) enc_verdict(js, enc, mode, t, flag);
 }
 
 __global__ void store_kernel(g6_jstate js, int ni, const int *__restrict__ ilist,
@@ -318,9 +329,13 @@ __global__ void store_kernel(g6_jstate js, int ni, const int *__restrict__ ilist
 }
 
 // t + dt >= 0 always, so the IEEE bit pattern orders like an unsigned int.
-__global__ void sched_init(unsigned long long *dmin, int *dni) {
+// The previous block's encounter verdict, if one is pending, is taken here:
+// this kernel is the first of the next block, after that block's corrector.
+__global__ void sched_init(unsigned long long *dmin, int *dni, g6_jstate js,
+                           g6_enc_verdict_args v) {
   *dmin = 0x7ff0000000000000ull;  // +inf
   *dni = 0;
+  if (v.enc) enc_verdict(js, v.enc, v.mode, v.t, v.flag);
 }
 
 __global__ void sched_min(g6_jstate js, int nj, unsigned long long *dmin) {
@@ -459,13 +474,23 @@ extern "C" int g6k_store_forces(const g6_jstate *js, int ni, const int *ilist, c
 }
 
 extern "C" int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni, double *d_tnext,
-                            double *d_scratch, int scratch_len, cudaStream_t st) {
+                            double *d_scratch, int scratch_len,
+                            const g6_enc_verdict_args *verdict, cudaStream_t st) {
   if (nj <= 0 || scratch_len < 1) return -1;
   unsigned long long *dmin = reinterpret_cast<unsigned long long *>(d_scratch);
   int grid = (nj + PT - 1) / PT;
   const int cap_grid = 4 * g6k_sm_count();
   if (grid > cap_grid) grid = cap_grid;
-  sched_init<<<1, 1, 0, st>>>(dmin, d_ni);
+  g6_enc_verdict_args v;
+  if (verdict) {
+    v = *verdict;
+  } else {
+    v.enc = NULL;
+    v.mode = 0;
+    v.t = 0;
+    v.flag = NULL;
+  }
+  sched_init<<<1, 1, 0, st>>>(dmin, d_ni, *js, v);
   sched_min<<<grid, PT, 0, st>>>(*js, nj, dmin);
   sched_list<<<grid, PT, 0, st>>>(*js, nj, dmin, d_ilist, d_ni, d_tnext);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
@@ -475,8 +500,9 @@ extern "C" int g6k_enc_check(const g6_jstate *js, const double *rad, int ni, con
                              const int *nn, double tnext, double rmin, double *part_d,
                              int *part_i, unsigned *counter, g6_enc *enc, cudaStream_t st) {
   if (ni <= 0) return 0;
-  enc_check_kernel<<<(ni + PT - 1) / PT, PT, 0, st>>>(*js, rad, ni, ilist, nn, tnext, rmin,
-                                                      part_d, part_i, counter, enc);
+  // 4 lanes per particle, 32 particles per 128-thread block
+  enc_check_kernel<<<(ni + 31) / 32, 128, 0, st>>>(*js, rad, ni, ilist, nn, tnext, rmin, part_d,
+                                                   part_i, counter, enc);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

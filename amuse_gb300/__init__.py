@@ -51,7 +51,7 @@ EXT_SYMBOLS = [
     "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
     "g6x_set_fixed_jerk", "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp",
     "g6x_fixed_step_adjoint", "g6x_fixed_run", "g6x_fixed_adjoint_run",
-    "g6x_set_encounters", "g6x_set_radius", "g6x_encounter",
+    "g6x_set_encounters", "g6x_set_radius", "g6x_encounter", "g6x_knn",
 ]
 
 # Encounter-check modes of g6x_set_encounters (bits).
@@ -112,6 +112,7 @@ def load():
     lib.g6x_set_encounters.argtypes = [I, D]
     lib.g6x_set_radius.argtypes = [I, _pd]
     lib.g6x_encounter.argtypes = [_pi, _pd]
+    lib.g6x_knn.argtypes = [I, I, D, I, _pi, _pi, _pd]
     lib.g6x_step_all.argtypes = [D]
     lib.g6x_correct.argtypes = [I, _pi, D, D, _pd, _pd]
     _pll = ctypes.POINTER(ctypes.c_longlong)
@@ -375,6 +376,18 @@ class G6X(G6):
         pair = lambda a, b: None if a < 0 else (int(a), int(b))
         return dict(close=pair(ids[0], ids[1]), coll=pair(ids[2], ids[3]), stopped=int(out[0]),
                     t=float(out[1]), rmax_close=float(out[2]), rmax_coll=float(out[3]))
+
+    def knn(self, nj, k=12, slots=None, t=0.0):
+        """The k nearest neighbours of the listed slots (all nj by default)
+        among slots [0, nj) at time t: (ids [ni, k] int32, -1 where fewer
+        than k others exist; d2 [ni, k] squared distances, sorted)."""
+        slots = _i32(np.arange(nj) if slots is None else slots)
+        ni = len(slots)
+        ids = np.empty((ni, k), np.int32)
+        d2 = np.empty((ni, k))
+        _check(self.lib.g6x_knn(int(k), int(nj), float(t), ni, _ptr(slots, ctypes.c_int),
+                                _ptr(ids, ctypes.c_int), _ptr(d2, ctypes.c_double)), "g6x_knn")
+        return ids, d2
 
     def correct(self, slots, tnext, eta, acc, jerk):
         slots = _i32(slots)

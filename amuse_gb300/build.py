@@ -25,7 +25,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kern_force.cu", "kern_predict.cu", "kern_step.cu", "kern_ngb.cu", "kern_batch.cu",
-              "kern_fixed.cu"]
+              "kern_fixed.cu", "kern_knn.cu"]
 C_SOURCES = ["g6_host.c"]
 
 
@@ -58,7 +58,8 @@ def build(verbose=False, force=False):
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIB, exist_ok=True)
-    headers = [os.path.join(CSRC, "g6_dev.h"), os.path.join(INCLUDE, "g6.h")]
+    headers = [os.path.join(CSRC, "g6_dev.h"), os.path.join(CSRC, "f32x2.cuh"),
+               os.path.join(INCLUDE, "g6.h")]
     jobs = []
     objs = []
     for src in CU_SOURCES:

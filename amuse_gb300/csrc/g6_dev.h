@@ -128,6 +128,15 @@ int g6k_enc_verdict(const g6_jstate *js, g6_enc *enc, int mode, double tnext, in
 int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni,
                  double *d_tnext, double *d_scratch, int scratch_len,
                  const g6_enc_verdict_args *verdict, cudaStream_t st);
+/* k nearest neighbours (kern_knn.cu): for each of ni listed slots, the k
+ * (1..G6_KNN_MAX) nearest other j in [0, nj) by FP64 distance of the
+ * positions predicted to t, ties to the smaller slot.  The split records
+ * must hold the j-system predicted to t.  ids (particle ids, -1 when fewer
+ * than k others) and d2 (+inf there) are [ni][k] device arrays.          */
+#define G6_KNN_MAX 32
+size_t g6k_knn_scratch_bytes(int nj, int ni, int k);
+int g6k_knn(const g6_jstate *js, int nj, double t, int k, int ni, const int *slots, int *ids,
+            double *d2, void *scratch, size_t scratch_bytes, cudaStream_t st);
 /* Initial time steps (jdata.cc:503-564 without the median limit). */
 int g6k_initial_step(const g6_jstate *js, int nj, double eta, double fac,
                      double limit, double system_time, cudaStream_t st);
@@ -145,6 +154,17 @@ int g6k_store_forces(const g6_jstate *js, int ni, const int *ilist,
 #endif
 
 #ifdef __CUDACC__
+/* ph4's prediction of one position component, x + dt*(v + 0.5*dt*(a +
+   dt*j/3)) with its rounding order and no contraction (predict_all,
+   src/amuse_ph4/src/jdata.cc:736-744; the host i-prediction idata.cc:346-365
+   is the same expression); dt == 0 copies. */
+__device__ __forceinline__ double g6_predict_x(double x, double v, double a, double j,
+                                               double dt) {
+  if (dt == 0) return x;
+  const double hdt = __dmul_rn(0.5, dt);
+  return __dadd_rn(
+      x, __dmul_rn(dt, __dadd_rn(v, __dmul_rn(hdt, __dadd_rn(a, __ddiv_rn(__dmul_rn(dt, j), 3.0))))));
+}
 /* Split-record field f of slot s (f: 0 xh, 1 yh, 2 zh, 3 m, 4 xl, 5 yl,
    6 zl, 7 pad, 8 vx, 9 vy, 10 vz, 11 pad) in the pair layout above. */
 __device__ __forceinline__ float *g6_split_field(void *base, int s, int f) {

@@ -142,6 +142,9 @@ typedef struct {
   int *d_encp_i;
   unsigned *d_enc_ctr;
   int enc_cap; /* CTAs the partial buffers hold */
+  /* k nearest neighbours (g6x_knn) */
+  void *d_knn;
+  size_t knn_bytes;
   /* statistics */
   int timing;
   double st_predict_ms, st_force_ms, st_pairs, st_pred_bytes, st_nj;
@@ -471,6 +474,7 @@ int g6_close_(int *id) {
   cudaFree(G.d_rnn);
   cudaFree(G.d_rad); cudaFree(G.d_enc); cudaFree(G.d_encp_d); cudaFree(G.d_encp_i);
   cudaFree(G.d_enc_ctr);
+  cudaFree(G.d_knn);
   cudaEventDestroy(G.ev_done); cudaEventDestroy(G.ev_upd);
   cudaEventDestroy(G.ev_t0); cudaEventDestroy(G.ev_t1); cudaEventDestroy(G.ev_t2);
   cudaStreamDestroy(G.st);
@@ -1218,6 +1222,55 @@ int g6x_set_radius(int n, const double *radius) {
   rc = ensure_radius(n);
   if (rc) return rc;
   CK(cudaMemcpy(G.d_rad, radius, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+/* ---- k nearest neighbours (extension API) ---- */
+int g6x_knn(int k, int nj, double t, int ni, const int *slots, int *ids, double *d2) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (k < 1 || k > G6_KNN_MAX || ni < 0 || nj < 1 || nj > G.js.cap || (ni > 0 && !slots)) {
+    seterr("g6x_knn: k=%d nj=%d ni=%d", k, nj, ni);
+    return G6_ERR_ARG;
+  }
+  if (ni == 0) return 0;
+  if (!ids || !d2) return G6_ERR_ARG;
+  for (int i = 0; i < ni; i++)
+    if (slots[i] < 0 || slots[i] >= nj) {
+      seterr("g6x_knn: slot %d out of [0, %d)", slots[i], nj);
+      return G6_ERR_ARG;
+    }
+  rc = flush_updates();
+  if (rc) return rc;
+  /* the filter reads the split records: predict them to t */
+  if (g6k_predict(&G.js, nj, t, G6_PREC_SPLIT, G.st)) return G6_ERR_CUDA;
+  G.pred_valid = 0;
+  const size_t io = (sizeof(int) * 2 + sizeof(double)) * (size_t)ni * (size_t)k + 256;
+  const size_t need = g6k_knn_scratch_bytes(nj, ni, k) + io + sizeof(int) * (size_t)ni + 512;
+  if (need > G.knn_bytes) {
+    cudaFree(G.d_knn);
+    G.d_knn = NULL;
+    G.knn_bytes = 0;
+    CK(cudaMalloc(&G.d_knn, need));
+    G.knn_bytes = need;
+  }
+  char *p = (char *)G.d_knn;
+  int *d_slots = (int *)p;
+  p += ((sizeof(int) * (size_t)ni + 255) / 256) * 256;
+  int *d_ids = (int *)p;
+  p += ((sizeof(int) * (size_t)ni * k + 255) / 256) * 256;
+  double *d_d2 = (double *)p;
+  p += ((sizeof(double) * (size_t)ni * k + 255) / 256) * 256;
+  const size_t rest = G.knn_bytes - (size_t)(p - (char *)G.d_knn);
+  CK(cudaMemcpyAsync(d_slots, slots, sizeof(int) * (size_t)ni, cudaMemcpyHostToDevice, G.st));
+  rc = g6k_knn(&G.js, nj, t, k, ni, d_slots, d_ids, d_d2, p, rest, G.st);
+  if (rc) {
+    seterr("knn launch failed (%d)", rc);
+    return G6_ERR_CUDA;
+  }
+  CK(cudaMemcpyAsync(ids, d_ids, sizeof(int) * (size_t)ni * k, cudaMemcpyDeviceToHost, G.st));
+  CK(cudaMemcpyAsync(d2, d_d2, sizeof(double) * (size_t)ni * k, cudaMemcpyDeviceToHost, G.st));
+  CK(cudaStreamSynchronize(G.st));
   return 0;
 }
 

@@ -36,6 +36,7 @@
 // FP32 partials folded into FP64 totals) or in FP64.
 #include <cuda_runtime.h>
 
+#include "f32x2.cuh"
 #include "g6_dev.h"
 
 struct __align__(32) G6D4 {
@@ -248,40 +249,6 @@ struct __align__(16) VJPair {
 };
 constexpr int VIPT = 2;
 constexpr int VT2 = 128;
-
-typedef unsigned long long f2x;
-__device__ __forceinline__ f2x f2_add(f2x a, f2x b) {
-  f2x d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
-  f2x d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2x f2_mul(f2x a, f2x b) {
-  f2x d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c) {
-  f2x d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ f2x f2_pack(float lo, float hi) {
-  f2x r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void f2_unpack(f2x v, float &lo, float &hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f2x f2_of(const float2 &v) {
-  return *reinterpret_cast<const f2x *>(&v);
-}
-__device__ __forceinline__ f2x f2_dup(float v) { return f2_pack(v, v); }
 
 __device__ __forceinline__ float rsqrt_approx(float x) {
   float y;

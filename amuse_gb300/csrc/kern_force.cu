@@ -42,6 +42,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "f32x2.cuh"
 #include "g6_dev.h"
 
 // 32-byte aligned FP64 quadruple (CUDA 13 deprecates the unaligned double4).
@@ -90,7 +91,7 @@ enum { ERR_TMA_TIMEOUT = 1, ERR_SHAPE = 2 };
 struct __align__(16) RecS {
   float2 xh, yh, zh, m, xl, yl, zl, pad0, vx, vy, vz, pad1;
 };
-struct __align__(16) RecD {
+struct __align__(32) RecD {
   G6D4 p, v;
 };
 static_assert(sizeof(RecS) == 96, "split record pair");
@@ -174,49 +175,6 @@ __device__ __forceinline__ float rcp_approx(float x) {
   float y;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
-}
-
-// ------------------------------------------------------ packed f32x2 ---
-// Two floats in one 64-bit register pair; each op is the IEEE
-// round-to-nearest scalar op on both halves (no contraction).
-typedef unsigned long long f2x;
-__device__ __forceinline__ f2x f2_add(f2x a, f2x b) {
-  f2x d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
-  f2x d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2x f2_mul(f2x a, f2x b) {
-  f2x d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c) {
-  f2x d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ f2x f2_pack(float lo, float hi) {
-  f2x r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ float f2_lo(f2x v) {
-  float lo, hi;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-  return lo;
-}
-__device__ __forceinline__ float f2_hi(f2x v) {
-  float lo, hi;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-  return hi;
-}
-__device__ __forceinline__ f2x f2_of(const float2 &v) {
-  return *reinterpret_cast<const f2x *>(&v);
 }
 
 // ------------------------------------------------------- float-float ---

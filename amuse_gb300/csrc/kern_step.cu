@@ -145,14 +145,6 @@ __global__ void correct_kernel(g6_jstate js, int ni, const int *__restrict__ ili
   if (nn) js.nn[s] = nn[i];
 }
 
-// ph4's prediction of one position component (predict_all, jdata.cc:736-744;
-// the same expression as the host i-prediction, idata.cc:346-365).
-__device__ __forceinline__ double predict_x(double x, double v, double a, double j, double dt) {
-  if (dt == 0) return x;
-  const double hdt = dmul(0.5, dt);
-  return dadd(x, dmul(dt, dadd(v, dmul(hdt, dadd(a, ddiv(dmul(dt, j), 3.0))))));
-}
-
 // ---- encounter check ----
 // A candidate pair (i slot s, its nearest neighbour j) with its ratio r.
 // ph4 keeps the first i of its list with the largest r (strict >); the
@@ -223,8 +215,8 @@ __global__ void enc_check_kernel(g6_jstate js, const double *__restrict__ rad, i
   if (valid && k < 3) {
     const int cap = js.cap;
     const int a = k * cap + s, b = k * cap + jn;
-    const double xi = predict_x(js.x[a], js.v[a], js.a[a], js.j[a], dsub(tnext, js.t[s]));
-    const double xj = predict_x(js.x[b], js.v[b], js.a[b], js.j[b], dsub(tnext, js.t[jn]));
+    const double xi = g6_predict_x(js.x[a], js.v[a], js.a[a], js.j[a], dsub(tnext, js.t[s]));
+    const double xj = g6_predict_x(js.x[b], js.v[b], js.a[b], js.j[b], dsub(tnext, js.t[jn]));
     const double dx = dsub(xj, xi);
     p = dmul(dx, dx);
   }

@@ -9,9 +9,12 @@ one (which is bench.py).  Each prints one JSON line.
   python -m amuse_gb300.workloads precision [--n 1048576]
       Split vs FP64 per-particle force errors on all N and the energy drift
       over 64 block steps.
-  python -m amuse_gb300.workloads salpeter [--n 65536] [--t-end 0.25]
+  python -m amuse_gb300.workloads salpeter [--n 65536] [--t-end 0.25] [--encounters]
       Salpeter-IMF Plummer block-step run on the device, then split vs FP64
-      forces at ni = 1 ... N.
+      forces at ni = 1 ... N; --encounters repeats the run with ph4's
+      encounter check and reports its cost.
+  python -m amuse_gb300.workloads knn [--n 1048576] [--k 12]
+      The k nearest neighbours of every particle (g6x_knn), timed.
   python -m amuse_gb300.workloads adjoint [--n 16384] [--nsteps 256]
       Differentiable fixed-step Hermite: timing of forward and backward in
       split precision and FP64, split vs FP64 gradients, and finite
@@ -355,6 +358,31 @@ def run_salpeter(args):
     return out
 
 
+def run_knn(args):
+    """The k nearest neighbours of every particle (the lists ph4's
+    get_densities_on_gpu builds, gpu.cc:568-866) for a Plummer sphere of N
+    particles: one g6x_knn call over all N, timed after a warm-up call; and
+    the same for a 1024-particle subset."""
+    import amuse_gb300 as ag
+    from amuse_gb300 import ic
+    n, k = args.n, args.k
+    g6 = ag.G6X(0)
+    rng = np.random.RandomState(args.seed)
+    m, x, v = ic.plummer(n, rng=rng)
+    g6.load_particles(m, x, v)
+    out = {"workload": f"plummer N={n}, k={k} nearest neighbours of every particle, seed {args.seed}"}
+    for label, slots in (("all", None), ("subset1024", rng.choice(n, min(1024, n), replace=False))):
+        g6.knn(n, k=k, slots=slots)                   # warm-up (allocation, attributes)
+        t0 = time.perf_counter()
+        ids, d2 = g6.knn(n, k=k, slots=slots)
+        sec = time.perf_counter() - t0
+        ni = n if slots is None else len(slots)
+        out[label] = {"ni": ni, "seconds": sec, "pair_distances_per_s": ni * (n - 1) / sec,
+                      "median_kth_distance": float(np.sqrt(np.median(d2[:, k - 1])))}
+        print(json.dumps(out), flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -386,6 +414,10 @@ def main():
     sa.add_argument("--fp64", action="store_true")
     sa.add_argument("--encounters", action="store_true",
                     help="repeat the run with the encounter check on and report its cost")
+    kn = sub.add_parser("knn")
+    kn.add_argument("--n", type=int, default=1 << 20)
+    kn.add_argument("--k", type=int, default=12)
+    kn.add_argument("--seed", type=int, default=3)
     a = ap.parse_args()
     if a.cmd == "batch":
         run_batch(a)
@@ -395,6 +427,8 @@ def main():
         run_precision(a)
     elif a.cmd == "salpeter":
         run_salpeter(a)
+    elif a.cmd == "knn":
+        run_knn(a)
 
 
 if __name__ == "__main__":

@@ -204,6 +204,16 @@ int g6x_run_stats(double out[4]);
 int g6x_set_encounters(int mode, double rmin);
 int g6x_set_radius(int n, const double *radius);
 int g6x_encounter(int ids[4], double out[4]);
+/* The k (1..32) nearest neighbours of each listed slot among the j-slots
+   [0, nj), positions predicted to t with ph4's predictor: the lists that
+   ph4's get_densities_on_gpu (src/amuse_ph4/src/gpu.cc:568-866) builds
+   from GRAPE neighbour lists and reduces with save_neighbors
+   (gpu.cc:534-558) to the knn nearest, sorted by squared distance.  Exact
+   in FP64 (an FP32 pre-filter with a proven error slack rejects only
+   particles farther than the current k-th); ties go to the smaller slot.
+   Host arrays: slots[ni]; out ids[ni][k] (particle ids, -1 when fewer than
+   k others exist), d2[ni][k] squared distances (+inf there).  Blocking. */
+int g6x_knn(int k, int nj, double t, int ni, const int *slots, int *ids, double *d2);
 int g6x_energy(double *kinetic, double *potential);
 int g6x_step_all(double tnext);
 /* FP64 corrector + Aarseth step (idata.cc:399-514) applied on the device to

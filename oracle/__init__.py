@@ -65,6 +65,8 @@ def port():
                                     _c_int, _dp, _dp, _dp, _dp, _dp, _dp, _c_long, _c_int,
                                     _c_dbl, _dp]
         lib.orc_run_enc.restype = _c_long
+        lib.orc_knn.argtypes = [_c_int, _dp, _c_int, _c_int, _ip, _ip, _dp]
+        lib.orc_knn.restype = None
         lib.orc_smalln.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_int, _c_dbl, _dp, _c_long]
         lib.orc_smalln.restype = _c_long
         lib.orc_hermite_fixed.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_int, _dp,
@@ -160,6 +162,20 @@ def run(mass, pos, vel, eps2, eta, t_end, threads=1, lib=None, ids=None, max_blo
                             time, step, stats, max_blocks)
     return dict(pos=pos, vel=vel, acc=acc, jerk=jerk, pot=pot, time=time, timestep=step,
                 E0=stats[0], E1=stats[1], total_steps=stats[2], t=stats[3], blocks=blocks)
+
+
+def knn(pos, k, slots=None):
+    """save_neighbors (gpu.cc:534-558) over all other particles: the k
+    nearest (indices, squared distances), ties to the smaller index;
+    -1 / inf past the last."""
+    pos = _c(pos)
+    n = len(pos)
+    slots = _c(np.arange(n) if slots is None else slots, np.int32)
+    ni = len(slots)
+    out_j = np.empty((ni, k), np.int32)
+    out_d2 = np.empty((ni, k))
+    port().orc_knn(n, pos, k, ni, slots, out_j, out_d2)
+    return out_j, out_d2
 
 
 ENC_CHECK, ENC_STOP_COLL, ENC_STOP_CLOSE = 1, 2, 4

@@ -24,6 +24,9 @@
  *                      jdata::advance_and_check_encounter (jdata.cc:797-850)
  *   orc_hermite_fixed  src/amuse_hermite/interface.cc:266-281,387-552
  *                      (shared fixed-step Hermite, test_mode)
+ *   orc_knn            src/amuse_ph4/src/gpu.cc:534-558 (save_neighbors:
+ *                      all other particles by squared distance, the first
+ *                      knn kept), over the whole j-system
  */
 #include <math.h>
 #include <pthread.h>
@@ -710,4 +713,45 @@ void orc_hermite_fixed(int n, const double *mass, double *pos, double *vel, doub
   if (acc_out) memcpy(acc_out, acc, b);
   if (jerk_out) memcpy(jerk_out, jerk, b);
   free(acc); free(jerk); free(op); free(ov); free(oa); free(oj);
+}
+
+/* ------------------------------------------------------------------ */
+/* k nearest neighbours: save_neighbors (gpu.cc:534-558) applied to the  */
+/* complete list of other particles, as get_densities_on_gpu            */
+/* (gpu.cc:568-866) intends: r_sq = sum_k (pos[i][k] - pos[j][k])^2 in   */
+/* component order, ascending; ties (which std::sort leaves unordered)  */
+/* to the smaller index.  pos[n][3] are the (predicted) positions.       */
+/* out_j[ni][k] (-1 past the last), out_d2[ni][k] (+inf there).          */
+/* ------------------------------------------------------------------ */
+void orc_knn(int n, const double *pos, int k, int ni, const int *slots,
+             int *out_j, double *out_d2) {
+  for (int q = 0; q < ni; q++) {
+    const int i = slots[q];
+    int *lj = out_j + (size_t)q * k;
+    double *ld = out_d2 + (size_t)q * k;
+    int cnt = 0;
+    for (int j = 0; j < n; j++) {
+      if (j == i) continue;
+      double r_sq = 0;
+      for (int c = 0; c < 3; c++) {
+        double d = pos[3 * i + c] - pos[3 * j + c];
+        r_sq += d * d;
+      }
+      if (cnt == k && !(r_sq < ld[k - 1] || (r_sq == ld[k - 1] && j < lj[k - 1])))
+        continue;
+      int p = cnt < k ? cnt : k - 1;
+      while (p > 0 && (r_sq < ld[p - 1] || (r_sq == ld[p - 1] && j < lj[p - 1]))) {
+        ld[p] = ld[p - 1];
+        lj[p] = lj[p - 1];
+        p--;
+      }
+      ld[p] = r_sq;
+      lj[p] = j;
+      if (cnt < k) cnt++;
+    }
+    for (int p = cnt; p < k; p++) {
+      lj[p] = -1;
+      ld[p] = INFINITY;
+    }
+  }
 }

@@ -181,16 +181,24 @@ __global__ void __launch_bounds__(KT) knn_kernel(KArgs ka) {
     knn_load_tile(tile, gj, tj);
     __syncthreads();
     if (active) {
+      // Two record pairs (four j) per step: two independent FP32 chains and
+      // one early-out test.  The kept set does not depend on the order in
+      // which candidates arrive.
       const int npair = min(KRPT, (j1 - tj + 1) / 2);
-      for (int p = 0; p < npair; p++) {
-        float ra, rb;
-        knn_r2f(tile[p], ip, ra, rb);
-        if (fminf(ra, rb) > F) continue;
+      for (int p = 0; p < npair; p += 2) {
+        float rr[4];
+        knn_r2f(tile[p], ip, rr[0], rr[1]);
+        if (p + 1 < npair) {
+          knn_r2f(tile[p + 1], ip, rr[2], rr[3]);
+        } else {
+          rr[2] = rr[3] = __int_as_float(0x7f800000);
+        }
+        if (fminf(fminf(rr[0], rr[1]), fminf(rr[2], rr[3])) > F) continue;
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < 4; h++) {
           const int j = tj + 2 * p + h;
-          const float r = h ? rb : ra;
-          if (r > F || j >= j1 || j == self) continue;
+          const float r = rr[h];
+          if ((h >= 2 && p + 1 >= npair) || r > F || j >= j1 || j == self) continue;
           if (cnt == KP) {
             const float lr = lf[(KP - 1) * KT + tid];
             if (!(r < lr || (r == lr && j < ls[(KP - 1) * KT + tid]))) continue;

@@ -71,6 +71,15 @@ def test_calls_before_open_fail_cleanly(lib_built):
         assert lib.g6_set_ti_(ctypes.byref(cid), ctypes.byref(ti)) == -1
         assert lib.g6_open_(ctypes.byref(cid)) in (-5, -3)
         assert lib.g6_npipes_() == 16384
+        # extension calls: G6_ERR_NOT_OPEN before any device work
+        slots = (ctypes.c_int * 1)(0)
+        ids = (ctypes.c_int * 12)()
+        d2 = (ctypes.c_double * 12)()
+        assert lib.g6x_set_encounters(ag.ENC_STOP_COLLISION, 0.0) == -1
+        assert lib.g6x_set_radius(0, None) == -1
+        assert lib.g6x_encounter(None, None) == -1
+        assert lib.g6x_knn(12, 10, 0.0, 1, slots, ids, d2) == -1
+        assert lib.g6x_run(1.0, None, None) == -1
 
 
 def _has_gpu():

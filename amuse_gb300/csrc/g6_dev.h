@@ -103,13 +103,13 @@ typedef struct {
   int stopped;                  /* 1 collision, 2 close pair (bits) */
   int pad;
 } g6_enc;
-/* A block whose stopping decision (g6k_enc_verdict) is still to be taken. */
+/* A block whose stopping decision (g6k_enc_decide) is still to be taken. */
 typedef struct {
   g6_enc *enc; /* NULL: none */
   int mode;
   double t;
   int *flag;
-} g6_enc_verdict_args;
+} g6_enc_decision_args;
 /* Pre-corrector pass over the block: nn[i] is the nearest j slot of ilist[i]
  * from the force; distances are recomputed in FP64 from both particles
  * predicted to tnext.  part_d >= 2 * ceil(ni/32), part_i >= 4 * ceil(ni/32),
@@ -119,15 +119,15 @@ int g6k_enc_check(const g6_jstate *js, const double *rad, int ni, const int *ili
                   unsigned *counter, g6_enc *enc, cudaStream_t st);
 /* Post-corrector: ids of the pairs, the collision test on the corrected
  * state, stop bits into enc->stopped and *flag.                              */
-int g6k_enc_verdict(const g6_jstate *js, g6_enc *enc, int mode, double tnext, int *flag,
+int g6k_enc_decide(const g6_jstate *js, g6_enc *enc, int mode, double tnext, int *flag,
                     cudaStream_t st);
 /* Block scheduler: tnext = min(t+dt); ilist = slots with t+dt == tnext.
  * Writes tnext to *d_tnext and the count to *d_ni. scratch >= 2*grid.
- * verdict (or NULL): the previous block's pending encounter verdict, taken
+ * decision (or NULL): the previous block's pending encounter stopping decision, taken
  * by the scheduler's first kernel (after that block's corrector). */
 int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni,
                  double *d_tnext, double *d_scratch, int scratch_len,
-                 const g6_enc_verdict_args *verdict, cudaStream_t st);
+                 const g6_enc_decision_args *decision, cudaStream_t st);
 /* k nearest neighbours (kern_knn.cu): for each of ni listed slots, the k
  * (1..G6_KNN_MAX) nearest other j in [0, nj) by FP64 distance of the
  * positions predicted to t, ties to the smaller slot.  The split records

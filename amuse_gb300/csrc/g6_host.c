@@ -1386,7 +1386,7 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
     if (rc) return rc;
     CK(cudaMemsetAsync(d_stop, 0, sizeof(int), G.st));
   }
-  g6_enc_verdict_args pend; /* the last block's verdict, taken by the next schedule */
+  g6_enc_decision_args pend; /* the last block's stopping decision, taken by the next schedule */
   memset(&pend, 0, sizeof(pend));
   while (G.run_t < t_end && nb != max_blocks) {
     ilist_identity_n = 0;
@@ -1427,8 +1427,8 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
     nb++;
     ns += ni;
   }
-  /* the loop ended on time or block count: the last block's verdict */
-  if (pend.enc && g6k_enc_verdict(&G.js, pend.enc, pend.mode, pend.t, pend.flag, G.st))
+  /* the loop ended on time or block count: the last block's stopping decision */
+  if (pend.enc && g6k_enc_decide(&G.js, pend.enc, pend.mode, pend.t, pend.flag, G.st))
     return G6_ERR_CUDA;
   CK(cudaStreamSynchronize(G.st));
   run_stats[0] = (double)nb;

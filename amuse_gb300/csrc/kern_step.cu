@@ -273,7 +273,7 @@ __global__ void enc_check_kernel(g6_jstate js, const double *__restrict__ rad, i
 // the current state of the pair, vr < EPS r v with EPS = 0.001
 // (jdata.cc:797,822-848).  mode bits: 2 stop on an approaching collision
 // pair, 4 stop on any close pair.  One thread.
-__device__ void enc_verdict(const g6_jstate &js, g6_enc *enc, int mode, double t, int *flag) {
+__device__ void enc_decide(const g6_jstate &js, g6_enc *enc, int mode, double t, int *flag) {
   const int cap = js.cap;
   for (int p = 0; p < 2; p++) {
     enc->close_id[p] = enc->close_slot[p] >= 0 ? js.id[enc->close_slot[p]] : -1;
@@ -300,8 +300,8 @@ __device__ void enc_verdict(const g6_jstate &js, g6_enc *enc, int mode, double t
   *flag = stop;
 }
 
-__global__ void enc_verdict_kernel(g6_jstate js, g6_enc *enc, int mode, double t, int *flag) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) enc_verdict(js, enc, mode, t, flag);
+__global__ void enc_decide_kernel(g6_jstate js, g6_enc *enc, int mode, double t, int *flag) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) enc_decide(js, enc, mode, t, flag);
 }
 
 __global__ void store_kernel(g6_jstate js, int ni, const int *__restrict__ ilist,
@@ -321,13 +321,13 @@ __global__ void store_kernel(g6_jstate js, int ni, const int *__restrict__ ilist
 }
 
 // t + dt >= 0 always, so the IEEE bit pattern orders like an unsigned int.
-// The previous block's encounter verdict, if one is pending, is taken here:
+// The previous block's encounter stopping decision, if one is pending, is taken here:
 // this kernel is the first of the next block, after that block's corrector.
 __global__ void sched_init(unsigned long long *dmin, int *dni, g6_jstate js,
-                           g6_enc_verdict_args v) {
+                           g6_enc_decision_args v) {
   *dmin = 0x7ff0000000000000ull;  // +inf
   *dni = 0;
-  if (v.enc) enc_verdict(js, v.enc, v.mode, v.t, v.flag);
+  if (v.enc) enc_decide(js, v.enc, v.mode, v.t, v.flag);
 }
 
 __global__ void sched_min(g6_jstate js, int nj, unsigned long long *dmin) {
@@ -467,15 +467,15 @@ extern "C" int g6k_store_forces(const g6_jstate *js, int ni, const int *ilist, c
 
 extern "C" int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni, double *d_tnext,
                             double *d_scratch, int scratch_len,
-                            const g6_enc_verdict_args *verdict, cudaStream_t st) {
+                            const g6_enc_decision_args *decision, cudaStream_t st) {
   if (nj <= 0 || scratch_len < 1) return -1;
   unsigned long long *dmin = reinterpret_cast<unsigned long long *>(d_scratch);
   int grid = (nj + PT - 1) / PT;
   const int cap_grid = 4 * g6k_sm_count();
   if (grid > cap_grid) grid = cap_grid;
-  g6_enc_verdict_args v;
-  if (verdict) {
-    v = *verdict;
+  g6_enc_decision_args v;
+  if (decision) {
+    v = *decision;
   } else {
     v.enc = NULL;
     v.mode = 0;
@@ -498,9 +498,9 @@ extern "C" int g6k_enc_check(const g6_jstate *js, const double *rad, int ni, con
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
-extern "C" int g6k_enc_verdict(const g6_jstate *js, g6_enc *enc, int mode, double tnext,
+extern "C" int g6k_enc_decide(const g6_jstate *js, g6_enc *enc, int mode, double tnext,
                                int *flag, cudaStream_t st) {
-  enc_verdict_kernel<<<1, 32, 0, st>>>(*js, enc, mode, tnext, flag);
+  enc_decide_kernel<<<1, 32, 0, st>>>(*js, enc, mode, tnext, flag);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

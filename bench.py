@@ -21,7 +21,8 @@ Reported next to it:
   roofline     the force kernel against the FP32 peak, 60 flop/pair (ph4's
                convention, src/amuse_ph4/src/jdata.cc:1038);
   cpu_baseline the oracle port of ph4's CPU force loop on the host cores
-               (bounded i-sample against all N j).
+               (bounded i-sample against all N j), all cores, and one core
+               in cpu_baseline.single_core.
 
 --impl reference times the reference's CPU force path (ph4's
 idata::get_partial_acc_and_jerk restated in oracle/, all host threads).
@@ -180,6 +181,13 @@ def cpu_baseline(mass, pos, vel, seconds, threads):
             "kind": "port",
             "sample": f"{ni} i-particles x {n} j (ph4 idata::get_partial_acc_and_jerk "
                       f"restated in oracle/g6_oracle.c, {threads} threads, {dt:.1f} s)"}
+
+
+def single_core_baseline(mass, pos, vel, cpu_seconds):
+    """The same loop on one core (a short sample: a fifth of the all-core
+    budget, at most 3 s)."""
+    one = cpu_baseline(mass, pos, vel, min(3.0, cpu_seconds / 5), 1)
+    return {"value": one["value"], "unit": one["unit"], "cores": 1, "sample": one["sample"]}
 
 
 def run_reference(args):
@@ -345,6 +353,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(mass, pos, vel, args.cpu_seconds, os.cpu_count() or 1)
+        cpu["single_core"] = single_core_baseline(mass, pos, vel, args.cpu_seconds)
 
     if rank == 0:
         line = {

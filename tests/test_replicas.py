@@ -84,3 +84,15 @@ def test_reference_arm_rank0_prints_one_line(tmp_path):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_cpu_baselines_all_cores_and_one_core():
+    """bench.py's host-core baselines (the oracle port): the all-core rate
+    and the one-core rate on a small Plummer sphere."""
+    sys.path.insert(0, ROOT)
+    import bench
+    mass, pos, vel = bench.workload(1024)
+    allc = bench.cpu_baseline(mass, pos, vel, 0.2, os.cpu_count() or 1)
+    one = bench.single_core_baseline(mass, pos, vel, 0.5)
+    assert allc["value"] > 0 and one["value"] > 0 and one["cores"] == 1
+    assert allc["kind"] == "port" and "1 threads" in one["sample"]

@@ -8,7 +8,9 @@ mirrors its interface for Python callers and tests:
   g6_set_j_particle, g6calc_firsthalf/lasthalf(2), neighbour lists) with the
   reference's argument meaning (lib/sapporo_light/g6lib.h:5-51);
 * :class:`G6X`     -- the extension API (device-resident state, the FP64
-  corrector / block-step driver, precision selection, statistics);
+  corrector / block-step driver with ph4's encounter check, k nearest
+  neighbours, batched few-body systems, the fixed-step path, precision
+  selection, statistics);
 * :func:`driver`   -- ``libg6drive.so``, the C caller that chunks a force
   call by npipes the way ph4's gpu.cc does.
 

@@ -67,3 +67,28 @@ def test_oracle_encounter_off_is_plain_run():
     b = oracle.run(c["mass"], c["pos0"], c["vel0"], 1e-4, 0.14, 0.25)
     assert np.array_equal(a["pos"], b["pos"]) and a["blocks"] == b["blocks"]
     assert a["stopped"] == 0 and a["close"] is None and a["coll"] is None
+
+
+def test_oracle_massless_pairs_are_not_encounters():
+    """ph4 skips a pair whose members are both massless (idata.cc:648);
+    one massive member is enough (and a CPU-mode force never picks a
+    massless neighbour, idata.cc:193)."""
+    m = np.array([1.0, 0.0, 0.0])
+    x = np.array([[0.0, 0.0, 0.0], [5.0, 0.0, 0.0], [5.001, 0.0, 0.0]])
+    v = np.array([[0.0, 0.0, 0.0], [0.0, 0.45, 0.0], [0.0, 0.45, 0.0]])
+    r = oracle.run_enc(m, np.full(3, 0.01), x, v, 0.0, 0.14, 0.01,
+                       mode=oracle.ENC_CHECK, rmin=0.1)
+    # the two test particles are 0.001 apart but massless: no pair; their
+    # nearest massive neighbour (the central mass) is far away
+    assert r["close"] is None and r["coll"] is None
+
+
+def test_oracle_explicit_rmin():
+    """rmin given explicitly replaces ph4's 2/n."""
+    m = np.array([0.5, 0.5])
+    x = np.array([[-0.05, 0.0, 0.0], [0.05, 0.0, 0.0]])
+    v = np.array([[0.0, -1.0, 0.0], [0.0, 1.0, 0.0]])
+    r = oracle.run_enc(m, np.zeros(2), x, v, 0.0, 0.14, 1e-3, mode=oracle.ENC_CHECK, rmin=0.2)
+    assert r["rmin"] == 0.2 and r["close"] is not None and r["rmax_close"] >= 1.0
+    r2 = oracle.run_enc(m, np.zeros(2), x, v, 0.0, 0.14, 1e-3, mode=oracle.ENC_CHECK, rmin=0.05)
+    assert r2["rmin"] == 0.05 and r2["close"] is None

@@ -133,6 +133,8 @@ def main():
     r = oracle.run(m, x, v, 1e-6, 0.01, 0.125, lib="ref")
     save("run_plummer256_eps1e-6.npz", mass=m, pos0=x, vel0=v, eps2=1e-6, eta=0.01,
          t_end=0.125, **{k: np.asarray(r[k]) for k in r})
+    smalln_fixtures(oracle)
+    encounter_fixtures(oracle)
 
 
 def smalln_fixtures(oracle):

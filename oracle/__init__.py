@@ -33,9 +33,19 @@ def build_port():
     subprocess.check_call(["make", "-s", "-C", HERE, "port"])
 
 
-def build_ref(ref_root="/root/reference"):
-    """Compile the unmodified ph4 CPU objects (needs the reference sources)."""
-    subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}", "-j8"])
+def ref_root():
+    """The AMUSE checkout named by the AMUSE_REF environment variable, or None."""
+    r = os.environ.get("AMUSE_REF")
+    return r if r and os.path.isdir(os.path.join(r, "src", "amuse_ph4", "src")) else None
+
+
+def build_ref(root=None):
+    """Compile the unmodified ph4 CPU objects (needs the reference sources,
+    at ``root`` or $AMUSE_REF)."""
+    root = root or ref_root()
+    if root is None:
+        raise RuntimeError("set AMUSE_REF to the AMUSE checkout to build oracle/_ref")
+    subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={root}", "-j8"])
 
 
 def port():

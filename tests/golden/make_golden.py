@@ -9,7 +9,7 @@ Runs in the development container only (it needs the reference checkout):
     smallN few-body runs: smallN.cc:906-1117 with dt_crit = 0, block-step
     runs with the encounter check: idata.cc:620-700, jdata.cc:797-850).
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+Usage:  AMUSE_REF=<checkout> python tests/golden/make_golden.py [--ref <checkout>]
                                           [--only smalln|encounters]
 """
 import argparse
@@ -48,9 +48,11 @@ def save(name, **arrays):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("AMUSE_REF"))
     ap.add_argument("--only", default=None, choices=[None, "smalln", "encounters"])
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give --ref or set AMUSE_REF to the AMUSE checkout")
     sys.path.insert(0, os.path.join(args.ref, "src"))
     import oracle
     oracle.build_ref(args.ref)

@@ -102,3 +102,27 @@ def test_driver_ffi_stub_compiles(tmp_path, lib_built):
     subprocess.run(["gcc", str(src), "-I", os.path.dirname(HEADER), "-L", ag.LIB_DIR,
                     "-lsapporo", "-Wl,-rpath," + ag.LIB_DIR, "-o", str(exe)], check=True)
     assert exe.exists()
+
+
+def test_ph4_gpu_mode_links_against_libsapporo(lib_built):
+    """The real drop-in: the UNMODIFIED ph4 sources built in GPU mode
+    (-DGPU -DNOMPI: src/amuse_ph4/src/gpu.cc:36-492 and grape.cc:6-147 call
+    the GRAPE-6 API) link against libsapporo.so.  ph4's own by-value wrappers
+    (grape.cc) are the definitions in the executable; every trailing-
+    underscore ABI symbol they call is left to libsapporo.so.  Needs the
+    reference checkout (AMUSE_REF); compile and link only."""
+    import oracle
+    if oracle.ref_root() is None:
+        pytest.skip("AMUSE_REF does not name a reference checkout")
+    here = os.path.dirname(oracle.__file__)
+    subprocess.run(["make", "-s", "-C", here, "link", "-j8"], check=True)
+    exe = os.path.join(here, "_ref", "ph4_gpu_run")
+    syms = subprocess.run(["nm", exe], capture_output=True, text=True, check=True).stdout
+    defined = {ln.split()[-1] for ln in syms.splitlines() if " T " in ln}
+    undefined = {ln.split()[-1] for ln in syms.splitlines() if ln.strip().startswith("U ")}
+    for s in ag.ABI_SYMBOLS:
+        assert s in undefined, s           # resolved by libsapporo.so at run time
+        assert s[:-1] in defined, s[:-1]   # ph4's strong wrapper, not the library's weak one
+    dyn = subprocess.run(["readelf", "-d", exe], capture_output=True, text=True,
+                         check=True).stdout
+    assert "[libsapporo.so]" in dyn

@@ -79,6 +79,9 @@ def port():
         lib.orc_knn.restype = None
         lib.orc_smalln.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_int, _c_dbl, _dp, _c_long]
         lib.orc_smalln.restype = _c_long
+        lib.orc_smalln_unpert.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_int, _c_dbl,
+                                          _c_dbl, _c_dbl, _c_dbl, _c_int, _dp, _c_long, _ip]
+        lib.orc_smalln_unpert.restype = _c_long
         lib.orc_hermite_fixed.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_int, _dp,
                                           _dp]
         lib.orc_hermite_fixed.restype = None
@@ -242,16 +245,39 @@ def run_enc(mass, radius, pos, vel, eps2, eta, t_end, mode=ENC_CHECK | ENC_STOP_
 
 def smalln(mass, pos, vel, eta, t_end, n_iter=2, lib=None, dt_crit=0.0, max_steps=0):
     """smallN's few-body integrator without unperturbed binaries (smallN.cc).
-    Returns (pos, vel, t_final, steps); steps is None for the reference."""
+    Returns (pos, vel, t_final, steps); steps is None for the reference.
+    lib="ref" runs the unmodified smallN with the given dt_crit (0 disables
+    its unperturbed binaries); it raises if a binary node is left at the
+    end with dt_crit = 0."""
     mass, pos, vel = _c(mass), _c(pos).copy(), _c(vel).copy()
     t = np.zeros(1)
     if lib == "ref":
         rc = ref().ph4ref_smalln(len(mass), mass, pos, vel, eta, t_end, dt_crit, t)
-        if rc != 0:
+        if rc != 0 and dt_crit == 0.0:
             raise RuntimeError("smallN built a binary node")
         return pos, vel, float(t[0]), None
     steps = port().orc_smalln(len(mass), mass, pos, vel, eta, n_iter, t_end, t, max_steps)
     return pos, vel, float(t[0]), int(steps)
+
+
+# smallN's unperturbed-binary defaults (src/amuse_ph4/src/hdyn.cc:10-14 and the
+# smallN worker's gamma, src/amuse_smalln/interface.cc:72)
+SMALLN_DT_CRIT, SMALLN_R2_CRIT, SMALLN_GAMMA = 1e-3, 1e-2, 1e-6
+
+
+def smalln_unpert(mass, pos, vel, eta, t_end, n_iter=2, dt_crit=SMALLN_DT_CRIT,
+                  r2_crit=SMALLN_R2_CRIT, gamma=SMALLN_GAMMA, allow_full=True, max_steps=0):
+    """smallN with its unperturbed-binary treatment (restated in
+    g6_oracle.c: orc_smalln_unpert).  Returns (pos, vel, t_final, steps,
+    binaries formed)."""
+    mass, pos, vel = _c(mass), _c(pos).copy(), _c(vel).copy()
+    t = np.zeros(1)
+    nb = np.zeros(1, np.int32)
+    steps = port().orc_smalln_unpert(len(mass), mass, pos, vel, eta, n_iter, t_end, dt_crit,
+                                     r2_crit, gamma, 1 if allow_full else 0, t, max_steps, nb)
+    if steps < 0:
+        raise ValueError("more than 64 bodies")
+    return pos, vel, float(t[0]), int(steps), int(nb[0])
 
 
 def hermite_fixed(mass, pos, vel, eps2, dt, nsteps):

@@ -755,3 +755,507 @@ void orc_knn(int n, const double *pos, int k, int ni, const int *slots,
     }
   }
 }
+
+/* ------------------------------------------------------------------ */
+/* smallN with unperturbed binaries: smallN.cc:906-1117 with           */
+/* smallN_unpert.cc:44-88 (is_unperturbed_and_approaching), :233-360   */
+/* (create_binary), :367-460 (time_to_radius, dt_perturbers), :567-774 */
+/* (extend_or_end_binary) and smallN.cc:127-240 (forces between        */
+/* top-level nodes resolved into their leaves), :380-470 (components   */
+/* advanced on their Kepler orbits).  The binary tree is one level     */
+/* deep, as smallN builds it.  Differences, stated:                    */
+/*   - the two-body motion comes from a universal-variable Kepler      */
+/*     propagator (Stumpff functions, Newton on the universal anomaly; */
+/*     the published two-body solution), not smallN's kepler class;    */
+/*   - the energy correction at the end of a partially unperturbed     */
+/*     segment rescales the relative velocity to absorb the change of  */
+/*     the tidal potential (the form smallN_unpert.cc:612-625 keeps    */
+/*     under #if 0); the angular-momentum term is not applied;         */
+/*   - the perturber of a candidate pair is searched among top-level   */
+/*     nodes (smallN_unpert.cc:65-75 walks all leaves, whose           */
+/*     positions under a binary node are relative to it).              */
+/* pos/vel in place (all n bodies resolved at the end); returns steps. */
+/* ------------------------------------------------------------------ */
+#define SNU_NB 8 /* binaries per system at most */
+
+typedef struct {
+  int li, lj;           /* leader slot (holds the CM node) and companion */
+  double mi, mj;        /* component masses */
+  double r0[3], v0[3];  /* relative state x_j - x_i at time t0 */
+  double t0, t_pred;    /* reference time, end of the unperturbed segment */
+  double tidal;         /* tidal potential at the start of the segment */
+  int full;             /* fully unperturbed: components frozen at r0, v0 */
+} snu_bin;
+
+static double snu_stumpff_c(double z) {
+  if (z > 1e-6) return (1 - cos(sqrt(z))) / z;
+  if (z < -1e-6) return (cosh(sqrt(-z)) - 1) / (-z);
+  return 0.5 - z / 24 + z * z / 720;
+}
+static double snu_stumpff_s(double z) {
+  if (z > 1e-6) {
+    double s = sqrt(z);
+    return (s - sin(s)) / (s * s * s);
+  }
+  if (z < -1e-6) {
+    double s = sqrt(-z);
+    return (sinh(s) - s) / (s * s * s);
+  }
+  return 1.0 / 6 - z / 120 + z * z / 5040;
+}
+
+/* Two-body relative motion over dt (mu = G M): universal variables. */
+static void snu_kepler(double mu, const double r0[3], const double v0[3], double dt, double r[3],
+                       double v[3]) {
+  double rn = sqrt(r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2]);
+  double v2 = v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2];
+  double rv = r0[0] * v0[0] + r0[1] * v0[1] + r0[2] * v0[2];
+  double alpha = 2 / rn - v2 / mu, smu = sqrt(mu);
+  if (dt == 0) {
+    for (int k = 0; k < 3; k++) r[k] = r0[k], v[k] = v0[k];
+    return;
+  }
+  double x = alpha > 0 ? smu * dt * alpha : smu * dt / rn; /* initial guess */
+  for (int it = 0; it < 100; it++) {
+    double z = alpha * x * x, C = snu_stumpff_c(z), S = snu_stumpff_s(z);
+    double F = rv / smu * x * x * C + (1 - alpha * rn) * x * x * x * S + rn * x - smu * dt;
+    double dF = rv / smu * x * (1 - z * S) + (1 - alpha * rn) * x * x * C + rn;
+    double dx = F / dF;
+    x -= dx;
+    if (fabs(dx) <= 1e-15 * fabs(x)) break;
+  }
+  double z = alpha * x * x, C = snu_stumpff_c(z), S = snu_stumpff_s(z);
+  double f = 1 - x * x * C / rn, g = dt - x * x * x * S / smu;
+  for (int k = 0; k < 3; k++) r[k] = f * r0[k] + g * v0[k];
+  double rr = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  double fd = smu / (rr * rn) * (alpha * x * x * x * S - x), gd = 1 - x * x * C / rr;
+  for (int k = 0; k < 3; k++) v[k] = fd * r0[k] + gd * v0[k];
+}
+
+/* Time to the next pericentre and the period (inf unless bound) of the
+ * relative orbit; returns 0 if the pair is not approaching its pericentre
+ * (smallN_unpert.cc:252-266: mean anomaly >= 0). */
+static int snu_peri(double mu, const double r[3], const double v[3], double *dt_peri,
+                    double *period) {
+  double rn = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  double rv = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
+  if (rv >= 0) return 0;
+  double alpha = 2 / rn - v2 / mu;
+  double h[3] = {r[1] * v[2] - r[2] * v[1], r[2] * v[0] - r[0] * v[2], r[0] * v[1] - r[1] * v[0]};
+  double p = (h[0] * h[0] + h[1] * h[1] + h[2] * h[2]) / mu;
+  double e = sqrt(fmax(0.0, 1 - p * alpha));
+  *period = INFINITY;
+  if (fabs(alpha) * rn < 1e-8 || e < 1e-12) { /* ~parabolic (Barker) or degenerate */
+    double D = rv / sqrt(mu * p);
+    *dt_peri = -0.5 * sqrt(p * p * p / mu) * (D + D * D * D / 3);
+    if (alpha > 0) *period = 2 * M_PI / sqrt(mu * alpha * alpha * alpha);
+    return *dt_peri > 0;
+  }
+  double M, n;
+  if (alpha > 0) {
+    double a = 1 / alpha;
+    double cE = (1 - rn * alpha) / e, sE = rv / (e * sqrt(mu * a));
+    double E = atan2(sE, cE);
+    M = E - e * sin(E);
+    n = sqrt(mu * alpha * alpha * alpha);
+    *period = 2 * M_PI / n;
+  } else {
+    double sF = rv / (e * sqrt(-mu / alpha));
+    double F = asinh(sF);
+    M = e * sF - F;
+    n = sqrt(-mu * alpha * alpha * alpha);
+  }
+  if (M >= 0) return 0;
+  *dt_peri = -M / n;
+  return 1;
+}
+
+typedef struct {
+  int n, nb;
+  int node[64];      /* node (leader slot) of each slot; -1: companion slot */
+  snu_bin b[SNU_NB];
+  int bin_of[64];    /* binary index of a leader slot, -1: single */
+  double lx[64][3], lv[64][3]; /* predicted leaves of binary members */
+} snu_tree;
+
+/* Predicted leaves of binary q at time t from its CM's predicted state
+ * (smallN.cc:380-470: Kepler motion; frozen when fully unperturbed). */
+static void snu_resolve(snu_tree *T, const sn_body *b, int q, double t) {
+  const snu_bin *B = &T->b[q];
+  double r[3], v[3];
+  if (B->full)
+    for (int k = 0; k < 3; k++) r[k] = B->r0[k], v[k] = B->v0[k];
+  else
+    snu_kepler(B->mi + B->mj, B->r0, B->v0, t - B->t0, r, v);
+  double M = B->mi + B->mj, fi = B->mj / M, fj = B->mi / M;
+  const sn_body *C = &b[B->li];
+  for (int k = 0; k < 3; k++) {
+    T->lx[B->li][k] = C->pp[k] - fi * r[k];
+    T->lv[B->li][k] = C->pv[k] - fi * v[k];
+    T->lx[B->lj][k] = C->pp[k] + fj * r[k];
+    T->lv[B->lj][k] = C->pv[k] + fj * v[k];
+  }
+}
+
+/* Resolved forces on top-level nodes (smallN.cc:127-240, 316-363);
+ * returns min step^2, and the node pair that set it. */
+static double snu_forces(snu_tree *T, sn_body *b, int *imin, int *jmin) {
+  int n = T->n;
+  double lx[64][3], lv[64][3], lm[64];
+  int ln[64];
+  for (int s = 0; s < n; s++) {
+    int leader = T->node[s] >= 0 ? T->node[s] : -1;
+    if (leader < 0) { /* a companion: find its binary */
+      for (int q = 0; q < T->nb; q++)
+        if (T->b[q].lj == s) leader = T->b[q].li;
+    }
+    ln[s] = leader;
+    int q = T->bin_of[leader];
+    if (q >= 0) {
+      lm[s] = s == T->b[q].li ? T->b[q].mi : T->b[q].mj;
+      for (int k = 0; k < 3; k++) lx[s][k] = T->lx[s][k], lv[s][k] = T->lv[s][k];
+    } else {
+      lm[s] = b[s].m;
+      for (int k = 0; k < 3; k++) lx[s][k] = b[s].pp[k], lv[s][k] = b[s].pv[k];
+    }
+  }
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < 3; k++) b[i].acc[k] = b[i].jerk[k] = 0;
+  double min_ts2 = ORC_INF;
+  *imin = *jmin = -1;
+  for (int A = 0; A < n; A++) {
+    if (T->node[A] != A) continue; /* top-level nodes are their own leader */
+    for (int Bn = A + 1; Bn < n; Bn++) {
+      if (T->node[Bn] != Bn) continue;
+      double F[3] = {0, 0, 0}, J[3] = {0, 0, 0}, mind2 = ORC_INF;
+      for (int a = 0; a < n; a++) {
+        if (ln[a] != A) continue;
+        double fi[3] = {0, 0, 0}, ji[3] = {0, 0, 0};
+        for (int c = 0; c < n; c++) {
+          if (ln[c] != Bn) continue;
+          double dx[3], dv[3];
+          for (int k = 0; k < 3; k++) dx[k] = lx[c][k] - lx[a][k], dv[k] = lv[c][k] - lv[a][k];
+          double d2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+          double d = sqrt(d2), d3 = d2 * d;
+          double xv = dx[0] * dv[0] + dx[1] * dv[1] + dx[2] * dv[2];
+          for (int k = 0; k < 3; k++) {
+            fi[k] += lm[c] * dx[k] / d3;
+            ji[k] += lm[c] * (dv[k] / d3 - 3 * dx[k] * xv / (d3 * d2));
+          }
+          if (d2 < mind2) mind2 = d2;
+        }
+        for (int k = 0; k < 3; k++) F[k] += lm[a] * fi[k], J[k] += lm[a] * ji[k];
+      }
+      double dvc[3];
+      for (int k = 0; k < 3; k++) dvc[k] = b[Bn].pv[k] - b[A].pv[k];
+      double vel2 = dvc[0] * dvc[0] + dvc[1] * dvc[1] + dvc[2] * dvc[2];
+      double md = sqrt(mind2);
+      double ts2 = fmin(0.5 * mind2 * md / (b[A].m + b[Bn].m), mind2 / fabs(vel2));
+      for (int k = 0; k < 3; k++) {
+        b[A].acc[k] += F[k] / b[A].m;
+        b[A].jerk[k] += J[k] / b[A].m;
+        b[Bn].acc[k] -= F[k] / b[Bn].m;
+        b[Bn].jerk[k] -= J[k] / b[Bn].m;
+      }
+      if (ts2 < min_ts2) {
+        min_ts2 = ts2;
+        *imin = A;
+        *jmin = Bn;
+      }
+    }
+  }
+  return min_ts2;
+}
+
+static double snu_dist(const double a[3], const double b[3]) {
+  double d[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
+  return sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+}
+
+/* Tidal potential of the other top-level nodes on leaves (xi, xj) around
+ * the CM xc (smallN_unpert.cc:17-40). */
+static double snu_tidal(const snu_tree *T, const sn_body *b, int self, double mi, double mj,
+                        const double xi[3], const double xj[3], const double xc[3],
+                        int skip) {
+  double phi = 0, mc = mi + mj;
+  for (int k = 0; k < T->n; k++) {
+    if (T->node[k] != k || k == self || k == skip) continue;
+    phi += b[k].m * (-mi / snu_dist(xi, b[k].pos) - mj / snu_dist(xj, b[k].pos) +
+                     mc / snu_dist(xc, b[k].pos));
+  }
+  return phi;
+}
+
+static double snu_time_to_radius(double dr, double vr, double ar) {
+  if (dr <= 0) return 0;
+  double dt = ORC_INF;
+  if (vr < 0) dt = -dr / vr;
+  if (ar < 0) dt = fmin(dt, sqrt(-2 * dr / ar));
+  return dt;
+}
+
+long orc_smalln_unpert(int n, const double *mass, double *pos, double *vel, double eta,
+                       int n_iter, double t_end, double dt_crit, double r2_crit, double gamma,
+                       int allow_full, double *t_out, long max_steps, int *nbin_out) {
+  if (n > 64) return -1;
+  const double gamma2 = gamma * gamma, gamma_inv3 = pow(fmax(gamma2, 1e-120), -1.0 / 6);
+  sn_body *b = (sn_body *)calloc((size_t)n, sizeof(sn_body));
+  snu_tree T;
+  memset(&T, 0, sizeof(T));
+  T.n = n;
+  for (int i = 0; i < n; i++) {
+    T.node[i] = i;
+    T.bin_of[i] = -1;
+    b[i].m = mass[i];
+    for (int k = 0; k < 3; k++) {
+      b[i].pos[k] = b[i].pp[k] = pos[3 * i + k];
+      b[i].vel[k] = b[i].pv[k] = vel[3 * i + k];
+    }
+  }
+  int bim, bjm, nbin_made = 0;
+  double t = 0;
+  double dt = eta * sqrt(snu_forces(&T, b, &bim, &bjm));
+  long steps = 0;
+  while (t < t_end && (max_steps <= 0 || steps < max_steps)) {
+    /* take_a_step (smallN.cc:553-682) with the unperturbed limit */
+    double lim = ORC_INF;
+    for (int q = 0; q < T.nb; q++) lim = fmin(lim, T.b[q].t_pred - t);
+    int nit = n_iter;
+    if (dt >= lim) {
+      dt = lim;
+      nit = 0;
+    }
+    /* predict_loworder_all (hdyn.h:192-201: with the stored old force) */
+    double tn = t + dt, h = dt, h3 = h / 3, h2 = h / 2;
+    for (int i = 0; i < n; i++) {
+      if (T.node[i] != i) continue;
+      for (int k = 0; k < 3; k++) {
+        b[i].pp[k] = ((b[i].ojerk[k] * h3 + b[i].oacc[k]) * h2 + b[i].vel[k]) * h + b[i].pos[k];
+        b[i].pv[k] = (b[i].ojerk[k] * h2 + b[i].oacc[k]) * h + b[i].vel[k];
+      }
+    }
+    /* store_old_force */
+    double oa[64][3], oj[64][3];
+    for (int i = 0; i < n; i++)
+      for (int k = 0; k < 3; k++) oa[i][k] = b[i].acc[k], oj[i][k] = b[i].jerk[k];
+    for (int q = 0; q < T.nb; q++) snu_resolve(&T, b, q, tn);
+    double new_dt = dt, end_dt = dt;
+    for (int it = 0; it <= nit; it++) {
+      double prev = new_dt;
+      end_dt = eta * sqrt(snu_forces(&T, b, &bim, &bjm));
+      if (it < nit) {
+        new_dt = 0.5 * (dt + end_dt);
+        new_dt = dt + 0.5 * (end_dt - dt) * (new_dt / prev);
+        if (new_dt >= lim) {
+          new_dt = lim;
+          nit = 0;
+        }
+      }
+      for (int i = 0; i < n; i++) {
+        if (T.node[i] != i) continue;
+        if (new_dt != prev) {
+          double dt_off = new_dt - 0.5 * prev, theta = 0.5 * prev, tau = dt_off / theta;
+          double inv_theta = 1 / theta, tau2 = tau * tau, tau3 = tau2 * tau;
+          for (int k = 0; k < 3; k++) {
+            double pa = b[i].acc[k], pj = b[i].jerk[k];
+            b[i].acc[k] = 0.25 * (oa[i][k] * (2 - 3 * tau + tau3) + pa * (2 + 3 * tau - tau3) +
+                                  oj[i][k] * theta * (1 - tau - tau2 + tau3) +
+                                  pj * theta * (-1 - tau + tau2 + tau3));
+            b[i].jerk[k] = 0.25 * (oa[i][k] * inv_theta * 3 * (-1 + tau2) +
+                                   pa * inv_theta * 3 * (1 - tau2) +
+                                   oj[i][k] * (-1 - 2 * tau + 3 * tau2) +
+                                   pj * (-1 + 2 * tau + 3 * tau2));
+          }
+        }
+        double nd2 = new_dt * new_dt;
+        for (int k = 0; k < 3; k++) {
+          b[i].pv[k] = b[i].vel[k] + new_dt * (b[i].acc[k] + oa[i][k]) / 2 -
+                       nd2 * (b[i].jerk[k] - oj[i][k]) / 12;
+          b[i].pp[k] = b[i].pos[k] + new_dt * (b[i].pv[k] + b[i].vel[k]) / 2 -
+                       nd2 * (b[i].acc[k] - oa[i][k]) / 12;
+        }
+      }
+      for (int q = 0; q < T.nb; q++) snu_resolve(&T, b, q, t + new_dt);
+    }
+    for (int i = 0; i < n; i++) {
+      if (T.node[i] != i) continue;
+      for (int k = 0; k < 3; k++) {
+        b[i].pos[k] = b[i].pp[k];
+        b[i].vel[k] = b[i].pv[k];
+        b[i].oacc[k] = oa[i][k];
+        b[i].ojerk[k] = oj[i][k];
+      }
+    }
+    dt = end_dt;
+    t = t + new_dt;
+    steps++;
+
+    /* tree changes (smallN.cc:1022-1060) */
+    int changed = 0;
+    /* is_unperturbed_and_approaching (smallN_unpert.cc:44-88) + create_binary */
+    if (bim >= 0 && dt <= dt_crit && T.bin_of[bim] < 0 && T.bin_of[bjm] < 0 && T.nb < SNU_NB) {
+      int i = bim, j = bjm;
+      double dx[3], dvv[3];
+      for (int k = 0; k < 3; k++) dx[k] = b[i].pos[k] - b[j].pos[k], dvv[k] = b[i].vel[k] - b[j].vel[k];
+      double d2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+      double rv = dx[0] * dvv[0] + dx[1] * dvv[1] + dx[2] * dvv[2];
+      if (d2 <= r2_crit && rv <= 0) {
+        double M = b[i].m + b[j].m, cm[3], cmv[3];
+        for (int k = 0; k < 3; k++) {
+          cm[k] = (b[i].m * b[i].pos[k] + b[j].m * b[j].pos[k]) / M;
+          cmv[k] = (b[i].m * b[i].vel[k] + b[j].m * b[j].vel[k]) / M;
+        }
+        double maxp = 0, nnd2 = 0;
+        int kk = -1;
+        for (int k2 = 0; k2 < n; k2++) {
+          if (T.node[k2] != k2 || k2 == i || k2 == j) continue;
+          double e2 = 0;
+          for (int k = 0; k < 3; k++) e2 += (b[k2].pos[k] - cm[k]) * (b[k2].pos[k] - cm[k]);
+          double p2 = b[k2].m * b[k2].m / e2;
+          if (p2 > maxp) maxp = p2, nnd2 = e2, kk = k2;
+        }
+        int unp = 1;
+        if (kk >= 0) {
+          double g2 = 4 * pow(b[kk].m / M, 2) * pow(d2 / nnd2, 3);
+          unp = g2 < gamma2;
+        }
+        double r[3], v[3], dtp, per;
+        for (int k = 0; k < 3; k++) r[k] = b[j].pos[k] - b[i].pos[k], v[k] = b[j].vel[k] - b[i].vel[k];
+        if (unp && snu_peri(M, r, v, &dtp, &per)) {
+          snu_bin *B = &T.b[T.nb];
+          B->li = i;
+          B->lj = j;
+          B->mi = b[i].m;
+          B->mj = b[j].m;
+          for (int k = 0; k < 3; k++) B->r0[k] = r[k], B->v0[k] = v[k];
+          B->t0 = t;
+          B->t_pred = 2 * (t + dtp) - t;
+          B->full = 0;
+          B->tidal = snu_tidal(&T, b, i, b[i].m, b[j].m, b[i].pos, b[j].pos, cm, j);
+          b[i].m = M;
+          for (int k = 0; k < 3; k++) {
+            b[i].pos[k] = b[i].pp[k] = cm[k];
+            b[i].vel[k] = b[i].pv[k] = cmv[k];
+            b[i].oacc[k] = b[i].ojerk[k] = 0; /* a new node */
+          }
+          T.node[j] = -1;
+          T.bin_of[i] = T.nb;
+          T.nb++;
+          nbin_made++;
+          changed = 1;
+        }
+      }
+    }
+    /* extend_or_end_binary for segments that end now */
+    for (int q = 0; q < T.nb; q++) {
+      snu_bin *B = &T.b[q];
+      if (B->t_pred > t) continue;
+      int i = B->li, j = B->lj;
+      double M = B->mi + B->mj, r[3], v[3];
+      if (B->full)
+        for (int k = 0; k < 3; k++) r[k] = B->r0[k], v[k] = B->v0[k];
+      else
+        snu_kepler(M, B->r0, B->v0, t - B->t0, r, v);
+      double xi[3], xj[3];
+      for (int k = 0; k < 3; k++) {
+        xi[k] = b[i].pos[k] - B->mj / M * r[k];
+        xj[k] = b[i].pos[k] + B->mi / M * r[k];
+      }
+      double tid = snu_tidal(&T, b, i, B->mi, B->mj, xi, xj, b[i].pos, j);
+      if (!B->full) {
+        double mu = B->mi * B->mj / M, v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+        double fac = 1 - 2 * (tid - B->tidal) / (mu * v2);
+        if (fac > 0)
+          for (int k = 0; k < 3; k++) v[k] *= sqrt(fac);
+      }
+      /* extension by whole periods while no perturber can arrive
+         (dt_perturbers, smallN_unpert.cc:402-460) */
+      double rn = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+      double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+      double alpha = 2 / rn - v2 / M;
+      double dtp = -1, period = ORC_INF;
+      if (allow_full && alpha > 0) {
+        double a = 1 / alpha;
+        period = 2 * M_PI / sqrt(M * alpha * alpha * alpha);
+        dtp = ORC_INF;
+        for (int k2 = 0; k2 < n; k2++) {
+          if (T.node[k2] != k2 || k2 == i) continue;
+          double rp = gamma_inv3 * a * cbrt(2 * b[k2].m / M);
+          double dp[3], dvl[3], da[3];
+          for (int k = 0; k < 3; k++) {
+            dp[k] = b[k2].pos[k] - b[i].pos[k];
+            dvl[k] = b[k2].vel[k] - b[i].vel[k];
+            da[k] = b[k2].acc[k] - b[i].acc[k];
+          }
+          double dr = sqrt(dp[0] * dp[0] + dp[1] * dp[1] + dp[2] * dp[2]);
+          double vr = (dvl[0] * dp[0] + dvl[1] * dp[1] + dvl[2] * dp[2]) / dr;
+          double ar = (da[0] * dp[0] + da[1] * dp[1] + da[2] * dp[2]) / dr;
+          double tr = snu_time_to_radius(dr - rp, vr, ar);
+          if (tr < dtp) dtp = tr;
+          if (tr <= 0) break;
+        }
+        dtp *= 0.5;
+      }
+      if (dtp >= period) {
+        B->t_pred += floor(dtp / period) * period;
+        B->full = 1;
+        B->tidal = tid;
+        for (int k = 0; k < 3; k++) B->r0[k] = r[k], B->v0[k] = v[k];
+        B->t0 = t;
+        continue;
+      }
+      /* terminate: the components become top-level nodes again */
+      b[j].m = B->mj;
+      b[i].m = B->mi;
+      double cx[3], cv[3];
+      for (int k = 0; k < 3; k++) cx[k] = b[i].pos[k], cv[k] = b[i].vel[k];
+      for (int k = 0; k < 3; k++) {
+        b[i].pos[k] = b[i].pp[k] = cx[k] - B->mj / M * r[k];
+        b[i].vel[k] = b[i].pv[k] = cv[k] - B->mj / M * v[k];
+        b[j].pos[k] = b[j].pp[k] = cx[k] + B->mi / M * r[k];
+        b[j].vel[k] = b[j].pv[k] = cv[k] + B->mi / M * v[k];
+        b[i].oacc[k] = b[i].ojerk[k] = b[j].oacc[k] = b[j].ojerk[k] = 0;
+      }
+      T.node[j] = j;
+      T.bin_of[i] = -1;
+      T.b[q] = T.b[T.nb - 1];
+      if (q < T.nb - 1) T.bin_of[T.b[q].li] = q;
+      T.nb--;
+      q--;
+      changed = 1;
+    }
+    if (changed) {
+      for (int i = 0; i < n; i++)
+        for (int k = 0; k < 3; k++) b[i].pp[k] = b[i].pos[k], b[i].pv[k] = b[i].vel[k];
+      for (int q = 0; q < T.nb; q++) snu_resolve(&T, b, q, t);
+      dt = eta * sqrt(snu_forces(&T, b, &bim, &bjm));
+    }
+  }
+  /* resolve the binaries left at the end into their components */
+  for (int q = 0; q < T.nb; q++) {
+    snu_bin *B = &T.b[q];
+    int i = B->li, j = B->lj;
+    double M = B->mi + B->mj, r[3], v[3];
+    if (B->full)
+      for (int k = 0; k < 3; k++) r[k] = B->r0[k], v[k] = B->v0[k];
+    else
+      snu_kepler(M, B->r0, B->v0, t - B->t0, r, v);
+    for (int k = 0; k < 3; k++) {
+      double cx = b[i].pos[k], cv = b[i].vel[k];
+      b[i].pos[k] = cx - B->mj / M * r[k];
+      b[i].vel[k] = cv - B->mj / M * v[k];
+      b[j].pos[k] = cx + B->mi / M * r[k];
+      b[j].vel[k] = cv + B->mi / M * v[k];
+    }
+  }
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < 3; k++) {
+      pos[3 * i + k] = b[i].pos[k];
+      vel[3 * i + k] = b[i].vel[k];
+    }
+  if (t_out) *t_out = t;
+  if (nbin_out) *nbin_out = nbin_made;
+  free(b);
+  return steps;
+}

@@ -284,22 +284,34 @@ int ph4ref_smalln(int n, const double *mass, double *pos, double *vel, double et
     prev = bn;
   }
   smallN_evolve(b, t_end, _INFINITY_, _INFINITY_, _INFINITY_, 0, "");
-  int i = 0;
+  // Report every leaf by its index; the leaves of a binary node hold
+  // positions relative to it (smallN.cc:427-436), so add the node's.
+  // Returns the number of binary nodes left at the end.
+  int nbin = 0;
   for_all_daughters(hdyn, b, bi) {
-    if (bi->get_oldest_daughter()) {  // a binary node: report its leaves' CM
-      std::cout.rdbuf(old);
-      return -1;
+    hdyn *od = bi->get_oldest_daughter();
+    if (od) {
+      nbin++;
+      for (hdyn *leaf = od; leaf; leaf = leaf->get_younger_sister()) {
+        vec p = bi->get_pos() + leaf->get_pos(), v = bi->get_vel() + leaf->get_vel();
+        const int i = leaf->get_index() - 1;
+        for (int k = 0; k < 3; k++) {
+          pos[3 * i + k] = p[k];
+          vel[3 * i + k] = v[k];
+        }
+      }
+      continue;
     }
     vec p = bi->get_pos(), v = bi->get_vel();
+    const int i = bi->get_index() - 1;
     for (int k = 0; k < 3; k++) {
       pos[3 * i + k] = p[k];
       vel[3 * i + k] = v[k];
     }
-    i++;
   }
   *t_out = b->get_system_time();
   std::cout.rdbuf(old);
-  return 0;
+  return nbin;
 }
 
 }  // extern "C"

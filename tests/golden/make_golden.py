@@ -49,7 +49,7 @@ def save(name, **arrays):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("AMUSE_REF"))
-    ap.add_argument("--only", default=None, choices=[None, "smalln", "encounters"])
+    ap.add_argument("--only", default=None, choices=[None, "smalln", "encounters", "unpert"])
     args = ap.parse_args()
     if not args.ref:
         ap.error("give --ref or set AMUSE_REF to the AMUSE checkout")
@@ -60,6 +60,8 @@ def main():
         return smalln_fixtures(oracle)
     if args.only == "encounters":
         return encounter_fixtures(oracle)
+    if args.only == "unpert":
+        return smalln_unpert_fixtures(oracle)
 
     # 1. IC generators (pins amuse_gb300/ic.py).
     np.random.seed(1)
@@ -137,6 +139,7 @@ def main():
          t_end=0.125, **{k: np.asarray(r[k]) for k in r})
     smalln_fixtures(oracle)
     encounter_fixtures(oracle)
+    smalln_unpert_fixtures(oracle)
 
 
 def smalln_fixtures(oracle):
@@ -154,6 +157,64 @@ def smalln_fixtures(oracle):
         out.update({f"s{k}_mass": m, f"s{k}_pos0": x, f"s{k}_vel0": v, f"s{k}_pos": p,
                     f"s{k}_vel": vv, f"s{k}_t": t})
     save("smalln_systems.npz", nsys=len(out) // 6, eta=0.14, t_end=2 * tcr, **out)
+
+
+def hierarchical(kind, seed):
+    """Few-body systems with hard binaries, in the CM frame: "triple" (an
+    eccentric inner binary and a third body on a bound outer orbit), "quad"
+    (two binaries on a bound orbit), "field" (a binary among 6 single
+    stars).  Used for smallN's unperturbed-binary treatment."""
+    rng = np.random.RandomState(seed)
+
+    def binary(m1, m2, a, e):
+        r = a * (1 + e)
+        vrel = np.sqrt((m1 + m2) * (1 - e) / r)
+        x = np.array([[-m2 / (m1 + m2) * r, 0, 0], [m1 / (m1 + m2) * r, 0, 0]])
+        v = np.array([[0, -m2 / (m1 + m2) * vrel, 0], [0, m1 / (m1 + m2) * vrel, 0]])
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))  # random orientation
+        return x @ q.T, v @ q.T
+
+    if kind == "triple":
+        m = np.array([0.4, 0.4, 0.2]) * rng.uniform(0.8, 1.2, 3)
+        xb, vb = binary(m[0], m[1], 0.01, rng.uniform(0.1, 0.8))
+        d = rng.uniform(0.8, 1.2)
+        x = np.vstack([xb, [[0, d, 0]]])
+        v = np.vstack([vb, [[0.8 * np.sqrt(m.sum() / d), 0, 0]]])
+    elif kind == "quad":
+        m = np.full(4, 0.25) * rng.uniform(0.8, 1.2, 4)
+        x1, v1 = binary(m[0], m[1], 0.01, rng.uniform(0.1, 0.7))
+        x2, v2 = binary(m[2], m[3], 0.015, rng.uniform(0.1, 0.7))
+        x = np.vstack([x1 + [-0.6, 0, 0], x2 + [0.6, 0, 0]])
+        vo = 0.5 * np.sqrt(m.sum() / 1.2)
+        v = np.vstack([v1 + [0, -vo, 0], v2 + [0, vo, 0]])
+    else:
+        m = np.concatenate([[0.3, 0.3], np.full(6, 0.4 / 6)])
+        xb, vb = binary(m[0], m[1], 0.005, rng.uniform(0.2, 0.9))
+        xf = rng.normal(0, 1.0, (6, 3))
+        vf = rng.normal(0, 0.3, (6, 3))
+        x, v = np.vstack([xb, xf]), np.vstack([vb, vf])
+    cm = (m[:, None] * x).sum(0) / m.sum()
+    cv = (m[:, None] * v).sum(0) / m.sum()
+    return m, x - cm, v - cv
+
+
+SMALLN_UNPERT_CASES = [("triple", 1, 2.0), ("triple", 2, 2.0), ("triple", 3, 4.0),
+                       ("quad", 4, 2.0), ("field", 5, 1.0), ("field", 6, 1.0)]
+
+
+def smalln_unpert_fixtures(oracle):
+    """9. smallN WITH its unperturbed binaries (the worker's defaults:
+    dt_crit 1e-3, r2_crit 1e-2, gamma 1e-6, full unperturbed motion allowed)
+    on systems with hard binaries, through the unmodified smallN objects
+    (the leaves of binary nodes left at the end reported in absolute
+    coordinates)."""
+    out = {}
+    for k, (kind, seed, t_end) in enumerate(SMALLN_UNPERT_CASES):
+        m, x, v = hierarchical(kind, seed)
+        p, vv, t, _ = oracle.smalln(m, x, v, 0.14, t_end, lib="ref", dt_crit=1e-3)
+        out.update({f"s{k}_mass": m, f"s{k}_pos0": x, f"s{k}_vel0": v, f"s{k}_pos": p,
+                    f"s{k}_vel": vv, f"s{k}_t": t, f"s{k}_t_end": t_end})
+    save("smalln_unpert.npz", nsys=len(SMALLN_UNPERT_CASES), eta=0.14, **out)
 
 
 # (n, seed, radius, mode): collision stops (radius R for all particles) and

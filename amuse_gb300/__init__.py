@@ -47,7 +47,8 @@ ABI_SYMBOLS = [
 ]
 BYVALUE_SYMBOLS = [s[:-1] for s in ABI_SYMBOLS]
 EXT_SYMBOLS = [
-    "g6x_set_precision", "g6x_get_precision", "g6x_set_npipes", "g6x_last_error", "g6x_load",
+    "g6x_set_precision", "g6x_get_precision", "g6x_set_refine", "g6x_refine_stats",
+    "g6x_test_wait_expiry", "g6x_set_npipes", "g6x_last_error", "g6x_load",
     "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
     "g6x_energy", "g6x_run_stats", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
     "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
@@ -99,6 +100,9 @@ def load():
     lib.g6_read_neighbour_list_.argtypes = [_pi]
     lib.g6_get_neighbour_list_.argtypes = [_pi, _pi, _pi, _pi, _pi]
     lib.g6x_set_precision.argtypes = [I]
+    lib.g6x_set_refine.argtypes = [D]
+    lib.g6x_refine_stats.argtypes = [_pi]
+    lib.g6x_test_wait_expiry.argtypes = [I]
     lib.g6x_set_npipes.argtypes = [I]
     lib.g6x_last_error.restype = ctypes.c_char_p
     lib.g6x_load.argtypes = [I, _pi, _pd, _pd, _pd, _pd, _pd, _pd, _pd]
@@ -257,6 +261,20 @@ class G6X(G6):
 
     def get_precision(self):
         return self.lib.g6x_get_precision()
+
+    def set_refine(self, kappa):
+        """Condition-number limit of the split refinement pass (0: no FP64 redo)."""
+        _check(self.lib.g6x_set_refine(float(kappa)), "g6x_set_refine")
+
+    def refine_stats(self):
+        """Last call's refinement queue: queued, queued for kappa, overflow."""
+        out = np.zeros(3, np.int32)
+        _check(self.lib.g6x_refine_stats(_ptr(out, ctypes.c_int)), "g6x_refine_stats")
+        return dict(queued=int(out[0]), kappa=int(out[1]), overflow=int(out[2]))
+
+    def test_wait_expiry(self, on=True):
+        """Test hook: the next force call's bounded wait expires (20 ms)."""
+        _check(self.lib.g6x_test_wait_expiry(1 if on else 0), "g6x_test_wait_expiry")
 
     def set_npipes(self, n):
         _check(self.lib.g6x_set_npipes(n), "g6x_set_npipes")

@@ -74,7 +74,26 @@ typedef struct {
   int hjerk;   /* 1: jerk as the hermite code forms it, (r.v) / r^2 with the
                   unsoftened r^2 (src/amuse_hermite/interface.cc:440-449,486);
                   needs want_nn = 0 and force_jl 0 or 1 */
+  /* split precision only: the refinement pass (kern_force.cu, refine_kernel)
+     that makes the nearest neighbour exact and redoes ill-conditioned sums
+     in FP64.  refine: a g6k_refine_bytes() device buffer, zeroed once at
+     allocation (NULL: no refinement, and the split-j merge runs as a second
+     kernel); kappa: condition number above which acc and pot are redone in
+     FP64 (0: never; < 0: no refinement pass at all, the buffer then only
+     holds the force kernel's split-merge tickets). */
+  void *refine;
+  double kappa;
+  /* test hook: the first CTA waits for its first tile on a barrier that
+     nothing arrives on, with a 20 ms limit, so the bounded wait expires and
+     the call ends with the error word set (no trap, no unbounded spin) */
+  int stall_test;
 } g6_force_args;
+
+/* Size of the refinement buffer (fixed; allocated once per context). */
+size_t g6k_refine_bytes(void);
+/* Last refinement: out[0] particles queued, out[1] of them because of the
+   condition number, out[2] the largest queue that overflowed (0: none).  */
+int g6k_refine_read(const void *refine, int out[3], cudaStream_t st);
 
 /* Launch shape actually used (reported by g6k_force). */
 typedef struct {
@@ -164,6 +183,11 @@ __device__ __forceinline__ double g6_predict_x(double x, double v, double a, dou
   const double hdt = __dmul_rn(0.5, dt);
   return __dadd_rn(
       x, __dmul_rn(dt, __dadd_rn(v, __dmul_rn(hdt, __dadd_rn(a, __ddiv_rn(__dmul_rn(dt, j), 3.0))))));
+}
+/* ph4's predicted velocity component, v + dt*(a + 0.5*dt*j) (jdata.cc:741-743). */
+__device__ __forceinline__ double g6_predict_v(double v, double a, double j, double dt) {
+  if (dt == 0) return v;
+  return __dadd_rn(v, __dmul_rn(dt, __dadd_rn(a, __dmul_rn(__dmul_rn(0.5, dt), j))));
 }
 /* Split-record field f of slot s (f: 0 xh, 1 yh, 2 zh, 3 m, 4 xl, 5 yl,
    6 zl, 7 pad, 8 vx, 9 vy, 10 vz, 11 pad) in the pair layout above. */

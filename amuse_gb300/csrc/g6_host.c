@@ -26,11 +26,15 @@
 #include "g6_dev.h"
 
 int g6k_clamp_steps(const g6_jstate *js, int nj, double dtmax, cudaStream_t st);
+int g6k_static_scratch_addr(void **out);
 int g6k_neighbours(const g6_jstate *js, int nj, int ni, int prec, const double *ipos,
                    const double *h2, const int *iself, int *out, int maxn, cudaStream_t st);
 
 #define G6_DEFAULT_CAP 131072
 #define G6_DEFAULT_NPIPES 16384
+/* Condition-number limit above which split acc/pot are redone in FP64
+   (kern_force.cu: "condition-number refinement"). */
+#define G6_DEFAULT_KAPPA 48.0
 
 /* ------------------------------------------------------------ id map --- */
 /* Open addressing id -> slot (ids are arbitrary ints). */
@@ -145,6 +149,17 @@ typedef struct {
   /* k nearest neighbours (g6x_knn) */
   void *d_knn;
   size_t knn_bytes;
+  /* split-precision refinement queue (nearest-neighbour proof, FP64 redo of
+     ill-conditioned sums) and the force kernel's split-merge tickets: fixed
+     size, allocated at open */
+  void *d_refine;
+  double kappa;
+  /* device address of the no-allocation entry point's fixed scratch array,
+     looked up at open with the library's device current */
+  void *d_static;
+  /* test hook: the next force call's first CTA waits on a barrier that
+     nothing arrives on (g6x_test_wait_expiry) */
+  int stall_next;
   /* statistics */
   int timing;
   double st_predict_ms, st_force_ms, st_pairs, st_pred_bytes, st_nj;
@@ -377,12 +392,23 @@ static int predict_if_needed(int nj) {
   return 0;
 }
 
+/* The refinement pass of split-precision g6 forces (the fixed-step path
+   passes kappa < 0 and keeps plain split arithmetic).  The buffer is passed
+   in every case: the force kernel also keeps its split-merge tickets there. */
+static void refine_args(g6_force_args *a) {
+  a->refine = G.d_refine;
+  if (a->kappa >= 0.0) a->kappa = G.kappa;
+}
+
 /* Run one force evaluation whose inputs are already on the device. */
 static int run_force(g6_force_args *a) {
   size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->hjerk ? 1 : a->force_jl,
                                   a->force_nsplit);
   int rc = ensure_scratch(need);
   if (rc) return rc;
+  refine_args(a);
+  a->stall_test = G.stall_next;
+  G.stall_next = 0;
   a->scratch = G.d_scratch;
   a->scratch_bytes = G.scratch_bytes;
   a->js = &G.js;
@@ -442,11 +468,26 @@ int g6_open_(int *id) {
   G.prec = G6_PREC_SPLIT;
   e = getenv("G6_PRECISION");
   if (e && (!strcmp(e, "fp64") || !strcmp(e, "FP64"))) G.prec = G6_PREC_FP64;
+  G.kappa = G6_DEFAULT_KAPPA;
+  e = getenv("G6_KAPPA");
+  if (e && atof(e) >= 0.0) G.kappa = atof(e);
   G.is_open = 1;
   int rc = grow_j(G6_DEFAULT_CAP);
   if (rc == 0) rc = ensure_io(G.npipes < 4096 ? G.npipes : 4096);
+  if (rc == 0) {
+    if (cudaMalloc(&G.d_refine, g6k_refine_bytes()) != cudaSuccess ||
+        cudaMemset(G.d_refine, 0, g6k_refine_bytes()) != cudaSuccess) {
+      seterr("cannot allocate the refinement buffer");
+      rc = G6_ERR_NOMEM;
+    }
+  }
+  /* Loads the force module, so its fixed 16 MiB array is taken here. */
+  if (rc == 0 && g6k_static_scratch_addr(&G.d_static) != 0) {
+    seterr("cannot obtain the device address of the fixed scratch array");
+    rc = G6_ERR_CUDA;
+  }
   if (rc) {
-    G.is_open = 0;
+    g6_close_(id);
     return rc;
   }
   return 0;
@@ -475,6 +516,7 @@ int g6_close_(int *id) {
   cudaFree(G.d_rad); cudaFree(G.d_enc); cudaFree(G.d_encp_d); cudaFree(G.d_encp_i);
   cudaFree(G.d_enc_ctr);
   cudaFree(G.d_knn);
+  cudaFree(G.d_refine);
   cudaEventDestroy(G.ev_done); cudaEventDestroy(G.ev_upd);
   cudaEventDestroy(G.ev_t0); cudaEventDestroy(G.ev_t1); cudaEventDestroy(G.ev_t2);
   cudaStreamDestroy(G.st);
@@ -899,6 +941,26 @@ int g6x_set_precision(int prec) {
   return 0;
 }
 int g6x_get_precision(void) { return G.prec; }
+int g6x_set_refine(double kappa) {
+  if (!(kappa >= 0.0)) return G6_ERR_ARG;
+  G.kappa = kappa;
+  return 0;
+}
+int g6x_test_wait_expiry(int on) {
+  int rc = check_open();
+  if (rc) return rc;
+  G.stall_next = on ? 1 : 0;
+  return 0;
+}
+int g6x_refine_stats(int out[3]) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (g6k_refine_read(G.d_refine, out, G.st)) {
+    seterr("cannot read the refinement queue");
+    return G6_ERR_CUDA;
+  }
+  return 0;
+}
 int g6x_set_npipes(int npipes) {
   if (npipes < 1 || npipes > (1 << 20)) return G6_ERR_ARG;
   G.npipes = npipes;
@@ -1514,10 +1576,13 @@ int g6x_energy(double *kinetic, double *potential) {
  * synchronisation and latency of cudaMalloc/cudaFree in its step loop.  The
  * j-system must already be resident (loaded and sized by earlier calls); the
  * split-j partial sums go to a fixed 16 MiB device array inside the library
- * instead of the growable scratch buffer.  Calls needing more than that, a
- * larger j-store, or a larger update buffer are refused, never allocated. */
+ * instead of the growable scratch buffer.  That array is taken, and its device
+ * address looked up, in g6_open; the refinement queue is allocated there too.
+ * Calls needing more than that, a larger j-store, or a larger update buffer
+ * are refused, never allocated. */
 size_t g6k_static_scratch_capacity(void);
-int g6k_force_static(const g6_force_args *a, g6_shape *shape, cudaStream_t st, size_t *need_out);
+int g6k_force_static(const g6_force_args *a, void *static_addr, g6_shape *shape,
+                     cudaStream_t st, size_t *need_out);
 
 int g6x_force_dev_noalloc(double ti, double eps2, int nj, int ni, const double *d_xi,
                           const double *d_vi, const int *d_self_slot, double *d_acc,
@@ -1567,8 +1632,10 @@ int g6x_force_dev_noalloc(double ti, double eps2, int nj, int ni, const double *
   a.want_nn = d_nn != NULL;
   a.js = &G.js;
   a.err = G.d_err;
+  refine_args(&a); /* fixed buffer, allocated at open */
   size_t need = 0;
-  rc = g6k_force_static(&a, &G.shape, G.st, &need);
+  if (G.timing && !G.predicted_this_call) cudaEventRecord(G.ev_t1, G.st);
+  rc = g6k_force_static(&a, G.d_static, &G.shape, G.st, &need);
   if (rc == -4) {
     seterr("g6x_force_dev_noalloc: ni=%d, nj=%d needs %zu B of split-j scratch, more than the "
            "fixed %zu B; use g6x_force_dev or fewer i-particles per call", ni, nj, need,
@@ -1579,8 +1646,15 @@ int g6x_force_dev_noalloc(double ti, double eps2, int nj, int ni, const double *
     seterr("g6x_force_dev_noalloc: launch failed (%d)", rc);
     return G6_ERR_CUDA;
   }
+  if (G.timing) cudaEventRecord(G.ev_t2, G.st);
+  G.st_pairs = (double)ni * (double)(nj - 1);
+  G.st_nj = nj;
+  G.st_pred_bytes = G.predicted_this_call
+                        ? (double)nj * (15.0 * 8.0 + (G.prec == G6_PREC_FP64 ? 64.0 : 48.0))
+                        : 0.0;
   if (sync) {
     CK(cudaStreamSynchronize(G.st));
+    collect_timing();
     return read_err_word();
   }
   return 0;
@@ -1935,6 +2009,7 @@ static int fixed_force_async(int n, double eps2, const double *d_x, const double
   a.jerk = d_j;
   a.pot = G.d_rpot;
   a.hjerk = fx_form == G6_JERK_HERMITE;
+  a.kappa = -1.0; /* the adjoint differentiates plain split arithmetic */
   return run_force(&a);
 }
 

@@ -40,6 +40,7 @@
 //   * A tile that holds the self slot of one of the warp's i-particles takes
 //     a checked copy of the loop (rinv = 0, r2 -> +inf for self).
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "f32x2.cuh"
@@ -73,6 +74,18 @@ namespace {
 #ifndef G6_IPT_F64
 #define G6_IPT_F64 4
 #endif
+#ifndef G6_JCHUNK
+#define G6_JCHUNK 32  // split: records per jerk fold
+#endif
+#ifndef G6_TOT_SMEM
+#define G6_TOT_SMEM 2  // split: compensated totals in shared memory (2: with NN only)
+#endif
+#ifndef G6_S1
+#define G6_S1 1  // split: accumulate the condition number's sum
+#endif
+#ifndef G6_S1_HALF
+#define G6_S1_HALF 0  // split: sum over the even j of each record pair only (x2)
+#endif
 constexpr int NT = G6_NT;    // threads per CTA
 constexpr int TJ = G6_TILE;  // j records per tile
 // i-particles per thread: the split kernel's packed f32x2 pair terms need
@@ -82,6 +95,7 @@ constexpr int IPT_F64 = G6_IPT_F64;
 constexpr int UNROLL = G6_UNROLL;  // j-loop unroll factor
 constexpr int JLMAX = TJ < NT ? TJ : NT;  // j-lanes per i at most
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound per wait
+constexpr unsigned long long STALL_TEST_NS = 20000000ull;  // 20 ms under the test hook
 
 enum { ERR_TMA_TIMEOUT = 1, ERR_SHAPE = 2 };
 
@@ -140,24 +154,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 // Bounded wait that also gives up when another warp of the CTA raised
-// *abort (false in both cases).
+// *abort (false in both cases, or after limit_ns of global time).
 __device__ __forceinline__ bool mbar_wait_abortable(uint64_t *bar, uint32_t parity,
-                                                    volatile int *abort) {
+                                                    volatile int *abort,
+                                                    unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = gtimer();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort) return false;
-    if (gtimer() - t0 > WAIT_NS) return false;
+    if (gtimer() - t0 > limit_ns) return false;
   }
 }
-// Bounded wait: false after WAIT_NS of global time.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+// Bounded wait: false after limit_ns of global time.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = gtimer();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (gtimer() - t0 > WAIT_NS) return false;
+    if (gtimer() - t0 > limit_ns) return false;
   }
 }
 
@@ -196,6 +212,8 @@ __device__ __forceinline__ void ff_add(float &ah, float &al, float bh, float bl)
   al = __fsub_rn(e, __fsub_rn(ah, s));
 }
 
+struct KParams;
+
 // ------------------------------------------------------------ policies ---
 struct SplitP {
   using Rec = RecS;
@@ -208,14 +226,16 @@ struct SplitP {
     f2x xh, yh, zh, xl, yl, zl, vx, vy, vz;
   };
   struct Part {  // per-fold-period partial sums, one per half
-    f2x a[3], j[3], p;
+    f2x a[3], j[3], p, s;
   };
-  struct Tot {  // compensated totals
-    float ah[3], al[3], jh[3], jl[3], ph, pl;
+  struct Tot {  // compensated totals (s: plain sum, an estimate)
+    float ah[3], al[3], jh[3], jl[3], ph, pl, s;
   };
-  struct Out {  // partial record exchanged between CTAs, 64 B
+  struct Out {  // partial record exchanged between CTAs, 72 B
     float2 a[3], j[3], p;
-    float nnr2;
+    float nnr2;   // smallest nearest-neighbour key (r^2 + eps^2, FP32)
+    float nnr2b;  // second smallest key over the other j
+    float s1;     // sum of m / (r^2 + eps^2): the condition number's numerator
     int nn;
   };
   __device__ static void split(double d, float &h, float &l) {
@@ -249,11 +269,13 @@ struct SplitP {
 #pragma unroll
     for (int k = 0; k < 3; k++) q.a[k] = q.j[k] = 0ull;
     q.p = 0ull;
+    q.s = 0ull;
   }
   __device__ static void zero(Tot &t) {
 #pragma unroll
     for (int k = 0; k < 3; k++) t.ah[k] = t.al[k] = t.jh[k] = t.jl[k] = 0.f;
     t.ph = t.pl = 0.f;
+    t.s = 0.f;
   }
   __device__ static void fold(Tot &t, const Part &q) {
 #pragma unroll
@@ -265,6 +287,7 @@ struct SplitP {
     }
     ff_acc(t.ph, t.pl, f2_lo(q.p));
     ff_acc(t.ph, t.pl, f2_hi(q.p));
+    t.s += G6_S1_HALF ? 2.f * f2_lo(q.s) : f2_lo(q.s) + f2_hi(q.s);
   }
   // r^2 + eps^2 of both j of a record (the nearest-neighbour key): the main
   // loop and the re-scan use this same arithmetic, so the keys are
@@ -281,6 +304,13 @@ struct SplitP {
   // HJ: the jerk as the hermite code forms it (src/amuse_hermite/
   // interface.cc:440-449,469-486): the (r.v) factor divided by the
   // UNsoftened r^2.
+  //
+  // NN keeps the smallest key of the tile (nnmin, one FMNMX per j); the
+  // kernel turns the tile minima into the smallest and second smallest key
+  // over all j, whose gap decides whether the FP32 argmin is provably ph4's
+  // FP64 nearest neighbour (finish() below).  Without HJ the sum of
+  // m / (r^2 + eps^2) (Part::s) is kept for the condition number of the
+  // acceleration sum.
   template <bool CHECK, bool NN, bool HJ = false>
   __device__ static __forceinline__ void pair(const I &s, const Rec &r, f2x eps2, Part &q,
                                               float &nnmin, int selfrel) {
@@ -326,28 +356,52 @@ struct SplitP {
     q.j[1] = f2_fma(mr3i, f2_fma(a3, dy, dvy), q.j[1]);
     q.j[2] = f2_fma(mr3i, f2_fma(a3, dz, dvz), q.j[2]);
     q.p = f2_add(q.p, mri);
+    if (!HJ && G6_S1) {
+      if (G6_S1_HALF)  // one scalar FMA (half the FMA-pipe cycles of a packed one)
+        q.s = f2_pack(fmaf(f2_lo(mri), ra, f2_lo(q.s)), 0.f);
+      else
+        q.s = f2_fma(mri, rinv, q.s);
+    }
   }
-  // Nearest-neighbour re-scan of one record: the first of its j (in slot
-  // order) whose key equals best and that is not the i itself.
-  __device__ static __forceinline__ bool rescan(const I &s, const Rec &r, f2x eps2, float best,
-                                                int slot0, int self, int &idx) {
+  // Nearest-neighbour re-scan of one record of the best tile: the first j
+  // (in slot order) whose key equals best and that is not the i itself
+  // becomes idx; every other key lowers m2 (the second smallest key).
+  __device__ static __forceinline__ void rescan(const I &s, const Rec &r, f2x eps2, float best,
+                                                int slot0, int self, int &idx, float &m2) {
     f2x dx, dy, dz;
     const f2x r2 = r2e(s, r, eps2, dx, dy, dz);
-    if (f2_lo(r2) == best && slot0 != self) {
-      idx = slot0;
-      return true;
+    const float kk[2] = {f2_lo(r2), f2_hi(r2)};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      if (slot0 + h == self) continue;
+      if (idx < 0 && kk[h] == best)
+        idx = slot0 + h;
+      else
+        m2 = fminf(m2, kk[h]);
     }
-    if (f2_hi(r2) == best && slot0 + 1 != self) {
-      idx = slot0 + 1;
-      return true;
+  }
+  // Mid-tile fold of the jerk partial sums alone: the jerk sum cancels more
+  // than the others, so it is folded every JCHUNK records.
+  static constexpr bool JFOLD = true;
+  // shared-memory totals free registers: they pay off in the nearest-
+  // neighbour variant, not in the plain one (measured)
+  template <bool NN>
+  __host__ __device__ static constexpr bool tot_shared() {
+    return G6_TOT_SMEM == 1 || (G6_TOT_SMEM == 2 && NN);
+  }
+  __device__ static void fold_jerk(Tot &t, Part &q) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      ff_acc(t.jh[k], t.jl[k], f2_lo(q.j[k]));
+      ff_acc(t.jh[k], t.jl[k], f2_hi(q.j[k]));
+      q.j[k] = 0ull;
     }
-    return false;
   }
   __device__ static f2x eps(double eps2) {
     const float e = (float)eps2 + (float)(1.0 / 4503599627370496.0);  // + 2^-52 (ph4)
     return f2_pack(e, e);
   }
-  __device__ static void to_out(const Tot &t, float nnr2, int nn, Out &o) {
+  __device__ static void to_out(const Tot &t, float nnr2, float nnr2b, int nn, Out &o) {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       o.a[k] = make_float2(t.ah[k], t.al[k]);
@@ -355,6 +409,8 @@ struct SplitP {
     }
     o.p = make_float2(t.ph, t.pl);
     o.nnr2 = nnr2;
+    o.nnr2b = nnr2b;
+    o.s1 = t.s;
     o.nn = nn;
   }
   __device__ static void merge(Out &a, const Out &b) {
@@ -364,10 +420,14 @@ struct SplitP {
       ff_add(a.j[k].x, a.j[k].y, b.j[k].x, b.j[k].y);
     }
     ff_add(a.p.x, a.p.y, b.p.x, b.p.y);
+    a.s1 += b.s1;
+    // second smallest of the four keys: min(max of the minima, min of the seconds)
+    const float m2 = fminf(fmaxf(a.nnr2, b.nnr2), fminf(a.nnr2b, b.nnr2b));
     if (b.nnr2 < a.nnr2 || (b.nnr2 == a.nnr2 && b.nn < a.nn)) {
       a.nnr2 = b.nnr2;
       a.nn = b.nn;
     }
+    a.nnr2b = m2;
   }
   __device__ static void write_final(const Out &o, int i, double *acc, double *jerk,
                                      double *pot) {
@@ -378,6 +438,7 @@ struct SplitP {
     }
     pot[i] = -((double)o.p.x + (double)o.p.y);
   }
+  __device__ static void finish(const Out &o, int i, const KParams &kp);
 };
 
 struct F64P {
@@ -451,6 +512,12 @@ struct F64P {
     y = y * __fma_rn(-hx * y, y, 1.5);
     return y;
   }
+  // ph4's nearest-neighbour key: the unsoftened r^2 summed in component
+  // order without contraction (idata.cc:200-205,214-218), so the argmin
+  // (first slot on equal keys) is ph4's nn bit for bit.
+  __device__ static __forceinline__ double nnkey(double dx, double dy, double dz) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  }
   template <bool CHECK, bool NN, bool HJ = false>
   __device__ static __forceinline__ void pair(const I &s, const Rec &r, double eps2, Part &q,
                                               double &nnmin, int selfrel) {
@@ -458,11 +525,10 @@ struct F64P {
     double dx, dy, dz;
     const double r2 = r2e(s, r, eps2, dx, dy, dz);
     double rinv = rsqrt64(r2);
-    if (CHECK) {
-      rinv = is_self ? 0.0 : rinv;
-      if (NN) nnmin = fmin(nnmin, is_self ? __longlong_as_double(0x7ff0000000000000ll) : r2);
-    } else if (NN) {
-      nnmin = fmin(nnmin, r2);
+    if (CHECK) rinv = is_self ? 0.0 : rinv;
+    if (NN) {
+      const double key = nnkey(dx, dy, dz);
+      nnmin = fmin(nnmin, is_self ? __longlong_as_double(0x7ff0000000000000ll) : key);
     }
     const double dvx = r.v.x - s.vx, dvy = r.v.y - s.vy, dvz = r.v.z - s.vz;
     const double rv = dx * dvx + dy * dvy + dz * dvz;
@@ -484,16 +550,22 @@ struct F64P {
     q.j[2] = fma(mr3i, fma(a3, dz, dvz), q.j[2]);
     q.p += mri;
   }
-  __device__ static __forceinline__ bool rescan(const I &s, const Rec &r, double eps2,
-                                                double best, int slot0, int self, int &idx) {
+  __device__ static __forceinline__ void rescan(const I &s, const Rec &r, double eps2,
+                                                double best, int slot0, int self, int &idx,
+                                                double &m2) {
+    (void)m2;  // the FP64 key is ph4's own: no gap to prove
     double dx, dy, dz;
-    if (r2e(s, r, eps2, dx, dy, dz) == best && slot0 != self) {
-      idx = slot0;
-      return true;
-    }
+    (void)r2e(s, r, eps2, dx, dy, dz);
+    if (idx < 0 && slot0 != self && nnkey(dx, dy, dz) == best) idx = slot0;
+  }
+  static constexpr bool JFOLD = false;
+  template <bool NN>
+  __host__ __device__ static constexpr bool tot_shared() {
     return false;
   }
-  __device__ static void to_out(const Tot &t, double nnr2, int nn, Out &o) {
+  __device__ static void fold_jerk(Tot &, Part &) {}
+  __device__ static void to_out(const Tot &t, double nnr2, double nnr2b, int nn, Out &o) {
+    (void)nnr2b;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       o.a[k] = t.a[k];
@@ -525,7 +597,19 @@ struct F64P {
     }
     pot[i] = -o.p;
   }
+  __device__ static void finish(const Out &o, int i, const KParams &kp);
 };
+
+// A partial record written by another CTA of this launch: read around L1.
+template <class O>
+__device__ __forceinline__ O load_out_cg(const O *p) {
+  O r;
+  const int *src = reinterpret_cast<const int *>(p);
+  int *dst = reinterpret_cast<int *>(&r);
+#pragma unroll
+  for (int w = 0; w < (int)(sizeof(O) / 4); w++) dst[w] = __ldcg(src + w);
+  return r;
+}
 
 // Shuffle helpers for Out (field by field).
 template <class O>
@@ -552,7 +636,172 @@ struct KParams {
   int *err;
   int want_nn;
   int hjerk;  // the hermite code's jerk form (JL = 1, no nn only)
+  // nearest-neighbour proof and refinement queue (split precision)
+  g6_jstate js;   // FP64 state: ph4-predicted positions of i and nn
+  double ti;      // prediction time of the records
+  void *refine;   // refinement buffer (NULL: none)
+  double kappa2;  // squared condition-number limit (0: no FP64 redo)
+  // bounded waits: limit per wait; stall (test hook) makes CTA (0, 0) wait
+  // for its first tile on a barrier that nothing arrives on
+  unsigned long long wait_ns;
+  int stall;
+  unsigned *xtick;  // per-i-group tickets for the in-kernel split merge (NULL: second pass)
 };
+
+// ------------------------------------------------ nearest neighbour proof ---
+//
+// ph4's nearest neighbour (idata.cc:200-226) is the j with the smallest FP64
+// r^2 = (dx^2 + dy^2) + dz^2 of the ph4-predicted positions, the first j on
+// equal values.  The split kernel ranks j by the FP32 key k = r^2 + eps^2
+// of the double-single records.  Bound (the argument of kern_knn.cu, with
+// the softening added first in the FMA chain): with X >= |coordinate| of i
+// and of every j within distance sqrt(D) of i, E = 2^-30 X and e the FP32
+// softening, any j with ph4 r^2 <= D has
+//     k <= Tk(D) = (1 + 2^-16)(D + e) + 4 E sqrt(D) + 4 E^2.
+// So if the second smallest key m2 exceeds Tk(D_f), D_f the FP64 r^2 of the
+// FP32 argmin j_f, every other j has ph4 r^2 > D_f and j_f is ph4's nearest
+// neighbour.  X = max |x_i| + sqrt(D_f) covers every j that could beat it.
+// Otherwise (near-equal keys, e.g. distance ties) the i-particle is queued
+// and refine_kernel ranks every j with k <= Tk(D_f) in FP64.
+//
+// ---------------------------------------------- condition-number refinement
+//
+// The FP32 pair terms carry a few ulps each, so the relative error of the
+// acceleration grows with the condition number of its sum,
+// kappa = sum m / (r^2 + eps^2) / |a| (about 1e-8 kappa at N = 2^20; the
+// particles near the centre of a cluster, where the pulls cancel, reach
+// kappa ~ 100-300).  i-particles with kappa above the caller's limit are
+// queued too, and refine_kernel recomputes their acceleration and potential
+// in FP64 from the same records (double-single positions exact in FP64); the
+// jerk keeps its split value.
+//
+// Refinement buffer (g6k_refine_bytes, zeroed once): a header, the queue
+// (i, reason, key bound), per-entry tickets, per-(entry, chunk) partial
+// records, and the force kernel's per-i-group tickets for its in-kernel
+// split merge.  refine_kernel leaves the header's count at zero.
+constexpr int RCAP = 16384;    // queue entries
+constexpr int RPCAP = 32768;   // partial records (entries x chunks)
+constexpr int RCHMAX = 64;     // j-chunks per entry at most
+constexpr int RNT = 256;       // refine_kernel threads per CTA
+constexpr int XTMAX = 8192;    // i-groups (grid.x) whose split merge runs in the force kernel
+enum { REF_ACC = 1, REF_NN = 2 };
+
+struct RefHdr {
+  unsigned count;     // entries queued by this call (reset by refine_kernel)
+  unsigned done;      // refine_kernel CTAs finished
+  unsigned overflow;  // largest count that exceeded RCAP (sticky until read)
+  unsigned last;      // count of the last refinement
+  unsigned last_acc;  // of which queued for the condition number
+  unsigned nacc;      // REF_ACC entries queued by this call
+  unsigned pad[2];
+};
+struct RefPart {  // one j-chunk of one entry, FP64
+  double a[3], p, r2;
+  int slot, pad;
+};
+struct RefBuf {
+  RefHdr h;
+  int list[RCAP];
+  int mode[RCAP];
+  float thr[RCAP];
+  unsigned ticket[RCAP];
+  RefPart part[RPCAP];
+  unsigned xtick[XTMAX];  // force kernel: CTAs of an i-group done (reset by the last)
+};
+
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+
+// FP64 position of j slot s predicted to ti with ph4's expression.
+__device__ __forceinline__ void jpos64(const g6_jstate &js, double ti, int s, double x[3]) {
+  const int cap = js.cap;
+  const double dt = dsub(ti, js.t[s]);
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    x[k] = g6_predict_x(js.x[k * cap + s], js.v[k * cap + s], js.a[k * cap + s],
+                        js.j[k * cap + s], dt);
+}
+// FP64 position of i-particle i as ph4 holds it: the caller's point, or the
+// listed slot predicted to ti.
+__device__ __forceinline__ void ipos64(const KParams &kp, int i, double x[3]) {
+  if (kp.ilist) {
+    jpos64(kp.js, kp.ti, kp.ilist[i], x);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; k++) x[k] = kp.ipos[3 * i + k];
+  }
+}
+// ph4's r^2 of j relative to i (dx = x_j - x_i), component order, no FMA.
+__device__ __forceinline__ double ph4_r2(const double xi[3], const double xj[3]) {
+  const double d0 = dsub(xj[0], xi[0]), d1 = dsub(xj[1], xi[1]), d2 = dsub(xj[2], xi[2]);
+  return __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+}
+// Tk(D) of the header, rounded up to FP32.
+__device__ __forceinline__ float nn_bound(double D, double e, const double xi[3]) {
+  const double sD = sqrt(D);
+  const double X = fmax(fabs(xi[0]), fmax(fabs(xi[1]), fabs(xi[2]))) + sD * (1.0 + 1.0 / 1048576.0);
+  const double E = X * (1.0 + 1.0 / 1048576.0) * (1.0 / 1073741824.0);
+  const double T = (1.0 + 1.0 / 65536.0) * (D + e) + 4.0 * E * sD + 4.0 * E * E;
+  return __double2float_ru(T);
+}
+// The FP32 softening of the split key (SplitP::eps), as a double.
+__device__ __forceinline__ double split_eps(double eps2) {
+  return (double)((float)eps2 + (float)(1.0 / 4503599627370496.0));
+}
+
+__device__ __forceinline__ void ref_enqueue(void *buf, int i, int mode, float thr) {
+  RefBuf *b = reinterpret_cast<RefBuf *>(buf);
+  const unsigned e = atomicAdd(&b->h.count, 1u);
+  if (mode & REF_ACC) atomicAdd(&b->h.nacc, 1u);
+  if (e < (unsigned)RCAP) {
+    b->list[e] = i;
+    b->mode[e] = mode;
+    b->thr[e] = thr;
+  }
+}
+
+__device__ __noinline__ void SplitP::finish(const Out &o, int i, const KParams &kp) {
+  write_final(o, i, kp.acc, kp.jerk, kp.pot);
+  int mode = 0;
+  float thr = 0.f;
+  if (kp.refine && kp.kappa2 > 0.0) {
+    double a2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double a = (double)o.a[k].x + (double)o.a[k].y;
+      a2 += a * a;
+    }
+    const double s1 = (double)o.s1;
+    if (s1 * s1 > kp.kappa2 * a2) mode |= REF_ACC;
+  }
+  const int nn = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
+  if (kp.want_nn) {
+    float r2out = __int_as_float(0x7f800000);
+    if (nn >= 0) {
+      double xi[3], xj[3];
+      ipos64(kp, i, xi);
+      jpos64(kp.js, kp.ti, nn, xj);
+      const double D = ph4_r2(xi, xj);
+      r2out = (float)D;
+      const float T = nn_bound(D, split_eps(kp.eps2), xi);
+      if (kp.refine && !(o.nnr2b > T)) {
+        mode |= REF_NN;
+        thr = T;
+      }
+    }
+    if (kp.nn) kp.nn[i] = nn;
+    if (kp.nn_r2) kp.nn_r2[i] = r2out;
+  } else if (kp.nn) {
+    kp.nn[i] = -1;
+  }
+  if (mode) ref_enqueue(kp.refine, i, mode, thr);
+}
+
+__device__ __noinline__ void F64P::finish(const Out &o, int i, const KParams &kp) {
+  write_final(o, i, kp.acc, kp.jerk, kp.pot);
+  const int nn = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
+  if (kp.nn) kp.nn[i] = kp.want_nn ? nn : -1;
+  if (kp.nn_r2) kp.nn_r2[i] = nn >= 0 ? (float)o.nnr2 : __int_as_float(0x7f800000);
+}
 
 // Number of j per thread between compensated folds.
 constexpr int FOLD_J = 64;
@@ -569,10 +818,12 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   constexpr int ISLOTS = NIL * IPT;      // i-particles per CTA
   constexpr int JPT = RPT / JL;          // records per thread per tile
   constexpr int FOLD_TILES = (FOLD_J / (JPT * JPR)) > 0 ? (FOLD_J / (JPT * JPR)) : 1;
+  constexpr int JCHUNK = JPT < G6_JCHUNK ? JPT : G6_JCHUNK;  // records per jerk fold (split)
   static_assert(JL >= 1 && JL <= JLMAX && JL <= RPT && (RPT % JL) == 0, "JL");
 
   __shared__ __align__(128) Rec tiles[NSTAGE][RPT];
   __shared__ __align__(8) uint64_t full[NSTAGE];
+  __shared__ __align__(8) uint64_t never;  // test hook: no arrival ever
   __shared__ int released[NSTAGE];
   __shared__ int issued_s;
   __shared__ volatile int abort_s;
@@ -616,6 +867,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
       mbar_init(&full[s], 1);
       released[s] = 0;
     }
+    mbar_init(&never, 1);
     issued_s = ntiles < NSTAGE ? ntiles : NSTAGE;
     abort_s = 0;
     fence_barrier_init();
@@ -630,14 +882,26 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
 
   const auto eps2 = P::eps(kp.eps2);  // eps^2 + 2^-52 (ph4)
   typename P::Part q[IPT];
-  typename P::Tot T[IPT];
-  R nnmin[IPT], nnbest[IPT];
+  // Compensated totals: in shared memory for the split nearest-neighbour
+  // variant (touched once per fold; it frees registers for the pair loop),
+  // in registers otherwise.  Layout [k][thread]: 15-word records,
+  // conflict-free.
+  constexpr bool TSH = P::template tot_shared<NN>();
+  __shared__ typename P::Tot tot_sh[TSH ? IPT * NT : 1];
+  typename P::Tot tot_reg[TSH ? 1 : IPT];
+  auto T = [&](int k) -> typename P::Tot & {
+    if constexpr (TSH)
+      return tot_sh[k * NT + threadIdx.x];
+    else
+      return tot_reg[k];
+  };
+  R nnmin[IPT], nnbest[IPT], nnm2[IPT];
   int nnidx[IPT], besttile[IPT];
 #pragma unroll
   for (int k = 0; k < IPT; k++) {
     P::zero(q[k]);
-    P::zero(T[k]);
-    nnmin[k] = nnbest[k] = (R)__int_as_float(0x7f800000);
+    P::zero(T(k));
+    nnmin[k] = nnbest[k] = nnm2[k] = (R)__int_as_float(0x7f800000);
     nnidx[k] = -1;
     besttile[k] = -1;
   }
@@ -650,7 +914,9 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   bool failed = false;
   for (int t = 0; t < ntiles; t++) {
     const int s = t % NSTAGE;
-    const bool ok = mbar_wait_abortable(&full[s], (t / NSTAGE) & 1, &abort_s);
+    const bool stall = kp.stall && t == 0 && blockIdx.x == 0 && blockIdx.y == 0;
+    const bool ok = stall ? mbar_wait_abortable(&never, 0, &abort_s, kp.wait_ns)
+                          : mbar_wait_abortable(&full[s], (t / NSTAGE) & 1, &abort_s, kp.wait_ns);
     if (!__all_sync(0xffffffffu, ok)) {
       failed = true;
       if (lane == 0) abort_s = 1;
@@ -665,13 +931,22 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
     for (int k = 0; k < IPT; k++) mine |= (unsigned)(self[k] - tj0) < (unsigned)TJ;
     const bool slow = __any_sync(0xffffffffu, mine);
 
+    // JCHUNK records between jerk folds (split: the jerk partials are
+    // folded more often than the rest; the last chunk folds with the tile).
     if (!slow) {
+#pragma unroll 1
+      for (int ub = 0; ub < JPT; ub += JCHUNK) {
 #pragma unroll UNROLL
-      for (int u = 0; u < JPT; u++) {
-        const Rec r = tile[jl + JL * u];
+        for (int u = ub; u < ub + JCHUNK; u++) {
+          const Rec r = tile[jl + JL * u];
 #pragma unroll
-        for (int k = 0; k < IPT; k++)
-          P::template pair<false, NN, HJ>(I[k], r, eps2, q[k], nnmin[k], 0);
+          for (int k = 0; k < IPT; k++)
+            P::template pair<false, NN, HJ>(I[k], r, eps2, q[k], nnmin[k], 0);
+        }
+        if (P::JFOLD && ub + JCHUNK < JPT) {
+#pragma unroll
+          for (int k = 0; k < IPT; k++) P::fold_jerk(T(k), q[k]);
+        }
       }
     } else {
       for (int u = 0; u < JPT; u++) {
@@ -681,24 +956,33 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
         for (int k = 0; k < IPT; k++)
           P::template pair<true, NN, HJ>(I[k], r, eps2, q[k], nnmin[k],
                                          self[k] - (tj0 + JPR * jj));
+        if (P::JFOLD && (u + 1) % JCHUNK == 0 && u + 1 < JPT) {
+#pragma unroll
+          for (int k = 0; k < IPT; k++) P::fold_jerk(T(k), q[k]);
+        }
       }
     }
 
-    // Nearest neighbour: remember the tile in which the running min last
-    // improved (strict <, so the earliest tile wins ties); its index within
-    // the tile is recovered once, after the loop.
+    // Nearest neighbour: nnmin holds this tile's smallest key.  Keep the
+    // smallest over the tiles (nnbest) and the tile where it occurs (strict
+    // <, so the earliest tile wins ties; the index within the tile is
+    // recovered once, after the loop), and fold the larger of the tile's
+    // and the running minimum into the second smallest key (nnm2).
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
       if (!NN) break;
-      const bool imp = nnmin[k] < nnbest[k];
-      nnbest[k] = imp ? nnmin[k] : nnbest[k];
+      const R tmin = nnmin[k];
+      nnm2[k] = fmin(nnm2[k], fmax(tmin, nnbest[k]));
+      const bool imp = tmin < nnbest[k];
+      nnbest[k] = imp ? tmin : nnbest[k];
       besttile[k] = imp ? t : besttile[k];
+      nnmin[k] = (R)__int_as_float(0x7f800000);
     }
 
     if ((t + 1) % FOLD_TILES == 0) {
 #pragma unroll
       for (int k = 0; k < IPT; k++) {
-        P::fold(T[k], q[k]);
+        P::fold(T(k), q[k]);
         P::zero(q[k]);
       }
     }
@@ -723,7 +1007,13 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
       atomicOr(kp.err, ERR_TMA_TIMEOUT);
       const int hi = issued_s;
       for (int u = hi - NSTAGE > 0 ? hi - NSTAGE : 0; u < hi; u++)
-        (void)mbar_wait_bounded(&full[u % NSTAGE], (u / NSTAGE) & 1);
+        (void)mbar_wait_bounded(&full[u % NSTAGE], (u / NSTAGE) & 1, kp.wait_ns);
+      // Still count this CTA in its i-group, so that the group's ticket
+      // returns to zero for the next launch (the results are void: the
+      // error word is set).
+      if (kp.nsplit > 1 && kp.xtick &&
+          atomicAdd(&kp.xtick[blockIdx.x], 1u) == (unsigned)(kp.nsplit - 1))
+        kp.xtick[blockIdx.x] = 0u;
     }
     return;
   }
@@ -736,10 +1026,9 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
     if (!NN || besttile[k] < 0) continue;
     const Rec *g = gj + besttile[k] * RPT;
     const int tj0 = js + besttile[k] * TJ;
-    bool found = false;
-    for (int u = 0; u < JPT && !found; u++) {
+    for (int u = 0; u < JPT; u++) {
       const int jj = jl + JL * u;
-      found = P::rescan(I[k], g[jj], eps2, nnbest[k], tj0 + JPR * jj, self[k], nnidx[k]);
+      P::rescan(I[k], g[jj], eps2, nnbest[k], tj0 + JPR * jj, self[k], nnidx[k], nnm2[k]);
     }
   }
 
@@ -747,8 +1036,8 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   typename P::Out o[IPT];
 #pragma unroll
   for (int k = 0; k < IPT; k++) {
-    P::fold(T[k], q[k]);
-    P::to_out(T[k], nnbest[k], nnidx[k], o[k]);
+    P::fold(T(k), q[k]);
+    P::to_out(T(k), nnbest[k], nnm2[k], nnidx[k], o[k]);
   }
   if (JL > 1) {
 #pragma unroll
@@ -788,19 +1077,56 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
       }
     }
   }
-  if (jl != 0) return;
+  if (jl == 0) {
 #pragma unroll
-  for (int k = 0; k < IPT; k++) {
-    if (!valid[k]) continue;
-    const int i = blockIdx.x * ISLOTS + k * NIL + il;
-    if (kp.nsplit == 1) {
-      P::write_final(o[k], i, kp.acc, kp.jerk, kp.pot);
-      if (kp.nn) kp.nn[i] = (o[k].nn >= 0 && o[k].nn < kp.nj) ? o[k].nn : -1;
-      if (kp.nn_r2) kp.nn_r2[i] = (float)o[k].nnr2;
-    } else {
-      reinterpret_cast<typename P::Out *>(kp.part)[(size_t)blockIdx.y * kp.ni_pad + i] = o[k];
+    for (int k = 0; k < IPT; k++) {
+      if (!valid[k]) continue;
+      const int i = blockIdx.x * ISLOTS + k * NIL + il;
+      if (kp.nsplit == 1) {
+        P::finish(o[k], i, kp);
+      } else {
+        reinterpret_cast<typename P::Out *>(kp.part)[(size_t)blockIdx.y * kp.ni_pad + i] = o[k];
+      }
     }
   }
+  if (kp.nsplit == 1 || !kp.xtick) return;
+
+  // ---- split merge in the last CTA of the i-group (no second launch): the
+  // CTA whose ticket completes the group merges the nsplit partial records
+  // of each of the group's i, a warp per i, lane l taking splits l, l+32, ...
+  // in order and the lanes merging in a fixed shuffle-down tree (as
+  // reduce_warp_kernel).  The ticket is reset for the next launch. ----
+  __shared__ int last_s;
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) last_s = atomicAdd(&kp.xtick[blockIdx.x], 1u) == (unsigned)(kp.nsplit - 1);
+  __syncthreads();
+  if (!last_s) return;
+  __threadfence();
+  using Out = typename P::Out;
+  const Out *part = reinterpret_cast<const Out *>(kp.part);
+  const int warp = tid >> 5;
+  const int i0 = blockIdx.x * ISLOTS;
+  for (int qq = warp; qq < ISLOTS; qq += NWARP) {
+    const int i = i0 + qq;
+    if (i >= kp.ni) break;
+    Out m = load_out_cg(part + (size_t)(lane < kp.nsplit ? lane : 0) * kp.ni_pad + i);
+    for (int sp = lane + 32; sp < kp.nsplit; sp += 32)
+      P::merge(m, load_out_cg(part + (size_t)sp * kp.ni_pad + i));
+    const int have = kp.nsplit < 32 ? kp.nsplit : 32;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      Out b;
+      const int *src = reinterpret_cast<const int *>(&m);
+      int *dst = reinterpret_cast<int *>(&b);
+#pragma unroll
+      for (int w = 0; w < (int)(sizeof(Out) / 4); w++)
+        dst[w] = __shfl_down_sync(0xffffffffu, src[w], off);
+      if (lane < off && lane + off < have) P::merge(m, b);
+    }
+    if (lane == 0) P::finish(m, i, kp);
+  }
+  if (tid == 0) kp.xtick[blockIdx.x] = 0u;
 }
 
 // Second pass: merge the nsplit partial records of each i in split order
@@ -812,9 +1138,7 @@ __global__ void reduce_kernel(KParams kp) {
   const typename P::Out *part = reinterpret_cast<const typename P::Out *>(kp.part);
   typename P::Out o = part[i];
   for (int s = 1; s < kp.nsplit; s++) P::merge(o, part[(size_t)s * kp.ni_pad + i]);
-  P::write_final(o, i, kp.acc, kp.jerk, kp.pot);
-  if (kp.nn) kp.nn[i] = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
-  if (kp.nn_r2) kp.nn_r2[i] = (float)o.nnr2;
+  P::finish(o, i, kp);
 }
 
 // The same merge with one warp per i, for small blocks, where the splits are
@@ -840,10 +1164,192 @@ __global__ void reduce_warp_kernel(KParams kp) {
       dst[w] = __shfl_down_sync(0xffffffffu, src[w], off);
     if (lane < off && lane + off < have) P::merge(o, b);
   }
-  if (lane == 0) {
-    P::write_final(o, i, kp.acc, kp.jerk, kp.pot);
-    if (kp.nn) kp.nn[i] = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
-    if (kp.nn_r2) kp.nn_r2[i] = (float)o.nnr2;
+  if (lane == 0) P::finish(o, i, kp);
+}
+
+// FP64 redo of the queued i-particles (see "nearest neighbour proof" and
+// "condition-number refinement" above).  A persistent grid walks the
+// (entry, j-chunk) units; each CTA reduces its unit in a fixed order and the
+// CTA that completes an entry's last chunk (atomic ticket) merges the chunks
+// in chunk order and overwrites that particle's results.  The chunk count
+// depends only on the number of queued entries, so results are
+// deterministic.  The last CTA to finish resets the queue.
+//
+// 1/sqrt(x): FP32 MUFU seed (relative error < 2^-22) and one Newton step,
+// relative error < 2^-42, far below the 1e-6 the pass is for.
+__device__ __forceinline__ double refine_rsqrt(double x) {
+  double y = (double)rsqrt_approx((float)x);
+  return y * __fma_rn(-0.5 * x * y, y, 1.5);
+}
+
+__global__ void __launch_bounds__(RNT) refine_kernel(KParams kp) {
+  RefBuf *b = reinterpret_cast<RefBuf *>(kp.refine);
+  __shared__ unsigned s_cnt;
+  __shared__ double s_sum[RNT / 32][5];
+  __shared__ int s_slot[RNT / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_cnt = *reinterpret_cast<volatile unsigned *>(&b->h.count);
+  __syncthreads();
+  const unsigned cnt = s_cnt;
+  const int ne = cnt > (unsigned)RCAP ? 0 : (int)cnt;
+  if (cnt > (unsigned)RCAP && blockIdx.x == 0 && tid == 0) atomicMax(&b->h.overflow, cnt);
+  int nch = 1;
+  if (ne > 0) {
+    nch = (4 * (int)gridDim.x + ne - 1) / ne;
+    nch = min(nch, RCHMAX);
+    nch = min(nch, RPCAP / ne);
+    nch = min(nch, max(1, kp.nj / 1024));
+    nch = max(nch, 1);
+  }
+  const int units = ne * nch;
+  const double eps2 = kp.eps2 + 1.0 / 4503599627370496.0;  // ph4's + 2^-52
+  const float e32 = (float)split_eps(kp.eps2);
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
+  const void *rec = kp.jrec;
+  for (int u = blockIdx.x; u < units; u += gridDim.x) {
+    const int e = u / nch, c = u - e * nch;
+    const int i = b->list[e];
+    const int mode = b->mode[e];
+    const float thr = b->thr[e];
+    const int j0 = (int)((long long)kp.nj * c / nch);
+    const int j1 = (int)((long long)kp.nj * (c + 1) / nch);
+    // The i-particle in the split kernel's own representation (double-single
+    // position), so that an i and a j copy of it at the same place give
+    // dx = 0 exactly, as there.
+    int self;
+    double xi[3], xi64[3];
+    float ih[3], il[3];
+    if (kp.ilist) {
+      const int slot = kp.ilist[i];
+      self = kp.iself ? kp.iself[i] : slot;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        ih[k] = g6_split_get(rec, slot, k);
+        il[k] = g6_split_get(rec, slot, 4 + k);
+      }
+    } else {
+      self = kp.iself ? kp.iself[i] : -1;
+#pragma unroll
+      for (int k = 0; k < 3; k++) SplitP::split(kp.ipos[3 * i + k], ih[k], il[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) xi[k] = (double)ih[k] + (double)il[k];
+    if (mode & REF_NN) ipos64(kp, i, xi64);
+    double sa[3] = {0.0, 0.0, 0.0}, sp = 0.0;
+    double br2 = inf;
+    int bslot = -1;
+    for (int j = j0 + tid; j < j1; j += RNT) {
+      if (j == self) continue;
+      if (mode & REF_ACC) {  // acceleration and potential; the jerk stays
+        double dx[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+          dx[k] = ((double)g6_split_get(rec, j, k) + (double)g6_split_get(rec, j, 4 + k)) - xi[k];
+        const double m = (double)g6_split_get(rec, j, 3);
+        const double r2 = __fma_rn(dx[2], dx[2], __fma_rn(dx[1], dx[1], __fma_rn(dx[0], dx[0], eps2)));
+        const double rinv = refine_rsqrt(r2);
+        const double mri = m * rinv;
+        const double mr3i = mri * (rinv * rinv);
+#pragma unroll
+        for (int k = 0; k < 3; k++) sa[k] = __fma_rn(mr3i, dx[k], sa[k]);
+        sp += mri;
+      }
+      if (mode & REF_NN) {
+        float d[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+          d[k] = __fadd_rn(__fsub_rn(g6_split_get(rec, j, k), ih[k]),
+                           __fsub_rn(g6_split_get(rec, j, 4 + k), il[k]));
+        const float key = __fmaf_rn(d[2], d[2], __fmaf_rn(d[1], d[1], __fmaf_rn(d[0], d[0], e32)));
+        if (key <= thr) {
+          double xj[3];
+          jpos64(kp.js, kp.ti, j, xj);
+          const double r2 = ph4_r2(xi64, xj);
+          if (r2 < br2 || (r2 == br2 && j < bslot)) {
+            br2 = r2;
+            bslot = j;
+          }
+        }
+      }
+    }
+    // fixed-order reduction: shuffle-down tree, then warps in order
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) sa[k] += __shfl_down_sync(0xffffffffu, sa[k], off);
+      sp += __shfl_down_sync(0xffffffffu, sp, off);
+      const double or2 = __shfl_down_sync(0xffffffffu, br2, off);
+      const int os = __shfl_down_sync(0xffffffffu, bslot, off);
+      if (or2 < br2 || (or2 == br2 && os >= 0 && (bslot < 0 || os < bslot))) {
+        br2 = or2;
+        bslot = os;
+      }
+    }
+    if (lane == 0) {
+      for (int k = 0; k < 3; k++) s_sum[warp][k] = sa[k];
+      s_sum[warp][3] = sp;
+      s_sum[warp][4] = br2;
+      s_slot[warp] = bslot;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      RefPart q;
+      for (int k = 0; k < 3; k++) q.a[k] = 0.0;
+      q.p = 0.0;
+      q.r2 = inf;
+      q.slot = -1;
+      q.pad = 0;
+      for (int w = 0; w < RNT / 32; w++) {
+        for (int k = 0; k < 3; k++) q.a[k] += s_sum[w][k];
+        q.p += s_sum[w][3];
+        if (s_slot[w] >= 0 && (s_sum[w][4] < q.r2 || (s_sum[w][4] == q.r2 && s_slot[w] < q.slot))) {
+          q.r2 = s_sum[w][4];
+          q.slot = s_slot[w];
+        }
+      }
+      b->part[e * nch + c] = q;
+      __threadfence();
+      const unsigned t = atomicAdd(&b->ticket[e], 1u);
+      if (t == (unsigned)(nch - 1)) {
+        __threadfence();
+        const volatile RefPart *vp = b->part + (size_t)e * nch;
+        double fa[3] = {0.0, 0.0, 0.0}, fp = 0.0, fr2 = inf;
+        int fs = -1;
+        for (int cc = 0; cc < nch; cc++) {
+          for (int k = 0; k < 3; k++) fa[k] += vp[cc].a[k];
+          fp += vp[cc].p;
+          const int sl = vp[cc].slot;
+          const double r2 = vp[cc].r2;
+          if (sl >= 0 && (r2 < fr2 || (r2 == fr2 && sl < fs))) {
+            fr2 = r2;
+            fs = sl;
+          }
+        }
+        if (mode & REF_ACC) {
+          for (int k = 0; k < 3; k++) kp.acc[3 * i + k] = fa[k];
+          kp.pot[i] = -fp;
+        }
+        if ((mode & REF_NN) && fs >= 0) {
+          if (kp.nn) kp.nn[i] = fs;
+          if (kp.nn_r2) kp.nn_r2[i] = (float)fr2;
+        }
+        b->ticket[e] = 0u;
+      }
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    const unsigned d = atomicAdd(&b->h.done, 1u);
+    if (d == gridDim.x - 1) {
+      b->h.last = cnt;
+      b->h.last_acc = b->h.nacc;
+      b->h.count = 0u;
+      b->h.nacc = 0u;
+      b->h.done = 0u;
+      __threadfence();
+    }
   }
 }
 
@@ -993,18 +1499,39 @@ int launch(const KParams &kp, int jl, int gx, cudaStream_t st) {
     default:
       return -2;
   }
-  if (kp.nsplit > 1) {
+  if (kp.nsplit > 1 && !kp.xtick) {
     if (kp.ni < 4096)
       reduce_warp_kernel<P><<<(kp.ni + 3) / 4, 128, 0, st>>>(kp);
     else
       reduce_kernel<P><<<(kp.ni + 127) / 128, 128, 0, st>>>(kp);
   }
+  if (kp.refine) refine_kernel<<<2 * sm_count(), RNT, 0, st>>>(kp);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
 }  // namespace
 
 extern "C" int g6k_sm_count(void) { return sm_count(); }
+
+extern "C" size_t g6k_refine_bytes(void) { return sizeof(RefBuf); }
+
+extern "C" int g6k_refine_read(const void *refine, int out[3], cudaStream_t st) {
+  RefHdr h;
+  if (cudaMemcpyAsync(&h, refine, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return -3;
+  out[0] = (int)h.last;
+  out[1] = (int)h.last_acc;
+  out[2] = (int)h.overflow;
+  if (h.overflow) {
+    const unsigned zero = 0;
+    cudaMemcpyAsync(reinterpret_cast<char *>(const_cast<void *>(refine)) +
+                        offsetof(RefHdr, overflow),
+                    &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
+    cudaStreamSynchronize(st);
+  }
+  return 0;
+}
 
 extern "C" size_t g6k_scratch_bytes(int ni, int nj, int prec, int force_jl, int force_nsplit) {
   int jl, nsplit, jsplit;
@@ -1043,6 +1570,16 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
   kp.err = a->err;
   kp.want_nn = a->want_nn;
   kp.hjerk = a->hjerk;
+  kp.js = *a->js;
+  kp.ti = a->ti;
+  // The refinement pass serves the split kernel's g6 results; the hermite
+  // jerk form and callers passing kappa < 0 (the fixed-step path) keep plain
+  // split arithmetic.
+  kp.refine =
+      (a->prec == G6_PREC_SPLIT && !a->hjerk && a->kappa >= 0.0) ? a->refine : nullptr;
+  kp.kappa2 = a->kappa > 0.0 ? a->kappa * a->kappa : 0.0;
+  kp.stall = a->stall_test;
+  kp.wait_ns = a->stall_test ? STALL_TEST_NS : WAIT_NS;
   const size_t need = nsplit > 1 ? g6k_scratch_bytes(a->ni, a->nj, a->prec, jl, nsplit) : 0;
   if (need > a->scratch_bytes) return -4;
   const int islots = (NT / jl) * (a->prec == G6_PREC_FP64 ? IPT_F64 : IPT_SPLIT);
@@ -1054,6 +1591,9 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
     shape->grid_y = nsplit;
     shape->threads = NT;
   }
+  kp.xtick = (a->refine && nsplit > 1 && gx <= XTMAX)
+                 ? reinterpret_cast<RefBuf *>(a->refine)->xtick
+                 : nullptr;
   if (a->prec == G6_PREC_FP64) {
     kp.jrec = a->js->jp_f64;
     return launch<F64P>(kp, jl, gx, st);
@@ -1068,37 +1608,40 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
 // The split-j partial sums normally live in a buffer that the host library
 // grows with cudaMalloc on demand.  g6k_force_static instead places them in
 // this file-scope array, which every GPU that loads the library holds (16 MiB)
-// until the process exits.  Its device address is looked up once per device,
-// on the first call made with that device current.  Every call shares the
-// array: nothing in it has to start at zero (each partial record is written
-// by exactly one CTA before the second pass reads it), and calls that overlap
-// on the GPU (different streams, or host threads) race on it.
+// until the process exits.  Host code cannot use the array's name as a device
+// address: g6k_static_scratch_addr looks the address up (cudaGetSymbolAddress)
+// with the caller's device current; the host library does that once in
+// g6_open and keeps it in its context until g6_close (a device reset needs
+// g6_close + g6_open).  The lookup also loads this module, so the array is
+// taken at g6_open, not at the first call.  Every call shares the array:
+// nothing in it has to start at zero (each partial record is written by
+// exactly one CTA before it is read), and calls that overlap on the GPU
+// (different streams, or host threads) race on it.
 #define G6_STATIC_SCRATCH_BYTES (16u << 20)
 static __device__ __align__(256) unsigned char g6_static_scratch[G6_STATIC_SCRATCH_BYTES];
 
 extern "C" size_t g6k_static_scratch_capacity(void) { return G6_STATIC_SCRATCH_BYTES; }
 
+// 0 and the array's device address on the current device, or -5.
+extern "C" int g6k_static_scratch_addr(void **out) {
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g6_static_scratch) != cudaSuccess || p == nullptr) return -5;
+  *out = p;
+  return 0;
+}
+
 // Returns 0, -1/-2/-3 as g6k_force, -4 when the launch shape needs more than
-// G6_STATIC_SCRATCH_BYTES of scratch (*need_out tells how much), -5 when the
-// array's device address cannot be obtained.
-extern "C" int g6k_force_static(const g6_force_args *a, g6_shape *shape, cudaStream_t st,
-                                size_t *need_out) {
-  static void *addr[64];
-  static int have[64];
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -5;
-  if (!have[dev]) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g6_static_scratch) != cudaSuccess || p == nullptr) return -5;
-    addr[dev] = p;
-    have[dev] = 1;
-  }
+// G6_STATIC_SCRATCH_BYTES of scratch (*need_out tells how much), -5 without
+// the array's address (static_addr from g6k_static_scratch_addr).
+extern "C" int g6k_force_static(const g6_force_args *a, void *static_addr, g6_shape *shape,
+                                cudaStream_t st, size_t *need_out) {
+  if (!static_addr) return -5;
   const size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->hjerk ? 1 : a->force_jl,
                                         a->force_nsplit);
   if (need_out) *need_out = need;
   if (need > G6_STATIC_SCRATCH_BYTES) return -4;
   g6_force_args b = *a;
-  b.scratch = addr[dev];
+  b.scratch = static_addr;
   b.scratch_bytes = G6_STATIC_SCRATCH_BYTES;
   return g6k_force(&b, shape, st);
 }

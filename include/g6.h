@@ -121,6 +121,27 @@ int g6_get_neighbour_list(int cluster_id, int ipipe, int maxlength, int *n_neigh
 /* Precision of subsequent force evaluations. */
 int g6x_set_precision(int prec);
 int g6x_get_precision(void);
+/* Split precision: every force call ends with a refinement pass.
+   - Nearest neighbour: the FP32 argmin is kept only where a proven FP32
+     error bound separates it from every other j; otherwise the candidates
+     within the bound are ranked by ph4's FP64 r^2 (first slot on equal
+     values), so nn is ph4's nearest neighbour.
+   - Condition number: i-particles whose kappa = sum m/(r^2+eps^2) / |acc|
+     exceeds the limit (default 48, env G6_KAPPA; 0 disables) get acc and
+     pot recomputed in FP64 from the same records (the jerk keeps its split
+     value).
+   g6x_refine_stats reports the last call's queue: out = {particles queued,
+   of which for kappa, largest queue that overflowed the 16384 entries since
+   the last read (then nothing was refined in that call)}. */
+int g6x_set_refine(double kappa);
+int g6x_refine_stats(int out[3]);
+/* Test hook for the force kernel's bounded waits: with on != 0, the next
+   force call's first CTA waits for its first j-tile on a barrier that
+   nothing arrives on, with a 20 ms limit instead of 2 s.  The wait expires,
+   the CTA raises its abort flag, drains the copies it issued and sets the
+   error word, so that call returns G6_ERR_KERNEL (no trap, no unbounded
+   spin); the hook then clears itself and later calls run normally. */
+int g6x_test_wait_expiry(int on);
 /* Change the i-chunk bound reported by g6_npipes (1 .. 1<<20). */
 int g6x_set_npipes(int npipes);
 /* Last error message ("" if none). */
@@ -138,8 +159,8 @@ int g6x_read(int n, double (*x)[3], double (*v)[3], double (*acc)[3], double (*j
 
 /* Blocking force on ni explicit i-particles (host arrays) against slots
    [0, nj) predicted to ti.  self_slot[i] (or NULL) is the slot to exclude;
-   nn[i] is a j SLOT (-1 none); nn_r2[i] = r^2 + eps2 of it (FP32); either
-   may be NULL.  Any ni (no npipes bound). */
+   nn[i] is a j SLOT (-1 none); nn_r2[i] = its squared distance r^2 (FP64
+   value rounded to FP32); either may be NULL.  Any ni (no npipes bound). */
 int g6x_force(double ti, double eps2, int nj, int ni, const double (*xi)[3],
               const double (*vi)[3], const int *self_slot, double (*acc)[3],
               double (*jerk)[3], double *pot, int *nn, float *nn_r2);
@@ -153,8 +174,9 @@ int g6x_force_dev(double ti, double eps2, int nj, int ni, const double *d_xi,
    may not allocate during the call -- device memory owned and budgeted by a
    host framework, or step loops that cannot absorb cudaMalloc's implicit
    synchronisation.  The split-j partial sums use a fixed 16 MiB array that
-   every GPU loading the library holds until exit; the first call on a device
-   looks up that array's address (do it before any stream capture).  A call
+   every GPU loading the library holds until exit; g6_open takes it and looks
+   up its device address (after a device reset, g6_close and g6_open again),
+   and allocates the fixed refinement queue the call also uses.  A call
    whose launch shape needs more scratch, or whose nj exceeds the j-store
    already allocated, or with more staged j updates than the update buffer
    holds, returns G6_ERR_ARG instead of allocating.  All calls share the

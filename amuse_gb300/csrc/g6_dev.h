@@ -140,13 +140,17 @@ int g6k_enc_check(const g6_jstate *js, const double *rad, int ni, const int *ili
  * state, stop bits into enc->stopped and *flag.                              */
 int g6k_enc_decide(const g6_jstate *js, g6_enc *enc, int mode, double tnext, int *flag,
                     cudaStream_t st);
-/* Block scheduler: tnext = min(t+dt); ilist = slots with t+dt == tnext.
- * Writes tnext to *d_tnext and the count to *d_ni. scratch >= 2*grid.
- * decision (or NULL): the previous block's pending encounter stopping decision, taken
- * by the scheduler's first kernel (after that block's corrector). */
-int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni,
-                 double *d_tnext, double *d_scratch, int scratch_len,
-                 const g6_enc_decision_args *decision, cudaStream_t st);
+/* g6x_run's two-kernel scheduler: sched_reset once per run (dmin2[0..1] =
+ * +inf, *d_ni = 0); per block sched_first (min of t + dt into dmin, *d_ni
+ * = 0, the pending stopping decision) then list_predict (kern_predict.cu:
+ * the slots with t + dt == tnext into d_ilist / *d_ni, tnext into *d_tnext,
+ * all j predicted to tnext in precision prec, *dmin_next = +inf).        */
+int g6k_sched_reset(unsigned long long *dmin2, int *d_ni, cudaStream_t st);
+int g6k_sched_first(const g6_jstate *js, int nj, unsigned long long *dmin, int *d_ni,
+                    const g6_enc_decision_args *decision, cudaStream_t st);
+int g6k_list_predict(const g6_jstate *js, int nj, int prec, const unsigned long long *dmin,
+                     unsigned long long *dmin_next, int *d_ilist, int *d_ni, double *d_tnext,
+                     cudaStream_t st);
 /* k nearest neighbours (kern_knn.cu): for each of ni listed slots, the k
  * (1..G6_KNN_MAX) nearest other j in [0, nj) by FP64 distance of the
  * positions predicted to t, ties to the smaller slot.  The split records

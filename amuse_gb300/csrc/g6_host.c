@@ -1450,11 +1450,21 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
   }
   g6_enc_decision_args pend; /* the last block's stopping decision, taken by the next schedule */
   memset(&pend, 0, sizeof(pend));
+  /* Per block: sched_first (min of t + dt), list_predict (the block list,
+     tnext, all j predicted to tnext), the mailbox copy and the one host
+     synchronisation, then the force on the block (split merge in the force
+     kernel, refinement pass), [encounter check], corrector.  The two
+     minima alternate by block parity: each list_predict resets the other. */
+  unsigned long long *dmin2 = (unsigned long long *)G.d_sched;
+  int parity = 0;
+  if (g6k_sched_reset(dmin2, G.d_ni, G.st)) return G6_ERR_CUDA;
   while (G.run_t < t_end && nb != max_blocks) {
     ilist_identity_n = 0;
-    if (g6k_schedule(&G.js, n, G.d_ilist, G.d_ni, G.d_tnext, G.d_sched, 4,
-                     pend.enc ? &pend : NULL, G.st))
+    if (g6k_sched_first(&G.js, n, dmin2 + parity, G.d_ni, pend.enc ? &pend : NULL, G.st) ||
+        g6k_list_predict(&G.js, n, G.prec, dmin2 + parity, dmin2 + (parity ^ 1), G.d_ilist,
+                         G.d_ni, G.d_tnext, G.st))
       return G6_ERR_CUDA;
+    parity ^= 1;
     pend.enc = NULL;
     /* one 16-byte copy into pinned memory: the only host round trip per block */
     CK(cudaMemcpyAsync(G.h_mail, G.d_mail, 16, cudaMemcpyDeviceToHost, G.st));
@@ -1469,6 +1479,11 @@ int g6x_run(double t_end, long long *blocks, double *particle_steps) {
       seterr("scheduler produced ni=%d tnext=%.17g at t=%.17g", ni, tn, G.run_t);
       return G6_ERR_STATE;
     }
+    /* list_predict has predicted every j to tn */
+    G.pred_valid = 1;
+    G.pred_t = tn;
+    G.pred_nj = n;
+    G.pred_prec = G.prec;
     rc = g6x_force_slots(tn, G.run_eps2, n, ni, G.d_ilist, G.d_racc, G.d_rjerk, G.d_rpot,
                          enc ? G.d_rnn : NULL, 0);
     if (rc) return rc;

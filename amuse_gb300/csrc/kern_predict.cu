@@ -6,7 +6,10 @@
 // Predictor: every j slot in [0, nj) is predicted to t_i in FP64 with ph4's
 // expression (src/amuse_ph4/src/jdata.cc:736-744):
 //   x_p = x + dt (v + dt/2 (a + dt j/3)),  v_p = v + dt (a + dt j/2),
-// copied unchanged when dt = 0, then packed for the force kernel:
+// copied unchanged when dt = 0 (for the FP64 records with ph4's rounding
+// order, bit for bit; the split records' double-single rounding hides the
+// difference, so there the compiler may contract), then packed for the
+// force kernel:
 //   split: x_p as a double-single pair (hi = rn(x_p), lo = rn(x_p - hi)),
 //          v_p and m in FP32                      -> 48 B record
 //   fp64 : x_p, v_p, m in FP64                     -> 64 B record
@@ -52,10 +55,10 @@ __global__ void scatter_kernel(g6_jstate js, const g6_jupd *__restrict__ upd, in
   }
 }
 
+// Predict slot s (< nj: ph4's expression in FP64; nj <= s < nj_pad: a
+// zero-mass record far away) and store its force record.
 template <int PREC>
-__global__ void __launch_bounds__(PT) predict_kernel(g6_jstate js, int nj, int nj_pad, double ti) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nj_pad) return;
+__device__ __forceinline__ void predict_one(const g6_jstate &js, int s, int nj, double ti) {
   const int cap = js.cap;
   double xp[3], vp[3], m;
   if (s < nj) {
@@ -66,6 +69,16 @@ __global__ void __launch_bounds__(PT) predict_kernel(g6_jstate js, int nj, int n
       for (int k = 0; k < 3; k++) {
         xp[k] = js.x[k * cap + s];
         vp[k] = js.v[k * cap + s];
+      }
+    } else if (PREC == G6_PREC_FP64) {
+      // the FP64 records (plain FP64 kernel, GPU oracle) carry ph4's
+      // expression with its rounding order, bit for bit
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const double x = js.x[k * cap + s], v = js.v[k * cap + s];
+        const double a = js.a[k * cap + s], j = js.j[k * cap + s];
+        xp[k] = g6_predict_x(x, v, a, j, dt);
+        vp[k] = g6_predict_v(v, a, j, dt);
       }
     } else {
 #pragma unroll
@@ -100,6 +113,35 @@ __global__ void __launch_bounds__(PT) predict_kernel(g6_jstate js, int nj, int n
   }
 }
 
+template <int PREC>
+__global__ void __launch_bounds__(PT) predict_kernel(g6_jstate js, int nj, int nj_pad, double ti) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nj_pad) return;
+  predict_one<PREC>(js, s, nj, ti);
+}
+
+// The block scheduler's second kernel fused with the predictor: the block
+// time tn is the minimum of t + dt found by sched_min_first (bits in
+// *dmin); each thread lists its slot if t + dt == tn (the block: ph4's
+// scheduler, src/amuse_ph4/src/scheduler.cc) and predicts it to tn.
+// *dmin_next, the other parity's minimum, is reset to +inf for the next
+// block.
+template <int PREC>
+__global__ void __launch_bounds__(PT) list_predict_kernel(g6_jstate js, int nj, int nj_pad,
+                                                          const unsigned long long *dmin,
+                                                          unsigned long long *dmin_next,
+                                                          int *ilist, int *dni, double *dtnext) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const double tn = __longlong_as_double((long long)*dmin);
+  if (s == 0) {
+    *dtnext = tn;
+    *dmin_next = 0x7ff0000000000000ull;
+  }
+  if (s >= nj_pad) return;
+  if (s < nj && js.t[s] + js.dt[s] == tn) ilist[atomicAdd(dni, 1)] = s;
+  predict_one<PREC>(js, s, nj, tn);
+}
+
 }  // namespace
 
 extern "C" int g6k_scatter(const g6_jstate *js, const g6_jupd *d_upd, int n, cudaStream_t st) {
@@ -117,5 +159,21 @@ extern "C" int g6k_predict(const g6_jstate *js, int nj, double ti, int prec, cud
     predict_kernel<G6_PREC_FP64><<<grid, PT, 0, st>>>(*js, nj, nj_pad, ti);
   else
     predict_kernel<G6_PREC_SPLIT><<<grid, PT, 0, st>>>(*js, nj, nj_pad, ti);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+extern "C" int g6k_list_predict(const g6_jstate *js, int nj, int prec,
+                                const unsigned long long *dmin, unsigned long long *dmin_next,
+                                int *d_ilist, int *d_ni, double *d_tnext, cudaStream_t st) {
+  if (nj <= 0) return 0;
+  const int nj_pad = (nj + G6_TILE - 1) / G6_TILE * G6_TILE;
+  if (nj_pad > js->cap) return -1;
+  const int grid = (nj_pad + PT - 1) / PT;
+  if (prec == G6_PREC_FP64)
+    list_predict_kernel<G6_PREC_FP64><<<grid, PT, 0, st>>>(*js, nj, nj_pad, dmin, dmin_next,
+                                                           d_ilist, d_ni, d_tnext);
+  else
+    list_predict_kernel<G6_PREC_SPLIT><<<grid, PT, 0, st>>>(*js, nj, nj_pad, dmin, dmin_next,
+                                                            d_ilist, d_ni, d_tnext);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }

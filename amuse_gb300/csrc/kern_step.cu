@@ -321,16 +321,16 @@ __global__ void store_kernel(g6_jstate js, int ni, const int *__restrict__ ilist
 }
 
 // t + dt >= 0 always, so the IEEE bit pattern orders like an unsigned int.
-// The previous block's encounter stopping decision, if one is pending, is taken here:
-// this kernel is the first of the next block, after that block's corrector.
-__global__ void sched_init(unsigned long long *dmin, int *dni, g6_jstate js,
-                           g6_enc_decision_args v) {
-  *dmin = 0x7ff0000000000000ull;  // +inf
-  *dni = 0;
-  if (v.enc) enc_decide(js, v.enc, v.mode, v.t, v.flag);
-}
-
-__global__ void sched_min(g6_jstate js, int nj, unsigned long long *dmin) {
+// First kernel of a block in g6x_run: the minimum of t + dt (into dmin,
+// which the previous block's list_predict_kernel reset to +inf), the block
+// count reset (the host has read the previous count), and the previous
+// block's encounter stopping decision (after that block's corrector).
+__global__ void sched_min_first(g6_jstate js, int nj, unsigned long long *dmin, int *dni,
+                                g6_enc_decision_args v) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *dni = 0;
+    if (v.enc) enc_decide(js, v.enc, v.mode, v.t, v.flag);
+  }
   __shared__ unsigned long long w[PT / 32];
   unsigned long long m = 0x7ff0000000000000ull;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nj; s += gridDim.x * blockDim.x) {
@@ -349,16 +349,9 @@ __global__ void sched_min(g6_jstate js, int nj, unsigned long long *dmin) {
   }
 }
 
-__global__ void sched_list(g6_jstate js, int nj, const unsigned long long *dmin, int *ilist,
-                           int *dni, double *dtnext) {
-  const double tn = __longlong_as_double((long long)*dmin);
-  if (blockIdx.x == 0 && threadIdx.x == 0) *dtnext = tn;
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nj; s += gridDim.x * blockDim.x) {
-    if (js.t[s] + js.dt[s] == tn) {
-      const int k = atomicAdd(dni, 1);
-      ilist[k] = s;
-    }
-  }
+__global__ void sched_reset(unsigned long long *dmin, int *dni) {
+  dmin[0] = dmin[1] = 0x7ff0000000000000ull;
+  *dni = 0;
 }
 
 __global__ void initial_step_kernel(g6_jstate js, int nj, double eta, double fac, double limit,
@@ -465,11 +458,19 @@ extern "C" int g6k_store_forces(const g6_jstate *js, int ni, const int *ilist, c
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
-extern "C" int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni, double *d_tnext,
-                            double *d_scratch, int scratch_len,
-                            const g6_enc_decision_args *decision, cudaStream_t st) {
-  if (nj <= 0 || scratch_len < 1) return -1;
-  unsigned long long *dmin = reinterpret_cast<unsigned long long *>(d_scratch);
+// g6x_run's scheduler, in two kernels per block with the predictor:
+// g6k_sched_reset once before the loop (both parities' minima +inf), then
+// per block g6k_sched_first (minimum into dmin[parity]) and
+// g6k_list_predict (kern_predict.cu: the block list, tnext, the prediction,
+// and dmin[1 - parity] reset for the next block).
+extern "C" int g6k_sched_reset(unsigned long long *dmin2, int *d_ni, cudaStream_t st) {
+  sched_reset<<<1, 1, 0, st>>>(dmin2, d_ni);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+extern "C" int g6k_sched_first(const g6_jstate *js, int nj, unsigned long long *dmin, int *d_ni,
+                               const g6_enc_decision_args *decision, cudaStream_t st) {
+  if (nj <= 0) return -1;
   int grid = (nj + PT - 1) / PT;
   const int cap_grid = 4 * g6k_sm_count();
   if (grid > cap_grid) grid = cap_grid;
@@ -482,9 +483,7 @@ extern "C" int g6k_schedule(const g6_jstate *js, int nj, int *d_ilist, int *d_ni
     v.t = 0;
     v.flag = NULL;
   }
-  sched_init<<<1, 1, 0, st>>>(dmin, d_ni, *js, v);
-  sched_min<<<grid, PT, 0, st>>>(*js, nj, dmin);
-  sched_list<<<grid, PT, 0, st>>>(*js, nj, dmin, d_ilist, d_ni, d_tnext);
+  sched_min_first<<<grid, PT, 0, st>>>(*js, nj, dmin, d_ni, v);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

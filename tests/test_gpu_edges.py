@@ -145,3 +145,23 @@ def test_close_and_reopen(g6):
     t = [torch.tensor(a, device="cuda") for a in (x, v, m)]
     xf, _ = hermite_fixed(t[0], t[1], t[2], eps2=1e-4, dt=1 / 256, nsteps=2)
     assert torch.isfinite(xf).all()
+
+
+def test_bounded_wait_expiry(g6):
+    """The force kernel's waits are bounded: with the test hook, the first
+    CTA waits on a barrier that nothing arrives on; after 20 ms the wait
+    gives up, the CTA drains its copies and sets the error word, and the call
+    returns G6_ERR_KERNEL.  The next call runs normally and is correct."""
+    np.random.seed(41)
+    n = 4096
+    m, x, v = ic.plummer(n)
+    g6.load_particles(m, x, v)
+    sel = np.arange(0, n, 8)
+    g6.test_wait_expiry(True)
+    with pytest.raises(ag.G6Error) as ei:
+        g6.force(0.0, 1e-4, n, x[sel], v[sel], self_slot=sel)
+    assert "error word" in str(ei.value)
+    out = g6.force(0.0, 1e-4, n, x[sel], v[sel], self_slot=sel)
+    ref = oracle.force(m, x, v, 1e-4, x[sel], v[sel])
+    e = np.linalg.norm(out["acc"] - ref["acc"], axis=1) / np.linalg.norm(ref["acc"], axis=1)
+    assert e.max() <= 1e-6

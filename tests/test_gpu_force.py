@@ -1,11 +1,18 @@
 """GPU parity of the force path through the C ABI, against the oracle.
 
-Tolerances (stated per quantity, split precision):
-  acc  : per-particle relative error |da|/|a| <= 1e-6 at p99, <= 1e-5 max
-  pot  : relative error <= 1e-6 max
-  jerk : relative error <= 1e-5 at p99 (FP32 velocities), reported
-  nn   : identical ids except at distance ties (FP64 r^2 within 1e-5 rel.)
-FP64 precision: acc/jerk/pot relative error <= 1e-12.
+Tolerances (per-particle relative errors against ph4's FP64 CPU loop):
+  split precision (FP32 pair terms on double-single positions, with the
+  refinement pass: ill-conditioned sums redone in FP64):
+    acc  : |da|/|a| <= 1e-6 for every particle
+    pot  : |dp|/|p| <= 1e-6 for every particle
+    jerk : |dj|/|j| <= JERK_P99_SPLIT at p99, <= JERK_MAX_SPLIT for every
+           particle (the jerk sum cancels more than the acceleration; its
+           error is stated, not bounded by the condition-number pass; at
+           N = 2^20 its p99 is 0.9e-6, on a few hundred particles of a small
+           system the p99 is the third-worst value)
+  FP64: acc/pot <= 1e-12, jerk <= 1e-12 at p99 and 1e-10 for every particle.
+  nn (both): the oracle's index (ph4: smallest FP64 r^2, first j on equal
+  values), except where the two indices' FP64 r^2 are equal.
 """
 import numpy as np
 import pytest
@@ -17,12 +24,34 @@ from conftest import golden
 
 pytestmark = pytest.mark.gpu
 
-TOL = {ag.SPLIT: dict(acc99=1e-6, accmax=1e-5, pot=1e-6, jerk99=1e-5),
-       ag.FP64: dict(acc99=1e-12, accmax=1e-12, pot=1e-12, jerk99=1e-12)}
+JERK_P99_SPLIT = 1.5e-6
+JERK_MAX_SPLIT = 1e-4
+TOL = {ag.SPLIT: dict(accmax=1e-6, pot=1e-6, jerk99=JERK_P99_SPLIT, jerkmax=JERK_MAX_SPLIT),
+       ag.FP64: dict(accmax=1e-12, pot=1e-12, jerk99=1e-12, jerkmax=1e-10)}
 
 
 def vrel(a, b):
     return np.linalg.norm(a - b, axis=-1) / np.maximum(np.linalg.norm(b, axis=-1), 1e-300)
+
+
+def ph4_r2(xj, xi):
+    """ph4's squared distance (idata.cc:200-205): dx = x_j - x_i, summed in
+    component order with IEEE operations (numpy does not contract)."""
+    d = xj - xi
+    return (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+
+
+def check_nn(got, want, jpos, ipos, label=""):
+    """nn equal to the oracle's except at exact FP64 distance ties."""
+    bad = np.nonzero(got != want)[0]
+    ties = 0
+    for i in bad:
+        assert got[i] >= 0, (label, i, got[i], want[i])
+        d_got = ph4_r2(jpos[got[i]], ipos[i])
+        d_want = ph4_r2(jpos[want[i]], ipos[i])
+        assert d_got == d_want, (label, i, got[i], want[i], d_got, d_want)
+        ties += 1
+    return ties
 
 
 def check_force(out, ref, prec, jpos=None, ipos=None, nn_is_id=False, label=""):
@@ -33,20 +62,13 @@ def check_force(out, ref, prec, jpos=None, ipos=None, nn_is_id=False, label=""):
     print(f"{label} prec={prec} acc p50={np.median(ea):.2e} p99={np.percentile(ea, 99):.2e} "
           f"max={ea.max():.2e} | jerk p99={np.percentile(ej, 99):.2e} max={ej.max():.2e} | "
           f"pot max={ep.max():.2e}")
-    assert np.percentile(ea, 99) <= t["acc99"]
     assert ea.max() <= t["accmax"]
     assert ep.max() <= t["pot"]
     assert np.percentile(ej, 99) <= t["jerk99"]
+    assert ej.max() <= t["jerkmax"]
     if "nn" in out and jpos is not None:
         got = out["nn"] - (1 if nn_is_id else 0)
-        want = ref["nn"]
-        bad = np.nonzero(got != want)[0]
-        for i in bad:
-            assert got[i] >= 0
-            d_got = np.sum((jpos[got[i]] - ipos[i]) ** 2)
-            d_want = np.sum((jpos[want[i]] - ipos[i]) ** 2)
-            assert abs(d_got - d_want) <= 1e-5 * d_want, (i, got[i], want[i], d_got, d_want)
-        return len(bad)
+        return check_nn(got, ref["nn"], jpos, ipos, label)
     return 0
 
 
@@ -266,3 +288,89 @@ def test_error_codes(g6):
     # a normal call still works afterwards
     acc, jerk, pot, nn = g6.calc(64, ids, x, v, 1e-4)
     assert np.all(np.isfinite(acc))
+
+
+# --- nearest neighbour: ties and near-ties, and the FP64 redo ------------
+
+def test_nn_lattice_ties(g6, prec):
+    """A cubic lattice with a power-of-two spacing: every particle has up to
+    six neighbours at exactly the same FP64 distance, and ph4 takes the first
+    (strict <).  The FP32 keys tie too, so the split path must rank the
+    candidates in FP64 and take the smallest slot."""
+    k = 8
+    g = np.arange(k) * 0.125
+    x = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3) - 0.4375
+    n = len(x)
+    m = np.full(n, 1.0 / n)
+    v = np.random.RandomState(4).normal(0, 0.1, (n, 3))
+    g6.load_particles(m, x, v)
+    out = g6.force(0.0, 1e-4, n, x, v, self_slot=np.arange(n))
+    ref = oracle.force(m, x, v, 1e-4, x, v)
+    assert np.array_equal(out["nn"], ref["nn"])
+    if prec == ag.SPLIT:
+        st = g6.refine_stats()
+        assert st["queued"] >= n // 2 and st["overflow"] == 0, st
+
+
+def test_nn_near_ties(g6, prec):
+    """Pairs of candidates whose distances differ by ~1e-9 relative (below
+    FP32 resolution): the FP32 keys cannot order them, the FP64 ranking must."""
+    rng = np.random.RandomState(21)
+    n = 3000
+    x = rng.uniform(-1, 1, (n, 3))
+    # for the first 200 particles, two companions at nearly equal distance
+    ncase = 200
+    d = 1e-3
+    u = rng.normal(size=(ncase, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    w = np.cross(u, rng.normal(size=(ncase, 3)))
+    w /= np.linalg.norm(w, axis=1)[:, None]
+    eps = rng.choice([-1, 1], ncase) * rng.uniform(1e-10, 1e-8, ncase)
+    x[n - 2 * ncase: n - ncase] = x[:ncase] + d * u
+    x[n - ncase:] = x[:ncase] + d * (1 + eps)[:, None] * w
+    m = np.full(n, 1.0 / n)
+    v = rng.normal(0, 0.3, (n, 3))
+    g6.load_particles(m, x, v)
+    sel = np.arange(ncase)
+    out = g6.force(0.0, 1e-6, n, x[sel], v[sel], self_slot=sel)
+    ref = oracle.force(m, x, v, 1e-6, x[sel], v[sel])
+    assert check_nn(out["nn"], ref["nn"], x, x[sel], "near-ties") == 0
+    assert np.array_equal(out["nn"], ref["nn"])
+
+
+def test_refine_ill_conditioned(g6):
+    """A particle near the centre of a shell of opposite pairs, one of them
+    displaced by 2%: the pulls cancel to ~1e-5 of their sum (condition number
+    ~1e5), so FP32 pair terms alone miss 1e-6 by orders of magnitude; the
+    FP64 redo must recover it."""
+    g6.set_precision(ag.SPLIT)
+    rng = np.random.RandomState(22)
+    nshell = 4000
+    u = rng.normal(size=(nshell // 2, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    shell = np.concatenate([u, -u]) * 0.5
+    shell[0] *= 1.02  # break the symmetry a little
+    centre = np.array([[1e-7, -2e-7, 3e-7]])
+    x = np.concatenate([centre, shell])
+    n = len(x)
+    m = np.full(n, 1.0 / n)
+    v = rng.normal(0, 0.1, (n, 3))
+    g6.load_particles(m, x, v)
+    sel = np.arange(16)
+    ref = oracle.force(m, x, v, 1e-6, x[sel], v[sel])
+    try:
+        g6.set_refine(0.0)
+        plain = g6.force(0.0, 1e-6, n, x[sel], v[sel], self_slot=sel)
+        g6.set_refine(48.0)
+        out = g6.force(0.0, 1e-6, n, x[sel], v[sel], self_slot=sel)
+        st = g6.refine_stats()
+    finally:
+        g6.set_refine(48.0)
+    e_plain = vrel(plain["acc"][:1], ref["acc"][:1])[0]
+    e = vrel(out["acc"], ref["acc"])
+    print(f"centre particle: acc rel err {e_plain:.2e} without, {e[0]:.2e} with the FP64 redo "
+          f"({st})")
+    assert e_plain > 1e-5  # the case does exercise the pass
+    assert st["kappa"] >= 1
+    assert e.max() <= 1e-6
+    assert np.max(np.abs(out["pot"] - ref["pot"]) / np.abs(ref["pot"])) <= 1e-6

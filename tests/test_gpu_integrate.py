@@ -99,3 +99,25 @@ def test_force_dev_without_nn(g6):
     ea = np.linalg.norm(da.cpu().numpy() - ref["acc"], axis=1) / np.linalg.norm(ref["acc"], axis=1)
     assert np.percentile(ea, 99) < 1e-6
     assert np.allclose(dp.cpu().numpy(), ref["pot"], rtol=1e-6)
+
+
+@pytest.mark.parametrize("prec", [ag.SPLIT, ag.FP64], ids=["split", "fp64"])
+def test_initial_step_bitexact(g6, prec):
+    """g6x_run_init's initial time steps (initial_step_kernel + the median
+    limit, jdata.cc:503-580 with force_initial_timestep(0.0625, 0.03125, 8),
+    interface.cc:29-31) equal the oracle's set_initial_timestep bit for bit,
+    on the config-1 particles, from the accelerations and jerks the device
+    stored at t = 0."""
+    g = golden("run_plummer1024_t1.npz")
+    n = len(g["mass"])
+    g6.set_precision(prec)
+    try:
+        g6.load_particles(g["mass"], g["pos0"], g["vel0"])
+        g6.run_init(float(g["eps2"]), float(g["eta"]))
+        st = g6.read_particles(n)
+    finally:
+        g6.set_precision(ag.SPLIT)
+    ref = oracle.initial_step(st["acc"], st["jerk"], float(g["eta"]), fac=0.0625,
+                              limit=0.03125, limitm=8.0)
+    assert np.array_equal(st["timestep"], ref)
+    assert np.all(st["time"] == 0.0)

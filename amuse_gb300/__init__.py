@@ -48,7 +48,7 @@ ABI_SYMBOLS = [
 BYVALUE_SYMBOLS = [s[:-1] for s in ABI_SYMBOLS]
 EXT_SYMBOLS = [
     "g6x_set_precision", "g6x_get_precision", "g6x_set_refine", "g6x_refine_stats",
-    "g6x_test_wait_expiry", "g6x_set_npipes", "g6x_last_error", "g6x_load",
+    "g6x_test_wait_expiry", "g6x_batch_unperturbed", "g6x_batch_binaries", "g6x_set_npipes", "g6x_last_error", "g6x_load",
     "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
     "g6x_energy", "g6x_run_stats", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
     "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
@@ -125,6 +125,8 @@ def load():
     lib.g6x_batch_run.argtypes = [I, _pi, _pd, _pd, _pd, _pd, D, I, ctypes.c_longlong, I, _pd,
                                   _pll, _pd, _pi, _pd]
     lib.g6x_batch_config.argtypes = [I, I]
+    lib.g6x_batch_unperturbed.argtypes = [I, D, D, D, I]
+    lib.g6x_batch_binaries.argtypes = [I, _pi]
     lib.g6x_batch_tune.argtypes = [I, _pi, _pd, _pd, _pd, _pd, D, I, I, D, _pd]
     lib.g6x_system_time.restype = D
     lib.g6x_timing.argtypes = [I]
@@ -444,6 +446,19 @@ class G6X(G6):
 
     def batch_config(self, warps_per_cta, ctas_per_sm):
         _check(self.lib.g6x_batch_config(warps_per_cta, ctas_per_sm), "g6x_batch_config")
+
+    def batch_unperturbed(self, on=True, dt_crit=1e-3, r2_crit=1e-2, gamma=1e-6,
+                          allow_full=True):
+        """smallN's unperturbed binaries in the fast and split batch modes
+        (defaults: the smallN worker's)."""
+        _check(self.lib.g6x_batch_unperturbed(1 if on else 0, dt_crit, r2_crit, gamma,
+                                              1 if allow_full else 0), "g6x_batch_unperturbed")
+
+    def batch_binaries(self, nsys):
+        """Binaries made per system in the last batch run."""
+        out = np.zeros(nsys, np.int32)
+        _check(self.lib.g6x_batch_binaries(nsys, _ptr(out, ctypes.c_int)), "g6x_batch_binaries")
+        return out
 
     def batch_tune(self, n_per_sys, t_end, mass, pos, vel, eta=0.14, n_iter=2, exact=False,
                    frac=0.1, mode=None):

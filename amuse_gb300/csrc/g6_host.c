@@ -1682,6 +1682,12 @@ int g6x_force_dev_noalloc(double ti, double eps2, int nj, int ni, const double *
  * when buffers or parameters change.  Launch shape (warps per CTA, CTAs per
  * SM) comes from g6x_batch_tune or defaults to 4 x 2. */
 int g6k_batch_max_n(void);
+int g6k_batch_launch_unp(int nsys, const int *order, const int *off, const double *t_end,
+                         const double *mass, double *pos, double *vel, double eta, int n_iter,
+                         long long max_steps, int mode, int warps_per_cta, int ctas,
+                         double dt_crit, double r2_crit, double gamma, int allow_full, int *queue,
+                         double *t_out, long long *steps_out, unsigned long long *wall_ns,
+                         int *status, int *nbin_out, cudaStream_t st);
 int g6k_batch_launch(int nsys, const int *order, const int *off, const double *t_end,
                      const double *mass, double *pos, double *vel, double eta, int n_iter,
                      long long max_steps, int exact, int warps_per_cta, int ctas, int *queue,
@@ -1700,24 +1706,35 @@ static struct {
   double g_eta;
   long long g_maxsteps;
   void *g_key;
+  /* smallN's unperturbed binaries (g6x_batch_unperturbed) */
+  int unp, unp_full;
+  double unp_dt_crit, unp_r2_crit, unp_gamma;
+  int *d_nbin;
+  int g_unp;
 } BT = {0, 0, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, 4, 2,
-        NULL, 0, 0, 0, 0, 0, 0.0, 0, NULL};
+        NULL, 0, 0, 0, 0, 0, 0.0, 0, NULL, 0, 0, 0.0, 0.0, 0.0, NULL, 0};
 
 static void batch_free(void) {
   cudaFree(BT.d_order); cudaFree(BT.d_off); cudaFree(BT.d_queue); cudaFree(BT.d_status);
   cudaFree(BT.d_tend); cudaFree(BT.d_mass); cudaFree(BT.d_pos); cudaFree(BT.d_vel);
-  cudaFree(BT.d_tout); cudaFree(BT.d_steps); cudaFree(BT.d_wall);
+  cudaFree(BT.d_tout); cudaFree(BT.d_steps); cudaFree(BT.d_wall); cudaFree(BT.d_nbin);
   if (BT.gexec) cudaGraphExecDestroy(BT.gexec);
-  const int wpc = BT.wpc, cps = BT.cps;
+  const int wpc = BT.wpc, cps = BT.cps, unp = BT.unp, full = BT.unp_full;
+  const double dc = BT.unp_dt_crit, r2 = BT.unp_r2_crit, g = BT.unp_gamma;
   memset(&BT, 0, sizeof(BT));
   BT.wpc = wpc;
   BT.cps = cps;
+  BT.unp = unp;
+  BT.unp_full = full;
+  BT.unp_dt_crit = dc;
+  BT.unp_r2_crit = r2;
+  BT.unp_gamma = g;
 }
 
 static int batch_ensure(int nsys, int nbody) {
   if (nsys > BT.cap_sys) {
     cudaFree(BT.d_order); cudaFree(BT.d_off); cudaFree(BT.d_tend); cudaFree(BT.d_tout);
-    cudaFree(BT.d_steps); cudaFree(BT.d_wall); cudaFree(BT.d_status);
+    cudaFree(BT.d_steps); cudaFree(BT.d_wall); cudaFree(BT.d_status); cudaFree(BT.d_nbin);
     BT.cap_sys = 0;
     size_t s = (size_t)nsys;
     if (cudaMalloc((void **)&BT.d_order, sizeof(int) * s) != cudaSuccess ||
@@ -1726,7 +1743,8 @@ static int batch_ensure(int nsys, int nbody) {
         cudaMalloc((void **)&BT.d_tout, sizeof(double) * s) != cudaSuccess ||
         cudaMalloc((void **)&BT.d_steps, sizeof(long long) * s) != cudaSuccess ||
         cudaMalloc((void **)&BT.d_wall, sizeof(unsigned long long) * s) != cudaSuccess ||
-        cudaMalloc((void **)&BT.d_status, sizeof(int) * s) != cudaSuccess) {
+        cudaMalloc((void **)&BT.d_status, sizeof(int) * s) != cudaSuccess ||
+        cudaMalloc((void **)&BT.d_nbin, sizeof(int) * s) != cudaSuccess) {
       seterr("cannot allocate batch buffers for %d systems", nsys);
       return G6_ERR_NOMEM;
     }
@@ -1758,18 +1776,25 @@ static int cmp_desc_n(const void *a, const void *b) {
 /* Launch through a (cached) CUDA graph: queue reset + persistent kernel. */
 static int batch_graph_launch(int nsys, double eta, int n_iter, long long max_steps, int exact) {
   const int ctas = BT.cps * g6k_sm_count();
+  const int unp = BT.unp && exact != G6_BATCH_EXACT;
   if (!BT.gexec || BT.g_nsys != nsys || BT.g_exact != exact || BT.g_niter != n_iter ||
       BT.g_eta != eta || BT.g_maxsteps != max_steps || BT.g_wpc != BT.wpc ||
-      BT.g_cps != BT.cps || BT.g_key != (void *)BT.d_pos) {
+      BT.g_cps != BT.cps || BT.g_key != (void *)BT.d_pos || BT.g_unp != unp) {
     if (BT.gexec) {
       cudaGraphExecDestroy(BT.gexec);
       BT.gexec = NULL;
     }
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(G.st, cudaStreamCaptureModeThreadLocal));
-    int rc = g6k_batch_launch(nsys, BT.d_order, BT.d_off, BT.d_tend, BT.d_mass, BT.d_pos,
-                              BT.d_vel, eta, n_iter, max_steps, exact, BT.wpc, ctas, BT.d_queue,
-                              BT.d_tout, BT.d_steps, BT.d_wall, BT.d_status, G.st);
+    int rc = unp ? g6k_batch_launch_unp(nsys, BT.d_order, BT.d_off, BT.d_tend, BT.d_mass,
+                                        BT.d_pos, BT.d_vel, eta, n_iter, max_steps, exact,
+                                        BT.wpc, ctas, BT.unp_dt_crit, BT.unp_r2_crit,
+                                        BT.unp_gamma, BT.unp_full, BT.d_queue, BT.d_tout,
+                                        BT.d_steps, BT.d_wall, BT.d_status, BT.d_nbin, G.st)
+                 : g6k_batch_launch(nsys, BT.d_order, BT.d_off, BT.d_tend, BT.d_mass, BT.d_pos,
+                                    BT.d_vel, eta, n_iter, max_steps, exact, BT.wpc, ctas,
+                                    BT.d_queue, BT.d_tout, BT.d_steps, BT.d_wall, BT.d_status,
+                                    G.st);
     cudaError_t e = cudaStreamEndCapture(G.st, &g);
     if (rc || e != cudaSuccess) {
       seterr("batch graph capture failed (%d, %s)", rc, cudaGetErrorString(e));
@@ -1790,8 +1815,27 @@ static int batch_graph_launch(int nsys, double eta, int n_iter, long long max_st
     BT.g_wpc = BT.wpc;
     BT.g_cps = BT.cps;
     BT.g_key = (void *)BT.d_pos;
+    BT.g_unp = unp;
   }
   CK(cudaGraphLaunch(BT.gexec, G.st));
+  return 0;
+}
+
+int g6x_batch_unperturbed(int on, double dt_crit, double r2_crit, double gamma, int allow_full) {
+  if (on && !(dt_crit >= 0 && r2_crit >= 0 && gamma > 0)) return G6_ERR_ARG;
+  BT.unp = on ? 1 : 0;
+  BT.unp_dt_crit = dt_crit;
+  BT.unp_r2_crit = r2_crit;
+  BT.unp_gamma = gamma;
+  BT.unp_full = allow_full ? 1 : 0;
+  return 0;
+}
+
+int g6x_batch_binaries(int nsys, int *nbin) {
+  int rc = check_open();
+  if (rc) return rc;
+  if (nsys <= 0 || nsys > BT.cap_sys || !nbin || !BT.d_nbin) return G6_ERR_ARG;
+  CK(cudaMemcpy(nbin, BT.d_nbin, sizeof(int) * (size_t)nsys, cudaMemcpyDeviceToHost));
   return 0;
 }
 
@@ -1812,6 +1856,15 @@ int g6x_batch_run(int nsys, const int *n_per_sys, const double *t_end, const dou
   if (nsys <= 0 || !n_per_sys || !t_end || !mass || !pos || !vel || n_iter < 0 || eta <= 0 ||
       exact < G6_BATCH_FAST || exact > G6_BATCH_SPLIT)
     return G6_ERR_ARG;
+  if (BT.unp && exact == G6_BATCH_EXACT) {
+    seterr("g6x_batch_run: the exact mode reproduces smallN without unperturbed binaries; "
+           "switch them off (g6x_batch_unperturbed) or use the fast or split mode");
+    return G6_ERR_ARG;
+  }
+  if (BT.unp && BT.wpc > 4) {
+    seterr("g6x_batch_run: with unperturbed binaries at most 4 warps per CTA");
+    return G6_ERR_ARG;
+  }
   const int maxn = g6k_batch_max_n();
   int *off = (int *)malloc(sizeof(int) * (size_t)(nsys + 1));
   int *pairs = (int *)malloc(sizeof(int) * 2 * (size_t)nsys);
@@ -1910,6 +1963,7 @@ int g6x_batch_tune(int nsys, const int *n_per_sys, const double *t_end, const do
   double best = 1e300;
   int bw = BT.wpc, bc = BT.cps;
   for (int k = 0; k < nshape; k++) {
+    if (BT.unp && shapes[k][0] > 4) continue; /* that kernel holds 4 warps per CTA at most */
     memcpy(p, pos, sizeof(double) * 3 * (size_t)nb);
     memcpy(v, vel, sizeof(double) * 3 * (size_t)nb);
     BT.wpc = shapes[k][0];

@@ -4,8 +4,10 @@
 // Each warp takes a system from a device work queue (an atomic counter over
 // a host-chosen order, largest systems first), integrates it to its end
 // time, writes it back and takes the next one, so uneven systems balance
-// themselves.  The integrator is smallN's (src/amuse_ph4/src/smallN.cc)
-// without the unperturbed-binary tree: a shared-step, time-symmetrised
+// themselves.  The integrator is smallN's (src/amuse_ph4/src/smallN.cc):
+// without the unperturbed-binary tree in batch_kernel (its EXACT mode is
+// bit-identical to smallN with dt_crit = 0), with it in batch_unp_kernel
+// (below) -- a shared-step, time-symmetrised
 // 4th-order Hermite scheme --
 //   predict_loworder (hdyn.h:192-201) from the stored old acc/jerk,
 //   n_iter + 1 force evaluations per step, each followed by
@@ -456,6 +458,725 @@ __global__ void batch_kernel(int nsys, const int *__restrict__ order, const int 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Unperturbed binaries (smallN's default treatment: src/amuse_ph4/src/
+// smallN.cc:1022-1060 and smallN_unpert.cc): after each step the pair that
+// set the time step becomes a binary node when it is approaching, closer
+// than r_crit, its step is below dt_crit and the strongest perturber's
+// tidal parameter gamma^2 = 4 (m_k/M)^2 (r^2/d_k^2)^3 is below gamma^2_unpert
+// (smallN_unpert.cc:44-88).  Its centre of mass is integrated like a body;
+// its components follow the two-body orbit (universal-variable Kepler
+// propagation) and are resolved for every force evaluation (forces between
+// top-level nodes are sums over their leaves, smallN.cc:127-240; the step
+// criterion takes the closest leaf pair with the nodes' masses and
+// velocities).  The unperturbed segment ends at the time the orbit returns
+// to the same separation past pericentre (smallN_unpert.cc:252-266, 335);
+// there the change of the tidal potential is absorbed into the relative
+// velocity, and the binary is either extended by whole periods (frozen
+// components) while no perturber can arrive (dt_perturbers,
+// smallN_unpert.cc:402-460, 682-704) or dissolved.  The same algorithm, with
+// the same stated differences from smallN, is the oracle's
+// orc_smalln_unpert.  FAST (FP64 pair terms) and SPLIT (FP32 pair terms)
+// modes; all tree decisions are taken redundantly by every lane of the
+// warp from shared data, so they are warp-uniform.
+constexpr int NB = 8;             // binaries per system at most
+constexpr int WARPS_MAX_UNP = 4;  // shared memory per warp is larger here
+
+struct BinRec {
+  int li, lj, full, pad;
+  double mi, mj, r0[3], v0[3], t0, tpred, tidal;
+};
+
+struct UnpParams {
+  double dt_crit, r2_crit, gamma2, gamma_inv3;
+  int allow_full;
+};
+
+struct UnpSmem {
+  union {  // leaves for the force loop; node positions/velocities for the tree logic
+    struct {
+      double pp[MAXN][3];
+      double pv[MAXN][3];
+    } d;
+    struct {
+      float ph[MAXN][3];
+      float pl[MAXN][3];
+      float vf[MAXN][3];
+    } f;
+  } A;
+  double la[MAXN][3], lj[MAXN][3];  // leaf forces, then node accelerations
+  double m[MAXN];                    // leaf masses
+  float mf[MAXN];
+  double nm[MAXN];                   // node masses (at node slots)
+  double cv[MAXN][3];                // node predicted velocities (at node slots)
+  float cvf[MAXN][3];
+  int nd[MAXN];                      // node (leader slot) of every leaf slot
+  BinRec bin[NB];
+  int nb;
+};
+
+__device__ __forceinline__ double kst_c(double z) {
+  if (z > 1e-6) return (1.0 - cos(sqrt(z))) / z;
+  if (z < -1e-6) return (cosh(sqrt(-z)) - 1.0) / (-z);
+  return 0.5 - z / 24.0 + z * z / 720.0;
+}
+__device__ __forceinline__ double kst_s(double z) {
+  if (z > 1e-6) {
+    const double q = sqrt(z);
+    return (q - sin(q)) / (q * q * q);
+  }
+  if (z < -1e-6) {
+    const double q = sqrt(-z);
+    return (sinh(q) - q) / (q * q * q);
+  }
+  return 1.0 / 6.0 - z / 120.0 + z * z / 5040.0;
+}
+
+// Two-body relative motion over dt (mu = G M), universal variables:
+// Newton iterations on the universal anomaly x of
+//   sqrt(mu) dt = (r0.v0 / sqrt(mu)) x^2 C(z) + (1 - alpha r0) x^3 S(z) + r0 x,
+// z = alpha x^2, then the f and g functions.
+__device__ void kep_prop(double mu, const double r0[3], const double v0[3], double dt,
+                         double r[3], double v[3]) {
+  const double rn = sqrt(r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2]);
+  const double v2 = v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2];
+  const double rv = r0[0] * v0[0] + r0[1] * v0[1] + r0[2] * v0[2];
+  const double alpha = 2.0 / rn - v2 / mu, smu = sqrt(mu);
+  if (dt == 0.0) {
+    for (int k = 0; k < 3; k++) r[k] = r0[k], v[k] = v0[k];
+    return;
+  }
+  double x = alpha > 0.0 ? smu * dt * alpha : smu * dt / rn;
+  for (int it = 0; it < 100; it++) {
+    const double z = alpha * x * x, C = kst_c(z), S = kst_s(z);
+    const double F = rv / smu * x * x * C + (1.0 - alpha * rn) * x * x * x * S + rn * x - smu * dt;
+    const double dF = rv / smu * x * (1.0 - z * S) + (1.0 - alpha * rn) * x * x * C + rn;
+    const double dx = F / dF;
+    x -= dx;
+    if (fabs(dx) <= 1e-15 * fabs(x)) break;
+  }
+  const double z = alpha * x * x, C = kst_c(z), S = kst_s(z);
+  const double f = 1.0 - x * x * C / rn, g = dt - x * x * x * S / smu;
+  for (int k = 0; k < 3; k++) r[k] = f * r0[k] + g * v0[k];
+  const double rr = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  const double fd = smu / (rr * rn) * (alpha * x * x * x * S - x), gd = 1.0 - x * x * C / rr;
+  for (int k = 0; k < 3; k++) v[k] = fd * r0[k] + gd * v0[k];
+}
+
+// Time to the next pericentre (0: not approaching it) and the period (inf
+// unless bound): mean anomaly from the eccentric (hyperbolic) anomaly;
+// Barker's equation near e = 1.
+__device__ int kep_peri(double mu, const double r[3], const double v[3], double *dt_peri,
+                        double *period) {
+  const double rn = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  const double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  const double rv = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
+  *period = __longlong_as_double(0x7ff0000000000000ll);
+  if (rv >= 0.0) return 0;
+  const double alpha = 2.0 / rn - v2 / mu;
+  const double h0 = r[1] * v[2] - r[2] * v[1], h1 = r[2] * v[0] - r[0] * v[2],
+               h2 = r[0] * v[1] - r[1] * v[0];
+  const double p = (h0 * h0 + h1 * h1 + h2 * h2) / mu;
+  const double e = sqrt(fmax(0.0, 1.0 - p * alpha));
+  if (fabs(alpha) * rn < 1e-8 || e < 1e-12) {
+    const double D = rv / sqrt(mu * p);
+    *dt_peri = -0.5 * sqrt(p * p * p / mu) * (D + D * D * D / 3.0);
+    if (alpha > 0.0) *period = 2.0 * M_PI / sqrt(mu * alpha * alpha * alpha);
+    return *dt_peri > 0.0;
+  }
+  double M, n;
+  if (alpha > 0.0) {
+    const double a = 1.0 / alpha;
+    const double E = atan2(rv / (e * sqrt(mu * a)), (1.0 - rn * alpha) / e);
+    M = E - e * sin(E);
+    n = sqrt(mu * alpha * alpha * alpha);
+    *period = 2.0 * M_PI / n;
+  } else {
+    const double sF = rv / (e * sqrt(-mu / alpha));
+    M = e * sF - asinh(sF);
+    n = sqrt(-mu * alpha * alpha * alpha);
+  }
+  if (M >= 0.0) return 0;
+  *dt_peri = -M / n;
+  return 1;
+}
+
+__device__ __forceinline__ double dist3(const double a[3], const double b[3]) {
+  const double d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2];
+  return sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+}
+
+// The relative state of a binary at time t (frozen when fully unperturbed).
+__device__ __forceinline__ void bin_rel(const BinRec &b, double t, double r[3], double v[3]) {
+  if (b.full) {
+    for (int k = 0; k < 3; k++) r[k] = b.r0[k], v[k] = b.v0[k];
+  } else {
+    kep_prop(b.mi + b.mj, b.r0, b.v0, t - b.t0, r, v);
+  }
+}
+
+// Tidal potential of the other top-level nodes on leaves (xi, xj) around
+// the centre of mass xc (smallN_unpert.cc:17-40); node positions in S.A.d.
+__device__ double tidal_pot(const UnpSmem &S, int n, int li, int lj, double mi, double mj,
+                            const double xi[3], const double xj[3], const double xc[3]) {
+  double phi = 0.0;
+  for (int k = 0; k < n; k++) {
+    if (S.nd[k] != k || k == li || k == lj) continue;
+    phi += S.nm[k] * (-mi / dist3(xi, S.A.d.pp[k]) - mj / dist3(xj, S.A.d.pp[k]) +
+                      (mi + mj) / dist3(xc, S.A.d.pp[k]));
+  }
+  return phi;
+}
+
+template <int MODE>
+__device__ __forceinline__ void unp_store_leaf(UnpSmem &S, int s, const double x[3],
+                                               const double v[3]) {
+  if (MODE == MODE_SPLIT) {
+    for (int k = 0; k < 3; k++) {
+      const float h = __double2float_rn(x[k]);
+      S.A.f.ph[s][k] = h;
+      S.A.f.pl[s][k] = __double2float_rn(x[k] - (double)h);
+      S.A.f.vf[s][k] = __double2float_rn(v[k]);
+    }
+  } else {
+    for (int k = 0; k < 3; k++) S.A.d.pp[s][k] = x[k], S.A.d.pv[s][k] = v[k];
+  }
+}
+
+// Resolved forces on the top-level nodes from the predicted states in B:
+// returns the system's min step^2 (warp-uniform) and the node pair setting it.
+template <int MODE>
+__device__ double unp_forces(UnpSmem &S, int n, int lane, Body B[2], double t, int *imin,
+                             int *jmin) {
+  __syncwarp();
+  // publish: node slots of this lane (singles: their leaf; leaders: both leaves)
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int s = lane + 32 * q;
+    if (s >= n || S.nd[s] != s) continue;
+    for (int k = 0; k < 3; k++) {
+      S.cv[s][k] = B[q].pv[k];
+      S.cvf[s][k] = __double2float_rn(B[q].pv[k]);
+    }
+    S.nm[s] = B[q].m;
+    int qb = -1;
+    for (int b = 0; b < S.nb; b++)
+      if (S.bin[b].li == s) qb = b;
+    if (qb < 0) {
+      unp_store_leaf<MODE>(S, s, B[q].pp, B[q].pv);
+    } else {
+      const BinRec &bb = S.bin[qb];
+      double r[3], v[3], xi[3], vi[3], xj[3], vj[3];
+      bin_rel(bb, t, r, v);
+      const double M = bb.mi + bb.mj, fi = bb.mj / M, fj = bb.mi / M;
+      for (int k = 0; k < 3; k++) {
+        xi[k] = B[q].pp[k] - fi * r[k];
+        vi[k] = B[q].pv[k] - fi * v[k];
+        xj[k] = B[q].pp[k] + fj * r[k];
+        vj[k] = B[q].pv[k] + fj * v[k];
+      }
+      unp_store_leaf<MODE>(S, bb.li, xi, vi);
+      unp_store_leaf<MODE>(S, bb.lj, xj, vj);
+    }
+  }
+  __syncwarp();
+  double ts2 = __longlong_as_double(0x7ff0000000000000ll);
+  int pmin = 0x7fffffff;  // node pair id a * MAXN + b (a < b) of ts2
+  double la[2][3], lj[2][3];
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int i = lane + 32 * q;
+    for (int k = 0; k < 3; k++) la[q][k] = lj[q][k] = 0.0;
+    if (i >= n) continue;
+    const int ni = S.nd[i];
+    if (MODE == MODE_SPLIT) {
+      float a[3] = {0.f, 0.f, 0.f}, jk[3] = {0.f, 0.f, 0.f};
+      for (int j = 0; j < n; j++) {
+        const int nj = S.nd[j];
+        if (nj == ni) continue;
+        float dx[3], dv[3], dc[3];
+        for (int k = 0; k < 3; k++) {
+          dx[k] = __fadd_rn(__fsub_rn(S.A.f.ph[j][k], S.A.f.ph[i][k]),
+                            __fsub_rn(S.A.f.pl[j][k], S.A.f.pl[i][k]));
+          dv[k] = S.A.f.vf[j][k] - S.A.f.vf[i][k];
+          dc[k] = S.cvf[nj][k] - S.cvf[ni][k];
+        }
+        const float d2 = fmaf(dx[2], dx[2], fmaf(dx[1], dx[1], dx[0] * dx[0]));
+        const float v2 = fmaf(dc[2], dc[2], fmaf(dc[1], dc[1], dc[0] * dc[0]));
+        const float mt = (float)(S.nm[ni] + S.nm[nj]);
+        float ts;
+        if (d2 >= 1e-18f) {
+          const float rinv = rsqrt_approx(d2);
+          const float rinv2 = rinv * rinv;
+          const float f = S.mf[j] * rinv * rinv2;
+          const float xv = fmaf(dx[2], dv[2], fmaf(dx[1], dv[1], dx[0] * dv[0]));
+          const float a3 = -3.0f * xv * rinv2;
+          for (int k = 0; k < 3; k++) {
+            a[k] = fmaf(f, dx[k], a[k]);
+            jk[k] = fmaf(f, fmaf(a3, dx[k], dv[k]), jk[k]);
+          }
+          ts = fminf(__fdividef(0.5f * d2 * (d2 * rinv), mt), __fdividef(d2, v2));
+        } else {  // too close for FP32: FP64
+          double X[3], W[3];
+          for (int k = 0; k < 3; k++) X[k] = (double)dx[k], W[k] = (double)dv[k];
+          const double dd2 = X[0] * X[0] + X[1] * X[1] + X[2] * X[2];
+          const double d = sqrt(dd2), ri2 = 1.0 / dd2, fd = S.m[j] * ri2 / d;
+          const double a3 = -3.0 * (X[0] * W[0] + X[1] * W[1] + X[2] * W[2]) * ri2;
+          for (int k = 0; k < 3; k++) {
+            la[q][k] += fd * X[k];
+            lj[q][k] += fd * (a3 * X[k] + W[k]);
+          }
+          ts = (float)fmin(0.5 * dd2 * d / (double)mt, dd2 / (double)v2);
+        }
+        const int pid = ni < nj ? ni * MAXN + nj : nj * MAXN + ni;
+        if ((double)ts < ts2 || ((double)ts == ts2 && pid < pmin)) {
+          ts2 = (double)ts;
+          pmin = pid;
+        }
+      }
+      for (int k = 0; k < 3; k++) la[q][k] += (double)a[k], lj[q][k] += (double)jk[k];
+    } else {
+      for (int j = 0; j < n; j++) {
+        const int nj = S.nd[j];
+        if (nj == ni) continue;
+        double dx[3], dv[3], dc[3];
+        for (int k = 0; k < 3; k++) {
+          dx[k] = S.A.d.pp[j][k] - S.A.d.pp[i][k];
+          dv[k] = S.A.d.pv[j][k] - S.A.d.pv[i][k];
+          dc[k] = S.cv[nj][k] - S.cv[ni][k];
+        }
+        const double d2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+        const double rinv = rsqrt64(d2);
+        const double rinv2 = rinv * rinv;
+        const double f = S.m[j] * rinv * rinv2;
+        const double a3 = -3.0 * (dx[0] * dv[0] + dx[1] * dv[1] + dx[2] * dv[2]) * rinv2;
+        for (int k = 0; k < 3; k++) {
+          la[q][k] = fma(f, dx[k], la[q][k]);
+          lj[q][k] = fma(f, fma(a3, dx[k], dv[k]), lj[q][k]);
+        }
+        const double v2 = dc[0] * dc[0] + dc[1] * dc[1] + dc[2] * dc[2];
+        const double d3 = d2 * d2 * rinv;
+        const double ts = fmin(0.5 * d3 / (S.nm[ni] + S.nm[nj]), d2 / v2);
+        const int pid = ni < nj ? ni * MAXN + nj : nj * MAXN + ni;
+        if (ts < ts2 || (ts == ts2 && pid < pmin)) {
+          ts2 = ts;
+          pmin = pid;
+        }
+      }
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int i = lane + 32 * q;
+    if (i < n)
+      for (int k = 0; k < 3; k++) S.la[i][k] = la[q][k], S.lj[i][k] = lj[q][k];
+  }
+  __syncwarp();
+  // node forces: mass-weighted leaf forces
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int s = lane + 32 * q;
+    for (int k = 0; k < 3; k++) B[q].acc[k] = B[q].jerk[k] = 0.0;
+    if (s >= n || S.nd[s] != s) continue;
+    int qb = -1;
+    for (int b = 0; b < S.nb; b++)
+      if (S.bin[b].li == s) qb = b;
+    if (qb < 0) {
+      for (int k = 0; k < 3; k++) B[q].acc[k] = S.la[s][k], B[q].jerk[k] = S.lj[s][k];
+    } else {
+      const BinRec &bb = S.bin[qb];
+      const double M = bb.mi + bb.mj;
+      for (int k = 0; k < 3; k++) {
+        B[q].acc[k] = (bb.mi * S.la[bb.li][k] + bb.mj * S.la[bb.lj][k]) / M;
+        B[q].jerk[k] = (bb.mi * S.lj[bb.li][k] + bb.mj * S.lj[bb.lj][k]) / M;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ot = __shfl_xor_sync(0xffffffffu, ts2, o);
+    const int op = __shfl_xor_sync(0xffffffffu, pmin, o);
+    if (ot < ts2 || (ot == ts2 && op < pmin)) {
+      ts2 = ot;
+      pmin = op;
+    }
+  }
+  *imin = pmin == 0x7fffffff ? -1 : pmin / MAXN;
+  *jmin = pmin == 0x7fffffff ? -1 : pmin % MAXN;
+  return ts2;
+}
+
+// Node states (after a step) into shared memory for the tree logic: positions
+// and velocities in A.d, accelerations in la, masses in nm.
+__device__ __forceinline__ void unp_publish_nodes(UnpSmem &S, int n, int lane, const Body B[2]) {
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int s = lane + 32 * q;
+    if (s >= n || S.nd[s] != s) continue;
+    for (int k = 0; k < 3; k++) {
+      S.A.d.pp[s][k] = B[q].pos[k];
+      S.A.d.pv[s][k] = B[q].vel[k];
+      S.la[s][k] = B[q].acc[k];
+    }
+    S.nm[s] = B[q].m;
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ void body_set(Body &b, double m, const double x[3], const double v[3]) {
+  b.m = m;
+  b.inv_m = 1.0 / m;
+  for (int k = 0; k < 3; k++) {
+    b.pos[k] = b.pp[k] = x[k];
+    b.vel[k] = b.pv[k] = v[k];
+    b.oacc[k] = b.ojerk[k] = 0.0;  // a node the tree has just made
+  }
+}
+
+// The tree changes after a step (smallN.cc:1022-1060): binary creation from
+// the pair that set the step, then the end of every segment due now.  Every
+// lane evaluates the same decisions from shared data; lane 0 writes the
+// shared records, the owners of the slots update their bodies.  Returns 0
+// (no change), 1 (changed), 3 (changed, a binary made).
+__device__ int unp_tree(UnpSmem &S, int n, int lane, Body B[2], double t, double dt_nat, int bim,
+                        int bjm, const UnpParams &P) {
+  unp_publish_nodes(S, n, lane, B);
+  int changed = 0;
+  // --- creation (is_unperturbed_and_approaching, create_binary)
+  if (bim >= 0 && S.nb < NB && dt_nat <= P.dt_crit) {
+    bool leaves = true;
+    for (int b = 0; b < S.nb; b++)
+      if (S.bin[b].li == bim || S.bin[b].li == bjm) leaves = false;
+    const int i = bim, j = bjm;
+    const double *xi = S.A.d.pp[i], *xj = S.A.d.pp[j], *vi = S.A.d.pv[i], *vj = S.A.d.pv[j];
+    double r[3], v[3];
+    for (int k = 0; k < 3; k++) r[k] = xj[k] - xi[k], v[k] = vj[k] - vi[k];
+    const double d2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    const double rv = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
+    if (leaves && d2 <= P.r2_crit && rv <= 0.0) {
+      const double mi = S.nm[i], mj = S.nm[j], M = mi + mj;
+      double cm[3], cmv[3];
+      for (int k = 0; k < 3; k++) {
+        cm[k] = (mi * xi[k] + mj * xj[k]) / M;
+        cmv[k] = (mi * vi[k] + mj * vj[k]) / M;
+      }
+      double maxp = 0.0, nnd2 = 0.0, mk = 0.0;
+      for (int k2 = 0; k2 < n; k2++) {
+        if (S.nd[k2] != k2 || k2 == i || k2 == j) continue;
+        double e2 = 0.0;
+        for (int k = 0; k < 3; k++) e2 += (S.A.d.pp[k2][k] - cm[k]) * (S.A.d.pp[k2][k] - cm[k]);
+        const double p2 = S.nm[k2] * S.nm[k2] / e2;
+        if (p2 > maxp) maxp = p2, nnd2 = e2, mk = S.nm[k2];
+      }
+      bool unp = true;
+      if (maxp > 0.0) {
+        const double q = d2 / nnd2;
+        unp = 4.0 * (mk / M) * (mk / M) * q * q * q < P.gamma2;
+      }
+      double dtp, per;
+      if (unp && kep_peri(M, r, v, &dtp, &per)) {
+        double pxi[3], pxj[3];
+        for (int k = 0; k < 3; k++) pxi[k] = xi[k], pxj[k] = xj[k];
+        const double tid = tidal_pot(S, n, i, j, mi, mj, pxi, pxj, cm);
+        __syncwarp();
+        if (lane == 0) {
+          BinRec &b = S.bin[S.nb];
+          b.li = i;
+          b.lj = j;
+          b.full = 0;
+          b.mi = mi;
+          b.mj = mj;
+          for (int k = 0; k < 3; k++) b.r0[k] = r[k], b.v0[k] = v[k];
+          b.t0 = t;
+          b.tpred = 2.0 * (t + dtp) - t;
+          b.tidal = tid;
+          S.nd[j] = i;
+          S.nm[i] = M;
+          for (int k = 0; k < 3; k++) S.A.d.pp[i][k] = cm[k], S.A.d.pv[i][k] = cmv[k];
+          S.nb++;
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++)
+          if (lane + 32 * q == i) body_set(B[q], M, cm, cmv);
+        __syncwarp();
+        changed = 3;
+      }
+    }
+  }
+  // --- segments ending now (extend_or_end_binary)
+  for (int qb = 0; qb < S.nb; qb++) {
+    const BinRec bb = S.bin[qb];
+    if (bb.tpred > t) continue;
+    const int i = bb.li, j = bb.lj;
+    const double M = bb.mi + bb.mj;
+    double r[3], v[3], xi[3], xj[3], xc[3], vc[3];
+    bin_rel(bb, t, r, v);
+    for (int k = 0; k < 3; k++) xc[k] = S.A.d.pp[i][k], vc[k] = S.A.d.pv[i][k];
+    for (int k = 0; k < 3; k++) {
+      xi[k] = xc[k] - bb.mj / M * r[k];
+      xj[k] = xc[k] + bb.mi / M * r[k];
+    }
+    const double tid = tidal_pot(S, n, i, j, bb.mi, bb.mj, xi, xj, xc);
+    if (!bb.full) {
+      const double mu = bb.mi * bb.mj / M, v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+      const double fac = 1.0 - 2.0 * (tid - bb.tidal) / (mu * v2);
+      if (fac > 0.0) {
+        const double sf = sqrt(fac);
+        for (int k = 0; k < 3; k++) v[k] *= sf;
+      }
+    }
+    const double rn = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    const double alpha = 2.0 / rn - (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / M;
+    double dtp = -1.0, period = __longlong_as_double(0x7ff0000000000000ll);
+    if (P.allow_full && alpha > 0.0) {
+      const double a = 1.0 / alpha;
+      period = 2.0 * M_PI / sqrt(M * alpha * alpha * alpha);
+      dtp = __longlong_as_double(0x7ff0000000000000ll);
+      for (int k2 = 0; k2 < n; k2++) {
+        if (S.nd[k2] != k2 || k2 == i) continue;
+        const double rp = P.gamma_inv3 * a * cbrt(2.0 * S.nm[k2] / M);
+        double dp[3], dvl[3], da[3];
+        for (int k = 0; k < 3; k++) {
+          dp[k] = S.A.d.pp[k2][k] - xc[k];
+          dvl[k] = S.A.d.pv[k2][k] - vc[k];
+          da[k] = S.la[k2][k] - S.la[i][k];
+        }
+        const double dr = sqrt(dp[0] * dp[0] + dp[1] * dp[1] + dp[2] * dp[2]);
+        const double vr = (dvl[0] * dp[0] + dvl[1] * dp[1] + dvl[2] * dp[2]) / dr;
+        const double ar = (da[0] * dp[0] + da[1] * dp[1] + da[2] * dp[2]) / dr;
+        const double dd = dr - rp;
+        double tr = 0.0;  // time_to_radius (smallN_unpert.cc:367-392)
+        if (dd > 0.0) {
+          tr = __longlong_as_double(0x7ff0000000000000ll);
+          if (vr < 0.0) tr = -dd / vr;
+          if (ar < 0.0) tr = fmin(tr, sqrt(-2.0 * dd / ar));
+        }
+        if (tr < dtp) dtp = tr;
+        if (tr <= 0.0) break;
+      }
+      dtp *= 0.5;
+    }
+    __syncwarp();
+    if (dtp >= period) {  // extend by whole periods, components frozen
+      if (lane == 0) {
+        BinRec &b = S.bin[qb];
+        b.tpred += floor(dtp / period) * period;
+        b.full = 1;
+        b.tidal = tid;
+        for (int k = 0; k < 3; k++) b.r0[k] = r[k], b.v0[k] = v[k];
+        b.t0 = t;
+      }
+      __syncwarp();
+      continue;
+    }
+    // dissolve: the components become top-level nodes again
+    double yi[3], yj[3], wi[3], wj[3];
+    for (int k = 0; k < 3; k++) {
+      yi[k] = xc[k] - bb.mj / M * r[k];
+      yj[k] = xc[k] + bb.mi / M * r[k];
+      wi[k] = vc[k] - bb.mj / M * v[k];
+      wj[k] = vc[k] + bb.mi / M * v[k];
+    }
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      if (lane + 32 * q == i) body_set(B[q], bb.mi, yi, wi);
+      if (lane + 32 * q == j) body_set(B[q], bb.mj, yj, wj);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      for (int k = 0; k < 3; k++) {
+        S.A.d.pp[i][k] = yi[k];
+        S.A.d.pv[i][k] = wi[k];
+        S.A.d.pp[j][k] = yj[k];
+        S.A.d.pv[j][k] = wj[k];
+      }
+      S.nd[j] = j;
+      S.nm[i] = bb.mi;
+      S.nm[j] = bb.mj;
+      S.bin[qb] = S.bin[S.nb - 1];
+      S.nb--;
+    }
+    __syncwarp();
+    qb--;
+    changed |= 1;
+  }
+  return changed;
+}
+
+template <int MODE>
+__global__ void batch_unp_kernel(int nsys, const int *__restrict__ order, const int *__restrict__ off,
+                                 const double *__restrict__ t_end_s, const double *__restrict__ mass,
+                                 double *pos, double *vel, double eta, int n_iter,
+                                 long long max_steps, int *queue, double *t_out,
+                                 long long *steps_out, unsigned long long *wall_ns, int *status,
+                                 int *nbin_out, UnpParams P) {
+  __shared__ UnpSmem smem[WARPS_MAX_UNP];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  UnpSmem &S = smem[w];
+  while (true) {
+    int qq0 = 0;
+    if (lane == 0) qq0 = atomicAdd(queue, 1);
+    qq0 = __shfl_sync(0xffffffffu, qq0, 0);
+    if (qq0 >= nsys) break;
+    const int s = order[qq0];
+    unsigned long long t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    const int base = off[s];
+    const int n = off[s + 1] - base;
+    const double t_end = t_end_s[s];
+    if (n < 2 || n > MAXN) {
+      if (lane == 0) {
+        status[s] = 2;
+        steps_out[s] = 0;
+        t_out[s] = 0.0;
+        nbin_out[s] = 0;
+      }
+      continue;
+    }
+    Body B[2];
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const int i = lane + 32 * q;
+      const int ii = i < n ? i : 0;
+      double x[3], v[3];
+      for (int k = 0; k < 3; k++) x[k] = pos[3 * (base + ii) + k], v[k] = vel[3 * (base + ii) + k];
+      body_set(B[q], mass[base + ii], x, v);
+      if (i < n) {
+        S.m[i] = B[q].m;
+        S.mf[i] = __double2float_rn(B[q].m);
+        S.nd[i] = i;
+      }
+    }
+    if (lane == 0) S.nb = 0;
+    __syncwarp();
+    int bim, bjm, made = 0;
+    double t = 0.0;
+    double dt = eta * sqrt(unp_forces<MODE>(S, n, lane, B, t, &bim, &bjm));
+    long long nsteps = 0;
+    int st = 0;
+    while (t < t_end) {
+      if (nsteps >= max_steps) {
+        st = 1;
+        break;
+      }
+      double lim = __longlong_as_double(0x7ff0000000000000ll);
+      for (int b = 0; b < S.nb; b++) lim = fmin(lim, S.bin[b].tpred - t);
+      int nit = n_iter;
+      if (dt >= lim) {
+        dt = lim;
+        nit = 0;
+      }
+      // predict_loworder (hdyn.h:192-201: with the stored old force)
+      const double h = dt, h3 = h / 3.0, h2 = h * 0.5;
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        if (lane + 32 * q >= n || S.nd[lane + 32 * q] != lane + 32 * q) continue;
+        for (int k = 0; k < 3; k++) {
+          const double oj = B[q].ojerk[k], oa = B[q].oacc[k];
+          B[q].pp[k] = fma(fma(fma(oj, h3, oa), h2, B[q].vel[k]), h, B[q].pos[k]);
+          B[q].pv[k] = fma(fma(oj, h2, oa), h, B[q].vel[k]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 2; q++)
+        for (int k = 0; k < 3; k++) B[q].oacc[k] = B[q].acc[k], B[q].ojerk[k] = B[q].jerk[k];
+      double new_dt = dt, end_dt = dt;
+      for (int it = 0; it <= nit; it++) {
+        const double prev = new_dt;
+        const double ts2 = unp_forces<MODE>(S, n, lane, B, t + new_dt, &bim, &bjm);
+        end_dt = eta * sqrt(ts2);
+        if (it < nit) {
+          new_dt = 0.5 * (dt + end_dt);
+          new_dt = dt + 0.5 * (end_dt - dt) * (new_dt / prev);
+          if (new_dt >= lim) {
+            new_dt = lim;
+            nit = 0;
+          }
+        }
+        const bool cj = new_dt != prev;
+        double tau = 0, tau2 = 0, tau3 = 0, theta = 0, inv_theta = 0;
+        if (cj) {
+          theta = 0.5 * prev;
+          tau = (new_dt - theta) / theta;
+          inv_theta = 1.0 / theta;
+          tau2 = tau * tau;
+          tau3 = tau2 * tau;
+        }
+        const double nd2 = new_dt * new_dt;
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+          Body &b = B[q];
+          for (int k = 0; k < 3; k++) {
+            if (cj) {
+              const double pa = b.acc[k], pj = b.jerk[k], oa = b.oacc[k], oj = b.ojerk[k];
+              b.acc[k] = 0.25 * (oa * (2 - 3 * tau + tau3) + pa * (2 + 3 * tau - tau3) +
+                                 oj * theta * (1 - tau - tau2 + tau3) +
+                                 pj * theta * (-1 - tau + tau2 + tau3));
+              b.jerk[k] = 0.25 * (oa * inv_theta * 3 * (-1 + tau2) + pa * inv_theta * 3 * (1 - tau2) +
+                                  oj * (-1 - 2 * tau + 3 * tau2) + pj * (-1 + 2 * tau + 3 * tau2));
+            }
+            b.pv[k] = b.vel[k] + new_dt * (b.acc[k] + b.oacc[k]) * 0.5 -
+                      nd2 * (b.jerk[k] - b.ojerk[k]) * (1.0 / 12.0);
+            b.pp[k] = b.pos[k] + new_dt * (b.pv[k] + b.vel[k]) * 0.5 -
+                      nd2 * (b.acc[k] - b.oacc[k]) * (1.0 / 12.0);
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 2; q++)
+        for (int k = 0; k < 3; k++) B[q].pos[k] = B[q].pp[k], B[q].vel[k] = B[q].pv[k];
+      dt = end_dt;
+      t = t + new_dt;
+      nsteps++;
+      const int tc = unp_tree(S, n, lane, B, t, dt, bim, bjm, P);
+      if (tc) {
+        if (tc & 2) made++;
+        dt = eta * sqrt(unp_forces<MODE>(S, n, lane, B, t, &bim, &bjm));
+      }
+    }
+    // resolve the binaries left at the end into their components
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const int i = lane + 32 * q;
+      if (i >= n || S.nd[i] != i) continue;
+      int qb = -1;
+      for (int b = 0; b < S.nb; b++)
+        if (S.bin[b].li == i) qb = b;
+      if (qb < 0) {
+        for (int k = 0; k < 3; k++) {
+          pos[3 * (base + i) + k] = B[q].pos[k];
+          vel[3 * (base + i) + k] = B[q].vel[k];
+        }
+      } else {
+        const BinRec &bb = S.bin[qb];
+        double r[3], v[3];
+        bin_rel(bb, t, r, v);
+        const double M = bb.mi + bb.mj;
+        for (int k = 0; k < 3; k++) {
+          pos[3 * (base + bb.li) + k] = B[q].pos[k] - bb.mj / M * r[k];
+          vel[3 * (base + bb.li) + k] = B[q].vel[k] - bb.mj / M * v[k];
+          pos[3 * (base + bb.lj) + k] = B[q].pos[k] + bb.mi / M * r[k];
+          vel[3 * (base + bb.lj) + k] = B[q].vel[k] + bb.mi / M * v[k];
+        }
+      }
+    }
+    if (lane == 0) {
+      unsigned long long t1;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+      t_out[s] = t;
+      steps_out[s] = nsteps;
+      wall_ns[s] = t1 - t0;
+      status[s] = st;
+      nbin_out[s] = made;
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void queue_reset(int *queue) { *queue = 0; }
 
 }  // namespace
@@ -484,5 +1205,37 @@ extern "C" int g6k_batch_launch(int nsys, const int *order, const int *off, cons
   else
     G6_BATCH(MODE_FAST);
 #undef G6_BATCH
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+// The same with smallN's unperturbed binaries (FAST or SPLIT pair terms):
+// dt_crit, r2_crit, gamma and allow_full as smallN's set_dt_crit,
+// set_r2_crit, set_gamma, set_allow_full_unperturbed; nbin_out[s] counts the
+// binaries made in system s.
+extern "C" int g6k_batch_launch_unp(int nsys, const int *order, const int *off,
+                                    const double *t_end, const double *mass, double *pos,
+                                    double *vel, double eta, int n_iter, long long max_steps,
+                                    int mode, int warps_per_cta, int ctas, double dt_crit,
+                                    double r2_crit, double gamma, int allow_full, int *queue,
+                                    double *t_out, long long *steps_out,
+                                    unsigned long long *wall_ns, int *status, int *nbin_out,
+                                    cudaStream_t st) {
+  if (warps_per_cta < 1 || warps_per_cta > WARPS_MAX_UNP || ctas < 1) return -2;
+  if (mode != MODE_FAST && mode != MODE_SPLIT) return -2;
+  UnpParams P;
+  P.dt_crit = dt_crit;
+  P.r2_crit = r2_crit;
+  P.gamma2 = gamma * gamma;
+  P.gamma_inv3 = pow(fmax(P.gamma2, 1e-120), -1.0 / 6.0);
+  P.allow_full = allow_full;
+  queue_reset<<<1, 1, 0, st>>>(queue);
+  if (mode == MODE_SPLIT)
+    batch_unp_kernel<MODE_SPLIT><<<ctas, 32 * warps_per_cta, 0, st>>>(
+        nsys, order, off, t_end, mass, pos, vel, eta, n_iter, max_steps, queue, t_out, steps_out,
+        wall_ns, status, nbin_out, P);
+  else
+    batch_unp_kernel<MODE_FAST><<<ctas, 32 * warps_per_cta, 0, st>>>(
+        nsys, order, off, t_end, mass, pos, vel, eta, n_iter, max_steps, queue, t_out, steps_out,
+        wall_ns, status, nbin_out, P);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }

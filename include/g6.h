@@ -278,6 +278,20 @@ int g6x_batch_run(int nsys, const int *n_per_sys, const double *t_end, const dou
 /* Launch shape of g6x_batch_run: warps (= systems in flight) per CTA and
    CTAs per SM. */
 int g6x_batch_config(int warps_per_cta, int ctas_per_sm);
+/* smallN's unperturbed binaries in the batch (fast and split modes; the
+   exact mode refuses them): after each step the pair that set the step
+   becomes a binary node when approaching, within sqrt(r2_crit), its step
+   below dt_crit and its tidal parameter below gamma (smallN_unpert.cc:
+   44-88); its centre of mass is integrated, its components follow the
+   Kepler orbit to the same separation past pericentre, where the change of
+   the tidal potential is absorbed and the binary is extended by whole
+   periods (allow_full) or dissolved.  smallN's worker defaults: dt_crit
+   1e-3, r2_crit 1e-2, gamma 1e-6, allow_full 1 (src/amuse_ph4/src/hdyn.cc:
+   10-14, src/amuse_smalln/interface.cc:72).  At most 8 binaries per system
+   at a time; with them on, at most 4 warps per CTA.  g6x_batch_binaries
+   reads the number of binaries each system of the last run made. */
+int g6x_batch_unperturbed(int on, double dt_crit, double r2_crit, double gamma, int allow_full);
+int g6x_batch_binaries(int nsys, int *nbin);
 /* Autotuner: time the candidate shapes on the given systems (end times
    scaled by frac; the inputs are not modified) and keep the fastest;
    out = {warps per CTA, CTAs per SM, ms}. */

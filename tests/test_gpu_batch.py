@@ -117,3 +117,85 @@ def test_autotuner(g6):
     assert best["warps_per_cta"] >= 1 and best["ctas_per_sm"] >= 1 and best["ms"] > 0
     r = g6.batch_run(ns, 0.05 * tcr, m, x, v)
     assert np.all(r["status"] == 0)
+
+
+# --- smallN's unperturbed binaries --------------------------------------------
+
+def _unpert_fixture():
+    from conftest import golden
+    g = golden("smalln_unpert.npz")
+    k = int(g["nsys"])
+    ns = np.array([len(g[f"s{i}_mass"]) for i in range(k)], np.int32)
+    cat = lambda key: np.concatenate([g[f"s{i}_{key}"] for i in range(k)])
+    t_end = np.array([float(g[f"s{i}_t_end"]) for i in range(k)])
+    return g, k, ns, cat, t_end
+
+
+@pytest.mark.parametrize("mode", ["fast", "split"])
+def test_unperturbed_binaries_follow_oracle_and_smalln(g6, mode):
+    """Hierarchical systems with hard binaries (tests/golden/smalln_unpert.npz,
+    written by the unmodified smallN with its unperturbed binaries): the batch
+    kernel with the same treatment ends where the oracle's restatement
+    (orc_smalln_unpert) and smallN end, to 1e-4 of the system size (fast:
+    FP64 pair terms; split: FP32 pair terms), having made binaries, in far
+    fewer steps than without them."""
+    g, k, ns, cat, t_end = _unpert_fixture()
+    g6.batch_unperturbed(True)
+    try:
+        r = g6.batch_run(ns, t_end, cat("mass"), cat("pos0"), cat("vel0"), eta=0.14, mode=mode)
+        nbin = g6.batch_binaries(k)
+    finally:
+        g6.batch_unperturbed(False)
+    plain = g6.batch_run(ns, t_end, cat("mass"), cat("pos0"), cat("vel0"), eta=0.14, mode=mode)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    for s in range(k):
+        a, b = off[s], off[s + 1]
+        m, x0, v0 = g[f"s{s}_mass"], g[f"s{s}_pos0"], g[f"s{s}_vel0"]
+        po, vo, to, so, nbo = oracle.smalln_unpert(m, x0, v0, 0.14, t_end[s])
+        scale = np.abs(x0).max()
+        d_or = np.abs(r["pos"][a:b] - po).max() / scale
+        d_ref = np.abs(r["pos"][a:b] - g[f"s{s}_pos"]).max() / scale
+        print(f"system {s} ({mode}): steps {r['steps'][s]} (plain {plain['steps'][s]}, oracle "
+              f"{so}), binaries {nbin[s]} (oracle {nbo}), |dx| vs oracle {d_or:.1e}, "
+              f"vs smallN {d_ref:.1e}")
+        assert r["status"][s] == 0
+        assert nbin[s] >= 1
+        assert d_or <= 1e-4 and d_ref <= 1e-4
+        assert r["steps"][s] < plain["steps"][s]
+
+
+def test_unperturbed_refused_in_exact_mode(g6):
+    g, k, ns, cat, t_end = _unpert_fixture()
+    g6.batch_unperturbed(True)
+    try:
+        with pytest.raises(ag.G6Error, match="exact"):
+            g6.batch_run(ns, t_end, cat("mass"), cat("pos0"), cat("vel0"), mode="exact")
+    finally:
+        g6.batch_unperturbed(False)
+
+
+def test_unperturbed_batching_workload_completes(g6):
+    """The batching configuration's systems (n ~ U[3, 64], Plummer r_vir =
+    1e-3, eps = 0) to 10 crossing times with the unperturbed treatment: no
+    system reaches the step budget, and the per-system energy error stays at
+    the level of the scheme's truncation error."""
+    ns, m, x, v, tcr = _systems(256, 3, 64, seed=9)
+    t_end = np.full(len(ns), 10.0 * tcr)
+    g6.batch_unperturbed(True)
+    try:
+        r = g6.batch_run(ns, t_end, m, x, v, mode="split", max_steps=250_000)
+        nbin = g6.batch_binaries(len(ns))
+    finally:
+        g6.batch_unperturbed(False)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    de = []
+    for s in range(len(ns)):
+        a, b = off[s], off[s + 1]
+        e0 = _energy(m[a:b], x[a:b], v[a:b])
+        de.append(abs((_energy(m[a:b], r["pos"][a:b], r["vel"][a:b]) - e0) / e0))
+    de = np.array(de)
+    print(f"binaries made: {nbin.sum()} in {np.sum(nbin > 0)} systems; |dE/E| median "
+          f"{np.median(de):.2e} p99 {np.percentile(de, 99):.2e} max {de.max():.2e}; steps max "
+          f"{r['steps'].max()}")
+    assert np.all(r["status"] == 0) and np.all(r["t_final"] >= t_end)
+    assert np.all(np.isfinite(de)) and np.median(de) < 1e-3

@@ -52,10 +52,14 @@ def run_batch(args):
     off = np.concatenate([[0], np.cumsum(ns)])
     g6 = ag.G6X(0)
     mode = getattr(args, "batch_mode", "split")
+    # smallN's unperturbed binaries (its default; not in the exact mode)
+    unpert = mode != "exact" and not getattr(args, "no_unpert", False)
+    g6.batch_unperturbed(unpert)
     out = {"workload": f"{args.nsys} few-body systems, n~U[3,64], Plummer r_vir=1e-3, eps=0, "
                        f"t_end=10 t_cross={t_end:.4g}, eta={args.eta}, smallN scheme "
-                       f"(n_iter=2, Kepler criterion), FP64 state, step cap "
-                       f"{args.max_steps}/system", "mode": mode}
+                       f"(n_iter=2, Kepler criterion"
+                       f"{', unperturbed binaries' if unpert else ''}), FP64 state, step cap "
+                       f"{args.max_steps}/system", "mode": mode, "unperturbed_binaries": unpert}
 
     # 1. autotune on 512 systems for 0.5% of the end time
     kt = min(args.nsys, 512)
@@ -76,6 +80,8 @@ def run_batch(args):
     t0 = time.perf_counter()
     r = g6.batch_run(ns, t_end, m, x, v, eta=args.eta, max_steps=args.max_steps, mode=mode)
     wall = time.perf_counter() - t0
+    nbin = g6.batch_binaries(args.nsys) if unpert else np.zeros(args.nsys, np.int32)
+    g6.batch_unperturbed(False)
     done = r["status"] == 0
     de, bad = [], []
     for s_ in range(args.nsys):
@@ -101,9 +107,11 @@ def run_batch(args):
                   "p90": float(np.percentile(r["steps"], 90)),
                   "p99": float(np.percentile(r["steps"], 99)), "max": int(r["steps"].max())},
         "completed": int(done.sum()), "capped": int((r["status"] == 1).sum()),
+        "binaries": {"made": int(nbin.sum()), "systems_with_binaries": int((nbin > 0).sum())},
     })
     print(json.dumps(out), flush=True)
-    sample = dict(ns=ns[:kc], mass=m[sc], pos=x[sc], vel=v[sc], t_end=t_end, off=off[:kc + 1])
+    sample = dict(ns=ns[:kc], mass=m[sc], pos=x[sc], vel=v[sc], t_end=t_end, off=off[:kc + 1],
+                  unpert=unpert)
     return out, sample
 
 
@@ -393,6 +401,7 @@ def main():
     b.add_argument("--max-steps", type=int, default=250_000)
     b.add_argument("--cpu-sample", type=int, default=64)
     b.add_argument("--batch-mode", default="split", choices=["fast", "exact", "split"])
+    b.add_argument("--no-unpert", action="store_true")
     d = sub.add_parser("adjoint")
     d.add_argument("--n", type=int, default=16384)
     d.add_argument("--nsteps", type=int, default=256)

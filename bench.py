@@ -88,6 +88,8 @@ def parse():
     ap.add_argument("--max-steps", type=int, default=250_000)
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--batch-mode", default="split", choices=["fast", "exact", "split"])
+    ap.add_argument("--no-unpert", action="store_true",
+                    help="batch without smallN's unperturbed binaries")
     # adjoint workload
     ap.add_argument("--nsteps", type=int, default=256)
     ap.add_argument("--fd-coords", type=int, default=32)
@@ -465,6 +467,9 @@ def run_secondary(args):
 
         def one(s):
             a, b = off[s], off[s + 1]
+            if smp["unpert"]:
+                return oracle.smalln_unpert(smp["mass"][a:b], smp["pos"][a:b], smp["vel"][a:b],
+                                            args.eta, smp["t_end"], max_steps=args.max_steps)
             return oracle.smalln(smp["mass"][a:b], smp["pos"][a:b], smp["vel"][a:b], args.eta,
                                  smp["t_end"], max_steps=args.max_steps)
 
@@ -475,7 +480,8 @@ def run_secondary(args):
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {
             "value": (len(off) - 1) / dt, "unit": "systems/s", "cores": threads, "kind": "port",
-            "sample": f"the first {len(off) - 1} systems (smallN restated in "
+            "sample": f"the first {len(off) - 1} systems (smallN"
+                      f"{' with unperturbed binaries' if smp['unpert'] else ''} restated in "
                       f"oracle/g6_oracle.c, same step cap), {dt:.1f} s"}
     else:
         args.seed = 7 if args.seed is None else args.seed

@@ -65,8 +65,14 @@ namespace {
 #ifndef G6_IPT
 #define G6_IPT 2
 #endif
+#ifndef G6_UNROLL_NN
+#define G6_UNROLL_NN 4  // j-loop unroll factor of the nearest-neighbour variant
+#endif
+#ifndef G6_ACHUNK
+#define G6_ACHUNK 0  // split: fold the acceleration partials with the jerk's
+#endif
 #ifndef G6_UNROLL
-#define G6_UNROLL 4
+#define G6_UNROLL 8
 #endif
 #ifndef G6_MINB
 #define G6_MINB 3
@@ -92,7 +98,8 @@ constexpr int TJ = G6_TILE;  // j records per tile
 // twice the registers per i, so it holds fewer i than the FP64 kernel.
 constexpr int IPT_SPLIT = G6_IPT;
 constexpr int IPT_F64 = G6_IPT_F64;
-constexpr int UNROLL = G6_UNROLL;  // j-loop unroll factor
+constexpr int UNROLL = G6_UNROLL;  // j-loop unroll factor (the best measured:
+                                    // 8 plain, 4 with the nearest neighbour)
 constexpr int JLMAX = TJ < NT ? TJ : NT;  // j-lanes per i at most
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound per wait
 constexpr unsigned long long STALL_TEST_NS = 20000000ull;  // 20 ms under the test hook
@@ -193,6 +200,13 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return y;
 }
 
+// max(a, b, c) in one ALU instruction (3-input max.f32).
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // ------------------------------------------------------- float-float ---
 // Knuth TwoSum folded into a (hi, lo) accumulator.
 __device__ __forceinline__ void ff_acc(float &hi, float &lo, float p) {
@@ -225,18 +239,21 @@ struct SplitP {
   struct I {  // i values duplicated into both halves
     f2x xh, yh, zh, xl, yl, zl, vx, vy, vz;
   };
-  struct Part {  // per-fold-period partial sums, one per half
+  struct Part {  // per-fold-period partial sums, one per half; maxima of m/r, 1/r
     f2x a[3], j[3], p, s;
+    float mp, r1;
   };
-  struct Tot {  // compensated totals (s: plain sum, an estimate)
-    float ah[3], al[3], jh[3], jl[3], ph, pl, s;
+  struct Tot {  // compensated totals (s: plain sum, an estimate), maxima
+    float ah[3], al[3], jh[3], jl[3], ph, pl, s, mp, r1;
   };
   struct Out {  // partial record exchanged between CTAs, 72 B
     float2 a[3], j[3], p;
     float nnr2;   // smallest nearest-neighbour key (r^2 + eps^2, FP32)
     float nnr2b;  // second smallest key over the other j
     float s1;     // sum of m / (r^2 + eps^2): the condition number's numerator
+    float mt;     // max m / r times max 1/r (softened): bounds the largest term
     int nn;
+    int pad;
   };
   __device__ static void split(double d, float &h, float &l) {
     h = __double2float_rn(d);
@@ -270,12 +287,13 @@ struct SplitP {
     for (int k = 0; k < 3; k++) q.a[k] = q.j[k] = 0ull;
     q.p = 0ull;
     q.s = 0ull;
+    q.mp = q.r1 = 0.f;
   }
   __device__ static void zero(Tot &t) {
 #pragma unroll
     for (int k = 0; k < 3; k++) t.ah[k] = t.al[k] = t.jh[k] = t.jl[k] = 0.f;
     t.ph = t.pl = 0.f;
-    t.s = 0.f;
+    t.s = t.mp = t.r1 = 0.f;
   }
   __device__ static void fold(Tot &t, const Part &q) {
 #pragma unroll
@@ -288,6 +306,8 @@ struct SplitP {
     ff_acc(t.ph, t.pl, f2_lo(q.p));
     ff_acc(t.ph, t.pl, f2_hi(q.p));
     t.s += G6_S1_HALF ? 2.f * f2_lo(q.s) : f2_lo(q.s) + f2_hi(q.s);
+    t.mp = fmaxf(t.mp, q.mp);
+    t.r1 = fmaxf(t.r1, q.r1);
   }
   // r^2 + eps^2 of both j of a record (the nearest-neighbour key): the main
   // loop and the re-scan use this same arithmetic, so the keys are
@@ -357,6 +377,10 @@ struct SplitP {
     q.j[2] = f2_fma(mr3i, f2_fma(a3, dz, dvz), q.j[2]);
     q.p = f2_add(q.p, mri);
     if (!HJ && G6_S1) {
+      // the largest single term m/(r^2+eps^2) is at most max(m rinv) max(rinv):
+      // two 3-input maxima on the ALU pipe
+      q.r1 = fmax3(q.r1, ra, rb);
+      q.mp = fmax3(q.mp, f2_lo(mri), f2_hi(mri));
       if (G6_S1_HALF)  // one scalar FMA (half the FMA-pipe cycles of a packed one)
         q.s = f2_pack(fmaf(f2_lo(mri), ra, f2_lo(q.s)), 0.f);
       else
@@ -395,6 +419,11 @@ struct SplitP {
       ff_acc(t.jh[k], t.jl[k], f2_lo(q.j[k]));
       ff_acc(t.jh[k], t.jl[k], f2_hi(q.j[k]));
       q.j[k] = 0ull;
+      if (G6_ACHUNK) {
+        ff_acc(t.ah[k], t.al[k], f2_lo(q.a[k]));
+        ff_acc(t.ah[k], t.al[k], f2_hi(q.a[k]));
+        q.a[k] = 0ull;
+      }
     }
   }
   __device__ static f2x eps(double eps2) {
@@ -411,7 +440,9 @@ struct SplitP {
     o.nnr2 = nnr2;
     o.nnr2b = nnr2b;
     o.s1 = t.s;
+    o.mt = t.mp * t.r1;
     o.nn = nn;
+    o.pad = 0;
   }
   __device__ static void merge(Out &a, const Out &b) {
 #pragma unroll
@@ -421,6 +452,7 @@ struct SplitP {
     }
     ff_add(a.p.x, a.p.y, b.p.x, b.p.y);
     a.s1 += b.s1;
+    a.mt = fmaxf(a.mt, b.mt);
     // second smallest of the four keys: min(max of the minima, min of the seconds)
     const float m2 = fminf(fmaxf(a.nnr2, b.nnr2), fminf(a.nnr2b, b.nnr2b));
     if (b.nnr2 < a.nnr2 || (b.nnr2 == a.nnr2 && b.nn < a.nn)) {
@@ -670,7 +702,10 @@ struct KParams {
 // acceleration grows with the condition number of its sum,
 // kappa = sum m / (r^2 + eps^2) / |a| (about 1e-8 kappa at N = 2^20; the
 // particles near the centre of a cluster, where the pulls cancel, reach
-// kappa ~ 100-300).  i-particles with kappa above the caller's limit are
+// kappa ~ 100-300), and with the largest single term over |a|, whose own
+// error does not average out (a massive neighbour pulling against the rest
+// of the cluster).  i-particles with kappa above the caller's limit, or
+// with a largest term (bounded by max m/r times max 1/r) above MU0 |a|, are
 // queued too, and refine_kernel recomputes their acceleration and potential
 // in FP64 from the same records (double-single positions exact in FP64); the
 // jerk keeps its split value.
@@ -685,6 +720,11 @@ constexpr int RCHMAX = 64;     // j-chunks per entry at most
 constexpr int RNT = 256;       // refine_kernel threads per CTA
 constexpr int XTMAX = 8192;    // i-groups (grid.x) whose split merge runs in the force kernel
 enum { REF_ACC = 1, REF_NN = 2 };
+// Largest single term over |a| above which the sum is redone in FP64: a
+// term carries up to ~5e-7 relative error (three times the 1.25e-7 of the
+// MUFU reciprocal square root, measured over all FP32 inputs in [1, 4), plus
+// roundings), so a term of 1.5 |a| alone can cost ~7e-7.
+constexpr double MU0 = 1.5;
 
 struct RefHdr {
   unsigned count;     // entries queued by this call (reset by refine_kernel)
@@ -770,8 +810,8 @@ __device__ __noinline__ void SplitP::finish(const Out &o, int i, const KParams &
       const double a = (double)o.a[k].x + (double)o.a[k].y;
       a2 += a * a;
     }
-    const double s1 = (double)o.s1;
-    if (s1 * s1 > kp.kappa2 * a2) mode |= REF_ACC;
+    const double s1 = (double)o.s1, mt = (double)o.mt;
+    if (s1 * s1 > kp.kappa2 * a2 || mt * mt > MU0 * MU0 * a2) mode |= REF_ACC;
   }
   const int nn = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
   if (kp.want_nn) {
@@ -936,7 +976,8 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
     if (!slow) {
 #pragma unroll 1
       for (int ub = 0; ub < JPT; ub += JCHUNK) {
-#pragma unroll UNROLL
+        constexpr int UNR = NN ? G6_UNROLL_NN : UNROLL;
+#pragma unroll UNR
         for (int u = ub; u < ub + JCHUNK; u++) {
           const Rec r = tile[jl + JL * u];
 #pragma unroll

@@ -51,7 +51,7 @@ EXT_SYMBOLS = [
     "g6x_test_wait_expiry", "g6x_batch_unperturbed", "g6x_batch_binaries", "g6x_set_npipes", "g6x_last_error", "g6x_load",
     "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
     "g6x_energy", "g6x_run_stats", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
-    "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stream",
+    "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stats_n", "g6x_stream",
     "g6x_set_fixed_jerk", "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp",
     "g6x_fixed_step_adjoint", "g6x_fixed_run", "g6x_fixed_adjoint_run",
     "g6x_set_encounters", "g6x_set_radius", "g6x_encounter", "g6x_knn",
@@ -131,6 +131,7 @@ def load():
     lib.g6x_system_time.restype = D
     lib.g6x_timing.argtypes = [I]
     lib.g6x_stats.argtypes = [_pd]
+    lib.g6x_stats_n.argtypes = [_pd, ctypes.c_int]
     lib.g6x_stream.restype = _vp
     lib.g6x_set_fixed_jerk.argtypes = [I]
     lib.g6x_fixed_force.argtypes = [I, D] + [_vp] * 5
@@ -489,9 +490,10 @@ class G6X(G6):
         self.lib.g6x_timing(1 if on else 0)
 
     def stats(self):
-        out = np.zeros(8)
-        self.lib.g6x_stats(_ptr(out, ctypes.c_double))
-        keys = ["predict_ms", "force_ms", "pairs", "jl", "nsplit", "grid_x", "predict_bytes", "nj"]
+        out = np.zeros(10)
+        self.lib.g6x_stats_n(_ptr(out, ctypes.c_double), 10)
+        keys = ["predict_ms", "force_ms", "pairs", "jl", "nsplit", "grid_x", "predict_bytes", "nj",
+                "kernel_ms", "refine_ms"]
         return dict(zip(keys, out.tolist()))
 
     def stream(self):

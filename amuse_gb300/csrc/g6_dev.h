@@ -87,6 +87,9 @@ typedef struct {
      nothing arrives on, with a 20 ms limit, so the bounded wait expires and
      the call ends with the error word set (no trap, no unbounded spin) */
   int stall_test;
+  /* optional: recorded on the stream between the force kernel (with its
+     split-j merge) and the refinement pass, to time the two apart */
+  cudaEvent_t ev_mid;
 } g6_force_args;
 
 /* Size of the refinement buffer (fixed; allocated once per context). */

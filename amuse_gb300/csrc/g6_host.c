@@ -105,7 +105,7 @@ static int idmap_get(const idmap *m, int k) {
 typedef struct {
   int is_open, device, npipes, prec;
   cudaStream_t st;
-  cudaEvent_t ev_done, ev_upd, ev_t0, ev_t1, ev_t2;
+  cudaEvent_t ev_done, ev_upd, ev_t0, ev_t1, ev_t2, ev_tm;
   g6_jstate js;
   /* host mirrors (size cap) */
   int *slot_id, *stage_pos;
@@ -163,6 +163,7 @@ typedef struct {
   /* statistics */
   int timing;
   double st_predict_ms, st_force_ms, st_pairs, st_pred_bytes, st_nj;
+  double st_kernel_ms, st_refine_ms; /* force_ms split at the refinement pass */
   g6_shape shape;
   int predicted_this_call;
   char err[256];
@@ -416,6 +417,7 @@ static int run_force(g6_force_args *a) {
   if (G.timing) {
     if (!G.predicted_this_call) cudaEventRecord(G.ev_t1, G.st);
   }
+  a->ev_mid = G.timing ? G.ev_tm : NULL;
   rc = g6k_force(a, &G.shape, G.st);
   if (rc) {
     seterr("force launch failed (%d)", rc);
@@ -437,6 +439,12 @@ static void collect_timing(void) {
   if (G.predicted_this_call && cudaEventElapsedTime(&ms, G.ev_t0, G.ev_t1) == cudaSuccess)
     G.st_predict_ms = ms;
   if (cudaEventElapsedTime(&ms, G.ev_t1, G.ev_t2) == cudaSuccess) G.st_force_ms = ms;
+  G.st_kernel_ms = G.st_force_ms;
+  G.st_refine_ms = 0;
+  if (cudaEventElapsedTime(&ms, G.ev_t1, G.ev_tm) == cudaSuccess) {
+    G.st_kernel_ms = ms;
+    G.st_refine_ms = G.st_force_ms - ms;
+  }
 }
 
 /* ===================================================== Part 1: g6 ABI === */
@@ -462,6 +470,7 @@ int g6_open_(int *id) {
   CK(cudaEventCreate(&G.ev_t0));
   CK(cudaEventCreate(&G.ev_t1));
   CK(cudaEventCreate(&G.ev_t2));
+  CK(cudaEventCreate(&G.ev_tm));
   G.npipes = G6_DEFAULT_NPIPES;
   const char *e = getenv("G6_NPIPES");
   if (e && atoi(e) > 0 && atoi(e) <= (1 << 20)) G.npipes = atoi(e);
@@ -519,6 +528,7 @@ int g6_close_(int *id) {
   cudaFree(G.d_refine);
   cudaEventDestroy(G.ev_done); cudaEventDestroy(G.ev_upd);
   cudaEventDestroy(G.ev_t0); cudaEventDestroy(G.ev_t1); cudaEventDestroy(G.ev_t2);
+  cudaEventDestroy(G.ev_tm);
   cudaStreamDestroy(G.st);
   free(G.slot_id);
   free(G.stage_pos);
@@ -972,21 +982,19 @@ int g6x_timing(int on) {
   G.timing = on ? 1 : 0;
   return 0;
 }
-int g6x_stats(double out[8]) {
+int g6x_stats_n(double *out, int n) {
+  if (!out || n < 0) return G6_ERR_ARG;
   if (G.timing && G.is_open) {
     cudaEventSynchronize(G.ev_t2);
     collect_timing();
   }
-  out[0] = G.st_predict_ms;
-  out[1] = G.st_force_ms;
-  out[2] = G.st_pairs;
-  out[3] = G.shape.jl;
-  out[4] = G.shape.nsplit;
-  out[5] = G.shape.grid_x;
-  out[6] = G.st_pred_bytes;
-  out[7] = G.st_nj;
+  const double v[10] = {G.st_predict_ms, G.st_force_ms, G.st_pairs, G.shape.jl,
+                        G.shape.nsplit,  G.shape.grid_x, G.st_pred_bytes, G.st_nj,
+                        G.st_kernel_ms,  G.st_refine_ms};
+  for (int k = 0; k < n && k < 10; k++) out[k] = v[k];
   return 0;
 }
+int g6x_stats(double out[8]) { return g6x_stats_n(out, 8); }
 
 int g6x_load(int n, const int *ids, const double *mass, const double (*x)[3],
              const double (*v)[3], const double (*acc)[3], const double (*jerk)[3],
@@ -1650,6 +1658,7 @@ int g6x_force_dev_noalloc(double ti, double eps2, int nj, int ni, const double *
   refine_args(&a); /* fixed buffer, allocated at open */
   size_t need = 0;
   if (G.timing && !G.predicted_this_call) cudaEventRecord(G.ev_t1, G.st);
+  a.ev_mid = G.timing ? G.ev_tm : NULL;
   rc = g6k_force_static(&a, G.d_static, &G.shape, G.st, &need);
   if (rc == -4) {
     seterr("g6x_force_dev_noalloc: ni=%d, nj=%d needs %zu B of split-j scratch, more than the "

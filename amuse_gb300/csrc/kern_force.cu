@@ -89,9 +89,6 @@ namespace {
 #ifndef G6_S1
 #define G6_S1 1  // split: accumulate the condition number's sum
 #endif
-#ifndef G6_S1_HALF
-#define G6_S1_HALF 0  // split: sum over the even j of each record pair only (x2)
-#endif
 constexpr int NT = G6_NT;    // threads per CTA
 constexpr int TJ = G6_TILE;  // j records per tile
 // i-particles per thread: the split kernel's packed f32x2 pair terms need
@@ -200,10 +197,16 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return y;
 }
 
-// max(a, b, c) in one ALU instruction (3-input max.f32).
+// max(a, b, c) and min(a, b, c) in one ALU instruction each (3-input
+// max.f32 / min.f32).
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
   float r;
   asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
   return r;
 }
 
@@ -239,12 +242,11 @@ struct SplitP {
   struct I {  // i values duplicated into both halves
     f2x xh, yh, zh, xl, yl, zl, vx, vy, vz;
   };
-  struct Part {  // per-fold-period partial sums, one per half; maxima of m/r, 1/r
+  struct Part {  // per-fold-period partial sums, one per half
     f2x a[3], j[3], p, s;
-    float mp, r1;
   };
-  struct Tot {  // compensated totals (s: plain sum, an estimate), maxima
-    float ah[3], al[3], jh[3], jl[3], ph, pl, s, mp, r1;
+  struct Tot {  // compensated totals (s: plain sum, an estimate), largest chunk of s
+    float ah[3], al[3], jh[3], jl[3], ph, pl, s, mt, pad;  // 17 words: odd stride
   };
   struct Out {  // partial record exchanged between CTAs, 72 B
     float2 a[3], j[3], p;
@@ -287,13 +289,12 @@ struct SplitP {
     for (int k = 0; k < 3; k++) q.a[k] = q.j[k] = 0ull;
     q.p = 0ull;
     q.s = 0ull;
-    q.mp = q.r1 = 0.f;
   }
   __device__ static void zero(Tot &t) {
 #pragma unroll
     for (int k = 0; k < 3; k++) t.ah[k] = t.al[k] = t.jh[k] = t.jl[k] = 0.f;
     t.ph = t.pl = 0.f;
-    t.s = t.mp = t.r1 = 0.f;
+    t.s = t.mt = 0.f;
   }
   __device__ static void fold(Tot &t, const Part &q) {
 #pragma unroll
@@ -305,9 +306,15 @@ struct SplitP {
     }
     ff_acc(t.ph, t.pl, f2_lo(q.p));
     ff_acc(t.ph, t.pl, f2_hi(q.p));
-    t.s += G6_S1_HALF ? 2.f * f2_lo(q.s) : f2_lo(q.s) + f2_hi(q.s);
-    t.mp = fmaxf(t.mp, q.mp);
-    t.r1 = fmaxf(t.r1, q.r1);
+    fold_s(t, q);
+  }
+  // The condition number's sum arrives in chunks of at most 32 j per half
+  // (the jerk fold period): the largest chunk bounds the largest single term
+  // m / (r^2 + eps^2) from above, for the price of one 3-input maximum per
+  // chunk rather than per pair.
+  __device__ static __forceinline__ void fold_s(Tot &t, const Part &q) {
+    t.s += f2_lo(q.s) + f2_hi(q.s);
+    t.mt = fmax3(t.mt, f2_lo(q.s), f2_hi(q.s));
   }
   // r^2 + eps^2 of both j of a record (the nearest-neighbour key): the main
   // loop and the re-scan use this same arithmetic, so the keys are
@@ -325,7 +332,7 @@ struct SplitP {
   // interface.cc:440-449,469-486): the (r.v) factor divided by the
   // UNsoftened r^2.
   //
-  // NN keeps the smallest key of the tile (nnmin, one FMNMX per j); the
+  // NN keeps the smallest key of the tile (nnmin, one 3-input minimum per j pair); the
   // kernel turns the tile minima into the smallest and second smallest key
   // over all j, whose gap decides whether the FP32 argmin is provably ph4's
   // FP64 nearest neighbour (finish() below).  Without HJ the sum of
@@ -343,10 +350,10 @@ struct SplitP {
       rb = selfrel == 1 ? 0.f : rb;
       if (NN) {
         const float inf = __int_as_float(0x7f800000);
-        nnmin = fminf(nnmin, fminf(selfrel == 0 ? inf : r2a, selfrel == 1 ? inf : r2b));
+        nnmin = fmin3(nnmin, selfrel == 0 ? inf : r2a, selfrel == 1 ? inf : r2b);
       }
     } else if (NN) {
-      nnmin = fminf(nnmin, fminf(r2a, r2b));
+      nnmin = fmin3(nnmin, r2a, r2b);
     }
     const f2x rinv = f2_pack(ra, rb);
     const f2x dvx = f2_sub(f2_of(r.vx), s.vx);
@@ -376,16 +383,7 @@ struct SplitP {
     q.j[1] = f2_fma(mr3i, f2_fma(a3, dy, dvy), q.j[1]);
     q.j[2] = f2_fma(mr3i, f2_fma(a3, dz, dvz), q.j[2]);
     q.p = f2_add(q.p, mri);
-    if (!HJ && G6_S1) {
-      // the largest single term m/(r^2+eps^2) is at most max(m rinv) max(rinv):
-      // two 3-input maxima on the ALU pipe
-      q.r1 = fmax3(q.r1, ra, rb);
-      q.mp = fmax3(q.mp, f2_lo(mri), f2_hi(mri));
-      if (G6_S1_HALF)  // one scalar FMA (half the FMA-pipe cycles of a packed one)
-        q.s = f2_pack(fmaf(f2_lo(mri), ra, f2_lo(q.s)), 0.f);
-      else
-        q.s = f2_fma(mri, rinv, q.s);
-    }
+    if (!HJ && G6_S1) q.s = f2_fma(mri, rinv, q.s);
   }
   // Nearest-neighbour re-scan of one record of the best tile: the first j
   // (in slot order) whose key equals best and that is not the i itself
@@ -404,8 +402,9 @@ struct SplitP {
         m2 = fminf(m2, kk[h]);
     }
   }
-  // Mid-tile fold of the jerk partial sums alone: the jerk sum cancels more
-  // than the others, so it is folded every JCHUNK records.
+  // Mid-tile fold of the jerk partial sums (and of the condition number's
+  // chunk): the jerk sum cancels more than the others, so it is folded every
+  // JCHUNK records.
   static constexpr bool JFOLD = true;
   // shared-memory totals free registers: they pay off in the nearest-
   // neighbour variant, not in the plain one (measured)
@@ -414,6 +413,10 @@ struct SplitP {
     return G6_TOT_SMEM == 1 || (G6_TOT_SMEM == 2 && NN);
   }
   __device__ static void fold_jerk(Tot &t, Part &q) {
+    if (G6_S1) {
+      fold_s(t, q);
+      q.s = 0ull;
+    }
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       ff_acc(t.jh[k], t.jl[k], f2_lo(q.j[k]));
@@ -440,7 +443,7 @@ struct SplitP {
     o.nnr2 = nnr2;
     o.nnr2b = nnr2b;
     o.s1 = t.s;
-    o.mt = t.mp * t.r1;
+    o.mt = t.mt;
     o.nn = nn;
     o.pad = 0;
   }
@@ -705,7 +708,8 @@ struct KParams {
 // kappa ~ 100-300), and with the largest single term over |a|, whose own
 // error does not average out (a massive neighbour pulling against the rest
 // of the cluster).  i-particles with kappa above the caller's limit, or
-// with a largest term (bounded by max m/r times max 1/r) above MU0 |a|, are
+// with a largest term (bounded by the largest partial sum over 32 j of one
+// thread) above MU0 |a|, are
 // queued too, and refine_kernel recomputes their acceleration and potential
 // in FP64 from the same records (double-single positions exact in FP64); the
 // jerk keeps its split value.
@@ -924,7 +928,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   typename P::Part q[IPT];
   // Compensated totals: in shared memory for the split nearest-neighbour
   // variant (touched once per fold; it frees registers for the pair loop),
-  // in registers otherwise.  Layout [k][thread]: 15-word records,
+  // in registers otherwise.  Layout [k][thread]: 17-word records,
   // conflict-free.
   constexpr bool TSH = P::template tot_shared<NN>();
   __shared__ typename P::Tot tot_sh[TSH ? IPT * NT : 1];
@@ -1510,7 +1514,7 @@ void choose_shape(int ni, int nj, int prec, int force_jl, int force_nsplit, int 
 }
 
 template <class P>
-int launch(const KParams &kp, int jl, int gx, cudaStream_t st) {
+int launch(const KParams &kp, int jl, int gx, cudaStream_t st, cudaEvent_t ev_mid) {
   dim3 grid(gx, kp.nsplit), block(NT);
   // Without nearest neighbours only the large-block shape has its own
   // instantiation; small blocks are latency-bound and keep the nn code.
@@ -1546,6 +1550,7 @@ int launch(const KParams &kp, int jl, int gx, cudaStream_t st) {
     else
       reduce_kernel<P><<<(kp.ni + 127) / 128, 128, 0, st>>>(kp);
   }
+  if (ev_mid) cudaEventRecord(ev_mid, st);
   if (kp.refine) refine_kernel<<<2 * sm_count(), RNT, 0, st>>>(kp);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
@@ -1637,10 +1642,10 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
                  : nullptr;
   if (a->prec == G6_PREC_FP64) {
     kp.jrec = a->js->jp_f64;
-    return launch<F64P>(kp, jl, gx, st);
+    return launch<F64P>(kp, jl, gx, st, a->ev_mid);
   }
   kp.jrec = a->js->jp_split;
-  return launch<SplitP>(kp, jl, gx, st);
+  return launch<SplitP>(kp, jl, gx, st, a->ev_mid);
 }
 
 // ---------------------------------------------------------------------------

@@ -252,6 +252,10 @@ double g6x_system_time(void);
    with CUDA events only while g6x_timing(1) is set. */
 int g6x_timing(int on);
 int g6x_stats(double out[8]);
+/* The same, n values at most (up to 10): out[8] the force kernel's ms (with
+   its split-j merge), out[9] the refinement pass's ms (out[1] = out[8] +
+   out[9] for split-precision calls). */
+int g6x_stats_n(double *out, int n);
 
 /* Batched few-body systems (the encounters AMUSE's multiples module hands
    to smallN): nsys independent systems of n_per_sys[s] bodies (2..64),

@@ -485,6 +485,9 @@ constexpr int WARPS_MAX_UNP = 4;  // shared memory per warp is larger here
 struct BinRec {
   int li, lj, full, pad;
   double mi, mj, r0[3], v0[3], t0, tpred, tidal;
+  // the last Kepler solution (universal anomaly, its dt, the separation):
+  // the next solve starts from it (dtw = 0: none yet)
+  double xw, dtw, rw;
 };
 
 struct UnpParams {
@@ -508,6 +511,7 @@ struct UnpSmem {
   double m[MAXN];                    // leaf masses
   float mf[MAXN];
   double nm[MAXN];                   // node masses (at node slots)
+  float nmf[MAXN];                   // the same in FP32 (split mode's step criterion)
   double cv[MAXN][3];                // node predicted velocities (at node slots)
   float cvf[MAXN][3];
   int nd[MAXN];                      // node (leader slot) of every leaf slot
@@ -515,52 +519,122 @@ struct UnpSmem {
   int nb;
 };
 
-__device__ __forceinline__ double kst_c(double z) {
-  if (z > 1e-6) return (1.0 - cos(sqrt(z))) / z;
-  if (z < -1e-6) return (cosh(sqrt(-z)) - 1.0) / (-z);
-  return 0.5 - z / 24.0 + z * z / 720.0;
-}
-__device__ __forceinline__ double kst_s(double z) {
-  if (z > 1e-6) {
-    const double q = sqrt(z);
-    return (q - sin(q)) / (q * q * q);
+// Stumpff functions C(z) = (1 - cos sqrt z) / z, S(z) = (sqrt z - sin sqrt z)
+// / z^(3/2) (cosh, sinh for z < 0), both from one sincos (one exp) of
+// sqrt(|z|) / 2: 1 - cos s = 2 sin^2(s/2) (no cancellation), sin s = 2
+// sin(s/2) cos(s/2).  Taylor series to z^6 for |z| < 0.1 (below 1e-17
+// relative).  FP64 transcendentals run at the FP64 rate, so one call per
+// Newton step rather than two.
+__device__ __forceinline__ void kst_cs(double z, double &C, double &S) {
+  if (z > 0.1) {
+    const double s = sqrt(z);
+    double sh, ch;
+    sincos(0.5 * s, &sh, &ch);
+    C = 2.0 * sh * sh / z;
+    S = (s - 2.0 * sh * ch) / (s * z);
+  } else if (z < -0.1) {
+    const double s = sqrt(-z), e = exp(0.5 * s), ei = 1.0 / e;
+    const double sh = 0.5 * (e - ei), ch = 0.5 * (e + ei);
+    C = 2.0 * sh * sh / -z;
+    S = (2.0 * sh * ch - s) / (s * -z);
+  } else {
+    C = 1.0 / 2 +
+        z * (-1.0 / 24 +
+             z * (1.0 / 720 +
+                  z * (-1.0 / 40320 +
+                       z * (1.0 / 3628800 + z * (-1.0 / 479001600 + z / 87178291200.0)))));
+    S = 1.0 / 6 +
+        z * (-1.0 / 120 +
+             z * (1.0 / 5040 +
+                  z * (-1.0 / 362880 +
+                       z * (1.0 / 39916800 + z * (-1.0 / 6227020800.0 + z / 1307674368000.0)))));
   }
-  if (z < -1e-6) {
-    const double q = sqrt(-z);
-    return (sinh(q) - q) / (q * q * q);
-  }
-  return 1.0 / 6.0 - z / 120.0 + z * z / 5040.0;
 }
 
-// Two-body relative motion over dt (mu = G M), universal variables:
-// Newton iterations on the universal anomaly x of
-//   sqrt(mu) dt = (r0.v0 / sqrt(mu)) x^2 C(z) + (1 - alpha r0) x^3 S(z) + r0 x,
-// z = alpha x^2, then the f and g functions.
+// Two-body relative motion over dt (mu = G M), universal variables: the
+// universal anomaly x solves
+//   F(x) = (r0.v0 / sqrt(mu)) x^2 C(z) + (1 - alpha r0) x^3 S(z) + r0 x - sqrt(mu) dt = 0,
+// z = alpha x^2, whose derivative is the separation r(x) > 0.  F being
+// monotonic, the root is bracketed and found by Newton steps that fall back
+// to bisection when a step leaves the bracket or does not halve the one
+// before last (a plain Newton iteration diverges on eccentric orbits near
+// pericentre).  The first guess is the mean-motion one, or, with a warm
+// start (*dtw > 0: the solution xw at dtw, separation rw, of the same
+// orbit), xw + sqrt(mu) (dt - dtw) / rw (dx/dt = sqrt(mu) / r); x grows with
+// dt, so xw then also bounds the root from one side.  The C and S of the
+// step whose correction is below 1e-15 x give the f and g functions.
 __device__ void kep_prop(double mu, const double r0[3], const double v0[3], double dt,
-                         double r[3], double v[3]) {
+                         double r[3], double v[3], double *xw = nullptr, double *dtw = nullptr,
+                         double *rw = nullptr) {
   const double rn = sqrt(r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2]);
   const double v2 = v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2];
   const double rv = r0[0] * v0[0] + r0[1] * v0[1] + r0[2] * v0[2];
   const double alpha = 2.0 / rn - v2 / mu, smu = sqrt(mu);
+  const double c1 = rv / smu, c2 = 1.0 - alpha * rn;
   if (dt == 0.0) {
     for (int k = 0; k < 3; k++) r[k] = r0[k], v[k] = v0[k];
     return;
   }
-  double x = alpha > 0.0 ? smu * dt * alpha : smu * dt / rn;
-  for (int it = 0; it < 100; it++) {
-    const double z = alpha * x * x, C = kst_c(z), S = kst_s(z);
-    const double F = rv / smu * x * x * C + (1.0 - alpha * rn) * x * x * x * S + rn * x - smu * dt;
-    const double dF = rv / smu * x * (1.0 - z * S) + (1.0 - alpha * rn) * x * x * C + rn;
-    const double dx = F / dF;
-    x -= dx;
-    if (fabs(dx) <= 1e-15 * fabs(x)) break;
+  auto Fx = [&](double x) {
+    double C, S;
+    kst_cs(alpha * x * x, C, S);
+    return c1 * x * x * C + c2 * x * x * x * S + rn * x - smu * dt;
+  };
+  const bool warm = xw && *dtw > 0.0 && dt > 0.0;
+  double x0 = alpha > 0.0 ? smu * dt * alpha : smu * dt / rn;  // sign of dt
+  double lo, hi;
+  if (warm) {
+    x0 = *xw + smu * (dt - *dtw) / *rw;
+    if (!(x0 > 0.0)) x0 = 0.5 * *xw;
+    // the root lies above xw when dt > dtw, below it otherwise (and above 0)
+    lo = dt >= *dtw ? *xw : 0.0;
+    hi = dt >= *dtw ? x0 : *xw;
+    if (x0 < lo || x0 > hi) x0 = 0.5 * (lo + hi);
+    if (dt >= *dtw) {
+      if (!(hi > lo)) hi = lo + fabs(lo) + 1e-300;
+      for (int k = 0; k < 200 && Fx(hi) < 0.0; k++) lo = hi, hi = 2.0 * hi;
+    }
+  } else if (dt > 0.0) {
+    lo = 0.0, hi = x0;
+    for (int k = 0; k < 200 && Fx(hi) < 0.0; k++) lo = hi, hi *= 2.0;
+  } else {
+    hi = 0.0, lo = x0;
+    for (int k = 0; k < 200 && Fx(lo) > 0.0; k++) hi = lo, lo *= 2.0;
   }
-  const double z = alpha * x * x, C = kst_c(z), S = kst_s(z);
+  double x = x0 > lo && x0 < hi ? x0 : 0.5 * (lo + hi);
+  double step_old = hi - lo, step = step_old, C = 0.5, S = 1.0 / 6;
+  for (int it = 0; it < 200; it++) {
+    const double z = alpha * x * x;
+    kst_cs(z, C, S);
+    const double F = c1 * x * x * C + c2 * x * x * x * S + rn * x - smu * dt;
+    const double dF = c1 * x * (1.0 - z * S) + c2 * x * x * C + rn;
+    if (F == 0.0 || fabs(F) <= 1e-15 * fabs(x * dF)) break;  // x is the root: C, S belong to it
+    if (F < 0.0)
+      lo = x;
+    else
+      hi = x;
+    double xn = x - F / dF;
+    if (!(xn > lo && xn < hi) || fabs(2.0 * F) > fabs(step_old * dF)) {
+      step_old = step;
+      step = 0.5 * (hi - lo);
+      xn = lo + step;
+    } else {
+      step_old = step;
+      step = F / dF;
+    }
+    if (xn == x) break;
+    x = xn;
+  }
   const double f = 1.0 - x * x * C / rn, g = dt - x * x * x * S / smu;
   for (int k = 0; k < 3; k++) r[k] = f * r0[k] + g * v0[k];
   const double rr = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
   const double fd = smu / (rr * rn) * (alpha * x * x * x * S - x), gd = 1.0 - x * x * C / rr;
   for (int k = 0; k < 3; k++) v[k] = fd * r0[k] + gd * v0[k];
+  if (xw && dt > 0.0) {
+    *xw = x;
+    *dtw = dt;
+    *rw = rr;
+  }
 }
 
 // Time to the next pericentre (0: not approaching it) and the period (inf
@@ -614,6 +688,15 @@ __device__ __forceinline__ void bin_rel(const BinRec &b, double t, double r[3], 
     kep_prop(b.mi + b.mj, b.r0, b.v0, t - b.t0, r, v);
   }
 }
+// The same, starting the Kepler solve from the binary's last solution and
+// keeping this one (the force evaluations: a few per step, at nearby times).
+__device__ __forceinline__ void bin_rel_warm(BinRec &b, double t, double r[3], double v[3]) {
+  if (b.full) {
+    for (int k = 0; k < 3; k++) r[k] = b.r0[k], v[k] = b.v0[k];
+  } else {
+    kep_prop(b.mi + b.mj, b.r0, b.v0, t - b.t0, r, v, &b.xw, &b.dtw, &b.rw);
+  }
+}
 
 // Tidal potential of the other top-level nodes on leaves (xi, xj) around
 // the centre of mass xc (smallN_unpert.cc:17-40); node positions in S.A.d.
@@ -659,15 +742,16 @@ __device__ double unp_forces(UnpSmem &S, int n, int lane, Body B[2], double t, i
       S.cvf[s][k] = __double2float_rn(B[q].pv[k]);
     }
     S.nm[s] = B[q].m;
+    S.nmf[s] = __double2float_rn(B[q].m);
     int qb = -1;
     for (int b = 0; b < S.nb; b++)
       if (S.bin[b].li == s) qb = b;
     if (qb < 0) {
       unp_store_leaf<MODE>(S, s, B[q].pp, B[q].pv);
     } else {
-      const BinRec &bb = S.bin[qb];
+      BinRec &bb = S.bin[qb];  // this lane's binary (its leader slot is the lane's)
       double r[3], v[3], xi[3], vi[3], xj[3], vj[3];
-      bin_rel(bb, t, r, v);
+      bin_rel_warm(bb, t, r, v);
       const double M = bb.mi + bb.mj, fi = bb.mj / M, fj = bb.mi / M;
       for (int k = 0; k < 3; k++) {
         xi[k] = B[q].pp[k] - fi * r[k];
@@ -690,10 +774,17 @@ __device__ double unp_forces(UnpSmem &S, int n, int lane, Body B[2], double t, i
     if (i >= n) continue;
     const int ni = S.nd[i];
     if (MODE == MODE_SPLIT) {
+      // FP32 throughout the loop (FP64 runs at 1/64 of the FP32 rate): the
+      // pairs within one node (the leaf itself, its binary companion) are
+      // evaluated with their terms masked to zero and their step to +inf,
+      // so the loop does not diverge; the smallest step and its node pair
+      // are kept in FP32 and merged into the FP64 minimum afterwards.
       float a[3] = {0.f, 0.f, 0.f}, jk[3] = {0.f, 0.f, 0.f};
+      float tsq = __int_as_float(0x7f800000);
+      int pq = 0x7fffffff;
       for (int j = 0; j < n; j++) {
         const int nj = S.nd[j];
-        if (nj == ni) continue;
+        const bool same = nj == ni;
         float dx[3], dv[3], dc[3];
         for (int k = 0; k < 3; k++) {
           dx[k] = __fadd_rn(__fsub_rn(S.A.f.ph[j][k], S.A.f.ph[i][k]),
@@ -703,10 +794,10 @@ __device__ double unp_forces(UnpSmem &S, int n, int lane, Body B[2], double t, i
         }
         const float d2 = fmaf(dx[2], dx[2], fmaf(dx[1], dx[1], dx[0] * dx[0]));
         const float v2 = fmaf(dc[2], dc[2], fmaf(dc[1], dc[1], dc[0] * dc[0]));
-        const float mt = (float)(S.nm[ni] + S.nm[nj]);
+        const float mt = S.nmf[ni] + S.nmf[nj];
         float ts;
-        if (d2 >= 1e-18f) {
-          const float rinv = rsqrt_approx(d2);
+        if (same || d2 >= 1e-18f) {
+          const float rinv = same ? 0.f : rsqrt_approx(d2);
           const float rinv2 = rinv * rinv;
           const float f = S.mf[j] * rinv * rinv2;
           const float xv = fmaf(dx[2], dv[2], fmaf(dx[1], dv[1], dx[0] * dv[0]));
@@ -715,7 +806,8 @@ __device__ double unp_forces(UnpSmem &S, int n, int lane, Body B[2], double t, i
             a[k] = fmaf(f, dx[k], a[k]);
             jk[k] = fmaf(f, fmaf(a3, dx[k], dv[k]), jk[k]);
           }
-          ts = fminf(__fdividef(0.5f * d2 * (d2 * rinv), mt), __fdividef(d2, v2));
+          ts = same ? __int_as_float(0x7f800000)
+                    : fminf(__fdividef(0.5f * d2 * (d2 * rinv), mt), __fdividef(d2, v2));
         } else {  // too close for FP32: FP64
           double X[3], W[3];
           for (int k = 0; k < 3; k++) X[k] = (double)dx[k], W[k] = (double)dv[k];
@@ -729,10 +821,14 @@ __device__ double unp_forces(UnpSmem &S, int n, int lane, Body B[2], double t, i
           ts = (float)fmin(0.5 * dd2 * d / (double)mt, dd2 / (double)v2);
         }
         const int pid = ni < nj ? ni * MAXN + nj : nj * MAXN + ni;
-        if ((double)ts < ts2 || ((double)ts == ts2 && pid < pmin)) {
-          ts2 = (double)ts;
-          pmin = pid;
+        if (ts < tsq || (ts == tsq && pid < pq)) {
+          tsq = ts;
+          pq = pid;
         }
+      }
+      if ((double)tsq < ts2 || ((double)tsq == ts2 && pq < pmin)) {
+        ts2 = (double)tsq;
+        pmin = pq;
       }
       for (int k = 0; k < 3; k++) la[q][k] += (double)a[k], lj[q][k] += (double)jk[k];
     } else {
@@ -889,6 +985,7 @@ __device__ int unp_tree(UnpSmem &S, int n, int lane, Body B[2], double t, double
           b.mj = mj;
           for (int k = 0; k < 3; k++) b.r0[k] = r[k], b.v0[k] = v[k];
           b.t0 = t;
+          b.dtw = 0.0;
           b.tpred = 2.0 * (t + dtp) - t;
           b.tidal = tid;
           S.nd[j] = i;
@@ -966,6 +1063,7 @@ __device__ int unp_tree(UnpSmem &S, int n, int lane, Body B[2], double t, double
         b.tidal = tid;
         for (int k = 0; k < 3; k++) b.r0[k] = r[k], b.v0[k] = v[k];
         b.t0 = t;
+        b.dtw = 0.0;
       }
       __syncwarp();
       continue;

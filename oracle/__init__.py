@@ -82,6 +82,8 @@ def port():
         lib.orc_smalln_unpert.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_int, _c_dbl,
                                           _c_dbl, _c_dbl, _c_dbl, _c_int, _dp, _c_long, _ip]
         lib.orc_smalln_unpert.restype = _c_long
+        lib.orc_kepler.argtypes = [_c_dbl, _dp, _dp, _c_dbl, _dp, _dp]
+        lib.orc_kepler.restype = None
         lib.orc_hermite_fixed.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_int, _dp,
                                           _dp]
         lib.orc_hermite_fixed.restype = None
@@ -278,6 +280,14 @@ def smalln_unpert(mass, pos, vel, eta, t_end, n_iter=2, dt_crit=SMALLN_DT_CRIT,
     if steps < 0:
         raise ValueError("more than 64 bodies")
     return pos, vel, float(t[0]), int(steps), int(nb[0])
+
+
+def kepler(mu, r0, v0, dt):
+    """The two-body propagator of orc_smalln_unpert: relative (r, v) after
+    dt from (r0, v0), total mass mu."""
+    r, v = np.zeros(3), np.zeros(3)
+    port().orc_kepler(float(mu), _c(r0), _c(v0), float(dt), r, v)
+    return r, v
 
 
 def hermite_fixed(mass, pos, vel, eps2, dt, nsteps):

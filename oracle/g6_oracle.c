@@ -787,42 +787,94 @@ typedef struct {
   int full;             /* fully unperturbed: components frozen at r0, v0 */
 } snu_bin;
 
+/* Stumpff functions C(z) = (1 - cos sqrt z) / z and S(z) = (sqrt z -
+ * sin sqrt z) / z^(3/2) (continued to z < 0 with cosh, sinh).  Near z = 0
+ * their Taylor series (terms to z^6, below 1e-17 relative for |z| < 0.1);
+ * elsewhere C through 2 sin^2(s/2), which does not cancel. */
 static double snu_stumpff_c(double z) {
-  if (z > 1e-6) return (1 - cos(sqrt(z))) / z;
-  if (z < -1e-6) return (cosh(sqrt(-z)) - 1) / (-z);
-  return 0.5 - z / 24 + z * z / 720;
+  if (z > 0.1) {
+    double h = sin(0.5 * sqrt(z));
+    return 2 * h * h / z;
+  }
+  if (z < -0.1) {
+    double h = sinh(0.5 * sqrt(-z));
+    return 2 * h * h / -z;
+  }
+  return 1.0 / 2 +
+         z * (-1.0 / 24 +
+              z * (1.0 / 720 +
+                   z * (-1.0 / 40320 +
+                        z * (1.0 / 3628800 + z * (-1.0 / 479001600 + z / 87178291200.0)))));
 }
 static double snu_stumpff_s(double z) {
-  if (z > 1e-6) {
+  if (z > 0.1) {
     double s = sqrt(z);
     return (s - sin(s)) / (s * s * s);
   }
-  if (z < -1e-6) {
+  if (z < -0.1) {
     double s = sqrt(-z);
     return (sinh(s) - s) / (s * s * s);
   }
-  return 1.0 / 6 - z / 120 + z * z / 5040;
+  return 1.0 / 6 +
+         z * (-1.0 / 120 +
+              z * (1.0 / 5040 +
+                   z * (-1.0 / 362880 +
+                        z * (1.0 / 39916800 + z * (-1.0 / 6227020800.0 + z / 1307674368000.0)))));
 }
 
-/* Two-body relative motion over dt (mu = G M): universal variables. */
+/* Two-body relative motion over dt (mu = G M): universal variables.  The
+ * universal anomaly x solves F(x) = (r0.v0/sqrt(mu)) x^2 C + (1 - alpha r0)
+ * x^3 S + r0 x - sqrt(mu) dt = 0, and dF/dx is the separation r(x) > 0, so
+ * F increases monotonically: the root is bracketed (doubling out from the
+ * mean-motion guess) and found by Newton steps that fall back to bisection
+ * when a step leaves the bracket or does not halve the previous one.  A
+ * plain Newton iteration from the mean-motion guess diverges on eccentric
+ * orbits near pericentre. */
 static void snu_kepler(double mu, const double r0[3], const double v0[3], double dt, double r[3],
                        double v[3]) {
   double rn = sqrt(r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2]);
   double v2 = v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2];
   double rv = r0[0] * v0[0] + r0[1] * v0[1] + r0[2] * v0[2];
-  double alpha = 2 / rn - v2 / mu, smu = sqrt(mu);
+  double alpha = 2 / rn - v2 / mu, smu = sqrt(mu), c1 = rv / smu, c2 = 1 - alpha * rn;
   if (dt == 0) {
     for (int k = 0; k < 3; k++) r[k] = r0[k], v[k] = v0[k];
     return;
   }
-  double x = alpha > 0 ? smu * dt * alpha : smu * dt / rn; /* initial guess */
-  for (int it = 0; it < 100; it++) {
+#define SNU_F(xx) \
+  (c1 * (xx) * (xx) * snu_stumpff_c(alpha * (xx) * (xx)) + \
+   c2 * (xx) * (xx) * (xx) * snu_stumpff_s(alpha * (xx) * (xx)) + rn * (xx) - smu * dt)
+  double x0 = alpha > 0 ? smu * dt * alpha : smu * dt / rn; /* same sign as dt */
+  double lo, hi;
+  if (dt > 0) {
+    lo = 0, hi = x0;
+    for (int k = 0; k < 200 && SNU_F(hi) < 0; k++) lo = hi, hi *= 2;
+  } else {
+    hi = 0, lo = x0;
+    for (int k = 0; k < 200 && SNU_F(lo) > 0; k++) hi = lo, lo *= 2;
+  }
+#undef SNU_F
+  double x = x0 > lo && x0 < hi ? x0 : 0.5 * (lo + hi);
+  double step_old = hi - lo, step = step_old;
+  for (int it = 0; it < 200; it++) {
     double z = alpha * x * x, C = snu_stumpff_c(z), S = snu_stumpff_s(z);
-    double F = rv / smu * x * x * C + (1 - alpha * rn) * x * x * x * S + rn * x - smu * dt;
-    double dF = rv / smu * x * (1 - z * S) + (1 - alpha * rn) * x * x * C + rn;
-    double dx = F / dF;
-    x -= dx;
-    if (fabs(dx) <= 1e-15 * fabs(x)) break;
+    double F = c1 * x * x * C + c2 * x * x * x * S + rn * x - smu * dt;
+    double dF = c1 * x * (1 - z * S) + c2 * x * x * C + rn;
+    if (F == 0) break;
+    if (F < 0) lo = x; else hi = x;
+    double xn = x - F / dF;
+    if (!(xn > lo && xn < hi) || fabs(2 * F) > fabs(step_old * dF)) {
+      step_old = step;
+      step = 0.5 * (hi - lo);
+      xn = lo + step;
+    } else {
+      step_old = step;
+      step = F / dF;
+    }
+    if (fabs(xn - x) <= 1e-15 * fabs(xn)) {
+      x = xn;
+      break;
+    }
+    x = xn;
   }
   double z = alpha * x * x, C = snu_stumpff_c(z), S = snu_stumpff_s(z);
   double f = 1 - x * x * C / rn, g = dt - x * x * x * S / smu;
@@ -830,6 +882,11 @@ static void snu_kepler(double mu, const double r0[3], const double v0[3], double
   double rr = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
   double fd = smu / (rr * rn) * (alpha * x * x * x * S - x), gd = 1 - x * x * C / rr;
   for (int k = 0; k < 3; k++) v[k] = fd * r0[k] + gd * v0[k];
+}
+
+/* The propagator, exported for the tests. */
+void orc_kepler(double mu, const double *r0, const double *v0, double dt, double *r, double *v) {
+  snu_kepler(mu, r0, v0, dt, r, v);
 }
 
 /* Time to the next pericentre and the period (inf unless bound) of the

@@ -698,17 +698,35 @@ __device__ __forceinline__ void bin_rel_warm(BinRec &b, double t, double r[3], d
   }
 }
 
+// Warp-wide sum and minimum (xor butterfly: every lane ends with the same
+// value, a + b being b + a).
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+__device__ __forceinline__ double warp_min(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(0xffffffffu, x, o));
+  return x;
+}
+
 // Tidal potential of the other top-level nodes on leaves (xi, xj) around
 // the centre of mass xc (smallN_unpert.cc:17-40); node positions in S.A.d.
-__device__ double tidal_pot(const UnpSmem &S, int n, int li, int lj, double mi, double mj,
-                            const double xi[3], const double xj[3], const double xc[3]) {
+// The whole warp calls it (uniform arguments); each lane sums its two node
+// slots (the tree's loops over nodes run at 1/32 of the FP64 work per lane).
+__device__ double tidal_pot(const UnpSmem &S, int n, int lane, int li, int lj, double mi,
+                            double mj, const double xi[3], const double xj[3],
+                            const double xc[3]) {
   double phi = 0.0;
-  for (int k = 0; k < n; k++) {
-    if (S.nd[k] != k || k == li || k == lj) continue;
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int k = lane + 32 * q;
+    if (k >= n || S.nd[k] != k || k == li || k == lj) continue;
     phi += S.nm[k] * (-mi / dist3(xi, S.A.d.pp[k]) - mj / dist3(xj, S.A.d.pp[k]) +
                       (mi + mj) / dist3(xc, S.A.d.pp[k]));
   }
-  return phi;
+  return warp_sum(phi);
 }
 
 template <int MODE>
@@ -957,13 +975,26 @@ __device__ int unp_tree(UnpSmem &S, int n, int lane, Body B[2], double t, double
         cm[k] = (mi * xi[k] + mj * xj[k]) / M;
         cmv[k] = (mi * vi[k] + mj * vj[k]) / M;
       }
+      // the strongest perturber (largest m^2 / d^2 from the CM; the first
+      // node on ties): each lane its two node slots, then a warp argmax
       double maxp = 0.0, nnd2 = 0.0, mk = 0.0;
-      for (int k2 = 0; k2 < n; k2++) {
-        if (S.nd[k2] != k2 || k2 == i || k2 == j) continue;
+      int kk = 0x7fffffff;
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        const int k2 = lane + 32 * q;
+        if (k2 >= n || S.nd[k2] != k2 || k2 == i || k2 == j) continue;
         double e2 = 0.0;
         for (int k = 0; k < 3; k++) e2 += (S.A.d.pp[k2][k] - cm[k]) * (S.A.d.pp[k2][k] - cm[k]);
         const double p2 = S.nm[k2] * S.nm[k2] / e2;
-        if (p2 > maxp) maxp = p2, nnd2 = e2, mk = S.nm[k2];
+        if (p2 > maxp) maxp = p2, nnd2 = e2, mk = S.nm[k2], kk = k2;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double op = __shfl_xor_sync(0xffffffffu, maxp, o);
+        const double od = __shfl_xor_sync(0xffffffffu, nnd2, o);
+        const double om = __shfl_xor_sync(0xffffffffu, mk, o);
+        const int ok = __shfl_xor_sync(0xffffffffu, kk, o);
+        if (op > maxp || (op == maxp && ok < kk)) maxp = op, nnd2 = od, mk = om, kk = ok;
       }
       bool unp = true;
       if (maxp > 0.0) {
@@ -974,7 +1005,7 @@ __device__ int unp_tree(UnpSmem &S, int n, int lane, Body B[2], double t, double
       if (unp && kep_peri(M, r, v, &dtp, &per)) {
         double pxi[3], pxj[3];
         for (int k = 0; k < 3; k++) pxi[k] = xi[k], pxj[k] = xj[k];
-        const double tid = tidal_pot(S, n, i, j, mi, mj, pxi, pxj, cm);
+        const double tid = tidal_pot(S, n, lane, i, j, mi, mj, pxi, pxj, cm);
         __syncwarp();
         if (lane == 0) {
           BinRec &b = S.bin[S.nb];
@@ -1008,13 +1039,14 @@ __device__ int unp_tree(UnpSmem &S, int n, int lane, Body B[2], double t, double
     const int i = bb.li, j = bb.lj;
     const double M = bb.mi + bb.mj;
     double r[3], v[3], xi[3], xj[3], xc[3], vc[3];
-    bin_rel(bb, t, r, v);
+    BinRec bw = bb;  // warm-started solve on a copy (every lane, same values)
+    bin_rel_warm(bw, t, r, v);
     for (int k = 0; k < 3; k++) xc[k] = S.A.d.pp[i][k], vc[k] = S.A.d.pv[i][k];
     for (int k = 0; k < 3; k++) {
       xi[k] = xc[k] - bb.mj / M * r[k];
       xj[k] = xc[k] + bb.mi / M * r[k];
     }
-    const double tid = tidal_pot(S, n, i, j, bb.mi, bb.mj, xi, xj, xc);
+    const double tid = tidal_pot(S, n, lane, i, j, bb.mi, bb.mj, xi, xj, xc);
     if (!bb.full) {
       const double mu = bb.mi * bb.mj / M, v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
       const double fac = 1.0 - 2.0 * (tid - bb.tidal) / (mu * v2);
@@ -1029,9 +1061,13 @@ __device__ int unp_tree(UnpSmem &S, int n, int lane, Body B[2], double t, double
     if (P.allow_full && alpha > 0.0) {
       const double a = 1.0 / alpha;
       period = 2.0 * M_PI / sqrt(M * alpha * alpha * alpha);
+      // time for any other node to come within the perturbation radius
+      // (dt_perturbers): each lane its two node slots, then a warp minimum
       dtp = __longlong_as_double(0x7ff0000000000000ll);
-      for (int k2 = 0; k2 < n; k2++) {
-        if (S.nd[k2] != k2 || k2 == i) continue;
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        const int k2 = lane + 32 * q;
+        if (k2 >= n || S.nd[k2] != k2 || k2 == i) continue;
         const double rp = P.gamma_inv3 * a * cbrt(2.0 * S.nm[k2] / M);
         double dp[3], dvl[3], da[3];
         for (int k = 0; k < 3; k++) {
@@ -1050,9 +1086,8 @@ __device__ int unp_tree(UnpSmem &S, int n, int lane, Body B[2], double t, double
           if (ar < 0.0) tr = fmin(tr, sqrt(-2.0 * dd / ar));
         }
         if (tr < dtp) dtp = tr;
-        if (tr <= 0.0) break;
       }
-      dtp *= 0.5;
+      dtp = 0.5 * warp_min(dtp);
     }
     __syncwarp();
     if (dtp >= period) {  // extend by whole periods, components frozen

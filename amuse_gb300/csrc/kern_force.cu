@@ -1490,8 +1490,19 @@ void choose_shape(int ni, int nj, int prec, int force_jl, int force_nsplit, int 
       const int tp = cand_tp[k], ns = cand_ns[k];
       const long long ctas = gx * ns;
       const long long waves = (ctas + slots - 1) / slots;
-      const double cost =
-          (double)waves * (tp * (A + B * (double)(TJ / jl)) + F) * (1.0 + 0.002 * ns);
+      // j-lanes (JL > 1) cost a few per cent per pair in large blocks
+      // (measured at 65536 i: JL = 2 ran 3 % slower than JL = 1 without the
+      // nearest neighbour and 6 % slower with it), where JL = 1 fills the
+      // GPU by splitting j alone
+      const double jl_pen = (jl > 1 && ni >= 16384) ? 1.05 : 1.0;
+      // each split adds per-CTA start-up, a partial record per i to write
+      // and merge, and (nearest neighbour) a re-scan of its best tile: 0.2 %
+      // per split against j sets of up to 2048 tiles (measured: 65536 i
+      // against 2^18 j ran 2 % slower at 16 splits than at 7), proportionally
+      // less against larger ones (2^20 j: 16 splits beat 7 by 1.5 %)
+      const double split_pen = 0.002 * ns * (ntiles > 2048 ? 2048.0 / ntiles : 1.0);
+      const double cost = (double)waves * (tp * (A + B * (double)(TJ / jl)) + F) *
+                          (1.0 + split_pen) * jl_pen;
       if (cost < best * 0.999) {
         best = cost;
         bjl = jl;

@@ -398,7 +398,7 @@ def main():
     b.add_argument("--nsys", type=int, default=4096)
     b.add_argument("--seed", type=int, default=1)
     b.add_argument("--eta", type=float, default=0.14)
-    b.add_argument("--max-steps", type=int, default=250_000)
+    b.add_argument("--max-steps", type=int, default=2_000_000)
     b.add_argument("--cpu-sample", type=int, default=64)
     b.add_argument("--batch-mode", default="split", choices=["fast", "exact", "split"])
     b.add_argument("--no-unpert", action="store_true")

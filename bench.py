@@ -85,7 +85,7 @@ def parse():
     ap.add_argument("--nsys", type=int, default=4096)
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--eta", type=float, default=0.14)
-    ap.add_argument("--max-steps", type=int, default=250_000)
+    ap.add_argument("--max-steps", type=int, default=2_000_000)
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--batch-mode", default="split", choices=["fast", "exact", "split"])
     ap.add_argument("--no-unpert", action="store_true",

@@ -183,7 +183,7 @@ def test_unperturbed_batching_workload_completes(g6):
     t_end = np.full(len(ns), 10.0 * tcr)
     g6.batch_unperturbed(True)
     try:
-        r = g6.batch_run(ns, t_end, m, x, v, mode="split", max_steps=250_000)
+        r = g6.batch_run(ns, t_end, m, x, v, mode="split", max_steps=2_000_000)
         nbin = g6.batch_binaries(len(ns))
     finally:
         g6.batch_unperturbed(False)

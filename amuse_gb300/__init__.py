@@ -270,10 +270,12 @@ class G6X(G6):
         _check(self.lib.g6x_set_refine(float(kappa)), "g6x_set_refine")
 
     def refine_stats(self):
-        """Last call's refinement queue: queued, queued for kappa, overflow."""
-        out = np.zeros(3, np.int32)
+        """Last call's refinement queue: queued, queued for kappa, overflow,
+        queued for a dominant term."""
+        out = np.zeros(4, np.int32)
         _check(self.lib.g6x_refine_stats(_ptr(out, ctypes.c_int)), "g6x_refine_stats")
-        return dict(queued=int(out[0]), kappa=int(out[1]), overflow=int(out[2]))
+        return dict(queued=int(out[0]), kappa=int(out[1]), overflow=int(out[2]),
+                    dominant=int(out[3]))
 
     def test_wait_expiry(self, on=True):
         """Test hook: the next force call's bounded wait expires (20 ms)."""

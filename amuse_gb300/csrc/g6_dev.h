@@ -95,8 +95,9 @@ typedef struct {
 /* Size of the refinement buffer (fixed; allocated once per context). */
 size_t g6k_refine_bytes(void);
 /* Last refinement: out[0] particles queued, out[1] of them because of the
-   condition number, out[2] the largest queue that overflowed (0: none).  */
-int g6k_refine_read(const void *refine, int out[3], cudaStream_t st);
+   condition number, out[2] the largest queue that overflowed (0: none),
+   out[3] of them because of a dominant term.  */
+int g6k_refine_read(const void *refine, int out[4], cudaStream_t st);
 
 /* Launch shape actually used (reported by g6k_force). */
 typedef struct {

@@ -962,7 +962,7 @@ int g6x_test_wait_expiry(int on) {
   G.stall_next = on ? 1 : 0;
   return 0;
 }
-int g6x_refine_stats(int out[3]) {
+int g6x_refine_stats(int out[4]) {
   int rc = check_open();
   if (rc) return rc;
   if (g6k_refine_read(G.d_refine, out, G.st)) {

@@ -80,6 +80,9 @@ namespace {
 #ifndef G6_IPT_F64
 #define G6_IPT_F64 4
 #endif
+#ifndef G6_XMERGE_MAX
+#define G6_XMERGE_MAX 2  // split merge in the force kernel up to this many i per group
+#endif
 #ifndef G6_JCHUNK
 #define G6_JCHUNK 32  // split: records per jerk fold
 #endif
@@ -707,12 +710,20 @@ struct KParams {
 // particles near the centre of a cluster, where the pulls cancel, reach
 // kappa ~ 100-300), and with the largest single term over |a|, whose own
 // error does not average out (a massive neighbour pulling against the rest
-// of the cluster).  i-particles with kappa above the caller's limit, or
-// with a largest term (bounded by the largest partial sum over 32 j of one
-// thread) above MU0 |a|, are
-// queued too, and refine_kernel recomputes their acceleration and potential
-// in FP64 from the same records (double-single positions exact in FP64); the
-// jerk keeps its split value.
+// of the cluster).  i-particles with kappa above the caller's limit are
+// queued (REF_ACC), and refine_kernel recomputes their acceleration and
+// potential in FP64 from the same records (double-single positions exact in
+// FP64).  Those with kappa below it but a largest term (bounded by the
+// largest partial sum over 32 j of one thread) above MU0 |a| are queued for
+// the cheaper REF_MT pass: the sum redone with the kernel's FP32 pair terms
+// but compensated (TwoSum) accumulation, every term above TAU |a| replaced
+// by its FP64 value.  That removes the dominant terms' own errors and the
+// FP32 partial sums' roundings relative to them, which are what does not
+// average out there; the remaining terms are each below TAU |a|, so their
+// random errors add up to ~1e-7 sqrt(TAU kappa) |a|.  Common in clusters
+// with a mass spectrum (a massive star near the i), REF_MT costs ~50 FP32
+// operations per pair where REF_ACC costs ~20 FP64 ones (each 1/64 the
+// FP32 rate).  In both the jerk keeps its split value.
 //
 // Refinement buffer (g6k_refine_bytes, zeroed once): a header, the queue
 // (i, reason, key bound), per-entry tickets, per-(entry, chunk) partial
@@ -723,12 +734,15 @@ constexpr int RPCAP = 32768;   // partial records (entries x chunks)
 constexpr int RCHMAX = 64;     // j-chunks per entry at most
 constexpr int RNT = 256;       // refine_kernel threads per CTA
 constexpr int XTMAX = 8192;    // i-groups (grid.x) whose split merge runs in the force kernel
-enum { REF_ACC = 1, REF_NN = 2 };
-// Largest single term over |a| above which the sum is redone in FP64: a
-// term carries up to ~5e-7 relative error (three times the 1.25e-7 of the
+enum { REF_ACC = 1, REF_NN = 2, REF_MT = 4 };
+// Largest single term over |a| above which the sum is redone (REF_MT): a
+// term carries up to ~7e-7 relative error (three times the 1.25e-7 of the
 // MUFU reciprocal square root, measured over all FP32 inputs in [1, 4), plus
-// roundings), so a term of 1.5 |a| alone can cost ~7e-7.
+// the roundings of r^2, the differences and the products), and a partial
+// sum holding it rounds every later term to its own ulp.
 constexpr double MU0 = 1.5;
+// Terms above TAU |a| are evaluated in FP64 in the REF_MT pass.
+constexpr float TAU = 0.005f;
 
 struct RefHdr {
   unsigned count;     // entries queued by this call (reset by refine_kernel)
@@ -737,7 +751,8 @@ struct RefHdr {
   unsigned last;      // count of the last refinement
   unsigned last_acc;  // of which queued for the condition number
   unsigned nacc;      // REF_ACC entries queued by this call
-  unsigned pad[2];
+  unsigned nmt;       // REF_MT entries queued by this call
+  unsigned last_mt;   // of the last refinement
 };
 struct RefPart {  // one j-chunk of one entry, FP64
   double a[3], p, r2;
@@ -747,7 +762,8 @@ struct RefBuf {
   RefHdr h;
   int list[RCAP];
   int mode[RCAP];
-  float thr[RCAP];
+  float thr[RCAP];     // REF_NN: the FP32 key bound
+  float thr_mt[RCAP];  // REF_MT: TAU |a|
   unsigned ticket[RCAP];
   RefPart part[RPCAP];
   unsigned xtick[XTMAX];  // force kernel: CTAs of an i-group done (reset by the last)
@@ -792,21 +808,24 @@ __device__ __forceinline__ double split_eps(double eps2) {
   return (double)((float)eps2 + (float)(1.0 / 4503599627370496.0));
 }
 
-__device__ __forceinline__ void ref_enqueue(void *buf, int i, int mode, float thr) {
+__device__ __forceinline__ void ref_enqueue(void *buf, int i, int mode, float thr,
+                                            float thr_mt) {
   RefBuf *b = reinterpret_cast<RefBuf *>(buf);
   const unsigned e = atomicAdd(&b->h.count, 1u);
   if (mode & REF_ACC) atomicAdd(&b->h.nacc, 1u);
+  if (mode & REF_MT) atomicAdd(&b->h.nmt, 1u);
   if (e < (unsigned)RCAP) {
     b->list[e] = i;
     b->mode[e] = mode;
     b->thr[e] = thr;
+    b->thr_mt[e] = thr_mt;
   }
 }
 
 __device__ __noinline__ void SplitP::finish(const Out &o, int i, const KParams &kp) {
   write_final(o, i, kp.acc, kp.jerk, kp.pot);
   int mode = 0;
-  float thr = 0.f;
+  float thr = 0.f, thr_mt = 0.f;
   if (kp.refine && kp.kappa2 > 0.0) {
     double a2 = 0.0;
 #pragma unroll
@@ -815,7 +834,12 @@ __device__ __noinline__ void SplitP::finish(const Out &o, int i, const KParams &
       a2 += a * a;
     }
     const double s1 = (double)o.s1, mt = (double)o.mt;
-    if (s1 * s1 > kp.kappa2 * a2 || mt * mt > MU0 * MU0 * a2) mode |= REF_ACC;
+    if (s1 * s1 > kp.kappa2 * a2) {
+      mode |= REF_ACC;
+    } else if (mt * mt > MU0 * MU0 * a2) {
+      mode |= REF_MT;
+      thr_mt = (float)((double)TAU * sqrt(a2));
+    }
   }
   const int nn = (o.nn >= 0 && o.nn < kp.nj) ? o.nn : -1;
   if (kp.want_nn) {
@@ -837,7 +861,7 @@ __device__ __noinline__ void SplitP::finish(const Out &o, int i, const KParams &
   } else if (kp.nn) {
     kp.nn[i] = -1;
   }
-  if (mode) ref_enqueue(kp.refine, i, mode, thr);
+  if (mode) ref_enqueue(kp.refine, i, mode, thr, thr_mt);
 }
 
 __device__ __noinline__ void F64P::finish(const Out &o, int i, const KParams &kp) {
@@ -1227,15 +1251,54 @@ __device__ __forceinline__ double refine_rsqrt(double x) {
   return y * __fma_rn(-0.5 * x * y, y, 1.5);
 }
 
+// One j of a REF_MT entry: the force kernel's FP32 term (same operations,
+// so the same value up to the final product's rounding) into compensated
+// FP32 sums, or, above thr = TAU |a|, the FP64 term into the FP64 sums.
+__device__ __forceinline__ void mt_term(float xh, float yh, float zh, float m, float xl, float yl,
+                                        float zl, const float ih[3], const float il[3],
+                                        const double xi[3], float e32, double eps2, float thr,
+                                        double sa[3], double &sp, float ah[3], float al[3],
+                                        float &ph, float &pl) {
+  const float jh[3] = {xh, yh, zh}, jl[3] = {xl, yl, zl};
+  float d[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) d[k] = __fadd_rn(__fsub_rn(jh[k], ih[k]), __fsub_rn(jl[k], il[k]));
+  const float r2f = __fmaf_rn(d[2], d[2], __fmaf_rn(d[1], d[1], __fmaf_rn(d[0], d[0], e32)));
+  const float rinv = rsqrt_approx(r2f);
+  const float mri = __fmul_rn(m, rinv);
+  if (__fmul_rn(mri, rinv) > thr) {
+    double dx[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) dx[k] = ((double)jh[k] + (double)jl[k]) - xi[k];
+    const double r2 = __fma_rn(dx[2], dx[2], __fma_rn(dx[1], dx[1], __fma_rn(dx[0], dx[0], eps2)));
+    const double ri = refine_rsqrt(r2);
+    const double mr = (double)m * ri;
+    const double mr3 = mr * (ri * ri);
+#pragma unroll
+    for (int k = 0; k < 3; k++) sa[k] = __fma_rn(mr3, dx[k], sa[k]);
+    sp += mr;
+  } else {
+    const float mr3i = __fmul_rn(mri, __fmul_rn(rinv, rinv));
+#pragma unroll
+    for (int k = 0; k < 3; k++) ff_acc(ah[k], al[k], __fmul_rn(mr3i, d[k]));
+    ff_acc(ph, pl, mri);
+  }
+}
+
 __global__ void __launch_bounds__(RNT) refine_kernel(KParams kp) {
   RefBuf *b = reinterpret_cast<RefBuf *>(kp.refine);
   __shared__ unsigned s_cnt;
   __shared__ double s_sum[RNT / 32][5];
   __shared__ int s_slot[RNT / 32];
+  __shared__ int s_last;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_cnt = *reinterpret_cast<volatile unsigned *>(&b->h.count);
   __syncthreads();
   const unsigned cnt = s_cnt;
+  if (cnt == 0) {  // nothing queued (most calls): record that and leave
+    if (blockIdx.x == 0 && tid == 0) b->h.last = b->h.last_acc = b->h.last_mt = 0u;
+    return;
+  }
   const int ne = cnt > (unsigned)RCAP ? 0 : (int)cnt;
   if (cnt > (unsigned)RCAP && blockIdx.x == 0 && tid == 0) atomicMax(&b->h.overflow, cnt);
   int nch = 1;
@@ -1255,9 +1318,13 @@ __global__ void __launch_bounds__(RNT) refine_kernel(KParams kp) {
     const int e = u / nch, c = u - e * nch;
     const int i = b->list[e];
     const int mode = b->mode[e];
-    const float thr = b->thr[e];
-    const int j0 = (int)((long long)kp.nj * c / nch);
-    const int j1 = (int)((long long)kp.nj * (c + 1) / nch);
+    const float thr = b->thr[e], thr_mt = b->thr_mt[e];
+    // chunk c: record pairs [p0, p1) (j from 2 p0 to 2 p1, nj at most)
+    const int npair = (kp.nj + 1) >> 1;
+    const int p0 = (int)((long long)npair * c / nch);
+    const int p1 = (int)((long long)npair * (c + 1) / nch);
+    const int j0 = 2 * p0;
+    const int j1 = 2 * p1 < kp.nj ? 2 * p1 : kp.nj;
     // The i-particle in the split kernel's own representation (double-single
     // position), so that an i and a j copy of it at the same place give
     // dx = 0 exactly, as there.
@@ -1281,10 +1348,31 @@ __global__ void __launch_bounds__(RNT) refine_kernel(KParams kp) {
     for (int k = 0; k < 3; k++) xi[k] = (double)ih[k] + (double)il[k];
     if (mode & REF_NN) ipos64(kp, i, xi64);
     double sa[3] = {0.0, 0.0, 0.0}, sp = 0.0;
+    float ah[3] = {0.f, 0.f, 0.f}, al[3] = {0.f, 0.f, 0.f}, ph = 0.f, pl = 0.f;  // REF_MT
     double br2 = inf;
     int bslot = -1;
-    for (int j = j0 + tid; j < j1; j += RNT) {
+    if (mode == REF_MT) {
+      // the common case alone: whole record pairs in four 16-byte loads,
+      // two pairs in flight per thread
+      const float4 *q4 = reinterpret_cast<const float4 *>(rec);
+#pragma unroll 2
+      for (int rp = p0 + tid; rp < p1; rp += RNT) {
+        const float4 A = __ldg(q4 + 6 * rp), B = __ldg(q4 + 6 * rp + 1);
+        const float4 C = __ldg(q4 + 6 * rp + 2), D = __ldg(q4 + 6 * rp + 3);
+        if (2 * rp != self && 2 * rp < kp.nj)
+          mt_term(A.x, A.z, B.x, B.z, C.x, C.z, D.x, ih, il, xi, e32, eps2, thr_mt, sa, sp, ah,
+                  al, ph, pl);
+        if (2 * rp + 1 != self && 2 * rp + 1 < kp.nj)
+          mt_term(A.y, A.w, B.y, B.w, C.y, C.w, D.y, ih, il, xi, e32, eps2, thr_mt, sa, sp, ah,
+                  al, ph, pl);
+      }
+    }
+    for (int j = j0 + tid; mode != REF_MT && j < j1; j += RNT) {
       if (j == self) continue;
+      if (mode & REF_MT)
+        mt_term(g6_split_get(rec, j, 0), g6_split_get(rec, j, 1), g6_split_get(rec, j, 2),
+                g6_split_get(rec, j, 3), g6_split_get(rec, j, 4), g6_split_get(rec, j, 5),
+                g6_split_get(rec, j, 6), ih, il, xi, e32, eps2, thr_mt, sa, sp, ah, al, ph, pl);
       if (mode & REF_ACC) {  // acceleration and potential; the jerk stays
         double dx[3];
 #pragma unroll
@@ -1316,6 +1404,11 @@ __global__ void __launch_bounds__(RNT) refine_kernel(KParams kp) {
           }
         }
       }
+    }
+    if (mode & REF_MT) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) sa[k] += (double)ah[k] + (double)al[k];
+      sp += (double)ph + (double)pl;
     }
     // fixed-order reduction: shuffle-down tree, then warps in order
 #pragma unroll
@@ -1354,23 +1447,41 @@ __global__ void __launch_bounds__(RNT) refine_kernel(KParams kp) {
       }
       b->part[e * nch + c] = q;
       __threadfence();
-      const unsigned t = atomicAdd(&b->ticket[e], 1u);
-      if (t == (unsigned)(nch - 1)) {
-        __threadfence();
-        const volatile RefPart *vp = b->part + (size_t)e * nch;
-        double fa[3] = {0.0, 0.0, 0.0}, fp = 0.0, fr2 = inf;
-        int fs = -1;
-        for (int cc = 0; cc < nch; cc++) {
-          for (int k = 0; k < 3; k++) fa[k] += vp[cc].a[k];
-          fp += vp[cc].p;
-          const int sl = vp[cc].slot;
-          const double r2 = vp[cc].r2;
-          if (sl >= 0 && (r2 < fr2 || (r2 == fr2 && sl < fs))) {
-            fr2 = r2;
-            fs = sl;
-          }
+      s_last = atomicAdd(&b->ticket[e], 1u) == (unsigned)(nch - 1);
+    }
+    __syncthreads();
+    // The CTA that completed the entry merges its chunks: warp 0, lane l
+    // taking chunks l and l + 32, then a fixed shuffle tree (the result does
+    // not depend on which CTA finished last).
+    if (s_last && warp == 0) {
+      __threadfence();
+      const volatile RefPart *vp = b->part + (size_t)e * nch;
+      double fa[3] = {0.0, 0.0, 0.0}, fp = 0.0, fr2 = inf;
+      int fs = -1;
+      for (int cc = lane; cc < nch; cc += 32) {
+        for (int k = 0; k < 3; k++) fa[k] += vp[cc].a[k];
+        fp += vp[cc].p;
+        const int sl = vp[cc].slot;
+        const double r2 = vp[cc].r2;
+        if (sl >= 0 && (r2 < fr2 || (r2 == fr2 && sl < fs))) {
+          fr2 = r2;
+          fs = sl;
         }
-        if (mode & REF_ACC) {
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) fa[k] += __shfl_down_sync(0xffffffffu, fa[k], off);
+        fp += __shfl_down_sync(0xffffffffu, fp, off);
+        const double or2 = __shfl_down_sync(0xffffffffu, fr2, off);
+        const int os = __shfl_down_sync(0xffffffffu, fs, off);
+        if (os >= 0 && (or2 < fr2 || (or2 == fr2 && (fs < 0 || os < fs)))) {
+          fr2 = or2;
+          fs = os;
+        }
+      }
+      if (lane == 0) {
+        if (mode & (REF_ACC | REF_MT)) {
           for (int k = 0; k < 3; k++) kp.acc[3 * i + k] = fa[k];
           kp.pot[i] = -fp;
         }
@@ -1390,8 +1501,10 @@ __global__ void __launch_bounds__(RNT) refine_kernel(KParams kp) {
     if (d == gridDim.x - 1) {
       b->h.last = cnt;
       b->h.last_acc = b->h.nacc;
+      b->h.last_mt = b->h.nmt;
       b->h.count = 0u;
       b->h.nacc = 0u;
+      b->h.nmt = 0u;
       b->h.done = 0u;
       __threadfence();
     }
@@ -1562,7 +1675,13 @@ int launch(const KParams &kp, int jl, int gx, cudaStream_t st, cudaEvent_t ev_mi
       reduce_kernel<P><<<(kp.ni + 127) / 128, 128, 0, st>>>(kp);
   }
   if (ev_mid) cudaEventRecord(ev_mid, st);
-  if (kp.refine) refine_kernel<<<2 * sm_count(), RNT, 0, st>>>(kp);
+  // refine_kernel: units of (entry, j-chunk), at most RCHMAX chunks per
+  // entry and ni entries, so small blocks get a small grid
+  if (kp.refine) {
+    const long long cap = (long long)kp.ni * RCHMAX;
+    const int grid = cap < 2LL * sm_count() ? (int)cap : 2 * sm_count();
+    refine_kernel<<<grid, RNT, 0, st>>>(kp);
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
@@ -1572,7 +1691,7 @@ extern "C" int g6k_sm_count(void) { return sm_count(); }
 
 extern "C" size_t g6k_refine_bytes(void) { return sizeof(RefBuf); }
 
-extern "C" int g6k_refine_read(const void *refine, int out[3], cudaStream_t st) {
+extern "C" int g6k_refine_read(const void *refine, int out[4], cudaStream_t st) {
   RefHdr h;
   if (cudaMemcpyAsync(&h, refine, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
@@ -1580,6 +1699,7 @@ extern "C" int g6k_refine_read(const void *refine, int out[3], cudaStream_t st) 
   out[0] = (int)h.last;
   out[1] = (int)h.last_acc;
   out[2] = (int)h.overflow;
+  out[3] = (int)h.last_mt;
   if (h.overflow) {
     const unsigned zero = 0;
     cudaMemcpyAsync(reinterpret_cast<char *>(const_cast<void *>(refine)) +
@@ -1648,7 +1768,14 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
     shape->grid_y = nsplit;
     shape->threads = NT;
   }
-  kp.xtick = (a->refine && nsplit > 1 && gx <= XTMAX)
+  // The in-kernel split merge runs in the one CTA that completes an i-group,
+  // a warp per i: it saves a launch where the group holds one or two i
+  // (JL = 128), but with more i per group that CTA's warps merge them one
+  // after another and the tail outlasts a second launch that gives every i
+  // its own warp (measured, force with merge: 722 i at JL = 4, 136 us in the
+  // kernel against 83 us with the second launch; 64 i at JL = 32, 44 us
+  // against 32 us; 1 i at JL = 128, 21 us against 24 us).
+  kp.xtick = (a->refine && nsplit > 1 && gx <= XTMAX && islots <= G6_XMERGE_MAX)
                  ? reinterpret_cast<RefBuf *>(a->refine)->xtick
                  : nullptr;
   if (a->prec == G6_PREC_FP64) {

@@ -127,14 +127,19 @@ int g6x_get_precision(void);
      within the bound are ranked by ph4's FP64 r^2 (first slot on equal
      values), so nn is ph4's nearest neighbour.
    - Condition number: i-particles whose kappa = sum m/(r^2+eps^2) / |acc|
-     exceeds the limit (default 48, env G6_KAPPA; 0 disables) get acc and
-     pot recomputed in FP64 from the same records (the jerk keeps its split
-     value).
+     exceeds the limit (default 48, env G6_KAPPA; 0 disables both passes)
+     get acc and pot recomputed in FP64 from the same records (the jerk
+     keeps its split value).
+   - Dominant term: i-particles below that limit whose largest single term
+     m/(r^2+eps^2) may exceed |acc| get acc and pot recomputed from the
+     same FP32 pair terms with compensated sums, the terms above 0.005 |acc|
+     in FP64.
    g6x_refine_stats reports the last call's queue: out = {particles queued,
    of which for kappa, largest queue that overflowed the 16384 entries since
-   the last read (then nothing was refined in that call)}. */
+   the last read (then nothing was refined in that call), of which for a
+   dominant term}. */
 int g6x_set_refine(double kappa);
-int g6x_refine_stats(int out[3]);
+int g6x_refine_stats(int out[4]);
 /* Test hook for the force kernel's bounded waits: with on != 0, the next
    force call's first CTA waits for its first j-tile on a barrier that
    nothing arrives on, with a 20 ms limit instead of 2 s.  The wait expires,

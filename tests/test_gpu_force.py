@@ -374,3 +374,44 @@ def test_refine_ill_conditioned(g6):
     assert st["kappa"] >= 1
     assert e.max() <= 1e-6
     assert np.max(np.abs(out["pot"] - ref["pot"]) / np.abs(ref["pot"])) <= 1e-6
+
+
+def test_refine_dominant_term(g6):
+    """i-particles between a cluster's centre and a massive star that pulls
+    against the cluster: one term is ~4 |a| while the condition number stays
+    below its limit, so the dominant-term pass (FP32 terms, compensated sums,
+    the large terms in FP64) must take them to acc <= 1e-6."""
+    g6.set_precision(ag.SPLIT)
+    rng = np.random.RandomState(23)
+    nc = 4000
+    r = rng.uniform(0, 1, nc) ** (1 / 3)
+    u = rng.normal(size=(nc, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    cluster = r[:, None] * u
+    star = np.array([[0.3, 0.0, 0.0]])
+    d, ni = 0.05, 256
+    th = rng.uniform(0, 0.35, ni)
+    ph = rng.uniform(0, 2 * np.pi, ni)
+    dirs = np.stack([np.cos(th), np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph)], 1)
+    xi = star - d * dirs
+    x = np.concatenate([xi, star, cluster])
+    n = len(x)
+    m = np.concatenate([np.full(ni, 1e-12), [1e-3], np.full(nc, 1.0 / nc)])
+    v = rng.normal(0, 0.1, (n, 3))
+    g6.load_particles(m, x, v)
+    sel = np.arange(ni)
+    ref = oracle.force(m, x, v, 1e-6, x[sel], v[sel])
+    try:
+        g6.set_refine(0.0)
+        plain = g6.force(0.0, 1e-6, n, x[sel], v[sel], self_slot=sel)
+        g6.set_refine(48.0)
+        out = g6.force(0.0, 1e-6, n, x[sel], v[sel], self_slot=sel)
+        st = g6.refine_stats()
+    finally:
+        g6.set_refine(48.0)
+    e_plain = vrel(plain["acc"], ref["acc"])
+    e = vrel(out["acc"], ref["acc"])
+    print(f"acc rel err: max {e_plain.max():.2e} without, {e.max():.2e} with the refinement ({st})")
+    assert st["dominant"] >= ni // 2 and st["overflow"] == 0, st
+    assert e.max() <= 1e-6
+    assert np.max(np.abs(out["pot"] - ref["pot"]) / np.abs(ref["pot"])) <= 1e-6

@@ -357,7 +357,8 @@ def run_ours(args):
         "acc": qstats(np.linalg.norm(d32[0] - d64[0], axis=1) / np.linalg.norm(d64[0], axis=1)),
         "jerk": qstats(np.linalg.norm(d32[1] - d64[1], axis=1) / np.linalg.norm(d64[1], axis=1)),
         "pot": qstats(np.abs(d32[2] - d64[2]) / np.abs(d64[2])),
-        "refined_in_fp64": refine_sub["kappa"]}
+        "refined": {"condition_fp64": refine_sub["kappa"],
+                    "dominant_term": refine_sub["dominant"]}}
 
     # the same split kernel with the nearest-neighbour search on (what
     # g6calc_lasthalf2 asks for), on a 65536-particle i-subset
@@ -440,9 +441,12 @@ def run_ours(args):
                          "flop_per_pair": FLOP_PER_PAIR, "force_ms": 1e3 * force_s},
             "refine": {"ms": statistics.mean(rms), "particles": refine_all["queued"],
                        "of_which_condition": refine_all["kappa"],
+                       "of_which_dominant_term": refine_all["dominant"],
                        "share_of_step": statistics.mean(rms) / (1e3 * total / args.steps),
-                       "what": "FP64 acc and pot of the i-particles whose FP32 sum is "
-                               "ill-conditioned (refine_kernel), after the force kernel"},
+                       "what": "refine_kernel after the force kernel: acc and pot redone in "
+                               "FP64 where the FP32 sum is ill-conditioned (kappa > 48), with "
+                               "compensated FP32 sums and the large terms in FP64 where one "
+                               "term exceeds 1.5 |a|"},
             "predictor": {"ms": statistics.mean(pms), "GB_s": pred_gbs,
                           "bytes_per_j": 15 * 8 + 4 + 48,
                           "hbm_peak_gbs": pk.get("hbm_gbs"),

@@ -59,7 +59,7 @@ def build(verbose=False, force=False):
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIB, exist_ok=True)
     headers = [os.path.join(CSRC, "g6_dev.h"), os.path.join(CSRC, "f32x2.cuh"),
-               os.path.join(INCLUDE, "g6.h")]
+               os.path.join(CSRC, "pdl.cuh"), os.path.join(INCLUDE, "g6.h")]
     jobs = []
     objs = []
     for src in CU_SOURCES:

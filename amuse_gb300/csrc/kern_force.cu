@@ -39,6 +39,7 @@
 //     with bit-identical arithmetic to find the index.
 //   * A tile that holds the self slot of one of the warp's i-particles takes
 //     a checked copy of the loop (rinv = 0, r2 -> +inf for self).
+#include "pdl.cuh"
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -900,6 +901,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
   const int jl = tid % JL;
   const int il = tid / JL;
   const int lane = tid & 31;
+  pdl_wait();  // the predictor's records and the block list are complete
 
   // ---- i-particles of this thread ----
   typename P::I I[IPT];
@@ -1070,6 +1072,7 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
     }
   }
 
+  pdl_trigger();  // j loop done: the next kernel of the chain may be scheduled
   if (__syncthreads_or(failed)) {
     // Drain the copies still in flight (bounded) before the CTA leaves.
     if (tid == 0) {
@@ -1202,6 +1205,8 @@ __global__ void __launch_bounds__(NT, P::MINB) force_kernel(KParams kp) {
 // (one thread per i; for large blocks).
 template <class P>
 __global__ void reduce_kernel(KParams kp) {
+  pdl_wait();
+  pdl_trigger();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= kp.ni) return;
   const typename P::Out *part = reinterpret_cast<const typename P::Out *>(kp.part);
@@ -1216,6 +1221,8 @@ __global__ void reduce_kernel(KParams kp) {
 // shuffle-down tree.  Deterministic for a given (ni, nsplit).
 template <class P>
 __global__ void reduce_warp_kernel(KParams kp) {
+  pdl_wait();
+  pdl_trigger();
   const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (i >= kp.ni) return;  // whole warps exit together
@@ -1286,6 +1293,8 @@ __device__ __forceinline__ void mt_term(float xh, float yh, float zh, float m, f
 }
 
 __global__ void __launch_bounds__(RNT) refine_kernel(KParams kp) {
+  pdl_wait();
+  pdl_trigger();
   RefBuf *b = reinterpret_cast<RefBuf *>(kp.refine);
   __shared__ unsigned s_cnt;
   __shared__ double s_sum[RNT / 32][5];
@@ -1670,9 +1679,9 @@ int launch(const KParams &kp, int jl, int gx, cudaStream_t st, cudaEvent_t ev_mi
   }
   if (kp.nsplit > 1 && !kp.xtick) {
     if (kp.ni < 4096)
-      reduce_warp_kernel<P><<<(kp.ni + 3) / 4, 128, 0, st>>>(kp);
+      launch_pdl(reduce_warp_kernel<P>, dim3((kp.ni + 3) / 4), dim3(128), 0, st, kp);
     else
-      reduce_kernel<P><<<(kp.ni + 127) / 128, 128, 0, st>>>(kp);
+      launch_pdl(reduce_kernel<P>, dim3((kp.ni + 127) / 128), dim3(128), 0, st, kp);
   }
   if (ev_mid) cudaEventRecord(ev_mid, st);
   // refine_kernel: units of (entry, j-chunk), at most RCHMAX chunks per
@@ -1680,7 +1689,7 @@ int launch(const KParams &kp, int jl, int gx, cudaStream_t st, cudaEvent_t ev_mi
   if (kp.refine) {
     const long long cap = (long long)kp.ni * RCHMAX;
     const int grid = cap < 2LL * sm_count() ? (int)cap : 2 * sm_count();
-    refine_kernel<<<grid, RNT, 0, st>>>(kp);
+    launch_pdl(refine_kernel, dim3(grid), dim3(RNT), 0, st, kp);
   }
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }

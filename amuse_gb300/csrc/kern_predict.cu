@@ -16,6 +16,7 @@
 // Slots [nj, roundup(nj, G6_TILE)) get zero-mass records far away so the force
 // kernel streams whole tiles.  Streams 15 doubles + 1 int per slot
 // (coalesced, component-major arrays) and writes one record.
+#include "pdl.cuh"
 #include <cuda_runtime.h>
 
 #include "g6_dev.h"
@@ -131,6 +132,8 @@ __global__ void __launch_bounds__(PT) list_predict_kernel(g6_jstate js, int nj, 
                                                           const unsigned long long *dmin,
                                                           unsigned long long *dmin_next,
                                                           int *ilist, int *dni, double *dtnext) {
+  pdl_wait();
+  pdl_trigger();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   const double tn = __longlong_as_double((long long)*dmin);
   if (s == 0) {
@@ -169,11 +172,11 @@ extern "C" int g6k_list_predict(const g6_jstate *js, int nj, int prec,
   const int nj_pad = (nj + G6_TILE - 1) / G6_TILE * G6_TILE;
   if (nj_pad > js->cap) return -1;
   const int grid = (nj_pad + PT - 1) / PT;
-  if (prec == G6_PREC_FP64)
-    list_predict_kernel<G6_PREC_FP64><<<grid, PT, 0, st>>>(*js, nj, nj_pad, dmin, dmin_next,
-                                                           d_ilist, d_ni, d_tnext);
-  else
-    list_predict_kernel<G6_PREC_SPLIT><<<grid, PT, 0, st>>>(*js, nj, nj_pad, dmin, dmin_next,
-                                                            d_ilist, d_ni, d_tnext);
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+  const cudaError_t e =
+      prec == G6_PREC_FP64
+          ? launch_pdl(list_predict_kernel<G6_PREC_FP64>, dim3(grid), dim3(PT), 0, st, *js, nj,
+                       nj_pad, dmin, dmin_next, d_ilist, d_ni, d_tnext)
+          : launch_pdl(list_predict_kernel<G6_PREC_SPLIT>, dim3(grid), dim3(PT), 0, st, *js, nj,
+                       nj_pad, dmin, dmin_next, d_ilist, d_ni, d_tnext);
+  return e == cudaSuccess ? 0 : -3;
 }

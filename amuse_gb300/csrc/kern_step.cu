@@ -15,6 +15,7 @@
 //   encounter check  idata::check_encounters (idata.cc:620-700) over a
 //                    block, and the COLLISION_DETECTION test of
 //                    jdata::advance_and_check_encounter (jdata.cc:797-850).
+#include "pdl.cuh"
 #include <cuda_runtime.h>
 #include <limits.h>
 #include <stdint.h>
@@ -64,6 +65,8 @@ __global__ void correct_kernel(g6_jstate js, int ni, const int *__restrict__ ili
                                double eta, const double *__restrict__ acc,
                                const double *__restrict__ jerk, const double *__restrict__ pot,
                                const int *__restrict__ nn) {
+  pdl_wait();
+  pdl_trigger();
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = g >> 2;
   const int k = g & 3;
@@ -327,6 +330,8 @@ __global__ void store_kernel(g6_jstate js, int ni, const int *__restrict__ ilist
 // block's encounter stopping decision (after that block's corrector).
 __global__ void sched_min_first(g6_jstate js, int nj, unsigned long long *dmin, int *dni,
                                 g6_enc_decision_args v) {
+  pdl_wait();
+  pdl_trigger();
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *dni = 0;
     if (v.enc) enc_decide(js, v.enc, v.mode, v.t, v.flag);
@@ -446,8 +451,10 @@ extern "C" int g6k_correct(const g6_jstate *js, int ni, const int *ilist, double
                            const int *nn, cudaStream_t st) {
   if (ni <= 0) return 0;
   // 4 lanes per particle, 32 particles per 128-thread block
-  correct_kernel<<<(ni + 31) / 32, 128, 0, st>>>(*js, ni, ilist, tnext, eta, acc, jerk, pot, nn);
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+  return launch_pdl(correct_kernel, dim3((ni + 31) / 32), dim3(128), 0, st, *js, ni, ilist, tnext,
+                    eta, acc, jerk, pot, nn) == cudaSuccess
+             ? 0
+             : -3;
 }
 
 extern "C" int g6k_store_forces(const g6_jstate *js, int ni, const int *ilist, const double *acc,
@@ -483,8 +490,10 @@ extern "C" int g6k_sched_first(const g6_jstate *js, int nj, unsigned long long *
     v.t = 0;
     v.flag = NULL;
   }
-  sched_min_first<<<grid, PT, 0, st>>>(*js, nj, dmin, d_ni, v);
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+  return launch_pdl(sched_min_first, dim3(grid), dim3(PT), 0, st, *js, nj, dmin, d_ni, v) ==
+                 cudaSuccess
+             ? 0
+             : -3;
 }
 
 extern "C" int g6k_enc_check(const g6_jstate *js, const double *rad, int ni, const int *ilist,

@@ -252,12 +252,12 @@ struct SplitP {
   struct Tot {  // compensated totals (s: plain sum, an estimate), largest chunk of s
     float ah[3], al[3], jh[3], jl[3], ph, pl, s, mt, pad;  // 17 words: odd stride
   };
-  struct Out {  // partial record exchanged between CTAs, 72 B
+  struct Out {  // partial record exchanged between CTAs, 80 B
     float2 a[3], j[3], p;
     float nnr2;   // smallest nearest-neighbour key (r^2 + eps^2, FP32)
     float nnr2b;  // second smallest key over the other j
     float s1;     // sum of m / (r^2 + eps^2): the condition number's numerator
-    float mt;     // max m / r times max 1/r (softened): bounds the largest term
+    float mt;     // largest partial sum of s over 32 j: bounds the largest term
     int nn;
     int pad;
   };
@@ -496,7 +496,7 @@ struct F64P {
   struct Tot {
     double a[3], j[3], p;
   };
-  struct Out {  // 80 B
+  struct Out {  // 72 B
     double a[3], j[3], p;
     double nnr2;
     int nn, pad;
@@ -742,8 +742,16 @@ enum { REF_ACC = 1, REF_NN = 2, REF_MT = 4 };
 // the roundings of r^2, the differences and the products), and a partial
 // sum holding it rounds every later term to its own ulp.
 constexpr double MU0 = 1.5;
-// Terms above TAU |a| are evaluated in FP64 in the REF_MT pass.
-constexpr float TAU = 0.005f;
+// Terms above TAU |a| are evaluated in FP64 in the REF_MT pass.  A warp
+// takes the FP64 branch whenever one of its lanes does, at 1/64 of the FP32
+// rate, so TAU is kept where few terms reach it: at 0.02 the remaining
+// terms' random errors stay below ~1e-7 sqrt(0.02 kappa) |a| (C2 at 65536
+// Salpeter: the same largest error as at 0.005, and the block loop 2 %
+// faster).
+#ifndef G6_TAU
+#define G6_TAU 0.02f
+#endif
+constexpr float TAU = G6_TAU;
 
 struct RefHdr {
   unsigned count;     // entries queued by this call (reset by refine_kernel)

@@ -294,6 +294,54 @@ def run_precision(args):
     return out
 
 
+def run_blocks(args):
+    """Config 2's system at fixed block sizes: for ni random slots of the
+    Salpeter N = 65536 system at t = 0, the GPU time of the force kernel (with
+    its split merge) and of the refinement pass (CUDA events), the refinement
+    queue and the launch shape; the median of the repeats after two warm-up
+    calls."""
+    import torch
+    import amuse_gb300 as ag
+    from amuse_gb300 import ic
+    n, eps2 = args.n, 1e-6
+    g6 = ag.G6X(0)
+    ilist = torch.arange(n, dtype=torch.int32, device="cuda")
+
+    def gpu_potential(mass, pos):
+        g6.load_particles(mass, pos, np.zeros_like(pos))
+        _, _, pot, _ = _slot_forces(g6, torch, ag.FP64, len(mass), len(mass), 0.0, ilist)
+        return 0.5 * float(np.sum(mass * pot))
+
+    rng = np.random.RandomState(args.seed)
+    m, x, v = ic.plummer_salpeter(n, mass_min=0.1, mass_max=100.0, rng=rng,
+                                  potential_energy=gpu_potential)
+    g6.load_particles(m, x, v)
+    g6.set_precision(ag.SPLIT)
+    rows = []
+    for ni in args.ni:
+        sel = np.sort(np.random.RandomState(ni).choice(n, ni, replace=False)).astype(np.int32)
+        il = torch.tensor(sel, device="cuda")
+        a = torch.empty((ni, 3), dtype=torch.float64, device="cuda")
+        j = torch.empty_like(a)
+        p = torch.empty(ni, dtype=torch.float64, device="cuda")
+        g6.timing(True)
+        ks, rs = [], []
+        for r in range(2 + args.reps):
+            g6.force_slots(0.0, eps2, n, il.data_ptr(), ni, a.data_ptr(), j.data_ptr(),
+                           p.data_ptr(), None)
+            st = g6.stats()
+            if r >= 2:
+                ks.append(st["kernel_ms"] * 1e3)
+                rs.append(st["refine_ms"] * 1e3)
+        g6.timing(False)
+        rows.append({"ni": ni, "force_us": float(np.median(ks)), "refine_us": float(np.median(rs)),
+                     "refine": g6.refine_stats(), "jl": int(st["jl"]),
+                     "nsplit": int(st["nsplit"])})
+    print(json.dumps({"workload": f"plummer N={n} Salpeter IMF (-2.35, 0.1-100) eps2={eps2}, "
+                                  f"seed {args.seed}, t = 0: force calls on ni random slots",
+                      "blocks": rows}), flush=True)
+
+
 def run_salpeter(args):
     """Config 2: Plummer N = 65536 with a Salpeter IMF (slope -2.35, mass
     range 0.1-100, total mass 1, re-scaled to virial after the masses),
@@ -423,6 +471,11 @@ def main():
     sa.add_argument("--fp64", action="store_true")
     sa.add_argument("--encounters", action="store_true",
                     help="repeat the run with the encounter check on and report its cost")
+    bl = sub.add_parser("blocks")
+    bl.add_argument("--n", type=int, default=65536)
+    bl.add_argument("--seed", type=int, default=1)
+    bl.add_argument("--reps", type=int, default=5)
+    bl.add_argument("--ni", type=int, nargs="+", default=[1, 16, 128, 722, 4096, 65536])
     kn = sub.add_parser("knn")
     kn.add_argument("--n", type=int, default=1 << 20)
     kn.add_argument("--k", type=int, default=12)
@@ -438,6 +491,8 @@ def main():
         run_salpeter(a)
     elif a.cmd == "knn":
         run_knn(a)
+    elif a.cmd == "blocks":
+        run_blocks(a)
 
 
 if __name__ == "__main__":

@@ -132,7 +132,7 @@ int g6x_get_precision(void);
      keeps its split value).
    - Dominant term: i-particles below that limit whose largest single term
      m/(r^2+eps^2) may exceed |acc| get acc and pot recomputed from the
-     same FP32 pair terms with compensated sums, the terms above 0.005 |acc|
+     same FP32 pair terms with compensated sums, the terms above 0.02 |acc|
      in FP64.
    g6x_refine_stats reports the last call's queue: out = {particles queued,
    of which for kappa, largest queue that overflowed the 16384 entries since

@@ -63,7 +63,7 @@ PRED_FP64_OPS = 36  # FP64-pipe operations per j of the split-record predictor
 # DRAM bytes (read + write) of one force launch at the default N = 2^20, from
 # one ncu capture of this benchmark (profiles/force_kernel_dram_n1048576.md).
 FORCE_TRAFFIC_N = 1 << 20
-FORCE_TRAFFIC_BYTES = 75132672 + 47213568
+FORCE_TRAFFIC_BYTES = 81806592 + 89248256
 N_DEFAULT = 1 << 20
 EPS2 = 1e-6
 ETA = 0.01

@@ -51,7 +51,7 @@ EXT_SYMBOLS = [
     "g6x_test_wait_expiry", "g6x_batch_unperturbed", "g6x_batch_binaries", "g6x_set_npipes", "g6x_last_error", "g6x_load",
     "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
     "g6x_energy", "g6x_run_stats", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
-    "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stats_n", "g6x_stream",
+    "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stats_n", "g6x_set_shape", "g6x_stream",
     "g6x_set_fixed_jerk", "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp",
     "g6x_fixed_step_adjoint", "g6x_fixed_run", "g6x_fixed_adjoint_run",
     "g6x_set_encounters", "g6x_set_radius", "g6x_encounter", "g6x_knn",
@@ -132,6 +132,7 @@ def load():
     lib.g6x_timing.argtypes = [I]
     lib.g6x_stats.argtypes = [_pd]
     lib.g6x_stats_n.argtypes = [_pd, ctypes.c_int]
+    lib.g6x_set_shape.argtypes = [ctypes.c_int, ctypes.c_int]
     lib.g6x_stream.restype = _vp
     lib.g6x_set_fixed_jerk.argtypes = [I]
     lib.g6x_fixed_force.argtypes = [I, D] + [_vp] * 5
@@ -500,6 +501,10 @@ class G6X(G6):
 
     def stream(self):
         return self.lib.g6x_stream()
+
+    def set_shape(self, jl=0, nsplit=0):
+        """Launch shape override (0: the cost model's choice)."""
+        _check(self.lib.g6x_set_shape(int(jl), int(nsplit)), "g6x_set_shape")
 
 
 def drive_load(mass, pos, vel, acc=None, jerk=None, t=None, dt=None, ids=None):

@@ -164,6 +164,7 @@ typedef struct {
   int timing;
   double st_predict_ms, st_force_ms, st_pairs, st_pred_bytes, st_nj;
   double st_kernel_ms, st_refine_ms; /* force_ms split at the refinement pass */
+  int shape_jl, shape_ns;            /* launch shape override (0: the cost model's) */
   g6_shape shape;
   int predicted_this_call;
   char err[256];
@@ -403,6 +404,8 @@ static void refine_args(g6_force_args *a) {
 
 /* Run one force evaluation whose inputs are already on the device. */
 static int run_force(g6_force_args *a) {
+  if (!a->force_jl && !a->hjerk) a->force_jl = G.shape_jl;
+  if (!a->force_nsplit) a->force_nsplit = G.shape_ns;
   size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->hjerk ? 1 : a->force_jl,
                                   a->force_nsplit);
   int rc = ensure_scratch(need);
@@ -951,6 +954,12 @@ int g6x_set_precision(int prec) {
   return 0;
 }
 int g6x_get_precision(void) { return G.prec; }
+int g6x_set_shape(int jl, int nsplit) {
+  if (jl < 0 || jl > 256 || (jl & (jl - 1)) || nsplit < 0) return G6_ERR_ARG;
+  G.shape_jl = jl;
+  G.shape_ns = nsplit;
+  return 0;
+}
 int g6x_set_refine(double kappa) {
   if (!(kappa >= 0.0)) return G6_ERR_ARG;
   G.kappa = kappa;

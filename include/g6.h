@@ -261,6 +261,11 @@ int g6x_stats(double out[8]);
    its split-j merge), out[9] the refinement pass's ms (out[1] = out[8] +
    out[9] for split-precision calls). */
 int g6x_stats_n(double *out, int n);
+/* Launch shape override for the following force calls: jl j-lanes per
+   i-particle (a power of two up to 256) and nsplit j-ranges, each 0 for the
+   cost model's choice (the default).  For tuning and measurement; results do
+   not depend on the shape beyond the FP32 summation order. */
+int g6x_set_shape(int jl, int nsplit);
 
 /* Batched few-body systems (the encounters AMUSE's multiples module hands
    to smallN): nsys independent systems of n_per_sys[s] bodies (2..64),

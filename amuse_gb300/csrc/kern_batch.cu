@@ -581,19 +581,18 @@ __device__ void kep_prop(double mu, const double r0[3], const double v0[3], doub
     return c1 * x * x * C + c2 * x * x * x * S + rn * x - smu * dt;
   };
   const bool warm = xw && *dtw > 0.0 && dt > 0.0;
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
   double x0 = alpha > 0.0 ? smu * dt * alpha : smu * dt / rn;  // sign of dt
   double lo, hi;
   if (warm) {
+    // The root lies above xw when dt >= dtw (F(xw) <= 0), else in (0, xw).
+    // No evaluation before the first Newton step: with hi = +inf, steps from
+    // below (F < 0, dF > 0) only move up, until one lands above the root and
+    // bounds it.
     x0 = *xw + smu * (dt - *dtw) / *rw;
-    if (!(x0 > 0.0)) x0 = 0.5 * *xw;
-    // the root lies above xw when dt > dtw, below it otherwise (and above 0)
     lo = dt >= *dtw ? *xw : 0.0;
-    hi = dt >= *dtw ? x0 : *xw;
-    if (x0 < lo || x0 > hi) x0 = 0.5 * (lo + hi);
-    if (dt >= *dtw) {
-      if (!(hi > lo)) hi = lo + fabs(lo) + 1e-300;
-      for (int k = 0; k < 200 && Fx(hi) < 0.0; k++) lo = hi, hi = 2.0 * hi;
-    }
+    hi = dt >= *dtw ? inf : *xw;
+    if (!(x0 > lo && x0 < hi)) x0 = hi < inf ? 0.5 * (lo + hi) : lo + fabs(lo) + 1e-300;
   } else if (dt > 0.0) {
     lo = 0.0, hi = x0;
     for (int k = 0; k < 200 && Fx(hi) < 0.0; k++) lo = hi, hi *= 2.0;
@@ -614,7 +613,7 @@ __device__ void kep_prop(double mu, const double r0[3], const double v0[3], doub
     else
       hi = x;
     double xn = x - F / dF;
-    if (!(xn > lo && xn < hi) || fabs(2.0 * F) > fabs(step_old * dF)) {
+    if (hi < inf && (!(xn > lo && xn < hi) || fabs(2.0 * F) > fabs(step_old * dF))) {
       step_old = step;
       step = 0.5 * (hi - lo);
       xn = lo + step;

@@ -104,7 +104,7 @@ typedef struct {
   int jl, nsplit, grid_x, grid_y, threads;
 } g6_shape;
 
-size_t g6k_scratch_bytes(int ni, int nj, int prec, int force_jl, int force_nsplit);
+size_t g6k_scratch_bytes(int ni, int nj, int prec, int nn, int force_jl, int force_nsplit);
 int g6k_sm_count(void);
 
 int g6k_scatter(const g6_jstate *js, const g6_jupd *d_upd, int n, cudaStream_t st);

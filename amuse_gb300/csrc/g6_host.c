@@ -406,7 +406,7 @@ static void refine_args(g6_force_args *a) {
 static int run_force(g6_force_args *a) {
   if (!a->force_jl && !a->hjerk) a->force_jl = G.shape_jl;
   if (!a->force_nsplit) a->force_nsplit = G.shape_ns;
-  size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->hjerk ? 1 : a->force_jl,
+  size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->want_nn, a->hjerk ? 1 : a->force_jl,
                                   a->force_nsplit);
   int rc = ensure_scratch(need);
   if (rc) return rc;

@@ -1555,17 +1555,20 @@ int sm_count() {
 // JL = 1) stay at JL = 1.  The last few shapes are cached (block steps
 // repeat the same ni).
 struct ShapeKey {
-  int ni, nj, prec, fjl, fns;
+  int ni, nj, prec, nn, fjl, fns;
   int jl, nsplit, jsplit;
 };
 ShapeKey g_shape_cache[256];
 
-void choose_shape(int ni, int nj, int prec, int force_jl, int force_nsplit, int *jl_out,
+void choose_shape(int ni, int nj, int prec, int nn, int force_jl, int force_nsplit, int *jl_out,
                   int *nsplit_out, int *jsplit_out) {
-  const unsigned h = ((unsigned)ni * 2654435761u ^ (unsigned)nj * 40503u ^ (unsigned)prec) & 255u;
+  nn = nn ? 1 : 0;
+  const unsigned h =
+      ((unsigned)ni * 2654435761u ^ (unsigned)nj * 40503u ^ (unsigned)prec ^ (unsigned)nn * 97u) &
+      255u;
   ShapeKey &c = g_shape_cache[h];
-  if (c.ni == ni && c.nj == nj && c.prec == prec && c.fjl == force_jl && c.fns == force_nsplit &&
-      c.jl > 0) {
+  if (c.ni == ni && c.nj == nj && c.prec == prec && c.nn == nn && c.fjl == force_jl &&
+      c.fns == force_nsplit && c.jl > 0) {
     *jl_out = c.jl;
     *nsplit_out = c.nsplit;
     *jsplit_out = c.jsplit;
@@ -1621,11 +1624,13 @@ void choose_shape(int ni, int nj, int prec, int force_jl, int force_nsplit, int 
       const long long ctas = gx * ns;
       const long long waves = (ctas + slots - 1) / slots;
       // Where the i-groups alone do not fill the GPU, CTAs are kept to at
-      // most 128 tiles: many short CTAs balance over the SMs as slots free
-      // up, better than a few long ones in one wave (measured, 16384 i
-      // against 2^20 j: 0.674 of peak at 7 splits of 586 tiles, 0.700 at 38
-      // or 57 splits; the wave count does not capture it).
-      if (gx < slots && tp > 128 && k + 1 < nc) continue;
+      // most 128 tiles (256 with the nearest neighbour, whose CTAs each
+      // re-scan a best tile at the end): many short CTAs balance over the
+      // SMs as slots free up, better than a few long ones in one wave
+      // (measured, 16384 i against 2^20 j: 0.674 of peak at 7 splits of 586
+      // tiles, 0.700 at 38 or 57 splits; the wave count does not capture
+      // it; with nn at 65536 i: 0.690 at 16 splits, 0.685 at 32).
+      if (gx < slots && tp > (nn ? 256 : 128) && k + 1 < nc) continue;
       // j-lanes (JL > 1) cost a few per cent per pair in large blocks
       // (measured at 65536 i: JL = 2 ran 3 % slower than JL = 1 without the
       // nearest neighbour and 6 % slower with it), where JL = 1 fills the
@@ -1653,6 +1658,7 @@ void choose_shape(int ni, int nj, int prec, int force_jl, int force_nsplit, int 
   c.ni = ni;
   c.nj = nj;
   c.prec = prec;
+  c.nn = nn;
   c.fjl = force_jl;
   c.fns = force_nsplit;
   c.jl = *jl_out;
@@ -1733,9 +1739,10 @@ extern "C" int g6k_refine_read(const void *refine, int out[4], cudaStream_t st) 
   return 0;
 }
 
-extern "C" size_t g6k_scratch_bytes(int ni, int nj, int prec, int force_jl, int force_nsplit) {
+extern "C" size_t g6k_scratch_bytes(int ni, int nj, int prec, int nn, int force_jl,
+                                    int force_nsplit) {
   int jl, nsplit, jsplit;
-  choose_shape(ni, nj, prec, force_jl, force_nsplit, &jl, &nsplit, &jsplit);
+  choose_shape(ni, nj, prec, nn, force_jl, force_nsplit, &jl, &nsplit, &jsplit);
   if (nsplit <= 1) return 0;
   const size_t rec = prec == G6_PREC_FP64 ? sizeof(F64P::Out) : sizeof(SplitP::Out);
   return (size_t)nsplit * (size_t)ni * rec;
@@ -1747,8 +1754,8 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
   if (!a->ilist && (!a->ipos || !a->ivel)) return -1;
   if (a->hjerk && (a->want_nn || (a->force_jl != 0 && a->force_jl != 1))) return -2;
   int jl, nsplit, jsplit;
-  choose_shape(a->ni, a->nj, a->prec, a->hjerk ? 1 : a->force_jl, a->force_nsplit, &jl, &nsplit,
-               &jsplit);
+  choose_shape(a->ni, a->nj, a->prec, a->want_nn, a->hjerk ? 1 : a->force_jl, a->force_nsplit,
+               &jl, &nsplit, &jsplit);
   if (jl < 1 || jl > JLMAX || (jl & (jl - 1))) return -2;
   KParams kp;
   kp.ni = a->ni;
@@ -1780,7 +1787,8 @@ extern "C" int g6k_force(const g6_force_args *a, g6_shape *shape, cudaStream_t s
   kp.kappa2 = a->kappa > 0.0 ? a->kappa * a->kappa : 0.0;
   kp.stall = a->stall_test;
   kp.wait_ns = a->stall_test ? STALL_TEST_NS : WAIT_NS;
-  const size_t need = nsplit > 1 ? g6k_scratch_bytes(a->ni, a->nj, a->prec, jl, nsplit) : 0;
+  const size_t need =
+      nsplit > 1 ? g6k_scratch_bytes(a->ni, a->nj, a->prec, a->want_nn, jl, nsplit) : 0;
   if (need > a->scratch_bytes) return -4;
   const int islots = (NT / jl) * (a->prec == G6_PREC_FP64 ? IPT_F64 : IPT_SPLIT);
   const int gx = (a->ni + islots - 1) / islots;
@@ -1843,7 +1851,8 @@ extern "C" int g6k_static_scratch_addr(void **out) {
 extern "C" int g6k_force_static(const g6_force_args *a, void *static_addr, g6_shape *shape,
                                 cudaStream_t st, size_t *need_out) {
   if (!static_addr) return -5;
-  const size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->hjerk ? 1 : a->force_jl,
+  const size_t need = g6k_scratch_bytes(a->ni, a->nj, a->prec, a->want_nn,
+                                        a->hjerk ? 1 : a->force_jl,
                                         a->force_nsplit);
   if (need_out) *need_out = need;
   if (need > G6_STATIC_SCRATCH_BYTES) return -4;

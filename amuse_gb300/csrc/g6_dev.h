@@ -12,8 +12,11 @@
  *                             split: 48 B per slot, stored in pairs of slots
  *                                    (2p, 2p+1) with every field a float2
  *                                    {slot 2p, slot 2p+1}, 96 B per pair:
- *                                    [xh yh zh m][xl yl zl 0][vx vy vz 0]
- *                                    (the force kernel's packed f32x2 loads)
+ *                                    [xh yh zh m][xl yl zl ml][vx vy vz 0]
+ *                                    (the force kernel's packed f32x2 loads;
+ *                                    m + ml is the FP64 mass to 2^-48, the
+ *                                    force kernel uses m, the refinement
+ *                                    pass both)
  *                             fp64 : 64 B {x,y,z,m}{vx,vy,vz,0}
  * Accelerations and jerks are stored unscaled (the GRAPE-6 a/2, j/6 inputs
  * are rescaled on the host), so the device predictor evaluates exactly
@@ -206,11 +209,11 @@ __device__ __forceinline__ float g6_split_get(const void *base, int s, int f) {
   return *g6_split_field((void *)base, s, f);
 }
 __device__ __forceinline__ void g6_split_store(void *base, int s, float xh, float yh, float zh,
-                                               float m, float xl, float yl, float zl, float vx,
-                                               float vy, float vz) {
+                                               float m, float ml, float xl, float yl, float zl,
+                                               float vx, float vy, float vz) {
   float *p = (float *)base + (size_t)(s >> 1) * 24 + (s & 1);
   p[0] = xh; p[2] = yh; p[4] = zh; p[6] = m;
-  p[8] = xl; p[10] = yl; p[12] = zl; p[14] = 0.f;
+  p[8] = xl; p[10] = yl; p[12] = zl; p[14] = ml;
   p[16] = vx; p[18] = vy; p[20] = vz; p[22] = 0.f;
 }
 #endif

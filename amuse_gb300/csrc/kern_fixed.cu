@@ -78,8 +78,10 @@ __global__ void records_kernel(int n, int n_pad, const double *__restrict__ x,
       h[k] = __double2float_rn(xp[k]);
       l[k] = __double2float_rn(xp[k] - (double)h[k]);
     }
-    g6_split_store(jp_split, s, h[0], h[1], h[2], __double2float_rn(mm), l[0], l[1], l[2],
-                   __double2float_rn(vp[0]), __double2float_rn(vp[1]), __double2float_rn(vp[2]));
+    const float mh = __double2float_rn(mm);
+    g6_split_store(jp_split, s, h[0], h[1], h[2], mh, __double2float_rn(mm - (double)mh), l[0],
+                   l[1], l[2], __double2float_rn(vp[0]), __double2float_rn(vp[1]),
+                   __double2float_rn(vp[2]));
   }
 }
 

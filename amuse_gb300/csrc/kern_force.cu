@@ -111,7 +111,7 @@ enum { ERR_TMA_TIMEOUT = 1, ERR_SHAPE = 2 };
 // {j even, j odd} (the global layout the predictor writes, g6_dev.h), so a
 // packed f32x2 instruction evaluates two j at once.
 struct __align__(16) RecS {
-  float2 xh, yh, zh, m, xl, yl, zl, pad0, vx, vy, vz, pad1;
+  float2 xh, yh, zh, m, xl, yl, zl, ml, vx, vy, vz, pad1;  // ml: the mass's low part
 };
 struct __align__(32) RecD {
   G6D4 p, v;
@@ -740,8 +740,10 @@ enum { REF_ACC = 1, REF_NN = 2, REF_MT = 4 };
 // term carries up to ~7e-7 relative error (three times the 1.25e-7 of the
 // MUFU reciprocal square root, measured over all FP32 inputs in [1, 4), plus
 // the roundings of r^2, the differences and the products), and a partial
-// sum holding it rounds every later term to its own ulp.
-constexpr double MU0 = 1.5;
+// sum holding it rounds every later term to its own ulp.  At 1.5 a particle
+// with a term of 1.4 |a| reached 1.23e-6 (a star pulling against a cluster,
+// 6000 bodies); at 1.0 the worst left unrefined is one term's error.
+constexpr double MU0 = 1.0;
 // Terms above TAU |a| are evaluated in FP64 in the REF_MT pass.  A warp
 // takes the FP64 branch whenever one of its lanes does, at 1/64 of the FP32
 // rate, so TAU is kept where few terms reach it: at 0.02 the remaining
@@ -1269,8 +1271,8 @@ __device__ __forceinline__ double refine_rsqrt(double x) {
 // One j of a REF_MT entry: the force kernel's FP32 term (same operations,
 // so the same value up to the final product's rounding) into compensated
 // FP32 sums, or, above thr = TAU |a|, the FP64 term into the FP64 sums.
-__device__ __forceinline__ void mt_term(float xh, float yh, float zh, float m, float xl, float yl,
-                                        float zl, const float ih[3], const float il[3],
+__device__ __forceinline__ void mt_term(float xh, float yh, float zh, float m, float ml, float xl,
+                                        float yl, float zl, const float ih[3], const float il[3],
                                         const double xi[3], float e32, double eps2, float thr,
                                         double sa[3], double &sp, float ah[3], float al[3],
                                         float &ph, float &pl) {
@@ -1287,16 +1289,24 @@ __device__ __forceinline__ void mt_term(float xh, float yh, float zh, float m, f
     for (int k = 0; k < 3; k++) dx[k] = ((double)jh[k] + (double)jl[k]) - xi[k];
     const double r2 = __fma_rn(dx[2], dx[2], __fma_rn(dx[1], dx[1], __fma_rn(dx[0], dx[0], eps2)));
     const double ri = refine_rsqrt(r2);
-    const double mr = (double)m * ri;
+    const double mr = ((double)m + (double)ml) * ri;
     const double mr3 = mr * (ri * ri);
 #pragma unroll
     for (int k = 0; k < 3; k++) sa[k] = __fma_rn(mr3, dx[k], sa[k]);
     sp += mr;
   } else {
+    // the FP32 term with the mass's high part, compensated; its low part
+    // (2^-24 of the term) goes straight into the low words
+    const float r3 = __fmul_rn(rinv, __fmul_rn(rinv, rinv));
     const float mr3i = __fmul_rn(mri, __fmul_rn(rinv, rinv));
+    const float lr3 = __fmul_rn(ml, r3);
 #pragma unroll
-    for (int k = 0; k < 3; k++) ff_acc(ah[k], al[k], __fmul_rn(mr3i, d[k]));
+    for (int k = 0; k < 3; k++) {
+      ff_acc(ah[k], al[k], __fmul_rn(mr3i, d[k]));
+      al[k] = __fmaf_rn(lr3, d[k], al[k]);
+    }
     ff_acc(ph, pl, mri);
+    pl = __fmaf_rn(ml, rinv, pl);
   }
 }
 
@@ -1377,25 +1387,26 @@ __global__ void __launch_bounds__(RNT) refine_kernel(KParams kp) {
         const float4 A = __ldg(q4 + 6 * rp), B = __ldg(q4 + 6 * rp + 1);
         const float4 C = __ldg(q4 + 6 * rp + 2), D = __ldg(q4 + 6 * rp + 3);
         if (2 * rp != self && 2 * rp < kp.nj)
-          mt_term(A.x, A.z, B.x, B.z, C.x, C.z, D.x, ih, il, xi, e32, eps2, thr_mt, sa, sp, ah,
-                  al, ph, pl);
+          mt_term(A.x, A.z, B.x, B.z, D.z, C.x, C.z, D.x, ih, il, xi, e32, eps2, thr_mt, sa, sp,
+                  ah, al, ph, pl);
         if (2 * rp + 1 != self && 2 * rp + 1 < kp.nj)
-          mt_term(A.y, A.w, B.y, B.w, C.y, C.w, D.y, ih, il, xi, e32, eps2, thr_mt, sa, sp, ah,
-                  al, ph, pl);
+          mt_term(A.y, A.w, B.y, B.w, D.w, C.y, C.w, D.y, ih, il, xi, e32, eps2, thr_mt, sa, sp,
+                  ah, al, ph, pl);
       }
     }
     for (int j = j0 + tid; mode != REF_MT && j < j1; j += RNT) {
       if (j == self) continue;
       if (mode & REF_MT)
         mt_term(g6_split_get(rec, j, 0), g6_split_get(rec, j, 1), g6_split_get(rec, j, 2),
-                g6_split_get(rec, j, 3), g6_split_get(rec, j, 4), g6_split_get(rec, j, 5),
-                g6_split_get(rec, j, 6), ih, il, xi, e32, eps2, thr_mt, sa, sp, ah, al, ph, pl);
+                g6_split_get(rec, j, 3), g6_split_get(rec, j, 7), g6_split_get(rec, j, 4),
+                g6_split_get(rec, j, 5), g6_split_get(rec, j, 6), ih, il, xi, e32, eps2, thr_mt,
+                sa, sp, ah, al, ph, pl);
       if (mode & REF_ACC) {  // acceleration and potential; the jerk stays
         double dx[3];
 #pragma unroll
         for (int k = 0; k < 3; k++)
           dx[k] = ((double)g6_split_get(rec, j, k) + (double)g6_split_get(rec, j, 4 + k)) - xi[k];
-        const double m = (double)g6_split_get(rec, j, 3);
+        const double m = (double)g6_split_get(rec, j, 3) + (double)g6_split_get(rec, j, 7);
         const double r2 = __fma_rn(dx[2], dx[2], __fma_rn(dx[1], dx[1], __fma_rn(dx[0], dx[0], eps2)));
         const double rinv = refine_rsqrt(r2);
         const double mri = m * rinv;

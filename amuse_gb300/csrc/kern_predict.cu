@@ -105,8 +105,10 @@ __device__ __forceinline__ void predict_one(const g6_jstate &js, int s, int nj, 
       h[k] = __double2float_rn(xp[k]);
       l[k] = __double2float_rn(xp[k] - (double)h[k]);
     }
-    g6_split_store(js.jp_split, s, h[0], h[1], h[2], __double2float_rn(m), l[0], l[1], l[2],
-                   __double2float_rn(vp[0]), __double2float_rn(vp[1]), __double2float_rn(vp[2]));
+    const float mh = __double2float_rn(m);
+    g6_split_store(js.jp_split, s, h[0], h[1], h[2], mh, __double2float_rn(m - (double)mh), l[0],
+                   l[1], l[2], __double2float_rn(vp[0]), __double2float_rn(vp[1]),
+                   __double2float_rn(vp[2]));
   } else {
     G6D4 *rec = reinterpret_cast<G6D4 *>(js.jp_f64) + 2 * (size_t)s;
     rec[0] = g6d4(xp[0], xp[1], xp[2], m);

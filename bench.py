@@ -446,7 +446,7 @@ def run_ours(args):
                        "what": "refine_kernel after the force kernel: acc and pot redone in "
                                "FP64 where the FP32 sum is ill-conditioned (kappa > 48), with "
                                "compensated FP32 sums and the large terms in FP64 where one "
-                               "term exceeds 1.5 |a|"},
+                               "term exceeds |a|"},
             "predictor": {"ms": statistics.mean(pms), "GB_s": pred_gbs,
                           "bytes_per_j": 15 * 8 + 4 + 48,
                           "hbm_peak_gbs": pk.get("hbm_gbs"),

@@ -415,3 +415,79 @@ def test_refine_dominant_term(g6):
     assert st["dominant"] >= ni // 2 and st["overflow"] == 0, st
     assert e.max() <= 1e-6
     assert np.max(np.abs(out["pot"] - ref["pot"]) / np.abs(ref["pot"])) <= 1e-6
+
+
+def _slot_force(g6, torch, n, sel, want_nn):
+    il = torch.tensor(np.asarray(sel, np.int32), device="cuda")
+    ni = len(sel)
+    acc = torch.empty((ni, 3), dtype=torch.float64, device="cuda")
+    jerk = torch.empty_like(acc)
+    pot = torch.empty(ni, dtype=torch.float64, device="cuda")
+    nn = torch.empty(ni, dtype=torch.int32, device="cuda") if want_nn else None
+    g6.force_slots(0.0, 1e-6, n, il.data_ptr(), ni, acc.data_ptr(), jerk.data_ptr(),
+                   pot.data_ptr(), nn.data_ptr() if want_nn else None)
+    return dict(acc=acc.cpu().numpy(), jerk=jerk.cpu().numpy(), pot=pot.cpu().numpy(),
+                nn=nn.cpu().numpy() if want_nn else None)
+
+
+@pytest.mark.parametrize("want_nn", [False, True])
+def test_refine_dominant_term_slots(g6, want_nn):
+    """The dominant-term case through g6x_force_slots (the block-step path),
+    with the nearest neighbour off (the pass's vectorised loop over record
+    pairs) and on (the general loop, which also ranks the neighbour)."""
+    torch = pytest.importorskip("torch")
+    g6.set_precision(ag.SPLIT)
+    rng = np.random.RandomState(29)
+    nc = 6000
+    r = rng.uniform(0, 1, nc) ** (1 / 3)
+    u = rng.normal(size=(nc, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    star = np.array([[0.3, 0.0, 0.0]])
+    ni = 200
+    th = rng.uniform(0, 0.35, ni)
+    ph = rng.uniform(0, 2 * np.pi, ni)
+    dirs = np.stack([np.cos(th), np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph)], 1)
+    x = np.concatenate([star - 0.05 * dirs, star, r[:, None] * u])
+    n = len(x)
+    m = np.concatenate([np.full(ni, 1e-12), [1e-3], np.full(nc, 1.0 / nc)])
+    v = rng.normal(0, 0.1, (n, 3))
+    g6.load_particles(m, x, v)
+    sel = np.arange(ni)
+    ref = oracle.force(m, x, v, 1e-6, x[sel], v[sel])
+    out = _slot_force(g6, torch, n, sel, want_nn)
+    st = g6.refine_stats()
+    e = vrel(out["acc"], ref["acc"])
+    print(f"nn={want_nn}: acc rel err max {e.max():.2e} ({st})")
+    assert st["dominant"] >= ni // 2 and st["overflow"] == 0, st
+    assert e.max() <= 1e-6
+    assert np.max(np.abs(out["pot"] - ref["pot"]) / np.abs(ref["pot"])) <= 1e-6
+    if want_nn:
+        assert check_nn(out["nn"], ref["nn"], x, x[sel], "dominant") == 0
+
+
+def test_results_do_not_depend_on_the_launch_shape(g6):
+    """g6x_set_shape: the same block under forced shapes (j-lanes, j-splits)
+    gives the same nearest neighbours and forces within the contract."""
+    torch = pytest.importorskip("torch")
+    g6.set_precision(ag.SPLIT)
+    np.random.seed(31)
+    n = 20000
+    m, x, v = ic.plummer(n, do_scale=False)
+    g6.load_particles(m, x, v)
+    sel = np.arange(0, n, 7)[:2048]
+    ref = oracle.force(m, x, v, 1e-6, x[sel], v[sel])
+    outs = []
+    try:
+        for jl, ns in [(0, 0), (1, 1), (1, 13), (4, 5), (32, 40)]:
+            g6.set_shape(jl, ns)
+            out = _slot_force(g6, torch, n, sel, True)
+            st = g6.stats()
+            # the split count is normalised to whole tiles per split
+            assert jl == 0 or (st["jl"] == jl and abs(st["nsplit"] - ns) <= 2), (jl, ns, st)
+            assert vrel(out["acc"], ref["acc"]).max() <= 1e-6, (jl, ns)
+            assert check_nn(out["nn"], ref["nn"], x, x[sel], f"shape {jl}x{ns}") == 0
+            outs.append(out)
+    finally:
+        g6.set_shape(0, 0)
+    for o in outs[1:]:
+        assert np.array_equal(o["nn"], outs[0]["nn"])

@@ -750,6 +750,9 @@ constexpr double MU0 = 1.0;
 // terms' random errors stay below ~1e-7 sqrt(0.02 kappa) |a| (C2 at 65536
 // Salpeter: the same largest error as at 0.005, and the block loop 2 %
 // faster).
+#ifndef G6_REF_UNITS
+#define G6_REF_UNITS 4  // refine_kernel: (entry, j-chunk) units per CTA to aim for
+#endif
 #ifndef G6_TAU
 #define G6_TAU 0.02f
 #endif
@@ -1330,7 +1333,13 @@ __global__ void __launch_bounds__(RNT) refine_kernel(KParams kp) {
   if (cnt > (unsigned)RCAP && blockIdx.x == 0 && tid == 0) atomicMax(&b->h.overflow, cnt);
   int nch = 1;
   if (ne > 0) {
-    nch = (4 * (int)gridDim.x + ne - 1) / ne;
+    // About one unit per CTA while the entries are few (each unit then
+    // covers more j and the CTA reduces once); four per CTA once they are
+    // many, for balance (measured on config 2's blocks: 8 entries 34 -> 24
+    // us, 25 entries 68 -> 40 us at one per CTA; 366 entries 282 us at four,
+    // 652 us at one)
+    const int upc = ne * 4 > (int)gridDim.x ? G6_REF_UNITS : 1;
+    nch = (upc * (int)gridDim.x + ne - 1) / ne;
     nch = min(nch, RCHMAX);
     nch = min(nch, RPCAP / ne);
     nch = min(nch, max(1, kp.nj / 1024));

@@ -51,7 +51,8 @@ EXT_SYMBOLS = [
     "g6x_test_wait_expiry", "g6x_batch_unperturbed", "g6x_batch_binaries", "g6x_set_npipes", "g6x_last_error", "g6x_load",
     "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
     "g6x_energy", "g6x_run_stats", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
-    "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stats_n", "g6x_set_shape", "g6x_stream",
+    "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stats_n", "g6x_set_shape", "g6x_check_structure",
+    "g6x_stream",
     "g6x_set_fixed_jerk", "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp",
     "g6x_fixed_step_adjoint", "g6x_fixed_run", "g6x_fixed_adjoint_run",
     "g6x_set_encounters", "g6x_set_radius", "g6x_encounter", "g6x_knn",
@@ -133,6 +134,8 @@ def load():
     lib.g6x_stats.argtypes = [_pd]
     lib.g6x_stats_n.argtypes = [_pd, ctypes.c_int]
     lib.g6x_set_shape.argtypes = [ctypes.c_int, ctypes.c_int]
+    lib.g6x_check_structure.argtypes = [ctypes.c_int, _pd, _pd, _pd, _pi, ctypes.c_char_p,
+                                        ctypes.c_int]
     lib.g6x_stream.restype = _vp
     lib.g6x_set_fixed_jerk.argtypes = [I]
     lib.g6x_fixed_force.argtypes = [I, D] + [_vp] * 5
@@ -505,6 +508,27 @@ class G6X(G6):
     def set_shape(self, jl=0, nsplit=0):
         """Launch shape override (0: the cost model's choice)."""
         _check(self.lib.g6x_set_shape(int(jl), int(nsplit)), "g6x_set_shape")
+
+
+def check_structure(mass, pos, vel):
+    """Structure of one few-body system (g6x_check_structure, host code):
+    returns dict(over, hierarchy_tested, top_of, summary).  over: every
+    top-level node escaping and stable (smallN's check_structure);
+    hierarchy_tested: a multiple above a binary was judged by the published
+    Mardling-Aarseth criterion where smallN uses Mardling's nstab; top_of:
+    per body, the smallest body index of its top-level node; summary: the
+    tree, a binary as "(first,second)" of body indices."""
+    lib = load()
+    m = _f64(mass)
+    n = len(m)
+    x, v = _f64(pos, (n, 3)), _f64(vel, (n, 3))
+    top = np.zeros(n, np.int32)
+    buf = ctypes.create_string_buffer(4096)
+    rc = lib.g6x_check_structure(n, _ptr(m, ctypes.c_double), _ptr(x, ctypes.c_double),
+                                 _ptr(v, ctypes.c_double), _ptr(top, ctypes.c_int), buf, 4096)
+    _check(rc if rc < 0 else 0, "g6x_check_structure")
+    return dict(over=bool(rc & 1), hierarchy_tested=bool(rc & 2), top_of=top,
+                summary=buf.value.decode())
 
 
 def drive_load(mass, pos, vel, acc=None, jerk=None, t=None, dt=None, ids=None):

@@ -26,7 +26,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kern_force.cu", "kern_predict.cu", "kern_step.cu", "kern_ngb.cu", "kern_batch.cu",
               "kern_fixed.cu", "kern_knn.cu"]
-C_SOURCES = ["g6_host.c"]
+C_SOURCES = ["g6_host.c", "g6_struct.c"]
 
 
 def cuda_home():

@@ -267,6 +267,22 @@ int g6x_stats_n(double *out, int n);
    not depend on the shape beyond the FP32 summation order. */
 int g6x_set_shape(int jl, int nsplit);
 
+/* Structure of one few-body system (n <= 64 bodies, G = 1, positions and
+   velocities in any common frame) and whether its interaction is over, as
+   smallN's check_structure decides it (src/amuse_ph4/src/analyze.cc:
+   866-1070) for the multiples hand-off: bodies are paired into binaries by
+   relative energy (only lightly perturbed pairs), escapers and stability
+   are flagged, and the interaction is over when every top-level node is
+   escaping and stable.  Host code; no device is needed.
+   top_of[n] (optional) receives, per body, the smallest body index of its
+   top-level node; summary (optional) the structure as text, a binary as
+   "(first,second)" of body indices, top-level nodes separated by spaces.
+   Returns bit 0 = over, bit 1 = a multiple above a binary was judged by the
+   published Mardling-Aarseth criterion (smallN consults Mardling's nstab
+   there, which this library does not restate), or G6_ERR_ARG. */
+int g6x_check_structure(int n, const double *mass, const double *pos, const double *vel,
+                        int *top_of, char *summary, int summary_cap);
+
 /* Batched few-body systems (the encounters AMUSE's multiples module hands
    to smallN): nsys independent systems of n_per_sys[s] bodies (2..64),
    stored back to back in mass/pos/vel, each integrated to t_end[s] with

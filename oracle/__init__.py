@@ -106,6 +106,8 @@ def ref():
         lib.ph4ref_run.argtypes = [_c_int, _dp, _ip, _dp, _dp, _c_dbl, _c_dbl, _c_dbl,
                                    _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         lib.ph4ref_smalln.argtypes = [_c_int, _dp, _dp, _dp, _c_dbl, _c_dbl, _c_dbl, _dp]
+        lib.ph4ref_check_structure.argtypes = [_c_int, _dp, _dp, _dp, ctypes.c_char_p, _c_int]
+        lib.ph4ref_check_structure.restype = _c_int
         lib.ph4ref_run_coll.argtypes = [_c_int, _dp, _dp, _ip, _dp, _dp, _c_dbl, _c_dbl,
                                         _c_dbl, _c_int, _dp, _dp, _dp, _dp, _dp, _dp]
         _ref_lib = lib
@@ -280,6 +282,14 @@ def smalln_unpert(mass, pos, vel, eta, t_end, n_iter=2, dt_crit=SMALLN_DT_CRIT,
     if steps < 0:
         raise ValueError("more than 64 bodies")
     return pos, vel, float(t[0]), int(steps), int(nb[0])
+
+
+def check_structure_ref(mass, pos, vel):
+    """smallN's check_structure and get_tree (the reference build): returns
+    (over, tree text) with binaries as "(first,second)" of 0-based indices."""
+    buf = ctypes.create_string_buffer(4096)
+    over = ref().ph4ref_check_structure(len(mass), _c(mass), _c(pos), _c(vel), buf, 4096)
+    return int(over), buf.value.decode()
 
 
 def kepler(mu, r0, v0, dt):

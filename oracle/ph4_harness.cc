@@ -314,4 +314,56 @@ int ph4ref_smalln(int n, const double *mass, double *pos, double *vel, double et
   return nbin;
 }
 
+// smallN's structure analysis (src/amuse_ph4/src/analyze.cc check_structure,
+// get_tree) on a flat system of n leaves: returns over (0-3; 2 is the
+// quasi-stable termination, which depends on the calls before this one) and
+// writes the decomposed tree as text, a binary as "(first,second)" of
+// 0-based body indices in daughter order, top-level nodes separated by
+// spaces.
+static int describe_ref(hdyn *b, char *s, int cap) {
+  hdyn *od = b->get_oldest_daughter();
+  if (!od) return snprintf(s, cap > 0 ? cap : 0, "%d", b->get_index() - 1);
+  int w = snprintf(s, cap > 0 ? cap : 0, "(");
+  w += describe_ref(od, s + w, cap > w ? cap - w : 0);
+  w += snprintf(s + w, cap > w ? cap - w : 0, ",");
+  w += describe_ref(od->get_younger_sister(), s + w, cap > w ? cap - w : 0);
+  w += snprintf(s + w, cap > w ? cap - w : 0, ")");
+  return w;
+}
+
+int ph4ref_check_structure(int n, const double *mass, const double *pos, const double *vel,
+                           char *summary, int cap) {
+  std::streambuf *old = std::cout.rdbuf(NULL);
+  hdyn *b = new hdyn;
+  b->set_system_time(0.0);
+  hdyn *prev = NULL;
+  for (int i = 0; i < n; i++) {
+    hdyn *bn = new hdyn;
+    bn->set_mass(mass[i]);
+    bn->set_pos(vec(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
+    bn->set_vel(vec(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]));
+    bn->set_index(i + 1);
+    bn->set_parent(b);
+    if (!prev) {
+      b->set_oldest_daughter(bn);
+    } else {
+      bn->set_older_sister(prev);
+      prev->set_younger_sister(bn);
+    }
+    prev = bn;
+  }
+  const int over = check_structure(b, _INFINITY_, 0);
+  hdyn *t = get_tree(b);
+  int w = 0;
+  if (cap > 0) summary[0] = 0;
+  for_all_daughters(hdyn, t, bi) {
+    if (w > 0) w += snprintf(summary + w, cap > w ? cap - w : 0, " ");
+    w += describe_ref(bi, summary + w, cap > w ? cap - w : 0);
+  }
+  rmtree(t);
+  rmtree(b);
+  std::cout.rdbuf(old);
+  return over;
+}
+
 }  // extern "C"

@@ -49,7 +49,8 @@ def save(name, **arrays):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("AMUSE_REF"))
-    ap.add_argument("--only", default=None, choices=[None, "smalln", "encounters", "unpert"])
+    ap.add_argument("--only", default=None,
+                    choices=[None, "smalln", "encounters", "unpert", "structure"])
     args = ap.parse_args()
     if not args.ref:
         ap.error("give --ref or set AMUSE_REF to the AMUSE checkout")
@@ -62,6 +63,8 @@ def main():
         return encounter_fixtures(oracle)
     if args.only == "unpert":
         return smalln_unpert_fixtures(oracle)
+    if args.only == "structure":
+        return structure_fixtures(oracle)
 
     # 1. IC generators (pins amuse_gb300/ic.py).
     np.random.seed(1)
@@ -140,6 +143,7 @@ def main():
     smalln_fixtures(oracle)
     encounter_fixtures(oracle)
     smalln_unpert_fixtures(oracle)
+    structure_fixtures(oracle)
 
 
 def smalln_fixtures(oracle):
@@ -246,6 +250,28 @@ def encounter_fixtures(oracle):
                     f"c{k}_blocks": r["blocks"], f"c{k}_pair": np.array(pair),
                     f"c{k}_pos": r["pos"], f"c{k}_vel": r["vel"], f"c{k}_rmin": r["rmin"]})
     save("encounter_runs.npz", ncase=len(ENCOUNTER_CASES), eps2=1e-4, eta=0.14, **out)
+
+
+def structure_fixtures(oracle):
+    """10. smallN's structure analysis (analyze.cc check_structure, get_tree)
+    on few-body states: the batching configuration's kind of system
+    (n = 3 ... 12, Plummer r_vir = 1e-3, eps = 0) evolved by the unmodified
+    smallN (no binary tree) to 0.5, 2, 6 and 20 crossing times; per state the
+    reference's over flag and its tree as text ("(first,second)" of 0-based
+    body indices, top-level nodes separated by spaces)."""
+    from amuse_gb300 import ic
+    ns, m, x, v, tcr = ic.encounter_batch(60, 3, 12, seed=11)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    out, k = {}, 0
+    for s in range(len(ns)):
+        a, b = off[s], off[s + 1]
+        for f in (0.5, 2.0, 6.0, 20.0):
+            p, vv, t, _ = oracle.smalln(m[a:b], x[a:b], v[a:b], 0.14, f * tcr, lib="ref")
+            over, tree = oracle.check_structure_ref(m[a:b], p, vv)
+            out.update({f"s{k}_mass": m[a:b], f"s{k}_pos": p, f"s{k}_vel": vv,
+                        f"s{k}_over": over, f"s{k}_tree": np.array(tree)})
+            k += 1
+    save("structure_states.npz", nstate=k, **out)
 
 
 if __name__ == "__main__":

@@ -23,13 +23,15 @@ of repeated states.  Each increment restarts the integrator from the
 returned state: unperturbed binaries are resolved at the end of an increment
 and found again in the next.
 """
+import time
+
 import numpy as np
 
 import amuse_gb300 as ag
 
 
 def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode="split",
-                       unperturbed=True, eta=0.14, max_steps=2_000_000):
+                       unperturbed=True, eta=0.14, max_steps=2_000_000, timing=None):
     """Advance every encounter until its interaction is over or end_time.
 
     systems: list of (mass[n], pos[n][3], vel[n][3]), n <= 64, each in its
@@ -38,7 +40,9 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     integrated time), over (0 not over by end_time, 1 over, 3 beyond the
     break scale), summary (the structure as g6x_check_structure writes it),
     top_of, checks (how many increments it took), steps, energy (initial and
-    final total energy)."""
+    final total energy).  timing (a dict, optional) receives launches,
+    batch_s (wall time of the batch calls, copies included), check_s (the
+    structure checks) and the active systems per launch."""
     ns = len(systems)
     end_time = np.broadcast_to(np.asarray(end_time, float), (ns,))
     delta_t = np.broadcast_to(np.asarray(delta_t, float), (ns,))
@@ -53,6 +57,8 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
                           over=0, summary="", top_of=None))
     e0 = [_energy(s["m"], s["x"], s["v"]) for s in state]
     active = list(range(ns))
+    t_batch = t_check = 0.0
+    per_launch = []
     if unperturbed:
         g6.batch_unperturbed(True)
     try:
@@ -60,10 +66,14 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
             # one batch launch per increment for every system still running
             dts = np.array([min(delta_t[s], end_time[s] - state[s]["t"]) for s in active])
             nper = np.array([len(state[s]["m"]) for s in active], np.int32)
+            per_launch.append(len(active))
+            t0 = time.perf_counter()
             r = g6.batch_run(nper, dts, np.concatenate([state[s]["m"] for s in active]),
                              np.concatenate([state[s]["x"] for s in active]),
                              np.concatenate([state[s]["v"] for s in active]), eta=eta,
                              max_steps=max_steps, mode=mode)
+            t1 = time.perf_counter()
+            t_batch += t1 - t0
             off = np.concatenate([[0], np.cumsum(nper)])
             still = []
             for q, s in enumerate(active):
@@ -82,9 +92,13 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
                 elif st["t"] < end_time[s] * (1 - 1e-12) and r["status"][q] == 0:
                     still.append(s)
             active = still
+            t_check += time.perf_counter() - t1
     finally:
         if unperturbed:
             g6.batch_unperturbed(False)
+    if timing is not None:
+        timing.update(launches=len(per_launch), batch_s=t_batch, check_s=t_check,
+                      active_per_launch=per_launch)
     return [dict(pos=st["x"], vel=st["v"], time=st["t"], over=st["over"],
                  summary=st["summary"], top_of=st["top_of"], checks=st["checks"],
                  steps=st["steps"], energy=(e0[k], _energy(st["m"], st["x"], st["v"])))

@@ -15,6 +15,12 @@ one (which is bench.py).  Each prints one JSON line.
       encounter check and reports its cost.
   python -m amuse_gb300.workloads knn [--n 1048576] [--k 12]
       The k nearest neighbours of every particle (g6x_knn), timed.
+  python -m amuse_gb300.workloads multiples [--nsys 4096]
+      nsys binary-single scatterings resolved together by the multiples
+      hand-off (amuse_gb300.multiples.resolve_encounters: batch launches of
+      delta_t = 10 with smallN's unperturbed binaries, the structure check
+      after each); encounters/s, outcomes, increments, energy.
+      (bench.py --workload multiples adds the host-core baseline.)
   python -m amuse_gb300.workloads adjoint [--n 16384] [--nsteps 256]
       Differentiable fixed-step Hermite: timing of forward and backward in
       split precision and FP64, split vs FP64 gradients, and finite
@@ -113,6 +119,94 @@ def run_batch(args):
     sample = dict(ns=ns[:kc], mass=m[sc], pos=x[sc], vel=v[sc], t_end=t_end, off=off[:kc + 1],
                   unpert=unpert)
     return out, sample
+
+
+def binary_single(seed, v_inf=0.6, b_max=1.5, d0=15.0):
+    """One binary-single scattering: a binary of 0.5 + 0.5 (a = 1, e uniform
+    in [0, 0.7], random orientation and phase) and a single of 0.5 coming in
+    from d0 with speed v_inf (0.6 is 0.69 of the critical speed, so most
+    encounters are resonant) and impact parameter up to b_max;
+    centre-of-mass frame, G = 1.  numpy RandomState(seed)."""
+    rng = np.random.RandomState(seed)
+    m = np.array([0.5, 0.5, 0.5])
+    a, e = 1.0, rng.uniform(0, 0.7)
+    E = rng.uniform(0, 2 * np.pi)
+    r = a * (1 - e * np.cos(E))
+    xr = np.array([a * (np.cos(E) - e), a * np.sqrt(1 - e * e) * np.sin(E), 0.0])
+    s = np.sqrt(1.0 * a) / r
+    vr = np.array([-s * np.sin(E), s * np.sqrt(1 - e * e) * np.cos(E), 0.0])
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    xr, vr = q @ xr, q @ vr
+    b = b_max * np.sqrt(rng.uniform())
+    x = np.array([-0.5 * xr, 0.5 * xr, [-d0, b, 0.0]])
+    v = np.array([-0.5 * vr, 0.5 * vr, [v_inf, 0.0, 0.0]])
+    cm = (m[:, None] * x).sum(0) / m.sum()
+    cv = (m[:, None] * v).sum(0) / m.sum()
+    return m, x - cm, v - cv
+
+
+def scattering_outcome(summary, over):
+    """flyby (the binary (0,1) survives), exchange (the single is in the
+    final binary), ionization (three singles), bound (a triple, or a
+    binary with the third body still bound to it) or unresolved."""
+    if not over:
+        return "unresolved"
+    if summary.count("(") > 1:
+        return "bound"
+    if summary == "(0,1) 2":
+        return "flyby"
+    if summary in ("(0,2) 1", "(1,2) 0"):
+        return "exchange"
+    if summary == "0 1 2":
+        return "ionization"
+    return "bound"
+
+
+def run_multiples(args):
+    """The multiples hand-off on the GPU: args.nsys binary-single scatterings
+    resolved together (end time args.end_time, increments args.delta_t).
+    Returns the JSON dict and the systems (all of them: the host loop over
+    the same encounters takes ~4 ms of one core each)."""
+    import amuse_gb300 as ag
+    from amuse_gb300 import multiples
+    systems = [binary_single(args.seed * 1_000_003 + k) for k in range(args.nsys)]
+    g6 = ag.G6X(0)
+    kw = dict(end_time=args.end_time, delta_t=args.delta_t, eta=args.eta,
+              max_steps=args.max_steps)
+    multiples.resolve_encounters(g6, systems[:64], **kw)  # warm (context, graphs, buffers)
+    tm = {}
+    t0 = time.perf_counter()
+    res = multiples.resolve_encounters(g6, systems, timing=tm, **kw)
+    wall = time.perf_counter() - t0
+    outc = {}
+    for r in res:
+        k = scattering_outcome(r["summary"], r["over"])
+        outc[k] = outc.get(k, 0) + 1
+    de = np.array([abs((r["energy"][1] - r["energy"][0]) / r["energy"][0]) for r in res])
+    checks = np.array([r["checks"] for r in res])
+    steps = np.array([r["steps"] for r in res])
+    resolved = int(sum(r["over"] != 0 for r in res))
+    out = {
+        "metric": "encounters/s (multiples hand-off to batched smallN)",
+        "value": args.nsys / wall, "unit": "encounters/s",
+        "workload": f"{args.nsys} binary-single scatterings (0.5+0.5, a=1, e~U[0,0.7]; "
+                    f"single 0.5 from d=15, v_inf=0.6, b<=1.5), end_time={args.end_time}, "
+                    f"delta_t={args.delta_t}, eta={args.eta}, smallN scheme with unperturbed "
+                    f"binaries (split mode), structure check after every increment",
+        "resolved": resolved, "resolved_per_s": resolved / wall, "outcomes": outc,
+        "wall_s": wall, "launches": tm["launches"], "batch_s": tm["batch_s"],
+        "check_s": tm["check_s"],
+        "active_per_launch": {"first": tm["active_per_launch"][0],
+                              "p50": float(np.median(tm["active_per_launch"]))},
+        "increments": {"p50": float(np.median(checks)), "p99": float(np.percentile(checks, 99)),
+                       "max": int(checks.max())},
+        "steps": {"total": int(steps.sum()), "p50": float(np.median(steps)),
+                  "max": int(steps.max())},
+        "dE_over_E": {"p50": float(np.median(de)), "p99": float(np.percentile(de, 99)),
+                      "max": float(de.max())},
+    }
+    print(json.dumps(out), flush=True)
+    return out, systems
 
 
 def run_adjoint(args):
@@ -476,6 +570,13 @@ def main():
     bl.add_argument("--seed", type=int, default=1)
     bl.add_argument("--reps", type=int, default=5)
     bl.add_argument("--ni", type=int, nargs="+", default=[1, 16, 128, 722, 4096, 65536])
+    mu = sub.add_parser("multiples")
+    mu.add_argument("--nsys", type=int, default=4096)
+    mu.add_argument("--seed", type=int, default=1)
+    mu.add_argument("--eta", type=float, default=0.14)
+    mu.add_argument("--end-time", type=float, default=1000.0)
+    mu.add_argument("--delta-t", type=float, default=10.0)
+    mu.add_argument("--max-steps", type=int, default=2_000_000)
     kn = sub.add_parser("knn")
     kn.add_argument("--n", type=int, default=1 << 20)
     kn.add_argument("--k", type=int, default=12)
@@ -493,6 +594,8 @@ def main():
         run_knn(a)
     elif a.cmd == "blocks":
         run_blocks(a)
+    elif a.cmd == "multiples":
+        run_multiples(a)
 
 
 if __name__ == "__main__":

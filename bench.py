@@ -35,6 +35,11 @@ Secondary workloads (one JSON line each; not the headline metric):
                       (amuse_gb300.workloads.run_batch) with the oracle's
                       smallN restatement timed on the host cores on the
                       same sample of systems as cpu_baseline;
+  --workload multiples  4096 binary-single scatterings resolved by the
+                      multiples hand-off (amuse_gb300.workloads.run_multiples)
+                      with the same loop on the host cores (the oracle's
+                      smallN with unperturbed binaries, then the structure
+                      check) on a sample of the encounters as cpu_baseline;
   --workload adjoint  the differentiable fixed-step Hermite at n = 16384
                       (amuse_gb300.workloads.run_adjoint) with the oracle's
                       restatement of the hermite code's step timed on the
@@ -80,7 +85,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="force", choices=["force", "batch", "adjoint"])
+    ap.add_argument("--workload", default="force", choices=["force", "batch", "multiples", "adjoint"])
     # batch workload
     ap.add_argument("--nsys", type=int, default=4096)
     ap.add_argument("--seed", type=int, default=None)
@@ -90,6 +95,9 @@ def parse():
     ap.add_argument("--batch-mode", default="split", choices=["fast", "exact", "split"])
     ap.add_argument("--no-unpert", action="store_true",
                     help="batch without smallN's unperturbed binaries")
+    # multiples workload
+    ap.add_argument("--end-time", type=float, default=1000.0)
+    ap.add_argument("--delta-t", type=float, default=10.0)
     # adjoint workload
     ap.add_argument("--nsteps", type=int, default=256)
     ap.add_argument("--fd-coords", type=int, default=32)
@@ -469,7 +477,8 @@ def run_ours(args):
 
 
 def run_secondary(args):
-    """The batch / adjoint workloads with their host-core baselines."""
+    """The batch / multiples / adjoint workloads with their host-core
+    baselines."""
     from amuse_gb300 import workloads
     import oracle
     oracle.build_port()
@@ -497,6 +506,34 @@ def run_secondary(args):
             "sample": f"the first {len(off) - 1} systems (smallN"
                       f"{' with unperturbed binaries' if smp['unpert'] else ''} restated in "
                       f"oracle/g6_oracle.c, same step cap), {dt:.1f} s"}
+    elif args.workload == "multiples":
+        args.seed = 1 if args.seed is None else args.seed
+        out, sample = workloads.run_multiples(args)
+        import amuse_gb300 as ag
+
+        def one(sys_):
+            # resolve_collision's loop on the host: smallN for delta_t, then
+            # the structure check, until over or the end time
+            m, x, v = sys_
+            t = 0.0
+            while t < args.end_time * (1 - 1e-12):
+                x, v, tf, _, _ = oracle.smalln_unpert(m, x, v, args.eta,
+                                                      min(args.delta_t, args.end_time - t),
+                                                      max_steps=args.max_steps)
+                t += tf
+                if ag.check_structure(m, x, v)["over"]:
+                    break
+
+        import concurrent.futures as cf
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(one, sample))
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "value": len(sample) / dt, "unit": "encounters/s", "cores": threads, "kind": "port",
+            "sample": f"all {len(sample)} encounters through the same loop (smallN with "
+                      f"unperturbed binaries restated in oracle/g6_oracle.c, FP64, then the "
+                      f"structure check), {dt:.1f} s"}
     else:
         args.seed = 7 if args.seed is None else args.seed
         args.n = 16384 if args.n == N_DEFAULT else args.n

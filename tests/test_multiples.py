@@ -7,29 +7,11 @@ import pytest
 
 import amuse_gb300 as ag
 import oracle
-from amuse_gb300 import multiples
+from amuse_gb300 import multiples, workloads
 
 
 def scattering(seed, v_inf=0.6, b_max=1.5, d0=15.0):
-    """A binary (0.5 + 0.5, a = 1, e from [0, 0.7], random orientation and
-    phase) and a single of mass 0.5 coming in from d0 with impact parameter
-    up to b_max; centre-of-mass frame, G = 1."""
-    rng = np.random.RandomState(seed)
-    m = np.array([0.5, 0.5, 0.5])
-    a, e = 1.0, rng.uniform(0, 0.7)
-    E = rng.uniform(0, 2 * np.pi)
-    r = a * (1 - e * np.cos(E))
-    xr = np.array([a * (np.cos(E) - e), a * np.sqrt(1 - e * e) * np.sin(E), 0.0])
-    s = np.sqrt(1.0 * a) / r
-    vr = np.array([-s * np.sin(E), s * np.sqrt(1 - e * e) * np.cos(E), 0.0])
-    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
-    xr, vr = q @ xr, q @ vr
-    b = b_max * np.sqrt(rng.uniform())
-    x = np.array([-0.5 * xr, 0.5 * xr, [-d0, b, 0.0]])
-    v = np.array([-0.5 * vr, 0.5 * vr, [v_inf, 0.0, 0.0]])
-    cm = (m[:, None] * x).sum(0) / m.sum()
-    cv = (m[:, None] * v).sum(0) / m.sum()
-    return m, x - cm, v - cv
+    return workloads.binary_single(seed, v_inf, b_max, d0)
 
 
 class HostBatch:
@@ -140,3 +122,12 @@ def test_resolve_encounters_on_the_gpu(g6):
         ids = sorted(int(t) for t in r["summary"].replace("(", " ").replace(")", " ")
                      .replace(",", " ").split())
         assert ids == [0, 1, 2]
+
+
+def test_scattering_outcomes():
+    f = workloads.scattering_outcome
+    assert f("(0,1) 2", 1) == "flyby"
+    assert f("(1,2) 0", 1) == f("(0,2) 1", 1) == "exchange"
+    assert f("0 1 2", 1) == "ionization"
+    assert f("((0,1),2)", 1) == "bound"
+    assert f("(0,1) 2", 0) == "unresolved"

@@ -52,6 +52,7 @@ EXT_SYMBOLS = [
     "g6x_read", "g6x_force", "g6x_force_dev", "g6x_force_dev_noalloc", "g6x_force_slots", "g6x_run_init", "g6x_run",
     "g6x_energy", "g6x_run_stats", "g6x_step_all", "g6x_correct", "g6x_batch_run", "g6x_batch_config",
     "g6x_batch_tune", "g6x_system_time", "g6x_timing", "g6x_stats", "g6x_stats_n", "g6x_set_shape", "g6x_check_structure",
+    "g6x_check_structure_batch",
     "g6x_stream",
     "g6x_set_fixed_jerk", "g6x_fixed_force", "g6x_fixed_step", "g6x_force_vjp",
     "g6x_fixed_step_adjoint", "g6x_fixed_run", "g6x_fixed_adjoint_run",
@@ -136,6 +137,8 @@ def load():
     lib.g6x_set_shape.argtypes = [ctypes.c_int, ctypes.c_int]
     lib.g6x_check_structure.argtypes = [ctypes.c_int, _pd, _pd, _pd, _pi, ctypes.c_char_p,
                                         ctypes.c_int]
+    lib.g6x_check_structure_batch.argtypes = [ctypes.c_int, _pi, _pd, _pd, _pd, _pi, _pi,
+                                              ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
     lib.g6x_stream.restype = _vp
     lib.g6x_set_fixed_jerk.argtypes = [I]
     lib.g6x_fixed_force.argtypes = [I, D] + [_vp] * 5
@@ -529,6 +532,34 @@ def check_structure(mass, pos, vel):
     _check(rc if rc < 0 else 0, "g6x_check_structure")
     return dict(over=bool(rc & 1), hierarchy_tested=bool(rc & 2), top_of=top,
                 summary=buf.value.decode())
+
+
+def check_structure_batch(n_per_sys, mass, pos, vel, nthreads=0, summary_cap=256):
+    """g6x_check_structure over many systems stored back to back, on the
+    host's cores (g6x_check_structure_batch).  Returns dict(over,
+    hierarchy_tested, top_of, summary): per-system arrays (top_of per body,
+    local indices) and a list of summaries."""
+    lib = load()
+    nper = _i32(n_per_sys)
+    ns = len(nper)
+    nb = int(nper.sum())
+    m = _f64(mass)
+    x, v = _f64(pos, (nb, 3)), _f64(vel, (nb, 3))
+    if len(m) != nb:
+        raise G6Error("g6x_check_structure_batch: mass has the wrong length")
+    flags = np.zeros(ns, np.int32)
+    top = np.zeros(nb, np.int32)
+    buf = ctypes.create_string_buffer(max(1, ns * summary_cap))
+    rc = lib.g6x_check_structure_batch(ns, _ptr(nper, ctypes.c_int), _ptr(m, ctypes.c_double),
+                                       _ptr(x, ctypes.c_double), _ptr(v, ctypes.c_double),
+                                       _ptr(flags, ctypes.c_int), _ptr(top, ctypes.c_int), buf,
+                                       summary_cap, int(nthreads))
+    _check(rc, "g6x_check_structure_batch")
+    raw = buf.raw
+    summ = [raw[k * summary_cap:(k + 1) * summary_cap].split(b"\0", 1)[0].decode()
+            for k in range(ns)]
+    return dict(over=(flags & 1).astype(bool), hierarchy_tested=(flags & 2).astype(bool),
+                top_of=top, summary=summ)
 
 
 def drive_load(mass, pos, vel, acc=None, jerk=None, t=None, dt=None, ids=None):

@@ -43,9 +43,12 @@
  * systems of singles and binaries.
  */
 #include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include "g6.h"
 
@@ -445,4 +448,68 @@ int g6x_check_structure(int n, const double *mass, const double *pos, const doub
   /* bit 0: over; bit 1: a multiple above a binary went through the
      hierarchy test (the decision smallN takes from nstab) */
   return over | (tested << 1);
+}
+
+/* Many systems at once: a pool of host threads takes systems from a shared
+   counter (the checks of a hand-off increment are independent). */
+typedef struct {
+  int nsys, cap;
+  const int *off;
+  const double *mass, *pos, *vel;
+  int *flags, *top_of;
+  char *summary;
+  atomic_int next;
+} st_batch;
+
+static void *st_worker(void *arg) {
+  st_batch *B = (st_batch *)arg;
+  for (;;) {
+    const int s = atomic_fetch_add(&B->next, 1);
+    if (s >= B->nsys) break;
+    const int a = B->off[s], n = B->off[s + 1] - a;
+    B->flags[s] = g6x_check_structure(n, B->mass + a, B->pos + 3 * (size_t)a,
+                                      B->vel + 3 * (size_t)a, B->top_of ? B->top_of + a : NULL,
+                                      B->summary ? B->summary + (size_t)s * B->cap : NULL,
+                                      B->summary ? B->cap : 0);
+  }
+  return NULL;
+}
+
+int g6x_check_structure_batch(int nsys, const int *n_per_sys, const double *mass,
+                              const double *pos, const double *vel, int *flags, int *top_of,
+                              char *summary, int summary_cap, int nthreads) {
+  if (nsys < 0 || (nsys > 0 && (!n_per_sys || !mass || !pos || !vel || !flags)))
+    return G6_ERR_ARG;
+  if (summary && summary_cap < 1) return G6_ERR_ARG;
+  if (nsys == 0) return 0;
+  int *off = (int *)malloc(sizeof(int) * ((size_t)nsys + 1));
+  if (!off) return G6_ERR_NOMEM;
+  off[0] = 0;
+  for (int s = 0; s < nsys; s++) {
+    if (n_per_sys[s] < 1 || n_per_sys[s] > ST_MAXN) {
+      free(off);
+      return G6_ERR_ARG;
+    }
+    off[s + 1] = off[s] + n_per_sys[s];
+  }
+  st_batch B = {nsys, summary_cap, off, mass, pos, vel, flags, top_of, summary, 0};
+  atomic_init(&B.next, 0);
+  if (nthreads <= 0) {
+    const long c = sysconf(_SC_NPROCESSORS_ONLN);
+    nthreads = c > 0 ? (int)c : 1;
+  }
+  if (nthreads > 64) nthreads = 64;
+  if (nthreads > (nsys + 7) / 8) nthreads = (nsys + 7) / 8;  /* >= 8 systems a thread */
+  pthread_t th[64];
+  int started = 0;
+  for (int t = 1; t < nthreads; t++) {
+    if (pthread_create(&th[started], NULL, st_worker, &B) != 0) break;
+    started++;
+  }
+  st_worker(&B);
+  for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+  free(off);
+  for (int s = 0; s < nsys; s++)
+    if (flags[s] < 0) return flags[s];
+  return 0;
 }

@@ -7,8 +7,8 @@ smallN's structure analysis calls the interaction over
 `resolve_encounters` takes a list of such encounters and advances all of them
 together on the GPU batch kernel (g6x_batch_run, smallN's scheme, one warp
 per system), checking each system's structure on the host after every
-increment (g6x_check_structure, smallN's check_structure restated) and
-retiring the systems whose interaction is over; the others continue in the
+increment (g6x_check_structure_batch: smallN's check_structure restated,
+on the host's cores) and retiring the systems whose interaction is over; the others continue in the
 next launch.
 
 Kept from resolve_collision's loop: increments of `delta_t` (its
@@ -47,51 +47,61 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     end_time = np.broadcast_to(np.asarray(end_time, float), (ns,))
     delta_t = np.broadcast_to(np.asarray(delta_t, float), (ns,))
     rlim2 = np.broadcast_to(np.asarray(break_scale, float) ** 2, (ns,))
-    state = []
-    for m, x, v in systems:
-        m = np.asarray(m, float)
-        if not 2 <= len(m) <= 64:
-            raise ValueError("encounters of 2 to 64 bodies")
-        state.append(dict(m=m, x=np.array(x, float).reshape(-1, 3),
-                          v=np.array(v, float).reshape(-1, 3), t=0.0, steps=0, checks=0,
-                          over=0, summary="", top_of=None))
-    e0 = [_energy(s["m"], s["x"], s["v"]) for s in state]
-    active = list(range(ns))
+    # all bodies in flat arrays; system s owns bodies off[s] .. off[s+1]-1
+    nper = np.array([len(m) for m, _, _ in systems], np.int32)
+    if ns and (nper.min() < 2 or nper.max() > 64):
+        raise ValueError("encounters of 2 to 64 bodies")
+    off = np.concatenate([[0], np.cumsum(nper)]).astype(np.int64)
+    M = np.concatenate([np.asarray(m, float) for m, _, _ in systems]) if ns else np.zeros(0)
+    X = np.concatenate([np.asarray(x, float).reshape(-1, 3) for _, x, _ in systems]) \
+        if ns else np.zeros((0, 3))
+    V = np.concatenate([np.asarray(v, float).reshape(-1, 3) for _, _, v in systems]) \
+        if ns else np.zeros((0, 3))
+    TOP = np.zeros(len(M), np.int32)
+    t = np.zeros(ns)
+    steps = np.zeros(ns, np.int64)
+    checks = np.zeros(ns, np.int64)
+    over = np.zeros(ns, np.int32)
+    summary = [""] * ns
+    e0 = [_energy(M[off[k]:off[k + 1]], X[off[k]:off[k + 1]], V[off[k]:off[k + 1]])
+          for k in range(ns)]
+    active = np.arange(ns)
     t_batch = t_check = 0.0
     per_launch = []
     if unperturbed:
         g6.batch_unperturbed(True)
     try:
-        while active:
+        while len(active):
             # one batch launch per increment for every system still running
-            dts = np.array([min(delta_t[s], end_time[s] - state[s]["t"]) for s in active])
-            nper = np.array([len(state[s]["m"]) for s in active], np.int32)
+            na = nper[active]
+            bodies = np.repeat(off[active] - np.concatenate([[0], np.cumsum(na)[:-1]]), na) \
+                + np.arange(int(na.sum()))
+            dts = np.minimum(delta_t[active], end_time[active] - t[active])
             per_launch.append(len(active))
             t0 = time.perf_counter()
-            r = g6.batch_run(nper, dts, np.concatenate([state[s]["m"] for s in active]),
-                             np.concatenate([state[s]["x"] for s in active]),
-                             np.concatenate([state[s]["v"] for s in active]), eta=eta,
+            r = g6.batch_run(na, dts, M[bodies], X[bodies], V[bodies], eta=eta,
                              max_steps=max_steps, mode=mode)
             t1 = time.perf_counter()
             t_batch += t1 - t0
-            off = np.concatenate([[0], np.cumsum(nper)])
-            still = []
+            # every system's structure at once, on the host's cores
+            c = ag.check_structure_batch(na, M[bodies], r["pos"], r["vel"])
+            X[bodies], V[bodies], TOP[bodies] = r["pos"], r["vel"], c["top_of"]
+            t[active] += r["t_final"]
+            steps[active] += r["steps"]
+            checks[active] += 1
+            for q in np.flatnonzero(c["over"]):
+                over[active[q]] = 1
+            if np.isfinite(rlim2[active]).any():
+                for q, s in enumerate(active):
+                    if not c["over"][q] and np.isfinite(rlim2[s]) and _beyond(
+                            M[off[s]:off[s + 1]], X[off[s]:off[s + 1]],
+                            TOP[off[s]:off[s + 1]], rlim2[s]):
+                        over[s] = 3
+            go = (over[active] == 0) & (t[active] < end_time[active] * (1 - 1e-12)) \
+                & (r["status"] == 0)
             for q, s in enumerate(active):
-                st = state[s]
-                st["x"] = r["pos"][off[q]:off[q + 1]].copy()
-                st["v"] = r["vel"][off[q]:off[q + 1]].copy()
-                st["t"] += float(r["t_final"][q])
-                st["steps"] += int(r["steps"][q])
-                st["checks"] += 1
-                c = ag.check_structure(st["m"], st["x"], st["v"])
-                st["summary"], st["top_of"] = c["summary"], c["top_of"]
-                if c["over"]:
-                    st["over"] = 1
-                elif np.isfinite(rlim2[s]) and _beyond(st, c["top_of"], rlim2[s]):
-                    st["over"] = 3
-                elif st["t"] < end_time[s] * (1 - 1e-12) and r["status"][q] == 0:
-                    still.append(s)
-            active = still
+                summary[s] = c["summary"][q]
+            active = active[go]
             t_check += time.perf_counter() - t1
     finally:
         if unperturbed:
@@ -99,19 +109,23 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     if timing is not None:
         timing.update(launches=len(per_launch), batch_s=t_batch, check_s=t_check,
                       active_per_launch=per_launch)
-    return [dict(pos=st["x"], vel=st["v"], time=st["t"], over=st["over"],
-                 summary=st["summary"], top_of=st["top_of"], checks=st["checks"],
-                 steps=st["steps"], energy=(e0[k], _energy(st["m"], st["x"], st["v"])))
-            for k, st in enumerate(state)]
+    out = []
+    for k in range(ns):
+        a, b = off[k], off[k + 1]
+        out.append(dict(pos=X[a:b].copy(), vel=V[a:b].copy(), time=float(t[k]),
+                        over=int(over[k]), summary=summary[k], top_of=TOP[a:b].copy(),
+                        checks=int(checks[k]), steps=int(steps[k]),
+                        energy=(e0[k], _energy(M[a:b], X[a:b], V[a:b]))))
+    return out
 
 
-def _beyond(st, top_of, rlim2):
+def _beyond(m_all, x_all, top_of, rlim2):
     """A top-level node (its centre of mass) farther than the break scale
     from the origin of the system's frame."""
     for t in np.unique(top_of):
         sel = top_of == t
-        m = st["m"][sel]
-        cm = (m[:, None] * st["x"][sel]).sum(0) / m.sum()
+        m = m_all[sel]
+        cm = (m[:, None] * x_all[sel]).sum(0) / m.sum()
         if cm @ cm > rlim2:
             return True
     return False

@@ -95,3 +95,31 @@ def test_structure_known_configurations():
 def test_structure_refuses_bad_sizes():
     with pytest.raises(ag.G6Error):
         ag.check_structure(np.ones(65), np.zeros((65, 3)), np.zeros((65, 3)))
+
+
+def test_structure_batch_equals_single_calls():
+    """g6x_check_structure_batch over the fixture states (threads 1 and 8)
+    returns what one call per system returns."""
+    from conftest import golden
+    g = golden("structure_states.npz")
+    n = int(g["nstate"])
+    ms = [g[f"s{k}_mass"] for k in range(n)]
+    xs = [g[f"s{k}_pos"] for k in range(n)]
+    vs = [g[f"s{k}_vel"] for k in range(n)]
+    nper = [len(m) for m in ms]
+    single = [ag.check_structure(m, x, v) for m, x, v in zip(ms, xs, vs)]
+    for th in (1, 8):
+        b = ag.check_structure_batch(nper, np.concatenate(ms), np.concatenate(xs),
+                                     np.concatenate(vs), nthreads=th)
+        off = np.concatenate([[0], np.cumsum(nper)])
+        for k, r in enumerate(single):
+            assert b["over"][k] == r["over"] and b["hierarchy_tested"][k] == r["hierarchy_tested"]
+            assert b["summary"][k] == r["summary"]
+            assert list(b["top_of"][off[k]:off[k + 1]]) == list(r["top_of"])
+
+
+def test_structure_batch_refuses_bad_sizes():
+    with pytest.raises(ag.G6Error):
+        ag.check_structure_batch([3, 65], np.ones(68), np.zeros((68, 3)), np.zeros((68, 3)))
+    with pytest.raises(ag.G6Error):
+        ag.check_structure_batch([3, 0], np.ones(3), np.zeros((3, 3)), np.zeros((3, 3)))

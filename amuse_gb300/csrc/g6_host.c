@@ -1700,13 +1700,13 @@ int g6x_force_dev_noalloc(double ti, double eps2, int nj, int ni, const double *
  * when buffers or parameters change.  Launch shape (warps per CTA, CTAs per
  * SM) comes from g6x_batch_tune or defaults to 4 x 2. */
 int g6k_batch_max_n(void);
-int g6k_batch_launch_unp(int nsys, const int *order, const int *off, const double *t_end,
+int g6k_batch_launch_unp(const int *order, const int *off, const double *t_end,
                          const double *mass, double *pos, double *vel, double eta, int n_iter,
                          long long max_steps, int mode, int warps_per_cta, int ctas,
                          double dt_crit, double r2_crit, double gamma, int allow_full, int *queue,
                          double *t_out, long long *steps_out, unsigned long long *wall_ns,
                          int *status, int *nbin_out, cudaStream_t st);
-int g6k_batch_launch(int nsys, const int *order, const int *off, const double *t_end,
+int g6k_batch_launch(const int *order, const int *off, const double *t_end,
                      const double *mass, double *pos, double *vel, double eta, int n_iter,
                      long long max_steps, int exact, int warps_per_cta, int ctas, int *queue,
                      double *t_out, long long *steps_out, unsigned long long *wall_ns,
@@ -1720,7 +1720,7 @@ static struct {
   unsigned long long *d_wall;
   int wpc, cps; /* warps per CTA, CTAs per SM */
   cudaGraphExec_t gexec;
-  int g_nsys, g_exact, g_niter, g_wpc, g_cps;
+  int g_exact, g_niter, g_wpc, g_cps;
   double g_eta;
   long long g_maxsteps;
   void *g_key;
@@ -1730,7 +1730,7 @@ static struct {
   int *d_nbin;
   int g_unp;
 } BT = {0, 0, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, 4, 2,
-        NULL, 0, 0, 0, 0, 0, 0.0, 0, NULL, 0, 0, 0.0, 0.0, 0.0, NULL, 0};
+        NULL, 0, 0, 0, 0, 0.0, 0, NULL, 0, 0, 0.0, 0.0, 0.0, NULL, 0};
 
 static void batch_free(void) {
   cudaFree(BT.d_order); cudaFree(BT.d_off); cudaFree(BT.d_queue); cudaFree(BT.d_status);
@@ -1780,7 +1780,8 @@ static int batch_ensure(int nsys, int nbody) {
     }
     BT.cap_body = nbody;
   }
-  if (!BT.d_queue && cudaMalloc((void **)&BT.d_queue, sizeof(int)) != cudaSuccess)
+  /* [0] the work counter, [1] the number of systems of the current launch */
+  if (!BT.d_queue && cudaMalloc((void **)&BT.d_queue, 2 * sizeof(int)) != cudaSuccess)
     return G6_ERR_NOMEM;
   return 0;
 }
@@ -1791,11 +1792,15 @@ static int cmp_desc_n(const void *a, const void *b) {
   return x[1] - y[1];
 }
 
-/* Launch through a (cached) CUDA graph: queue reset + persistent kernel. */
+/* Launch through a (cached) CUDA graph: queue reset + persistent kernel.
+   The kernel reads the number of systems from the device, so one graph
+   serves every batch size (a multiples hand-off shrinks the batch at every
+   increment). */
 static int batch_graph_launch(int nsys, double eta, int n_iter, long long max_steps, int exact) {
   const int ctas = BT.cps * g6k_sm_count();
   const int unp = BT.unp && exact != G6_BATCH_EXACT;
-  if (!BT.gexec || BT.g_nsys != nsys || BT.g_exact != exact || BT.g_niter != n_iter ||
+  CK(cudaMemcpyAsync(BT.d_queue + 1, &nsys, sizeof(int), cudaMemcpyHostToDevice, G.st));
+  if (!BT.gexec || BT.g_exact != exact || BT.g_niter != n_iter ||
       BT.g_eta != eta || BT.g_maxsteps != max_steps || BT.g_wpc != BT.wpc ||
       BT.g_cps != BT.cps || BT.g_key != (void *)BT.d_pos || BT.g_unp != unp) {
     if (BT.gexec) {
@@ -1804,12 +1809,12 @@ static int batch_graph_launch(int nsys, double eta, int n_iter, long long max_st
     }
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(G.st, cudaStreamCaptureModeThreadLocal));
-    int rc = unp ? g6k_batch_launch_unp(nsys, BT.d_order, BT.d_off, BT.d_tend, BT.d_mass,
+    int rc = unp ? g6k_batch_launch_unp(BT.d_order, BT.d_off, BT.d_tend, BT.d_mass,
                                         BT.d_pos, BT.d_vel, eta, n_iter, max_steps, exact,
                                         BT.wpc, ctas, BT.unp_dt_crit, BT.unp_r2_crit,
                                         BT.unp_gamma, BT.unp_full, BT.d_queue, BT.d_tout,
                                         BT.d_steps, BT.d_wall, BT.d_status, BT.d_nbin, G.st)
-                 : g6k_batch_launch(nsys, BT.d_order, BT.d_off, BT.d_tend, BT.d_mass, BT.d_pos,
+                 : g6k_batch_launch(BT.d_order, BT.d_off, BT.d_tend, BT.d_mass, BT.d_pos,
                                     BT.d_vel, eta, n_iter, max_steps, exact, BT.wpc, ctas,
                                     BT.d_queue, BT.d_tout, BT.d_steps, BT.d_wall, BT.d_status,
                                     G.st);
@@ -1825,7 +1830,6 @@ static int batch_graph_launch(int nsys, double eta, int n_iter, long long max_st
       BT.gexec = NULL;
       return G6_ERR_CUDA;
     }
-    BT.g_nsys = nsys;
     BT.g_exact = exact;
     BT.g_niter = n_iter;
     BT.g_eta = eta;

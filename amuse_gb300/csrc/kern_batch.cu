@@ -258,7 +258,7 @@ __device__ __forceinline__ void publish(WarpSmem &S, int n, int lane, const Body
 }
 
 template <int MODE>
-__global__ void batch_kernel(int nsys, const int *__restrict__ order, const int *__restrict__ off,
+__global__ void batch_kernel(const int *__restrict__ order, const int *__restrict__ off,
                              const double *__restrict__ t_end_s, const double *__restrict__ mass,
                              double *pos, double *vel, double eta, int n_iter,
                              long long max_steps, int *queue, double *t_out, long long *steps_out,
@@ -268,6 +268,7 @@ __global__ void batch_kernel(int nsys, const int *__restrict__ order, const int 
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   WarpSmem &S = smem[w];
+  const int nsys = queue[1];  // written by the host before the launch
   while (true) {
     int q = 0;
     if (lane == 0) q = atomicAdd(queue, 1);
@@ -1137,7 +1138,7 @@ __device__ int unp_tree(UnpSmem &S, int n, int lane, Body B[2], double t, double
 }
 
 template <int MODE>
-__global__ void batch_unp_kernel(int nsys, const int *__restrict__ order, const int *__restrict__ off,
+__global__ void batch_unp_kernel(const int *__restrict__ order, const int *__restrict__ off,
                                  const double *__restrict__ t_end_s, const double *__restrict__ mass,
                                  double *pos, double *vel, double eta, int n_iter,
                                  long long max_steps, int *queue, double *t_out,
@@ -1147,6 +1148,7 @@ __global__ void batch_unp_kernel(int nsys, const int *__restrict__ order, const 
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   UnpSmem &S = smem[w];
+  const int nsys = queue[1];  // written by the host before the launch
   while (true) {
     int qq0 = 0;
     if (lane == 0) qq0 = atomicAdd(queue, 1);
@@ -1309,7 +1311,7 @@ __global__ void batch_unp_kernel(int nsys, const int *__restrict__ order, const 
   }
 }
 
-__global__ void queue_reset(int *queue) { *queue = 0; }
+__global__ void queue_reset(int *queue) { queue[0] = 0; }
 
 }  // namespace
 
@@ -1317,8 +1319,10 @@ extern "C" int g6k_batch_max_n(void) { return MAXN; }
 
 // One persistent launch: grid = ctas_per_sm * SMs, warps_per_cta warps each.
 // Resets the queue counter first (same stream), so the pair can be captured
-// in a CUDA graph and replayed.
-extern "C" int g6k_batch_launch(int nsys, const int *order, const int *off, const double *t_end,
+// in a CUDA graph and replayed.  queue[0] is the counter, queue[1] the number
+// of systems, which the host writes before each replay (a graph then serves
+// every batch size).
+extern "C" int g6k_batch_launch(const int *order, const int *off, const double *t_end,
                                 const double *mass, double *pos, double *vel, double eta,
                                 int n_iter, long long max_steps, int exact, int warps_per_cta,
                                 int ctas, int *queue, double *t_out, long long *steps_out,
@@ -1327,7 +1331,7 @@ extern "C" int g6k_batch_launch(int nsys, const int *order, const int *off, cons
   if (exact < MODE_FAST || exact > MODE_SPLIT) return -2;
   queue_reset<<<1, 1, 0, st>>>(queue);
 #define G6_BATCH(M)                                                                           \
-  batch_kernel<M><<<ctas, 32 * warps_per_cta, 0, st>>>(nsys, order, off, t_end, mass, pos, vel, \
+  batch_kernel<M><<<ctas, 32 * warps_per_cta, 0, st>>>(order, off, t_end, mass, pos, vel,       \
                                                        eta, n_iter, max_steps, queue, t_out,    \
                                                        steps_out, wall_ns, status)
   if (exact == MODE_EXACT)
@@ -1344,7 +1348,7 @@ extern "C" int g6k_batch_launch(int nsys, const int *order, const int *off, cons
 // dt_crit, r2_crit, gamma and allow_full as smallN's set_dt_crit,
 // set_r2_crit, set_gamma, set_allow_full_unperturbed; nbin_out[s] counts the
 // binaries made in system s.
-extern "C" int g6k_batch_launch_unp(int nsys, const int *order, const int *off,
+extern "C" int g6k_batch_launch_unp(const int *order, const int *off,
                                     const double *t_end, const double *mass, double *pos,
                                     double *vel, double eta, int n_iter, long long max_steps,
                                     int mode, int warps_per_cta, int ctas, double dt_crit,
@@ -1363,11 +1367,11 @@ extern "C" int g6k_batch_launch_unp(int nsys, const int *order, const int *off,
   queue_reset<<<1, 1, 0, st>>>(queue);
   if (mode == MODE_SPLIT)
     batch_unp_kernel<MODE_SPLIT><<<ctas, 32 * warps_per_cta, 0, st>>>(
-        nsys, order, off, t_end, mass, pos, vel, eta, n_iter, max_steps, queue, t_out, steps_out,
+        order, off, t_end, mass, pos, vel, eta, n_iter, max_steps, queue, t_out, steps_out,
         wall_ns, status, nbin_out, P);
   else
     batch_unp_kernel<MODE_FAST><<<ctas, 32 * warps_per_cta, 0, st>>>(
-        nsys, order, off, t_end, mass, pos, vel, eta, n_iter, max_steps, queue, t_out, steps_out,
+        order, off, t_end, mass, pos, vel, eta, n_iter, max_steps, queue, t_out, steps_out,
         wall_ns, status, nbin_out, P);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }

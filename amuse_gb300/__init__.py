@@ -515,10 +515,11 @@ class G6X(G6):
 
 def check_structure(mass, pos, vel):
     """Structure of one few-body system (g6x_check_structure, host code):
-    returns dict(over, hierarchy_tested, top_of, summary).  over: every
-    top-level node escaping and stable (smallN's check_structure);
+    returns dict(over, hierarchy_tested, escaping, top_of, summary).  over:
+    every top-level node escaping and stable (smallN's check_structure);
     hierarchy_tested: a multiple above a binary was judged by the published
-    Mardling-Aarseth criterion where smallN uses Mardling's nstab; top_of:
+    Mardling-Aarseth criterion where smallN uses Mardling's nstab; escaping:
+    every top-level node escaping, stable or not; top_of:
     per body, the smallest body index of its top-level node; summary: the
     tree, a binary as "(first,second)" of body indices."""
     lib = load()
@@ -530,14 +531,14 @@ def check_structure(mass, pos, vel):
     rc = lib.g6x_check_structure(n, _ptr(m, ctypes.c_double), _ptr(x, ctypes.c_double),
                                  _ptr(v, ctypes.c_double), _ptr(top, ctypes.c_int), buf, 4096)
     _check(rc if rc < 0 else 0, "g6x_check_structure")
-    return dict(over=bool(rc & 1), hierarchy_tested=bool(rc & 2), top_of=top,
-                summary=buf.value.decode())
+    return dict(over=bool(rc & 1), hierarchy_tested=bool(rc & 2), escaping=bool(rc & 4),
+                top_of=top, summary=buf.value.decode())
 
 
 def check_structure_batch(n_per_sys, mass, pos, vel, nthreads=0, summary_cap=256):
     """g6x_check_structure over many systems stored back to back, on the
     host's cores (g6x_check_structure_batch).  Returns dict(over,
-    hierarchy_tested, top_of, summary): per-system arrays (top_of per body,
+    hierarchy_tested, escaping, top_of, summary): per-system arrays (top_of per body,
     local indices) and a list of summaries."""
     lib = load()
     nper = _i32(n_per_sys)
@@ -559,7 +560,7 @@ def check_structure_batch(n_per_sys, mass, pos, vel, nthreads=0, summary_cap=256
     summ = [raw[k * summary_cap:(k + 1) * summary_cap].split(b"\0", 1)[0].decode()
             for k in range(ns)]
     return dict(over=(flags & 1).astype(bool), hierarchy_tested=(flags & 2).astype(bool),
-                top_of=top, summary=summ)
+                escaping=(flags & 4).astype(bool), top_of=top, summary=summ)
 
 
 def drive_load(mass, pos, vel, acc=None, jerk=None, t=None, dt=None, ids=None):

@@ -33,10 +33,13 @@
  *     applies first (outer pericentre inside the inner apocentre, period
  *     ratio below 1).  Decisions agree wherever no multiple above a binary
  *     is tested; the return value says when one was;
- *   - no quasi-stability: smallN also ends an interaction whose unstable
- *     configuration repeats over 15 consecutive checks (a history kept in
- *     file statics, analyze.cc:909-956); a single call here returns 0 there,
- *     and the caller keeps integrating.
+ *   - no history: smallN also ends an interaction whose top-level nodes
+ *     all escape but are not all stable once the same top-level grouping
+ *     has been seen at more than 15 consecutive checks (quasi-stable, a
+ *     history kept in file statics, analyze.cc:909-956, 1031-1039).  A call
+ *     here is stateless; it reports "every top-level node escaping" in bit
+ *     2 and the grouping in the summary, and the caller keeps the history
+ *     (amuse_gb300.multiples does, per encounter).
  * The arithmetic follows the reference's expression order (vec.h products
  * summed ((x x + y y) + z z), positions relative to an ancestor summed from
  * the leaf upwards), so energies and decisions are bit-identical for
@@ -424,6 +427,7 @@ int g6x_check_structure(int n, const double *mass, const double *pos, const doub
     if (!is_escaper(T, k)) over = 0;
     if (!T->n[k].stable) stable = 0;
   }
+  const int escaping = over;  /* every top-level node escaping */
   if (!stable) over = 0;
   if (top_of) {
     for (int k = r->od; k >= 0; k = T->n[k].ys) {
@@ -446,8 +450,10 @@ int g6x_check_structure(int n, const double *mass, const double *pos, const doub
   const int tested = T->hier_tested;
   free(T);
   /* bit 0: over; bit 1: a multiple above a binary went through the
-     hierarchy test (the decision smallN takes from nstab) */
-  return over | (tested << 1);
+     hierarchy test (the decision smallN takes from nstab); bit 2: every
+     top-level node escaping, stable or not (where smallN's quasi-stable
+     ending applies, analyze.cc:958-990) */
+  return over | (tested << 1) | (escaping << 2);
 }
 
 /* Many systems at once: a pool of host threads takes systems from a shared

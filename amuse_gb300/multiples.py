@@ -13,15 +13,20 @@ next launch.
 
 Kept from resolve_collision's loop: increments of `delta_t` (its
 "initial_delta_t": it checks is_over after every such substep, whatever its
-outer step has grown to), the end time, the break scale (a top-level node
-farther than `break_scale` from the origin of the system's frame ends the
-encounter with over = 3, as smallN's is_over(rlimit)).  Not kept: the
-retries with perturbed initial conditions when an encounter does not end by
-`end_time` (those are returned with over = 0 for the caller to decide), and
-the quasi-stable termination (over = 2), which smallN takes from a history
-of repeated states.  Each increment restarts the integrator from the
-returned state: unperturbed binaries are resolved at the end of an increment
-and found again in the next.
+outer step has grown to), the end time, smallN's quasi-stable ending and the
+break scale.  Quasi-stable (over = 2, analyze.cc:909-990, 1031-1039): every
+top-level node escapes but not all are stable, and the top-level grouping
+has been the same at more than 15 consecutive checks.  smallN keeps that
+history in file statics shared by all the encounters its worker resolves;
+here each encounter has its own, starting empty.  Break scale (over = 3,
+analyze.cc:1050-1059): after an increment that did not end the encounter,
+a top-level body farther than `break_scale` from the origin of the system's
+frame (between increments every body is top-level in the integrator's
+tree).  Not kept: the retries with perturbed initial conditions when an
+encounter does not end by `end_time` (those are returned with over = 0 for
+the caller to decide).  Each increment restarts the integrator from the
+returned state: unperturbed binaries are resolved at the end of an
+increment and found again in the next.
 """
 import time
 
@@ -37,8 +42,8 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     systems: list of (mass[n], pos[n][3], vel[n][3]), n <= 64, each in its
     own frame (G = 1).  end_time, delta_t, break_scale: scalars or one per
     system.  Returns a list of dicts, one per system: pos, vel, time (the
-    integrated time), over (0 not over by end_time, 1 over, 3 beyond the
-    break scale), summary (the structure as g6x_check_structure writes it),
+    integrated time), over (0 not over by end_time, 1 over, 2 quasi-stable,
+    3 beyond the break scale), summary (the structure as g6x_check_structure writes it),
     top_of, checks (how many increments it took), steps, energy (initial and
     final total energy).  timing (a dict, optional) receives launches,
     batch_s (wall time of the batch calls, copies included), check_s (the
@@ -63,6 +68,8 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     checks = np.zeros(ns, np.int64)
     over = np.zeros(ns, np.int32)
     summary = [""] * ns
+    last_state = [None] * ns          # the top-level grouping at the last check
+    state_count = np.zeros(ns, np.int64)
     e0 = [_energy(M[off[k]:off[k + 1]], X[off[k]:off[k + 1]], V[off[k]:off[k + 1]])
           for k in range(ns)]
     active = np.arange(ns)
@@ -89,14 +96,19 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
             t[active] += r["t_final"]
             steps[active] += r["steps"]
             checks[active] += 1
-            for q in np.flatnonzero(c["over"]):
-                over[active[q]] = 1
+            for q, s in enumerate(active):
+                st = _grouping(c["summary"][q])
+                state_count[s] = state_count[s] + 1 if st == last_state[s] else 0
+                last_state[s] = st
+                if c["over"][q]:
+                    over[s] = 1
+                elif c["escaping"][q] and state_count[s] > QSTABLE_COUNT:
+                    over[s] = 2
             if np.isfinite(rlim2[active]).any():
-                for q, s in enumerate(active):
-                    if not c["over"][q] and np.isfinite(rlim2[s]) and _beyond(
-                            M[off[s]:off[s + 1]], X[off[s]:off[s + 1]],
-                            TOP[off[s]:off[s + 1]], rlim2[s]):
-                        over[s] = 3
+                r2 = np.einsum("ij,ij->i", r["pos"], r["pos"])
+                far = np.maximum.reduceat(r2, np.concatenate([[0], np.cumsum(na)[:-1]]))
+                hit = (over[active] == 0) & (far > rlim2[active])
+                over[active[hit]] = 3
             go = (over[active] == 0) & (t[active] < end_time[active] * (1 - 1e-12)) \
                 & (r["status"] == 0)
             for q, s in enumerate(active):
@@ -119,16 +131,20 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     return out
 
 
-def _beyond(m_all, x_all, top_of, rlim2):
-    """A top-level node (its centre of mass) farther than the break scale
-    from the origin of the system's frame."""
-    for t in np.unique(top_of):
-        sel = top_of == t
-        m = m_all[sel]
-        cm = (m[:, None] * x_all[sel]).sum(0) / m.sum()
-        if cm @ cm > rlim2:
-            return True
-    return False
+# smallN's min_qstable_count: quasi-stable once the grouping has been
+# unchanged at more than this many consecutive checks (analyze.cc:909-950)
+QSTABLE_COUNT = 15
+
+
+def _grouping(summary):
+    """The top-level grouping of a structure summary, in the order of the
+    top-level nodes: smallN's state string (analyze.cc:771-821) holds the
+    same information (each node's leaves, not its inner structure)."""
+    out = []
+    for tok in summary.split():
+        ids = tok.replace("(", " ").replace(")", " ").replace(",", " ").split()
+        out.append(tuple(sorted(int(i) for i in ids)))
+    return tuple(out)
 
 
 def _energy(m, x, v):

@@ -147,10 +147,15 @@ def binary_single(seed, v_inf=0.6, b_max=1.5, d0=15.0):
 
 def scattering_outcome(summary, over):
     """flyby (the binary (0,1) survives), exchange (the single is in the
-    final binary), ionization (three singles), bound (a triple, or a
-    binary with the third body still bound to it) or unresolved."""
+    final binary), ionization (three singles), bound (a stable triple),
+    quasi-stable (smallN's ending for a repeating unstable grouping),
+    break-scale or unresolved."""
     if not over:
         return "unresolved"
+    if over == 2:
+        return "quasi-stable"
+    if over == 3:
+        return "break-scale"
     if summary.count("(") > 1:
         return "bound"
     if summary == "(0,1) 2":

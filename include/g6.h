@@ -279,7 +279,9 @@ int g6x_set_shape(int jl, int nsplit);
    "(first,second)" of body indices, top-level nodes separated by spaces.
    Returns bit 0 = over, bit 1 = a multiple above a binary was judged by the
    published Mardling-Aarseth criterion (smallN consults Mardling's nstab
-   there, which this library does not restate), or G6_ERR_ARG. */
+   there, which this library does not restate), bit 2 = every top-level node
+   escaping, stable or not (smallN's quasi-stable ending needs it together
+   with a history of the grouping, which the caller keeps), or G6_ERR_ARG. */
 int g6x_check_structure(int n, const double *mass, const double *pos, const double *vel,
                         int *top_of, char *summary, int summary_cap);
 

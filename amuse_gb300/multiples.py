@@ -97,7 +97,7 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
             steps[active] += r["steps"]
             checks[active] += 1
             for q, s in enumerate(active):
-                st = _grouping(c["summary"][q])
+                st = grouping(c["summary"][q])
                 state_count[s] = state_count[s] + 1 if st == last_state[s] else 0
                 last_state[s] = st
                 if c["over"][q]:
@@ -136,7 +136,7 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
 QSTABLE_COUNT = 15
 
 
-def _grouping(summary):
+def grouping(summary):
     """The top-level grouping of a structure summary, in the order of the
     top-level nodes: smallN's state string (analyze.cc:771-821) holds the
     same information (each node's leaves, not its inner structure)."""

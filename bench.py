@@ -511,17 +511,25 @@ def run_secondary(args):
         out, sample = workloads.run_multiples(args)
         import amuse_gb300 as ag
 
+        from amuse_gb300 import multiples
+
         def one(sys_):
             # resolve_collision's loop on the host: smallN for delta_t, then
-            # the structure check, until over or the end time
+            # the structure check with smallN's quasi-stable history, until
+            # over or the end time (the decisions of resolve_encounters)
             m, x, v = sys_
             t = 0.0
+            last, count = None, 0
             while t < args.end_time * (1 - 1e-12):
                 x, v, tf, _, _ = oracle.smalln_unpert(m, x, v, args.eta,
                                                       min(args.delta_t, args.end_time - t),
                                                       max_steps=args.max_steps)
                 t += tf
-                if ag.check_structure(m, x, v)["over"]:
+                c = ag.check_structure(m, x, v)
+                g = multiples.grouping(c["summary"])
+                count = count + 1 if g == last else 0
+                last = g
+                if c["over"] or (c["escaping"] and count > multiples.QSTABLE_COUNT):
                     break
 
         import concurrent.futures as cf

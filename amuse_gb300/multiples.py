@@ -22,11 +22,26 @@ here each encounter has its own, starting empty.  Break scale (over = 3,
 analyze.cc:1050-1059): after an increment that did not end the encounter,
 a top-level body farther than `break_scale` from the origin of the system's
 frame (between increments every body is top-level in the integrator's
-tree).  Not kept: the retries with perturbed initial conditions when an
-encounter does not end by `end_time` (those are returned with over = 0 for
-the caller to decide).  Each increment restarts the integrator from the
-returned state: unperturbed binaries are resolved at the end of an
-increment and found again in the next.
+tree).  smallN itself also stops inside an increment once a top-level
+body passes the break scale (every NCHECK steps, smallN.cc:1008-1017); here
+the break-scale ending comes at the end of that increment.
+
+Retries (`min_break_scale`, resolve_collision's loop over loop_count,
+multiples.py:1763-2090): an encounter that has not ended by `end_time` is
+run again from its initial conditions, up to 10 passes in all, with the
+break scale multiplied by (min_break_scale / break_scale)^(2/10) at each
+pass.  Under Python 3 resolve_collision never takes its other branch (the
+end-time extension: `2*(loop_count/2) != loop_count` is never true with true
+division), so a pass differs from the one before only in its break scale.
+The integration is deterministic, so a pass replays the same checks: the
+over and quasi-stable decisions fire at the same checks as in the first
+pass (none, by the end time), and only the break scale can end it.  Each
+pass is therefore decided from the first pass's recorded checks (the
+largest body distance and the state at each), without integrating again.
+An encounter that no pass ends comes back with over = 0, where
+resolve_collision raises DidNotFinishException.  Each increment restarts
+the integrator from the returned state: unperturbed binaries are resolved
+at the end of an increment and found again in the next.
 """
 import time
 
@@ -36,7 +51,8 @@ import amuse_gb300 as ag
 
 
 def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode="split",
-                       unperturbed=True, eta=0.14, max_steps=2_000_000, timing=None):
+                       unperturbed=True, eta=0.14, max_steps=2_000_000, timing=None,
+                       min_break_scale=None):
     """Advance every encounter until its interaction is over or end_time.
 
     systems: list of (mass[n], pos[n][3], vel[n][3]), n <= 64, each in its
@@ -44,14 +60,23 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     system.  Returns a list of dicts, one per system: pos, vel, time (the
     integrated time), over (0 not over by end_time, 1 over, 2 quasi-stable,
     3 beyond the break scale), summary (the structure as g6x_check_structure writes it),
-    top_of, checks (how many increments it took), steps, energy (initial and
-    final total energy).  timing (a dict, optional) receives launches,
+    top_of, checks (how many increments it took, in the pass that ended it),
+    passes (1, or the retry that ended it), steps, energy (initial and
+    final total energy).  min_break_scale (scalar or one per system, with
+    a finite break_scale): the retries of resolve_collision.  timing (a dict, optional) receives launches,
     batch_s (wall time of the batch calls, copies included), check_s (the
     structure checks) and the active systems per launch."""
     ns = len(systems)
     end_time = np.broadcast_to(np.asarray(end_time, float), (ns,))
     delta_t = np.broadcast_to(np.asarray(delta_t, float), (ns,))
     rlim2 = np.broadcast_to(np.asarray(break_scale, float) ** 2, (ns,))
+    retry = min_break_scale is not None
+    if retry:
+        if not np.isfinite(rlim2).all():
+            raise ValueError("retries need a finite break_scale")
+        # the squared break scale shrinks by this factor from one pass to the next
+        fac2 = (np.broadcast_to(np.asarray(min_break_scale, float), (ns,)) ** 2 / rlim2) \
+            ** (2.0 / LOOP_MAX)
     # all bodies in flat arrays; system s owns bodies off[s] .. off[s+1]-1
     nper = np.array([len(m) for m, _, _ in systems], np.int32)
     if ns and (nper.min() < 2 or nper.max() > 64):
@@ -70,6 +95,8 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     summary = [""] * ns
     last_state = [None] * ns          # the top-level grouping at the last check
     state_count = np.zeros(ns, np.int64)
+    passes = np.ones(ns, np.int32)
+    record = [[] for _ in range(ns)] if retry else None  # the first pass's checks
     e0 = [_energy(M[off[k]:off[k + 1]], X[off[k]:off[k + 1]], V[off[k]:off[k + 1]])
           for k in range(ns)]
     active = np.arange(ns)
@@ -109,10 +136,25 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
                 far = np.maximum.reduceat(r2, np.concatenate([[0], np.cumsum(na)[:-1]]))
                 hit = (over[active] == 0) & (far > rlim2[active])
                 over[active[hit]] = 3
+                if retry:
+                    for q, s in enumerate(active):
+                        a, b = off[s], off[s + 1]
+                        record[s].append((far[q], t[s], steps[s], X[a:b].copy(), V[a:b].copy(),
+                                          TOP[a:b].copy(), c["summary"][q]))
             go = (over[active] == 0) & (t[active] < end_time[active] * (1 - 1e-12)) \
                 & (r["status"] == 0)
             for q, s in enumerate(active):
                 summary[s] = c["summary"][q]
+            if retry:
+                for q in np.flatnonzero(~go & (over[active] == 0) & (r["status"] == 0)):
+                    s = active[q]
+                    p, k = _retry_pass(record[s], rlim2[s], fac2[s])
+                    if p:
+                        _, t[s], steps[s], x_k, v_k, top_k, summary[s] = record[s][k]
+                        a, b = off[s], off[s + 1]
+                        X[a:b], V[a:b], TOP[a:b] = x_k, v_k, top_k
+                        over[s], passes[s], checks[s] = 3, p, k + 1
+                    record[s] = []
             active = active[go]
             t_check += time.perf_counter() - t1
     finally:
@@ -126,9 +168,24 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
         a, b = off[k], off[k + 1]
         out.append(dict(pos=X[a:b].copy(), vel=V[a:b].copy(), time=float(t[k]),
                         over=int(over[k]), summary=summary[k], top_of=TOP[a:b].copy(),
-                        checks=int(checks[k]), steps=int(steps[k]),
+                        checks=int(checks[k]), passes=int(passes[k]), steps=int(steps[k]),
                         energy=(e0[k], _energy(M[a:b], X[a:b], V[a:b]))))
     return out
+
+
+# resolve_collision's loop_max: passes over one encounter in all
+LOOP_MAX = 10
+
+
+def _retry_pass(rec, rlim2, fac2):
+    """The first retry pass (2 .. LOOP_MAX) whose break scale one of the
+    recorded checks passes, and that check; (0, -1) if none."""
+    far = np.array([e[0] for e in rec])
+    for p in range(2, LOOP_MAX + 1):
+        hit = np.flatnonzero(far > rlim2 * fac2 ** (p - 1))
+        if len(hit):
+            return p, int(hit[0])
+    return 0, -1
 
 
 # smallN's min_qstable_count: quasi-stable once the grouping has been

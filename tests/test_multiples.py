@@ -113,6 +113,50 @@ def test_resolve_decisions_against_smalln():
     assert quasi >= 5 and differ <= 2
 
 
+def retry_loop(m, x0, v0, end_time, delta_t, scale, min_scale, loop_max=10):
+    """resolve_collision's retries as it runs them: every pass integrates
+    again from the initial conditions, with the break scale multiplied by
+    (min_scale / scale)^(2 / loop_max) from one pass to the next."""
+    fac = (min_scale / scale) ** (2.0 / loop_max)
+    for p in range(1, loop_max + 1):
+        check = product_check()
+        x, v, t, checks = x0, v0, 0.0, 0
+        while t < end_time * (1 - 1e-12):
+            x, v, tf, _ = oracle.smalln(m, x, v, 0.14, min(delta_t, end_time - t))
+            t += tf
+            checks += 1
+            over, tree, _ = check(m, x, v)
+            if not over and (x * x).sum(1).max() > scale ** 2:
+                over = 3
+            if over:
+                return over, tree, checks, t, p, x
+        scale *= fac
+    return 0, tree, checks, t, loop_max, x
+
+
+def test_retries_match_rerunning_each_pass():
+    """Encounters stopped long before they can end (end time 40): the
+    retries shrink the break scale until it ends them; the replay of the
+    first pass's checks decides each as integrating every pass again does."""
+    systems = [scattering(s) for s in range(10)]
+    res = multiples.resolve_encounters(HostBatch(), systems, end_time=40.0, delta_t=10.0,
+                                       break_scale=100.0, min_break_scale=4.0)
+    seen = []
+    for (m, x, v), r in zip(systems, res):
+        over, tree, checks, t, p, xe = retry_loop(m, x, v, 40.0, 10.0, 100.0, 4.0)
+        assert (r["over"], r["summary"], r["checks"], r["passes"]) == (over, tree, checks, p)
+        assert r["time"] == t and np.array_equal(r["pos"], xe)
+        seen.append(p)
+    print("passes", seen)
+    assert len(set(seen)) >= 2 and max(seen) > 1
+
+
+def test_retries_need_a_finite_break_scale():
+    with pytest.raises(ValueError):
+        multiples.resolve_encounters(HostBatch(), [scattering(0)], end_time=10.0, delta_t=10.0,
+                                     min_break_scale=1.0)
+
+
 def test_break_scale_ends_an_encounter():
     m, x, v = scattering(3, v_inf=2.0)
     r = multiples.resolve_encounters(HostBatch(), [(m, x, v)], end_time=1e4, delta_t=5.0,

@@ -145,6 +145,38 @@ def binary_single(seed, v_inf=0.6, b_max=1.5, d0=15.0):
     return m, x - cm, v - cv
 
 
+def _kepler_binary(rng, m1, m2, a):
+    """Two bodies on a Kepler orbit of semi-major axis a, e uniform in
+    [0, 0.7], random phase and orientation, in their centre-of-mass frame."""
+    e = rng.uniform(0, 0.7)
+    E = rng.uniform(0, 2 * np.pi)
+    M = m1 + m2
+    r = a * (1 - e * np.cos(E))
+    xr = np.array([a * (np.cos(E) - e), a * np.sqrt(1 - e * e) * np.sin(E), 0.0])
+    s = np.sqrt(M * a) / r
+    vr = np.array([-s * np.sin(E), s * np.sqrt(1 - e * e) * np.cos(E), 0.0])
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    xr, vr = q @ xr, q @ vr
+    return np.array([-m2 / M * xr, m1 / M * xr]), np.array([-m2 / M * vr, m1 / M * vr])
+
+
+def binary_binary(seed, v_inf=0.5, b_max=2.0, d0=20.0):
+    """One binary-binary scattering: two binaries of 0.25 + 0.25 (a = 1 and
+    a uniform in [0.5, 1.5]) approaching at relative speed v_inf from d0
+    apart with impact parameter up to b_max; centre-of-mass frame, G = 1.
+    numpy RandomState(seed)."""
+    rng = np.random.RandomState(seed)
+    m = np.full(4, 0.25)
+    x1, v1 = _kepler_binary(rng, 0.25, 0.25, 1.0)
+    x2, v2 = _kepler_binary(rng, 0.25, 0.25, rng.uniform(0.5, 1.5))
+    b = b_max * np.sqrt(rng.uniform())
+    x = np.vstack([x1 + [d0 / 2, 0, 0], x2 + [-d0 / 2, b, 0]])
+    v = np.vstack([v1 + [-v_inf / 2, 0, 0], v2 + [v_inf / 2, 0, 0]])
+    cm = (m[:, None] * x).sum(0) / m.sum()
+    cv = (m[:, None] * v).sum(0) / m.sum()
+    return m, x - cm, v - cv
+
+
 def scattering_outcome(summary, over):
     """flyby (the binary (0,1) survives), exchange (the single is in the
     final binary), ionization (three singles), bound (a stable triple),

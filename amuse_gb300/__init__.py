@@ -535,9 +535,10 @@ def check_structure(mass, pos, vel):
                 top_of=top, summary=buf.value.decode())
 
 
-def check_structure_batch(n_per_sys, mass, pos, vel, nthreads=0, summary_cap=256):
+def check_structure_batch(n_per_sys, mass, pos, vel, nthreads=0, summary_cap=512):
     """g6x_check_structure over many systems stored back to back, on the
-    host's cores (g6x_check_structure_batch).  Returns dict(over,
+    host's cores (g6x_check_structure_batch; summary_cap 512 holds the
+    longest tree of 64 bodies).  Returns dict(over,
     hierarchy_tested, escaping, top_of, summary): per-system arrays (top_of per body,
     local indices) and a list of summaries."""
     lib = load()

@@ -127,3 +127,22 @@ def test_structure_batch_refuses_bad_sizes():
         ag.check_structure_batch([3, 65], np.ones(68), np.zeros((68, 3)), np.zeros((68, 3)))
     with pytest.raises(ag.G6Error):
         ag.check_structure_batch([3, 0], np.ones(3), np.zeros((3, 3)), np.zeros((3, 3)))
+
+
+def test_structure_summary_of_64_bodies_fits():
+    """64 bodies at rest in pairs of pairs of pairs (six levels, each 30
+    times tighter than the one above): the nested summary is long and comes
+    back whole from both entry points."""
+    x = np.zeros((64, 3))
+    for i in range(64):
+        for k in range(6):
+            x[i, k % 3] += (((i >> (5 - k)) & 1) - 0.5) * 30.0 ** -k
+    v = np.zeros((64, 3))
+    m = np.full(64, 1.0 / 64)
+    single = ag.check_structure(m, x, v)
+    assert single["summary"].count("(") == 63 and len(single["summary"]) > 256
+    batch = ag.check_structure_batch([64], m, x, v)
+    assert batch["summary"][0] == single["summary"]
+    ids = sorted(int(t) for t in single["summary"].replace("(", " ").replace(")", " ")
+                 .replace(",", " ").split())
+    assert ids == list(range(64))

@@ -173,6 +173,34 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     return out
 
 
+def resolve_serial(integrate, m, x, v, end_time, delta_t, break_scale=np.inf):
+    """One encounter the way resolve_collision runs it, with any host
+    integrator: integrate(m, x, v, dt) -> (x, v, dt_done) advances the
+    system by one increment.  The same decisions as resolve_encounters
+    (structure check, smallN's quasi-stable history, break scale; no
+    retries).  Returns (over, summary, checks, time, x, v)."""
+    m = np.asarray(m, float)
+    x = np.array(x, float).reshape(-1, 3)
+    v = np.array(v, float).reshape(-1, 3)
+    t, checks, last, count, summary = 0.0, 0, None, 0, ""
+    while t < end_time * (1 - 1e-12):
+        x, v, dt = integrate(m, x, v, min(delta_t, end_time - t))
+        t += dt
+        checks += 1
+        c = ag.check_structure(m, x, v)
+        summary = c["summary"]
+        g = grouping(summary)
+        count = count + 1 if g == last else 0
+        last = g
+        if c["over"]:
+            return 1, summary, checks, t, x, v
+        if c["escaping"] and count > QSTABLE_COUNT:
+            return 2, summary, checks, t, x, v
+        if np.isfinite(break_scale) and (x * x).sum(1).max() > break_scale ** 2:
+            return 3, summary, checks, t, x, v
+    return 0, summary, checks, t, x, v
+
+
 # resolve_collision's loop_max: passes over one encounter in all
 LOOP_MAX = 10
 

@@ -521,28 +521,18 @@ def run_secondary(args):
     elif args.workload == "multiples":
         args.seed = 1 if args.seed is None else args.seed
         out, sample = workloads.run_multiples(args)
-        import amuse_gb300 as ag
 
         from amuse_gb300 import multiples
 
+        def smalln_host(m, x, v, dt):
+            x, v, tf, _, _ = oracle.smalln_unpert(m, x, v, args.eta, dt,
+                                                  max_steps=args.max_steps)
+            return x, v, tf
+
         def one(sys_):
-            # resolve_collision's loop on the host: smallN for delta_t, then
-            # the structure check with smallN's quasi-stable history, until
-            # over or the end time (the decisions of resolve_encounters)
-            m, x, v = sys_
-            t = 0.0
-            last, count = None, 0
-            while t < args.end_time * (1 - 1e-12):
-                x, v, tf, _, _ = oracle.smalln_unpert(m, x, v, args.eta,
-                                                      min(args.delta_t, args.end_time - t),
-                                                      max_steps=args.max_steps)
-                t += tf
-                c = ag.check_structure(m, x, v)
-                g = multiples.grouping(c["summary"])
-                count = count + 1 if g == last else 0
-                last = g
-                if c["over"] or (c["escaping"] and count > multiples.QSTABLE_COUNT):
-                    break
+            # resolve_collision's loop on the host (the decisions of
+            # resolve_encounters) around the oracle's smallN
+            multiples.resolve_serial(smalln_host, *sys_, args.end_time, args.delta_t)
 
         import concurrent.futures as cf
         t0 = time.perf_counter()

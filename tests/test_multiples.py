@@ -178,6 +178,26 @@ def test_retries_need_a_finite_break_scale():
                                      min_break_scale=1.0)
 
 
+def test_serial_loop_decides_as_the_batched_one():
+    """resolve_serial (one encounter at a time, the loop the host-core
+    baseline runs) and resolve_encounters make the same decisions on the
+    same integrator."""
+    def integrate(m, x, v, dt):
+        x, v, tf, _ = oracle.smalln(m, x, v, 0.14, dt)
+        return x, v, tf
+    systems = [scattering(s) for s in range(16)] + [workloads.binary_binary(s) for s in range(8)]
+    res = multiples.resolve_encounters(HostBatch(), systems, end_time=400.0, delta_t=10.0,
+                                       break_scale=40.0)
+    kinds = set()
+    for (m, x, v), r in zip(systems, res):
+        over, summ, checks, t, xe, _ = multiples.resolve_serial(integrate, m, x, v, 400.0, 10.0,
+                                                                break_scale=40.0)
+        assert (r["over"], r["summary"], r["checks"], r["time"]) == (over, summ, checks, t)
+        assert np.array_equal(r["pos"], xe)
+        kinds.add(over)
+    assert {1, 2, 3} <= kinds
+
+
 def test_break_scale_ends_an_encounter():
     m, x, v = scattering(3, v_inf=2.0)
     r = multiples.resolve_encounters(HostBatch(), [(m, x, v)], end_time=1e4, delta_t=5.0,

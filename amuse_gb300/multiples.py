@@ -59,13 +59,17 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     own frame (G = 1).  end_time, delta_t, break_scale: scalars or one per
     system.  Returns a list of dicts, one per system: pos, vel, time (the
     integrated time), over (0 not over by end_time, 1 over, 2 quasi-stable,
-    3 beyond the break scale), summary (the structure as g6x_check_structure writes it),
-    top_of, checks (how many increments it took, in the pass that ended it),
-    passes (1, or the retry that ended it), steps, energy (initial and
-    final total energy).  min_break_scale (scalar or one per system, with
-    a finite break_scale): the retries of resolve_collision.  timing (a dict, optional) receives launches,
-    batch_s (wall time of the batch calls, copies included), check_s (the
-    structure checks) and the active systems per launch."""
+    3 beyond the break scale), summary (the structure as
+    g6x_check_structure writes it), top_of, checks (how many increments it
+    took, in the pass that ended it), passes (1, or the retry that ended
+    it), steps, status (the batch status of its last increment: 0, or 1 if
+    it stopped at max_steps), energy (initial and final total energy).
+    min_break_scale (scalar or one per system, with a finite break_scale):
+    the retries of resolve_collision.  unperturbed: smallN's unperturbed
+    binaries on for these launches (switched off again on return).  timing
+    (a dict, optional) receives launches, batch_s (wall time of the batch
+    calls, copies included), check_s (the structure checks) and the active
+    systems per launch."""
     ns = len(systems)
     end_time = np.broadcast_to(np.asarray(end_time, float), (ns,))
     delta_t = np.broadcast_to(np.asarray(delta_t, float), (ns,))
@@ -96,6 +100,7 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     last_state = [None] * ns          # the top-level grouping at the last check
     state_count = np.zeros(ns, np.int64)
     passes = np.ones(ns, np.int32)
+    status = np.zeros(ns, np.int32)
     record = [[] for _ in range(ns)] if retry else None  # the first pass's checks
     e0 = [_energy(M[off[k]:off[k + 1]], X[off[k]:off[k + 1]], V[off[k]:off[k + 1]])
           for k in range(ns)]
@@ -123,6 +128,7 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
             t[active] += r["t_final"]
             steps[active] += r["steps"]
             checks[active] += 1
+            status[active] = r["status"]
             for q, s in enumerate(active):
                 st = grouping(c["summary"][q])
                 state_count[s] = state_count[s] + 1 if st == last_state[s] else 0
@@ -169,6 +175,7 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
         out.append(dict(pos=X[a:b].copy(), vel=V[a:b].copy(), time=float(t[k]),
                         over=int(over[k]), summary=summary[k], top_of=TOP[a:b].copy(),
                         checks=int(checks[k]), passes=int(passes[k]), steps=int(steps[k]),
+                        status=int(status[k]),
                         energy=(e0[k], _energy(M[a:b], X[a:b], V[a:b]))))
     return out
 

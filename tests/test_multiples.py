@@ -26,12 +26,14 @@ class HostBatch:
         pos, vel = pos.copy(), vel.copy()
         tf = np.zeros(len(nper))
         steps = np.zeros(len(nper), np.int64)
+        status = np.zeros(len(nper), np.int32)
         for s in range(len(nper)):
             a, b = off[s], off[s + 1]
-            p, v, t, st = oracle.smalln(mass[a:b], pos[a:b], vel[a:b], eta, t_end[s])
+            p, v, t, st = oracle.smalln(mass[a:b], pos[a:b], vel[a:b], eta, t_end[s],
+                                        max_steps=max_steps)
             pos[a:b], vel[a:b], tf[s], steps[s] = p, v, t, st
-        return dict(pos=pos, vel=vel, t_final=tf, steps=steps,
-                    status=np.zeros(len(nper), np.int32))
+            status[s] = 1 if max_steps and st >= max_steps and t < t_end[s] else 0
+        return dict(pos=pos, vel=vel, t_final=tf, steps=steps, status=status)
 
 
 def direct_loop(m, x, v, end_time, delta_t, structure):
@@ -196,6 +198,15 @@ def test_serial_loop_decides_as_the_batched_one():
         assert np.array_equal(r["pos"], xe)
         kinds.add(over)
     assert {1, 2, 3} <= kinds
+
+
+def test_step_cap_retires_an_encounter():
+    """A system stopped by the step cap leaves the loop with over = 0 and
+    its status, after that increment."""
+    r = multiples.resolve_encounters(HostBatch(), [scattering(1), scattering(2)], end_time=400.0,
+                                     delta_t=10.0, max_steps=50)
+    for x in r:
+        assert x["status"] == 1 and x["over"] == 0 and x["checks"] == 1 and x["time"] < 10.0
 
 
 def test_break_scale_ends_an_encounter():

@@ -137,7 +137,7 @@ def load():
     lib.g6x_set_shape.argtypes = [ctypes.c_int, ctypes.c_int]
     lib.g6x_check_structure.argtypes = [ctypes.c_int, _pd, _pd, _pd, _pi, ctypes.c_char_p,
                                         ctypes.c_int]
-    lib.g6x_check_structure_batch.argtypes = [ctypes.c_int, _pi, _pd, _pd, _pd, _pi, _pi,
+    lib.g6x_check_structure_batch.argtypes = [ctypes.c_int, _pi, _pd, _pd, _pd, _pi, _pi, _pi,
                                               ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
     lib.g6x_stream.restype = _vp
     lib.g6x_set_fixed_jerk.argtypes = [I]
@@ -538,9 +538,10 @@ def check_structure(mass, pos, vel):
 def check_structure_batch(n_per_sys, mass, pos, vel, nthreads=0, summary_cap=512):
     """g6x_check_structure over many systems stored back to back, on the
     host's cores (g6x_check_structure_batch; summary_cap 512 holds the
-    longest tree of 64 bodies).  Returns dict(over,
-    hierarchy_tested, escaping, top_of, summary): per-system arrays (top_of per body,
-    local indices) and a list of summaries."""
+    longest tree of 64 bodies).  Returns dict(over, hierarchy_tested,
+    escaping, top_of, top_rank, summary): per-system arrays, per-body arrays
+    (top_of: local indices; top_rank: the position of the body's top-level
+    node in the tree's order) and a list of summaries."""
     lib = load()
     nper = _i32(n_per_sys)
     ns = len(nper)
@@ -551,17 +552,18 @@ def check_structure_batch(n_per_sys, mass, pos, vel, nthreads=0, summary_cap=512
         raise G6Error("g6x_check_structure_batch: mass has the wrong length")
     flags = np.zeros(ns, np.int32)
     top = np.zeros(nb, np.int32)
+    rank = np.zeros(nb, np.int32)
     buf = ctypes.create_string_buffer(max(1, ns * summary_cap))
     rc = lib.g6x_check_structure_batch(ns, _ptr(nper, ctypes.c_int), _ptr(m, ctypes.c_double),
                                        _ptr(x, ctypes.c_double), _ptr(v, ctypes.c_double),
-                                       _ptr(flags, ctypes.c_int), _ptr(top, ctypes.c_int), buf,
-                                       summary_cap, int(nthreads))
+                                       _ptr(flags, ctypes.c_int), _ptr(top, ctypes.c_int),
+                                       _ptr(rank, ctypes.c_int), buf, summary_cap, int(nthreads))
     _check(rc, "g6x_check_structure_batch")
     raw = buf.raw
     summ = [raw[k * summary_cap:(k + 1) * summary_cap].split(b"\0", 1)[0].decode()
             for k in range(ns)]
     return dict(over=(flags & 1).astype(bool), hierarchy_tested=(flags & 2).astype(bool),
-                escaping=(flags & 4).astype(bool), top_of=top, summary=summ)
+                escaping=(flags & 4).astype(bool), top_of=top, top_rank=rank, summary=summ)
 
 
 def drive_load(mass, pos, vel, acc=None, jerk=None, t=None, dt=None, ids=None):

@@ -382,8 +382,11 @@ static int describe(const st_tree *T, int k, char *s, int cap) {
   return w;
 }
 
-int g6x_check_structure(int n, const double *mass, const double *pos, const double *vel,
-                        int *top_of, char *summary, int summary_cap) {
+/* top_rank (optional): per body, the position of its top-level node in the
+   tree's order; equal arrays mean the same top-level grouping in the same
+   order, which is what smallN's state string records (analyze.cc:771-821). */
+static int st_check(int n, const double *mass, const double *pos, const double *vel,
+                    int *top_of, int *top_rank, char *summary, int summary_cap) {
   if (n < 1 || n > ST_MAXN || !mass || !pos || !vel) return G6_ERR_ARG;
   st_tree *T = (st_tree *)calloc(1, sizeof(st_tree));
   if (!T) return G6_ERR_NOMEM;
@@ -429,14 +432,18 @@ int g6x_check_structure(int n, const double *mass, const double *pos, const doub
   }
   const int escaping = over;  /* every top-level node escaping */
   if (!stable) over = 0;
-  if (top_of) {
-    for (int k = r->od; k >= 0; k = T->n[k].ys) {
+  if (top_of || top_rank) {
+    int rank = 0;
+    for (int k = r->od; k >= 0; k = T->n[k].ys, rank++) {
       int lv[ST_MAXN];
       const int c = leaves(T, k, lv);
       int first = n;
       for (int a = 0; a < c; a++)
         if (T->n[lv[a]].leaf < first) first = T->n[lv[a]].leaf;
-      for (int a = 0; a < c; a++) top_of[T->n[lv[a]].leaf] = first;
+      for (int a = 0; a < c; a++) {
+        if (top_of) top_of[T->n[lv[a]].leaf] = first;
+        if (top_rank) top_rank[T->n[lv[a]].leaf] = rank;
+      }
     }
   }
   if (summary && summary_cap > 0) {
@@ -456,13 +463,18 @@ int g6x_check_structure(int n, const double *mass, const double *pos, const doub
   return over | (tested << 1) | (escaping << 2);
 }
 
+int g6x_check_structure(int n, const double *mass, const double *pos, const double *vel,
+                        int *top_of, char *summary, int summary_cap) {
+  return st_check(n, mass, pos, vel, top_of, NULL, summary, summary_cap);
+}
+
 /* Many systems at once: a pool of host threads takes systems from a shared
    counter (the checks of a hand-off increment are independent). */
 typedef struct {
   int nsys, cap;
   const int *off;
   const double *mass, *pos, *vel;
-  int *flags, *top_of;
+  int *flags, *top_of, *top_rank;
   char *summary;
   atomic_int next;
 } st_batch;
@@ -473,17 +485,18 @@ static void *st_worker(void *arg) {
     const int s = atomic_fetch_add(&B->next, 1);
     if (s >= B->nsys) break;
     const int a = B->off[s], n = B->off[s + 1] - a;
-    B->flags[s] = g6x_check_structure(n, B->mass + a, B->pos + 3 * (size_t)a,
-                                      B->vel + 3 * (size_t)a, B->top_of ? B->top_of + a : NULL,
-                                      B->summary ? B->summary + (size_t)s * B->cap : NULL,
-                                      B->summary ? B->cap : 0);
+    B->flags[s] = st_check(n, B->mass + a, B->pos + 3 * (size_t)a, B->vel + 3 * (size_t)a,
+                           B->top_of ? B->top_of + a : NULL,
+                           B->top_rank ? B->top_rank + a : NULL,
+                           B->summary ? B->summary + (size_t)s * B->cap : NULL,
+                           B->summary ? B->cap : 0);
   }
   return NULL;
 }
 
 int g6x_check_structure_batch(int nsys, const int *n_per_sys, const double *mass,
                               const double *pos, const double *vel, int *flags, int *top_of,
-                              char *summary, int summary_cap, int nthreads) {
+                              int *top_rank, char *summary, int summary_cap, int nthreads) {
   if (nsys < 0 || (nsys > 0 && (!n_per_sys || !mass || !pos || !vel || !flags)))
     return G6_ERR_ARG;
   if (summary && summary_cap < 1) return G6_ERR_ARG;
@@ -498,7 +511,7 @@ int g6x_check_structure_batch(int nsys, const int *n_per_sys, const double *mass
     }
     off[s + 1] = off[s] + n_per_sys[s];
   }
-  st_batch B = {nsys, summary_cap, off, mass, pos, vel, flags, top_of, summary, 0};
+  st_batch B = {nsys, summary_cap, off, mass, pos, vel, flags, top_of, top_rank, summary, 0};
   atomic_init(&B.next, 0);
   if (nthreads <= 0) {
     const long c = sysconf(_SC_NPROCESSORS_ONLN);

@@ -97,7 +97,9 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
     checks = np.zeros(ns, np.int64)
     over = np.zeros(ns, np.int32)
     summary = [""] * ns
-    last_state = [None] * ns          # the top-level grouping at the last check
+    # smallN's state at the last check: per body the rank of its top-level
+    # node (equal ranks over a system: the same grouping in the same order)
+    RANK = np.full(len(M), -1, np.int32)
     state_count = np.zeros(ns, np.int64)
     passes = np.ones(ns, np.int32)
     status = np.zeros(ns, np.int32)
@@ -129,17 +131,15 @@ def resolve_encounters(g6, systems, end_time, delta_t, break_scale=np.inf, mode=
             steps[active] += r["steps"]
             checks[active] += 1
             status[active] = r["status"]
-            for q, s in enumerate(active):
-                st = grouping(c["summary"][q])
-                state_count[s] = state_count[s] + 1 if st == last_state[s] else 0
-                last_state[s] = st
-                if c["over"][q]:
-                    over[s] = 1
-                elif c["escaping"][q] and state_count[s] > QSTABLE_COUNT:
-                    over[s] = 2
+            starts = np.concatenate([[0], np.cumsum(na)[:-1]])
+            same = np.logical_and.reduceat(c["top_rank"] == RANK[bodies], starts)
+            state_count[active] = np.where(same, state_count[active] + 1, 0)
+            RANK[bodies] = c["top_rank"]
+            over[active[c["over"]]] = 1
+            over[active[~c["over"] & c["escaping"] & (state_count[active] > QSTABLE_COUNT)]] = 2
             if np.isfinite(rlim2[active]).any():
                 r2 = np.einsum("ij,ij->i", r["pos"], r["pos"])
-                far = np.maximum.reduceat(r2, np.concatenate([[0], np.cumsum(na)[:-1]]))
+                far = np.maximum.reduceat(r2, starts)
                 hit = (over[active] == 0) & (far > rlim2[active])
                 over[active[hit]] = 3
                 if retry:

@@ -288,11 +288,14 @@ int g6x_check_structure(int n, const double *mass, const double *pos, const doub
 /* g6x_check_structure for nsys systems of n_per_sys[s] bodies stored back to
    back, on nthreads host threads (<= 0: one per online core).  flags[s]
    receives system s's return value; top_of (optional) the per-body values,
-   indices local to each system; summary (optional) nsys strings of
-   summary_cap bytes each.  Returns 0, or the first system's error. */
+   indices local to each system; top_rank (optional) per body the position
+   of its top-level node in the tree's order (two checks with equal top_rank
+   have the same top-level grouping in the same order: smallN's "state");
+   summary (optional) nsys strings of summary_cap bytes each.  Returns 0, or
+   the first system's error. */
 int g6x_check_structure_batch(int nsys, const int *n_per_sys, const double *mass,
                               const double *pos, const double *vel, int *flags, int *top_of,
-                              char *summary, int summary_cap, int nthreads);
+                              int *top_rank, char *summary, int summary_cap, int nthreads);
 
 /* Batched few-body systems (the encounters AMUSE's multiples module hands
    to smallN): nsys independent systems of n_per_sys[s] bodies (2..64),

@@ -8,7 +8,7 @@ import pytest
 
 import amuse_gb300 as ag
 import oracle
-from amuse_gb300 import ic
+from amuse_gb300 import ic, multiples
 
 
 def test_structure_matches_reference_fixtures():
@@ -120,6 +120,10 @@ def test_structure_batch_equals_single_calls():
             assert b["over"][k] == r["over"] and b["hierarchy_tested"][k] == r["hierarchy_tested"]
             assert b["summary"][k] == r["summary"]
             assert list(b["top_of"][off[k]:off[k + 1]]) == list(r["top_of"])
+            # top_rank: the summary's top-level nodes, in its order
+            rank = b["top_rank"][off[k]:off[k + 1]]
+            groups = tuple(tuple(np.flatnonzero(rank == q)) for q in range(rank.max() + 1))
+            assert groups == multiples.grouping(r["summary"])
 
 
 def test_structure_batch_refuses_bad_sizes():

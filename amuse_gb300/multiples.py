@@ -8,8 +8,9 @@ smallN's structure analysis calls the interaction over
 together on the GPU batch kernel (g6x_batch_run, smallN's scheme, one warp
 per system), checking each system's structure on the host after every
 increment (g6x_check_structure_batch: smallN's check_structure restated,
-on the host's cores) and retiring the systems whose interaction is over; the others continue in the
-next launch.
+on the host's cores) and retiring the systems whose interaction is over;
+the others continue in the next launch.  `resolve_serial` is the same loop
+for one encounter around any host integrator.
 
 Kept from resolve_collision's loop: increments of `delta_t` (its
 "initial_delta_t": it checks is_over after every such substep, whatever its

@@ -979,6 +979,12 @@ static double snu_forces(snu_tree *T, sn_body *b, int *imin, int *jmin) {
   }
   for (int i = 0; i < n; i++)
     for (int k = 0; k < 3; k++) b[i].acc[k] = b[i].jerk[k] = 0;
+  /* the leaves of each top-level node, in ascending order (the order the
+     sums below take them in) */
+  int mem[64][64], nm[64];
+  for (int s = 0; s < n; s++) nm[s] = 0;
+  for (int s = 0; s < n; s++)
+    if (ln[s] >= 0) mem[ln[s]][nm[ln[s]]++] = s;
   double min_ts2 = ORC_INF;
   *imin = *jmin = -1;
   for (int A = 0; A < n; A++) {
@@ -986,11 +992,11 @@ static double snu_forces(snu_tree *T, sn_body *b, int *imin, int *jmin) {
     for (int Bn = A + 1; Bn < n; Bn++) {
       if (T->node[Bn] != Bn) continue;
       double F[3] = {0, 0, 0}, J[3] = {0, 0, 0}, mind2 = ORC_INF;
-      for (int a = 0; a < n; a++) {
-        if (ln[a] != A) continue;
+      for (int ia = 0; ia < nm[A]; ia++) {
+        const int a = mem[A][ia];
         double fi[3] = {0, 0, 0}, ji[3] = {0, 0, 0};
-        for (int c = 0; c < n; c++) {
-          if (ln[c] != Bn) continue;
+        for (int ic = 0; ic < nm[Bn]; ic++) {
+          const int c = mem[Bn][ic];
           double dx[3], dv[3];
           for (int k = 0; k < 3; k++) dx[k] = lx[c][k] - lx[a][k], dv[k] = lv[c][k] - lv[a][k];
           double d2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];

@@ -96,6 +96,19 @@ def test_structure_known_configurations():
             assert int(rr["over"]) == over and rr["summary"] == tree
 
 
+def test_structure_one_and_two_bodies():
+    """The smallest systems: one body is over on its own, a bound pair at
+    rest is one stable binary; both as smallN answers."""
+    cases = [(np.array([1.0]), np.zeros((1, 3)), np.zeros((1, 3)), "0"),
+             (np.array([0.5, 0.5]), np.array([[0.0, 0, 0], [1.0, 0, 0]]), np.zeros((2, 3)),
+              "(0,1)")]
+    for m, x, v, tree in cases:
+        r = ag.check_structure(m, x, v)
+        assert r["over"] and r["summary"] == tree
+        if oracle.ref_available():
+            assert oracle.check_structure_ref(m, x, v) == (1, tree)
+
+
 def test_structure_refuses_bad_sizes():
     with pytest.raises(ag.G6Error):
         ag.check_structure(np.ones(65), np.zeros((65, 3)), np.zeros((65, 3)))

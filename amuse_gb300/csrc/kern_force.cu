@@ -90,9 +90,6 @@ namespace {
 #ifndef G6_TOT_SMEM
 #define G6_TOT_SMEM 2  // split: compensated totals in shared memory (2: with NN only)
 #endif
-#ifndef G6_S1
-#define G6_S1 1  // split: accumulate the condition number's sum
-#endif
 constexpr int NT = G6_NT;    // threads per CTA
 constexpr int TJ = G6_TILE;  // j records per tile
 // i-particles per thread: the split kernel's packed f32x2 pair terms need
@@ -387,7 +384,7 @@ struct SplitP {
     q.j[1] = f2_fma(mr3i, f2_fma(a3, dy, dvy), q.j[1]);
     q.j[2] = f2_fma(mr3i, f2_fma(a3, dz, dvz), q.j[2]);
     q.p = f2_add(q.p, mri);
-    if (!HJ && G6_S1) q.s = f2_fma(mri, rinv, q.s);
+    if (!HJ) q.s = f2_fma(mri, rinv, q.s);  // the condition number's sum
   }
   // Nearest-neighbour re-scan of one record of the best tile: the first j
   // (in slot order) whose key equals best and that is not the i itself
@@ -417,10 +414,8 @@ struct SplitP {
     return G6_TOT_SMEM == 1 || (G6_TOT_SMEM == 2 && NN);
   }
   __device__ static void fold_jerk(Tot &t, Part &q) {
-    if (G6_S1) {
-      fold_s(t, q);
-      q.s = 0ull;
-    }
+    fold_s(t, q);
+    q.s = 0ull;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       ff_acc(t.jh[k], t.jl[k], f2_lo(q.j[k]));
